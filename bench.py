@@ -1,0 +1,355 @@
+#!/usr/bin/env python3
+"""Benchmark of the connected-components solve on GB300.
+
+Workload (one step = one CC solve): the 8192 x 8192 2D bond-percolation grid
+(each lattice edge kept with p = 0.5, seed 1; 67,108,864 vertices,
+134,191,308 directed CSR entries, uint32 ids), solved by the exp_contraction
+option (ExponentialContraction::FindComponents) with the reference's default
+Config (beta 0.1, seq 1, algorithm seed 1001 = seed + 0 + 1000), one rank.
+
+  value   Gedges/s = directed CSR entries / device time of the solve, input
+          resident in HBM (CUDA events on the library's stream)
+  e2e     the same metric through the C ABI with pinned HOST buffers: the
+          host->device copy of the CSR and the device->host copy of the
+          labels are inside the timed region
+  roofline  the dominant kernel's algorithmic bytes per launch / its average
+          CUDA-event duration, against the measured HBM copy bandwidth
+
+Inputs (1.07 GB CSR + 0.27 GB labels) are larger than the 129 MB L2, so no
+flush is needed between steps.
+
+--impl reference times the CPU restatement of the reference algorithm
+(oracle/, all host threads as ranks) on the same workload and prints the same
+JSON line with "impl": "reference".
+
+Multi-GPU (torchrun, N ranks): every rank solves its own replica (a single
+graph does not shard on this path: replicas only); value = N x E / max-over-
+ranks time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+GRID_X = GRID_Y = 8192
+GRID_P = 0.5
+INPUT_SEED = 1
+ALGO_SEED = 1001
+METRIC = "Gedges/s per CC solve (exp_contraction, 2D bond percolation 8192x8192, p=0.5)"
+UNIT = "Gedges/s"
+FALLBACK_HBM = 6800.0
+L2_BYTES = 129 * 1024 * 1024
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured (MEASURED_PEAKS.json hbm_gbs)"
+    return FALLBACK_HBM, "fallback 6.8 TB/s (MEASURED_PEAKS.json absent)"
+
+
+def traffic_from_profile(kernel: str):
+    """dram bytes per launch of `kernel` from the committed ncu summary."""
+    p = ROOT / "profiles" / "traffic.json"
+    if not p.exists():
+        return None, None
+    d = json.loads(p.read_text())
+    e = d.get(kernel)
+    if not e:
+        return None, None
+    return e.get("dram_bytes_per_launch"), e.get("source")
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons, sampled during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines: list[str] = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        time.sleep(0.25)
+        return self
+
+    def _read(self):
+        for ln in self.proc.stdout:
+            self.lines.append(ln.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            time.sleep(0.25)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = max(mx, float(f[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def make_graph():
+    import components_gb300 as cc
+    return cc.gen_grid(GRID_X, GRID_Y, GRID_P, seed=INPUT_SEED, id_bytes=4)
+
+
+def cpu_reference_run(G, steps, warmup, sample_rows=None):
+    """Time the oracle's restatement of ExponentialContraction with one
+    thread per rank, P = host cores.  Returns (Gedges/s, per-step s, sample)."""
+    import oracle
+    threads = os.cpu_count() or 1
+    os.environ.setdefault("OMP_NUM_THREADS", str(threads))
+    if sample_rows:
+        import components_gb300 as cc
+        Gs = cc.gen_grid(GRID_X, sample_rows, GRID_P, seed=INPUT_SEED, id_bytes=4)
+        sample = f"{GRID_X}x{sample_rows} rows of the same grid family (p={GRID_P}, seed {INPUT_SEED})"
+    else:
+        Gs = G
+        sample = f"full {GRID_X}x{GRID_Y} grid"
+    n, rp, col = oracle.csr_u64(Gs)
+    out = np.empty(n, np.uint64)
+    import ctypes as C
+    rounds = C.c_uint64()
+    times = []
+    for i in range(warmup + steps):
+        t0 = time.perf_counter()
+        oracle.lib().or_exp_contraction(n, rp, col, threads, 0.1, 1, 0, ALGO_SEED + i, out,
+                                        C.byref(rounds))
+        t = time.perf_counter() - t0
+        if i >= warmup:
+            times.append(t)
+    m = int(rp[-1])
+    mean = sum(times) / len(times)
+    return m / mean / 1e9, mean, threads, sample
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--cpu-steps", type=int, default=2)
+    ap.add_argument("--no-check", action="store_true")
+    args = ap.parse_args()
+    rank, world, local = dist_env()
+
+    if args.impl == "reference":
+        if rank != 0:
+            return 0
+        import __graft_entry__ as ge
+        import oracle
+        oracle.build()
+        ge.build()
+        G = make_graph()
+        gps, mean_s, threads, sample = cpu_reference_run(G, max(args.steps, 1), args.warmup)
+        line = {
+            "impl": "reference", "metric": METRIC, "value": gps, "unit": UNIT,
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": mean_s * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "u64", "data": "synthetic",
+            "config": {"workload": "grid2d 8192x8192 p=0.5, exp_contraction", "n": G.n,
+                       "m_dir": G.m, "ranks": threads, "beta": 0.1, "seq": 1},
+            "cpu_baseline": {"value": gps, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": sample + "; oracle/cc_oracle.c restatement of "
+                             "ExponentialContraction, one thread per rank"},
+            "e2e": {"value": gps, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        }
+        print(json.dumps(line))
+        return 0
+
+    import torch
+    import __graft_entry__ as ge
+    if rank == 0 or world == 1:
+        ge.build()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+        dist.barrier()
+        ge.build()
+    torch.cuda.set_device(local)
+    import components_gb300 as cc
+    from components_gb300 import _lib
+
+    G = make_graph()
+    n, m = G.n, G.m
+    conf = cc.Config(seed=ALGO_SEED)
+    ctx = cc.Context(local)
+    stream = torch.cuda.ExternalStream(ctx.stream_handle)
+    D = G.to_device(f"cuda:{local}")
+    lab = torch.empty(n, dtype=torch.int32, device=f"cuda:{local}")
+    solver = cc.ExponentialContraction(conf, 0, 1, ctx)
+
+    def barrier():
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+
+    # ---- device-resident solve -------------------------------------------
+    for _ in range(args.warmup):
+        solver.FindComponents(D, lab)
+    ctx.set_profiling(True)
+    barrier()
+    solve_ms, launches, kstats = [], 0, {}
+    with ClockSampler(local) as clocks:
+        ev0 = torch.cuda.Event(enable_timing=True)
+        ev1 = torch.cuda.Event(enable_timing=True)
+        ev0.record(stream)
+        for _ in range(args.steps):
+            solver.FindComponents(D, lab)
+            st = ctx.stats()
+            solve_ms.append(st["solve_ms"])
+            launches += st["kernel_launches"]
+            for k, v in st["kernels"].items():
+                a = kstats.setdefault(k, {"launches": 0, "ms": 0.0, "bytes": 0})
+                a["launches"] += v["launches"]
+                a["ms"] += v["ms"]
+                a["bytes"] += v["bytes"]
+        ev1.record(stream)
+        barrier()
+    ctx.set_profiling(False)
+    elapsed_ms = ev0.elapsed_time(ev1)
+    if world > 1:
+        t = torch.tensor([elapsed_ms], device=f"cuda:{local}")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        elapsed_ms = float(t.item())
+    ms_per_step = elapsed_ms / args.steps
+    value = world * m / (ms_per_step * 1e-3) / 1e9
+    clock = clocks.summary()
+
+    # labels checked against the oracle once (outside the timed region)
+    checked = None
+    if rank == 0 and not args.no_check:
+        import oracle
+        oracle.build()
+        want = oracle.uf_labels(G)
+        got = lab.cpu().numpy().view(np.uint32).astype(np.uint64)
+        checked = bool(np.array_equal(got, want))
+
+    # ---- end to end through the C ABI with pinned host buffers ---------------
+    Hp = G.pinned()
+    hlab = torch.empty(n, dtype=torch.int32).pin_memory()
+    for _ in range(max(1, args.warmup)):
+        solver.FindComponents(Hp, hlab)
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        solver.FindComponents(Hp, hlab)
+    barrier()
+    e2e_s = (time.perf_counter() - t0) / args.steps
+    if world > 1:
+        t = torch.tensor([e2e_s], device=f"cuda:{local}")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e_value = world * m / e2e_s / 1e9
+    if checked is not None:
+        checked = checked and bool(np.array_equal(hlab.numpy().view(np.uint32).astype(np.uint64),
+                                                  lab.cpu().numpy().view(np.uint32).astype(np.uint64)))
+
+    # ---- roofline of the dominant kernel -------------------------------------
+    top = max(kstats.items(), key=lambda kv: kv[1]["ms"]) if kstats else (None, None)
+    peak, peak_src = peaks()
+    roof = None
+    if top[0]:
+        name, k = top
+        per_launch_bytes = k["bytes"] / max(k["launches"], 1)
+        per_launch_ms = k["ms"] / max(k["launches"], 1)
+        achieved = per_launch_bytes / (per_launch_ms * 1e-3) / 1e9
+        traffic, traffic_src = traffic_from_profile(name)
+        roof = {"bound": "hbm", "kernel": name, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "traffic": traffic,
+                "algorithmic_bytes_per_launch": per_launch_bytes, "ms_per_launch": per_launch_ms,
+                "peak_source": peak_src, "traffic_source": traffic_src}
+    share = {k: v["ms"] / max(sum(x["ms"] for x in kstats.values()), 1e-12) for k, v in kstats.items()}
+
+    if world > 1:
+        torch.distributed.barrier()
+    if rank != 0:
+        return 0
+
+    # ---- CPU baseline: the oracle restatement on a bounded sample -------------
+    cpu = None
+    if world == 1 and args.cpu_steps > 0:
+        gps, mean_s, threads, sample = cpu_reference_run(G, args.cpu_steps, 1)
+        cpu = {"value": gps, "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": f"{sample}, {args.cpu_steps} timed solves after 1 warm-up "
+                         f"({mean_s:.2f} s each); oracle/cc_oracle.c restatement of "
+                         "ExponentialContraction with one thread per rank"}
+
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
+        "config": {"workload": "grid2d 8192x8192 p=0.5 (seed 1), exp_contraction, 1 rank",
+                   "n": n, "m_dir": m, "id_bytes": 4, "beta": 0.1, "seq": 1,
+                   "algo_seed": ALGO_SEED, "parallelism": f"replicas x{world}",
+                   "l2": "inputs larger than L2 (1.34 GB CSR+labels > 129 MB), no flush"},
+        "e2e": {"value": e2e_value, "unit": UNIT,
+                "h2d_bytes_per_step": 8 * (n + 1) + 4 * m, "d2h_bytes_per_step": 4 * n,
+                "ms_per_step": e2e_s * 1e3},
+        "gpu_launches": launches,
+        "roofline": roof,
+        "kernel_share": share,
+        "solve_ms_median": statistics.median(solve_ms) if solve_ms else None,
+        "labels_match_oracle": checked,
+        "clocks": clock,
+        "cpu_baseline": cpu,
+    }
+    print(json.dumps(line))
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,15 @@
+"""components_gb300: the connected-components hot path of sebalamm/components,
+built for one GB300 (sm_103a).
+
+Native parts (built in-tree by components_gb300.build):
+  _build/libccgpu.so  CUDA kernels and the C ABI of include/cc_gpu.h
+  _build/libccgen.so  seeded synthetic graph generators (include/cc_gen.h)
+"""
+from .config import Config, parse_parameters
+from .graph import StaticGraph, from_edges, gen_gnm, gen_grid, gen_rhg, read_metis
+from .solvers import (AllReduce, Context, ExponentialContraction, LocalContraction, Propagation,
+                      ShortcutPropagation, SOLVERS, find_components)
+
+__all__ = ["Config", "parse_parameters", "StaticGraph", "from_edges", "gen_gnm", "gen_grid",
+           "gen_rhg", "read_metis", "AllReduce", "Context", "ExponentialContraction",
+           "LocalContraction", "Propagation", "ShortcutPropagation", "SOLVERS", "find_components"]

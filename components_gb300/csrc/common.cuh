@@ -1,0 +1,180 @@
+// common.cuh - shared device helpers of libccgpu (sm_103a only).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <cstdio>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/cc_gpu.h"
+
+namespace ccg {
+
+// Internal failure: carries a status code up to the C ABI, which converts it
+// to an int return.  Nothing below the ABI calls exit().
+struct Error : std::runtime_error {
+  int status;
+  Error(int s, const std::string &msg) : std::runtime_error(msg), status(s) {}
+};
+
+#define CCG_CUDA(call)                                                        \
+  do {                                                                        \
+    cudaError_t e_ = (call);                                                  \
+    if (e_ != cudaSuccess) {                                                  \
+      int st_ = (e_ == cudaErrorMemoryAllocation) ? CC_ERR_OOM : CC_ERR_CUDA; \
+      throw ::ccg::Error(st_, std::string(#call) + " failed: " +              \
+                                  cudaGetErrorString(e_) + " at " +           \
+                                  __FILE__ + ":" + std::to_string(__LINE__)); \
+    }                                                                         \
+  } while (0)
+
+#define CCG_LAUNCH_CHECK() CCG_CUDA(cudaGetLastError())
+
+constexpr uint32_t kNone = 0xffffffffu;
+constexpr int kBlock = 256;
+constexpr int kSMs = 152;  // GB300: 2 dies x 76 SMs
+
+// Per-solve launch bookkeeping, reported through cc_stats.  With prof on,
+// tic()/toc() bracket single kernels with CUDA events on their stream; the
+// durations are read after the solve (cc_stats.kernels).
+struct Counters {
+  uint64_t launches = 0;
+  uint64_t bytes = 0;  // algorithmic bytes (formulas next to each launcher)
+  bool prof = false;
+  struct Rec {
+    const char *name;
+    cudaEvent_t a, b;
+    uint64_t bytes;
+  };
+  std::vector<Rec> recs;
+  void add(uint64_t nl, uint64_t b) {
+    launches += nl;
+    bytes += b;
+  }
+  cudaEvent_t tic(cudaStream_t s) {
+    if (!prof) return nullptr;
+    cudaEvent_t e;
+    if (cudaEventCreate(&e) != cudaSuccess) return nullptr;
+    cudaEventRecord(e, s);
+    return e;
+  }
+  void toc(cudaStream_t s, const char *name, cudaEvent_t a, uint64_t b) {
+    if (!prof || !a) return;
+    cudaEvent_t e;
+    if (cudaEventCreate(&e) != cudaSuccess) return;
+    cudaEventRecord(e, s);
+    recs.push_back({name, a, e, b});
+  }
+  void clear_recs() {
+    for (auto &r : recs) {
+      cudaEventDestroy(r.a);
+      cudaEventDestroy(r.b);
+    }
+    recs.clear();
+  }
+};
+
+// Error word written by kernels that read a caller's CSR: a bounds failure
+// records its code and the access is skipped (no fault, no trap).
+enum : int { kErrNone = 0, kErrBadOffsets = 1, kErrBadId = 2, kErrOverflow = 3 };
+__device__ __forceinline__ void set_err(int *err, int code) {
+  if (err) atomicCAS(err, 0, code);
+}
+
+// Stream-ordered device buffer drawn from the context's memory pool.  The pool
+// keeps freed blocks (release threshold = max), so steady-state solves do not
+// reach cudaMalloc.
+struct DevBuf {
+  void *p = nullptr;
+  size_t bytes = 0;
+  cudaStream_t s = nullptr;
+  cudaMemPool_t pool = nullptr;
+  DevBuf() = default;
+  DevBuf(size_t nbytes, cudaStream_t st, cudaMemPool_t pl) { alloc(nbytes, st, pl); }
+  void alloc(size_t nbytes, cudaStream_t st, cudaMemPool_t pl) {
+    release();
+    s = st;
+    pool = pl;
+    bytes = nbytes;
+    if (nbytes == 0) return;
+    CCG_CUDA(cudaMallocFromPoolAsync(&p, nbytes, pool, s));
+  }
+  void release() {
+    if (p) cudaFreeAsync(p, s);
+    p = nullptr;
+    bytes = 0;
+  }
+  ~DevBuf() { release(); }
+  DevBuf(const DevBuf &) = delete;
+  DevBuf &operator=(const DevBuf &) = delete;
+  DevBuf(DevBuf &&o) noexcept { *this = std::move(o); }
+  DevBuf &operator=(DevBuf &&o) noexcept {
+    release();
+    p = o.p; bytes = o.bytes; s = o.s; pool = o.pool;
+    o.p = nullptr; o.bytes = 0;
+    return *this;
+  }
+  template <class T> T *as() const { return static_cast<T *>(p); }
+};
+
+inline unsigned grid_for(uint64_t work, int block = kBlock, unsigned cap = kSMs * 16) {
+  uint64_t g = (work + block - 1) / block;
+  if (g == 0) g = 1;
+  if (g > cap) g = cap;
+  return (unsigned)g;
+}
+
+// ---- device helpers --------------------------------------------------------
+
+// Loads that bypass L1 so that values written by other SMs during the same
+// kernel are seen (L2 is the point of coherence).
+__device__ __forceinline__ uint32_t ld_cg(const uint32_t *p) { return __ldcg(p); }
+__device__ __forceinline__ uint64_t ld_cg(const uint64_t *p) {
+  return __ldcg(reinterpret_cast<const unsigned long long *>(p));
+}
+__device__ __forceinline__ void st_cg(uint32_t *p, uint32_t v) { __stcg(p, v); }
+__device__ __forceinline__ void st_cg(uint64_t *p, uint64_t v) {
+  __stcg(reinterpret_cast<unsigned long long *>(p), (unsigned long long)v);
+}
+
+template <class T>
+__device__ __forceinline__ uint32_t load_id(const T *col, uint64_t e) {
+  return (uint32_t)__ldg(col + e);
+}
+
+// Vertex -> virtual rank of the contiguous split n/P + (r < n%P)
+// (graph_io.h:308-313).
+struct PartMap {
+  uint32_t q, rm, big;  // q = n/P, rm = n%P, big = rm*(q+1)
+  __host__ __device__ PartMap() : q(0), rm(0), big(0) {}
+  __host__ __device__ PartMap(uint64_t n, uint32_t P) {
+    q = (uint32_t)(n / P);
+    rm = (uint32_t)(n % P);
+    big = rm * (q + 1);
+  }
+  __host__ __device__ __forceinline__ uint32_t part(uint32_t v) const {
+    return v < big ? v / (q + 1) : rm + (q ? (v - big) / q : 0);
+  }
+};
+
+// SplitMix64 finaliser: the counter-based hash behind every random variate.
+__host__ __device__ __forceinline__ uint64_t mix64(uint64_t z) {
+  z += 0x9e3779b97f4a7c15ull;
+  z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+  z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+  return z ^ (z >> 31);
+}
+__host__ __device__ __forceinline__ uint64_t hash3(uint64_t seed, uint64_t a, uint64_t b) {
+  return mix64(mix64(mix64(seed) ^ a) ^ (b * 0xd6e8feb86659fd93ull));
+}
+
+// Warp-aggregated "any lane set" flag: one atomicOr per warp.
+__device__ __forceinline__ void warp_flag(int pred, int *flag) {
+  unsigned b = __ballot_sync(__activemask(), pred);
+  if (b && (threadIdx.x & 31) == (unsigned)(__ffs(b) - 1)) atomicOr(flag, 1);
+}
+
+}  // namespace ccg

@@ -1,0 +1,119 @@
+// kernels.h - host-side launchers of the libccgpu kernels.
+//
+// Every launcher enqueues work on the given stream and adds its launch count
+// and algorithmic bytes to a Counters record.  The byte formulas are those of
+// the measurement contract: s_o = 8 (row offsets), s_i = id bytes, s_k = 8 (key
+// or label word).
+#pragma once
+
+#include "common.cuh"
+
+namespace ccg {
+
+// A CSR graph on the device.  idb is 4 or 8 for the caller's input graph and
+// 4 for every graph the library builds itself.
+struct Csr {
+  uint64_t n = 0, m = 0;
+  const uint64_t *rp = nullptr;
+  const void *col = nullptr;
+  int idb = 4;
+  int *err = nullptr;  // device error word for caller-provided graphs
+};
+
+// ---- union-find hook-and-compress (uf.cu) ---------------------------------
+// parent[v] <- minimum vertex id of v's component.  With pm != nullptr only
+// edges whose endpoints lie in the same virtual rank are used, so parent[v] is
+// the minimum id of v's partition-local component
+// (exponential_contraction.h:391-411 FindLocalComponents).
+void uf_components(const Csr &g, uint32_t *parent, const PartMap *pm,
+                   uint32_t hub_degree, cudaStream_t s, cudaMemPool_t pool,
+                   Counters &c);
+
+// Write uint32 labels to an id_bytes-wide output array.
+void widen_labels(const uint32_t *in, void *out, int out_bytes, uint64_t n,
+                  cudaStream_t s, Counters &c);
+
+// ---- scan / radix sort / component graph (sortcsr.cu) ----------------------
+// Stable LSD radix sort of uint64 keys on bits [0, bits); returns the buffer
+// (keys or tmp) that holds the result.
+uint64_t *radix_sort_u64(uint64_t *keys, uint64_t *tmp, uint64_t n, int bits,
+                         cudaStream_t s, cudaMemPool_t pool, Counters &c);
+
+// Result of contracting a graph along a vertex map.
+struct Contracted {
+  uint64_t n = 0, m = 0;
+  DevBuf rp, col;   // CSR of the contracted graph (uint32 ids)
+  DevBuf vid;       // per new vertex: original vertex id of its representative
+  DevBuf newid;     // per old cluster id: new vertex id or kNone
+};
+
+// Build the quotient graph: for every edge (v,w) of g with
+// cl[v] != cl[w] the undirected edge {cl[v], cl[w]}, deduplicated.  Cluster
+// ids lie in [0, ncl).  New vertices are the clusters with at least one edge,
+// numbered in increasing cluster-id order, so the order of cluster ids is
+// kept.  vid_of_cluster maps a cluster id to the original vertex id carried
+// over (nullptr = the cluster id itself).  With pm != nullptr only edges
+// between different virtual ranks are kept (cut edges).
+// Replaces CAGBuilder::PerformLocalContraction/BuildLocalContractionGraph
+// (cag_builder.h:160-230, 577-667) and DynamicContraction's conflicting-edge
+// routing and InsertAndClearEdges (dynamic_contraction.h:62-136, 251-290,
+// 513-559): relabel, compact, sort, dedup, CSR rebuild.
+void contract_graph(const Csr &g, const uint32_t *cl, uint64_t ncl,
+                    const uint32_t *vid_of_cluster, const PartMap *pm,
+                    Contracted &out, cudaStream_t s, cudaMemPool_t pool,
+                    Counters &c, uint32_t *host_mailbox);
+
+// ---- decomposition kernels (ldd.cu) ---------------------------------------
+// Threshold table of the deviate sampler: dev >= k  iff  u < T[k-1], with
+// T[k-1] = floor(2^64 exp(-beta k)), at most kGeoMax entries.
+constexpr int kGeoMax = 4096;
+int geo_table_build(double beta, std::vector<uint64_t> &t);
+void geo_table_upload(double beta, uint64_t *d_table, int *len_out, cudaStream_t s);
+
+// Copy of a caller CSR's ids as uint32 with bounds checks (ids < n, offsets
+// monotone and <= m); failures go to g.err.  Used before kernels that assume
+// a trusted uint32 graph.
+void sanitize_ids(const Csr &g, uint32_t *col32, cudaStream_t s, Counters &c);
+
+// Exponential-shift decomposition on g (exponential_contraction.h:439-628).
+// key[i] = (dev_i << 32) | i; relaxes key[i] = min(key[i], key[j] + 2^32)
+// over neighbours to the fixpoint.  cluster[i] = low 32 bits (centre index).
+// Returns the number of rounds, or -1 if max_rounds was hit.
+int ldd_decompose(const Csr &g, const uint32_t *vid, uint64_t seed, uint32_t level,
+                  const uint64_t *d_geo, int geo_len, bool gated, uint32_t *cluster,
+                  uint64_t *key, int max_rounds, cudaStream_t s, cudaMemPool_t pool,
+                  Counters &c, volatile int *host_flag, int *dev_flag);
+
+// Local contraction sweeps (local_contraction.h:157-300): uniform deviates in
+// [0,99], then two Jacobi sweeps of the lexicographic minimum over N[v].
+void local_sweeps(const Csr &g, const uint32_t *vid, uint64_t seed, uint32_t level,
+                  uint32_t *cluster, uint64_t *k0, uint64_t *k1, cudaStream_t s,
+                  Counters &c);
+
+// ---- propagation kernels (prop.cu) -----------------------------------------
+// Min-label propagation rounds (propagation.h:72-149) on lab (in place).
+int labels_propagate(const Csr &g, uint32_t *lab, int max_rounds, cudaStream_t s,
+                     cudaMemPool_t pool, Counters &c, volatile int *host_flag, int *dev_flag);
+// Shortcut propagation rounds (shortcut_propagation.h:124-376).
+int shortcut_propagate(const Csr &g, uint32_t *lab, uint32_t hitters, int max_rounds,
+                       cudaStream_t s, cudaMemPool_t pool, Counters &c,
+                       volatile int *host_flag, int *dev_flag);
+
+// out[i] = lab_next[newid[cl[i]]] if newid[cl[i]] != kNone else rep[cl[i]]
+// (label composition, replaces DynamicContraction::UndoContraction,
+// dynamic_contraction.h:568-658).
+void compose_labels(const uint32_t *cl, const uint32_t *newid, const uint32_t *lab_next,
+                    const uint32_t *rep, uint32_t *out, uint64_t n, cudaStream_t s,
+                    Counters &c);
+// lab[v] <- minimum vertex id among all u with lab[u] == lab[v]; lab values are
+// vertex ids in [0, n).  scratch: n uint32.
+void canonicalize(uint32_t *lab, uint32_t *scratch, uint64_t n, cudaStream_t s, Counters &c);
+// Count v with lab[v] == v (components, canonical labels).
+void count_roots(const uint32_t *lab, uint64_t n, unsigned long long *d_count,
+                 cudaStream_t s, Counters &c);
+// Gather: out[i] = src[idx[i]]
+void gather_u32(const uint32_t *src, const uint32_t *idx, uint32_t *out, uint64_t n,
+                cudaStream_t s, Counters &c);
+void iota_u32(uint32_t *out, uint64_t n, cudaStream_t s, Counters &c);
+
+}  // namespace ccg

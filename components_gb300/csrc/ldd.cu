@@ -1,0 +1,295 @@
+// ldd.cu - exponential-shift low-diameter decomposition and the local
+// contraction sweeps.
+//
+// Reference: ExponentialContraction::RunContractionLP
+// (exponential_contraction.h:439-628).  Every vertex draws a deviate
+// dev = (u64)Exp(beta) (:469-472) and then repeatedly adopts
+// (dev_w + 1, label_w) from a neighbour w when it is lexicographically
+// smaller than its own (dev, label) (:527-549), until no vertex changes.  The
+// fixpoint is  key(v) = min_u (dev_u + dist(u, v), label_u),  which does not
+// depend on the update order, so the decomposition (each vertex's centre) is
+// fully determined by the deviates.
+//
+// GB300 layout: one 64-bit key per vertex, (dev << 32) | index.  Vertex
+// indices of every level graph are numbered in increasing original-id order,
+// so comparing indices compares the reference's labels, and adding 2^32 is
+// the "+1" on the deviate.  A relaxation is then a u64 min; the centre is the
+// low word of the key.
+//
+// Deviates: the reference draws from std::exponential_distribution seeded per
+// vertex with a std::default_random_engine (:469-472).  Here a counter-based
+// hash of (seed, original id, level) gives a uniform 64-bit word u, and
+// dev = #{k >= 1 : u < T[k]} with T[k] = floor(2^64 exp(-beta k)): inverse
+// transform sampling of floor(Exp(beta)), which is geometric with
+// P(dev >= k) = exp(-beta k).  T is built on the host with a fixed sequence
+// of IEEE double operations (det_exp below), so the table, and with it every
+// deviate, is the same on every host.
+#include <cmath>
+#include <vector>
+
+#include "kernels.h"
+
+namespace ccg {
+
+// exp(x) for x <= 0 from range reduction by ln 2 and a Taylor series, with a
+// fixed evaluation order (no library call, no contraction into FMA), so that
+// the result is identical on every IEEE-754 host.
+double det_exp(double x) {
+  const double ln2 = 0.6931471805599453094172321;
+  double kf = std::floor(x / ln2 + 0.5);
+  volatile double r = x - kf * ln2;  // volatile: keep the two roundings
+  double rr = r;
+  double term = 1.0, sum = 1.0;
+  for (int i = 1; i < 30; ++i) {
+    term = term * rr;
+    term = term / (double)i;
+    sum = sum + term;
+  }
+  return std::ldexp(sum, (int)kf);
+}
+
+int geo_table_build(double beta, std::vector<uint64_t> &t) {
+  t.clear();
+  if (!(beta > 0.0)) return 0;
+  const int kmax = 4096;
+  for (int k = 1; k <= kmax; ++k) {
+    double p = det_exp(-beta * (double)k);
+    double x = std::ldexp(p, 64);
+    if (x < 1.0) break;
+    uint64_t v = x >= 18446744073709551615.0 ? ~0ull : (uint64_t)x;
+    t.push_back(v);
+  }
+  return (int)t.size();
+}
+
+namespace {
+
+__device__ __forceinline__ uint32_t geo_dev(uint64_t u, const uint64_t *__restrict__ T, int len) {
+  // T is non-increasing: {k : u < T[k-1]} is a prefix 1..j; find j.
+  int lo = 0, hi = len;  // answer in [lo, hi]
+  while (lo < hi) {
+    int mid = (lo + hi + 1) >> 1;
+    if (u < __ldg(T + mid - 1)) lo = mid;
+    else hi = mid - 1;
+  }
+  return (uint32_t)lo;
+}
+
+__global__ void k_ldd_init(uint64_t n, const uint32_t *__restrict__ vid, uint64_t seed,
+                           uint32_t level, const uint64_t *__restrict__ T, int len,
+                           uint64_t *__restrict__ key, unsigned int *__restrict__ maxdev) {
+  uint32_t mx = 0;
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n;
+       i += (uint64_t)gridDim.x * blockDim.x) {
+    uint64_t u = hash3(seed, vid[i], level);
+    uint32_t d = geo_dev(u, T, len);
+    key[i] = ((uint64_t)d << 32) | (uint32_t)i;
+    mx = d > mx ? d : mx;
+  }
+  for (int o = 16; o; o >>= 1) {
+    uint32_t y = __shfl_xor_sync(__activemask(), mx, o);
+    mx = y > mx ? y : mx;
+  }
+  if ((threadIdx.x & 31) == 0) atomicMax(maxdev, mx);
+}
+
+constexpr uint64_t kOne = 1ull << 32;
+constexpr uint64_t kRowLimit = 64;  // rows above this are relaxed warp-per-row
+
+// One Gauss-Seidel style sweep: key[v] <- min(key[v], min_w key[w] + 2^32).
+// Stale neighbour reads are upper bounds of the fixpoint, so in-place updates
+// converge to the same keys as the reference's sweeps.
+__global__ void k_ldd_round(uint64_t n, const uint64_t *__restrict__ rp,
+                            const uint32_t *__restrict__ col, uint64_t *key, int *flag) {
+  int changed = 0;
+  for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < n;
+       v += (uint64_t)gridDim.x * blockDim.x) {
+    uint64_t b = __ldg(rp + v), e = __ldg(rp + v + 1);
+    if (e - b > kRowLimit) continue;
+    uint64_t k = ld_cg(key + v), best = k;
+    for (uint64_t j = b; j < e; ++j) {
+      uint64_t kw = ld_cg(key + __ldg(col + j)) + kOne;
+      best = kw < best ? kw : best;
+    }
+    if (best < k) {
+      st_cg(key + v, best);
+      changed = 1;
+    }
+  }
+  warp_flag(changed, flag);
+}
+
+__global__ void k_ldd_round_hubs(const uint64_t *__restrict__ rp, const uint32_t *__restrict__ col,
+                                 const uint32_t *__restrict__ hubs,
+                                 const unsigned int *__restrict__ nh, uint64_t *key, int *flag) {
+  const unsigned lane = threadIdx.x & 31;
+  const uint64_t warp = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
+  const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+  const uint32_t nhubs = *nh;
+  int changed = 0;
+  for (uint64_t h = warp; h < nhubs; h += nwarps) {
+    uint32_t v = hubs[h];
+    uint64_t b = __ldg(rp + v), e = __ldg(rp + v + 1);
+    uint64_t best = ~0ull;
+    for (uint64_t j = b + lane; j < e; j += 32) {
+      uint64_t kw = ld_cg(key + __ldg(col + j)) + kOne;
+      best = kw < best ? kw : best;
+    }
+#pragma unroll
+    for (int o = 16; o; o >>= 1) {
+      uint64_t y = __shfl_xor_sync(0xffffffffu, best, o);
+      best = y < best ? y : best;
+    }
+    if (lane == 0) {
+      uint64_t k = ld_cg(key + v);
+      if (best < k) {
+        atomicMin(reinterpret_cast<unsigned long long *>(key + v), (unsigned long long)best);
+        changed = 1;
+      }
+    }
+  }
+  warp_flag(changed, flag);
+}
+
+__global__ void k_list_rows(uint64_t n, const uint64_t *__restrict__ rp, uint64_t limit,
+                            uint32_t *__restrict__ hubs, unsigned int *__restrict__ nh) {
+  for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < n;
+       v += (uint64_t)gridDim.x * blockDim.x)
+    if (rp[v + 1] - rp[v] > limit) hubs[atomicAdd(nh, 1u)] = (uint32_t)v;
+}
+
+// Start-time gated round t (RunContractionBFS, exponential_contraction.h:
+// 630-859): vertices whose key has deviate part t are final and push
+// key + 2^32 to their neighbours.  Ties are broken by label, as in the
+// sweeps, so both variants reach the same keys.
+__global__ void k_ldd_gated(uint64_t n, const uint64_t *__restrict__ rp,
+                            const uint32_t *__restrict__ col, uint64_t *key, uint32_t t) {
+  for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < n;
+       v += (uint64_t)gridDim.x * blockDim.x) {
+    uint64_t k = ld_cg(key + v);
+    if ((uint32_t)(k >> 32) != t) continue;
+    uint64_t kp = k + kOne;
+    uint64_t b = __ldg(rp + v), e = __ldg(rp + v + 1);
+    for (uint64_t j = b; j < e; ++j) {
+      uint32_t w = __ldg(col + j);
+      if (ld_cg(key + w) > kp)
+        atomicMin(reinterpret_cast<unsigned long long *>(key + w), (unsigned long long)kp);
+    }
+  }
+}
+
+__global__ void k_low_word(uint64_t n, const uint64_t *__restrict__ key, uint32_t *__restrict__ cl) {
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n;
+       i += (uint64_t)gridDim.x * blockDim.x)
+    cl[i] = (uint32_t)key[i];
+}
+
+// ---- local contraction (local_contraction.h:157-300) -----------------------
+__global__ void k_local_init(uint64_t n, const uint32_t *__restrict__ vid, uint64_t seed,
+                             uint32_t level, uint64_t *__restrict__ k0) {
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n;
+       i += (uint64_t)gridDim.x * blockDim.x) {
+    // uniform integer in [0, 99] (reference: uniform_int_distribution(0, 99))
+    uint32_t d = (uint32_t)(((hash3(seed, vid[i], level) >> 32) * 100ull) >> 32);
+    k0[i] = ((uint64_t)d << 32) | (uint32_t)i;
+  }
+}
+
+// Jacobi sweep: out[v] = min over N[v] (closed neighbourhood) of in[].
+__global__ void k_min_sweep(uint64_t n, const uint64_t *__restrict__ rp,
+                            const uint32_t *__restrict__ col, const uint64_t *__restrict__ in,
+                            uint64_t *__restrict__ out) {
+  for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < n;
+       v += (uint64_t)gridDim.x * blockDim.x) {
+    uint64_t b = __ldg(rp + v), e = __ldg(rp + v + 1);
+    uint64_t best = in[v];
+    for (uint64_t j = b; j < e; ++j) {
+      uint64_t kw = __ldg(in + __ldg(col + j));
+      best = kw < best ? kw : best;
+    }
+    out[v] = best;
+  }
+}
+
+}  // namespace
+
+void geo_table_upload(double beta, uint64_t *d_table, int *len_out, cudaStream_t s) {
+  std::vector<uint64_t> t;
+  int len = geo_table_build(beta, t);
+  if (len) CCG_CUDA(cudaMemcpyAsync(d_table, t.data(), 8 * len, cudaMemcpyHostToDevice, s));
+  CCG_CUDA(cudaStreamSynchronize(s));  // t is a host temporary
+  *len_out = len;
+}
+
+int ldd_decompose(const Csr &g, const uint32_t *vid, uint64_t seed, uint32_t level,
+                  const uint64_t *d_geo, int geo_len, bool gated, uint32_t *cluster,
+                  uint64_t *key, int max_rounds, cudaStream_t s, cudaMemPool_t pool,
+                  Counters &c, volatile int *host_flag, int *dev_flag) {
+  if (g.n == 0) return 0;
+  const uint32_t *col = static_cast<const uint32_t *>(g.col);
+  unsigned grid = grid_for(g.n, kBlock, kSMs * 32);
+  DevBuf mx(4, s, pool);
+  CCG_CUDA(cudaMemsetAsync(mx.p, 0, 4, s));
+  k_ldd_init<<<grid, kBlock, 0, s>>>(g.n, vid, seed, level, d_geo, geo_len, key,
+                                     mx.as<unsigned int>());
+  CCG_LAUNCH_CHECK();
+  c.add(1, 4 * g.n + 8 * g.n);
+  int rounds = 0;
+  const uint64_t round_bytes = 8 * (g.n + 1) + g.m * 4 + g.m * 8 + 2 * g.n * 8;
+  if (gated) {
+    uint32_t maxdev = 0;
+    CCG_CUDA(cudaMemcpyAsync(&maxdev, mx.p, 4, cudaMemcpyDeviceToHost, s));
+    CCG_CUDA(cudaStreamSynchronize(s));
+    for (uint32_t t = 0; t <= maxdev; ++t) {
+      k_ldd_gated<<<grid, kBlock, 0, s>>>(g.n, g.rp, col, key, t);
+      CCG_LAUNCH_CHECK();
+      ++rounds;
+    }
+    // every vertex is final once; every edge pushed once
+    c.add(rounds, 8 * (g.n + 1) + g.m * 4 + g.m * 8 + (uint64_t)rounds * g.n * 8);
+  } else {
+    DevBuf hubs(4 * (g.m / (kRowLimit + 1) + 1), s, pool), nh(4, s, pool);
+    CCG_CUDA(cudaMemsetAsync(nh.p, 0, 4, s));
+    k_list_rows<<<grid, kBlock, 0, s>>>(g.n, g.rp, kRowLimit, hubs.as<uint32_t>(),
+                                        nh.as<unsigned int>());
+    CCG_LAUNCH_CHECK();
+    for (;;) {
+      if (rounds >= max_rounds) return -1;
+      *host_flag = 0;
+      CCG_CUDA(cudaMemsetAsync(dev_flag, 0, sizeof(int), s));
+      k_ldd_round<<<grid, kBlock, 0, s>>>(g.n, g.rp, col, key, dev_flag);
+      CCG_LAUNCH_CHECK();
+      k_ldd_round_hubs<<<kSMs * 4, kBlock, 0, s>>>(g.rp, col, hubs.as<uint32_t>(),
+                                                   nh.as<unsigned int>(), key, dev_flag);
+      CCG_LAUNCH_CHECK();
+      CCG_CUDA(cudaMemcpyAsync((void *)host_flag, dev_flag, sizeof(int), cudaMemcpyDeviceToHost, s));
+      CCG_CUDA(cudaStreamSynchronize(s));
+      ++rounds;
+      c.add(2, round_bytes);
+      if (*host_flag == 0) break;
+    }
+  }
+  k_low_word<<<grid, kBlock, 0, s>>>(g.n, key, cluster);
+  CCG_LAUNCH_CHECK();
+  c.add(1, 12 * g.n);
+  return rounds;
+}
+
+void local_sweeps(const Csr &g, const uint32_t *vid, uint64_t seed, uint32_t level,
+                  uint32_t *cluster, uint64_t *k0, uint64_t *k1, cudaStream_t s, Counters &c) {
+  if (g.n == 0) return;
+  const uint32_t *col = static_cast<const uint32_t *>(g.col);
+  unsigned grid = grid_for(g.n, kBlock, kSMs * 32);
+  k_local_init<<<grid, kBlock, 0, s>>>(g.n, vid, seed, level, k0);
+  CCG_LAUNCH_CHECK();
+  k_min_sweep<<<grid, kBlock, 0, s>>>(g.n, g.rp, col, k0, k1);  // N(v)
+  CCG_LAUNCH_CHECK();
+  k_min_sweep<<<grid, kBlock, 0, s>>>(g.n, g.rp, col, k1, k0);  // N(N(v))
+  CCG_LAUNCH_CHECK();
+  k_low_word<<<grid, kBlock, 0, s>>>(g.n, k0, cluster);
+  CCG_LAUNCH_CHECK();
+  const uint64_t sweep = 8 * (g.n + 1) + g.m * 4 + g.m * 8 + 2 * g.n * 8;
+  c.add(4, 12 * g.n + 2 * sweep + 12 * g.n);
+}
+
+}  // namespace ccg

@@ -1,0 +1,329 @@
+// prop.cu - label propagation, shortcut (pointer-jumping) propagation, label
+// composition and canonicalisation.
+#include "kernels.h"
+
+namespace ccg {
+namespace {
+
+constexpr uint64_t kRowLimit = 64;
+
+__global__ void k_rows_over(uint64_t n, const uint64_t *__restrict__ rp, uint64_t limit,
+                            uint32_t *__restrict__ rows, unsigned int *__restrict__ nr) {
+  for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < n;
+       v += (uint64_t)gridDim.x * blockDim.x)
+    if (rp[v + 1] - rp[v] > limit) rows[atomicAdd(nr, 1u)] = (uint32_t)v;
+}
+
+// ---- Propagation (propagation.h:72-149) ------------------------------------
+// lab[v] <- min(lab[v], min_u lab[u]) in place.  The reference updates local
+// vertices in place during a sweep (SetVertexPayload) and sees ghosts from
+// the last exchange; on one device every vertex is local.
+__global__ void k_labels_round(uint64_t n, const uint64_t *__restrict__ rp,
+                               const uint32_t *__restrict__ col, uint32_t *lab, int *flag) {
+  int changed = 0;
+  for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < n;
+       v += (uint64_t)gridDim.x * blockDim.x) {
+    uint64_t b = __ldg(rp + v), e = __ldg(rp + v + 1);
+    if (e - b > kRowLimit) continue;
+    uint32_t l = ld_cg(lab + v), best = l;
+    for (uint64_t j = b; j < e; ++j) {
+      uint32_t x = ld_cg(lab + __ldg(col + j));
+      best = x < best ? x : best;
+    }
+    if (best < l) {
+      st_cg(lab + v, best);
+      changed = 1;
+    }
+  }
+  warp_flag(changed, flag);
+}
+
+__global__ void k_labels_round_rows(const uint64_t *__restrict__ rp, const uint32_t *__restrict__ col,
+                                    const uint32_t *__restrict__ rows,
+                                    const unsigned int *__restrict__ nr, uint32_t *lab, int *flag) {
+  const unsigned lane = threadIdx.x & 31;
+  const uint64_t warp = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
+  const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+  const uint32_t cnt = *nr;
+  int changed = 0;
+  for (uint64_t h = warp; h < cnt; h += nwarps) {
+    uint32_t v = rows[h];
+    uint64_t b = __ldg(rp + v), e = __ldg(rp + v + 1);
+    uint32_t best = kNone;
+    for (uint64_t j = b + lane; j < e; j += 32) {
+      uint32_t x = ld_cg(lab + __ldg(col + j));
+      best = x < best ? x : best;
+    }
+    best = __reduce_min_sync(0xffffffffu, best);
+    if (lane == 0 && best < ld_cg(lab + v)) {
+      atomicMin(lab + v, best);
+      changed = 1;
+    }
+  }
+  warp_flag(changed, flag);
+}
+
+// ---- ShortcutPropagation (shortcut_propagation.h:124-376) ------------------
+// Round, with f = current labels (g labels) and nf = labels_:
+//   FindMinLabels (:194-208):  nf[v] = min over N[v] of f
+//   Shortcut      (:225-357):  an update (f[v] -> nf[v]) for every v whose
+//                              label drops; a request for f[nf[v]]; both
+//                              answers are applied to every u with nf[u]
+//                              equal to the target
+//   CheckConvergence (:359-376): stop when nf == f everywhere.
+__global__ void k_sc_min(uint64_t n, const uint64_t *__restrict__ rp,
+                         const uint32_t *__restrict__ col, const uint32_t *__restrict__ f,
+                         uint32_t *__restrict__ nf, uint32_t *__restrict__ upd) {
+  for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < n;
+       v += (uint64_t)gridDim.x * blockDim.x) {
+    uint64_t b = __ldg(rp + v), e = __ldg(rp + v + 1);
+    if (e - b > kRowLimit) continue;
+    uint32_t l = f[v], best = l;
+    for (uint64_t j = b; j < e; ++j) {
+      uint32_t x = __ldg(f + __ldg(col + j));
+      best = x < best ? x : best;
+    }
+    nf[v] = best;
+    if (best < l) atomicMin(upd + l, best);
+  }
+}
+
+__global__ void k_sc_min_rows(const uint64_t *__restrict__ rp, const uint32_t *__restrict__ col,
+                              const uint32_t *__restrict__ rows, const unsigned int *__restrict__ nr,
+                              const uint32_t *__restrict__ f, uint32_t *__restrict__ nf,
+                              uint32_t *__restrict__ upd) {
+  const unsigned lane = threadIdx.x & 31;
+  const uint64_t warp = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
+  const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+  const uint32_t cnt = *nr;
+  for (uint64_t h = warp; h < cnt; h += nwarps) {
+    uint32_t v = rows[h];
+    uint64_t b = __ldg(rp + v), e = __ldg(rp + v + 1);
+    uint32_t best = kNone;
+    for (uint64_t j = b + lane; j < e; j += 32) {
+      uint32_t x = __ldg(f + __ldg(col + j));
+      best = x < best ? x : best;
+    }
+    best = __reduce_min_sync(0xffffffffu, best);
+    if (lane == 0) {
+      uint32_t l = f[v];
+      best = best < l ? best : l;
+      nf[v] = best;
+      if (best < l) atomicMin(upd + l, best);
+    }
+  }
+}
+
+// Heavy hitters (:210-223): labels held by more than n_part/h vertices.  The
+// set is sticky across rounds as in the reference (heavy_hitters_ is never
+// cleared).
+__global__ void k_sc_count(uint64_t n, const uint32_t *__restrict__ nf, uint32_t *__restrict__ cnt) {
+  for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < n;
+       v += (uint64_t)gridDim.x * blockDim.x)
+    atomicAdd(cnt + nf[v], 1u);
+}
+__global__ void k_sc_heavy(uint64_t n, const uint32_t *__restrict__ cnt, uint32_t thresh,
+                           uint8_t *__restrict__ heavy) {
+  for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < n;
+       v += (uint64_t)gridDim.x * blockDim.x)
+    if (cnt[v] > thresh) heavy[v] = 1;
+}
+
+__global__ void k_sc_jump(uint64_t n, const uint32_t *__restrict__ f, uint32_t *__restrict__ nf,
+                          const uint32_t *__restrict__ upd, const uint8_t *__restrict__ heavy,
+                          int *flag) {
+  int changed = 0;
+  for (uint64_t u = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; u < n;
+       u += (uint64_t)gridDim.x * blockDim.x) {
+    uint32_t t = nf[u];
+    uint32_t r = t;
+    if (!heavy || heavy[t]) {
+      uint32_t a = f[t];  // request l(l'(u)) answered by the owner of l'(u)
+      r = a < r ? a : r;
+    }
+    uint32_t up = upd[t];  // update messages addressed to target t
+    r = up < r ? up : r;
+    nf[u] = r;
+    changed |= (r != f[u]);
+  }
+  warp_flag(changed, flag);
+}
+
+// ---- composition / canonicalisation -----------------------------------------
+__global__ void k_compose(uint64_t n, const uint32_t *__restrict__ cl,
+                          const uint32_t *__restrict__ newid, const uint32_t *__restrict__ next,
+                          const uint32_t *__restrict__ rep, uint32_t *__restrict__ out) {
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n;
+       i += (uint64_t)gridDim.x * blockDim.x) {
+    uint32_t c = cl[i];
+    uint32_t id = newid[c];
+    out[i] = id != kNone ? next[id] : (rep ? rep[c] : c);
+  }
+}
+
+__global__ void k_canon_min(uint64_t n, const uint32_t *__restrict__ lab, uint32_t *__restrict__ mn) {
+  for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < n;
+       v += (uint64_t)gridDim.x * blockDim.x) {
+    uint32_t l = lab[v];
+    if ((uint32_t)v < ld_cg(mn + l)) atomicMin(mn + l, (uint32_t)v);
+  }
+}
+__global__ void k_canon_apply(uint64_t n, uint32_t *__restrict__ lab, const uint32_t *__restrict__ mn) {
+  for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < n;
+       v += (uint64_t)gridDim.x * blockDim.x)
+    lab[v] = mn[lab[v]];
+}
+__global__ void k_count_roots(uint64_t n, const uint32_t *__restrict__ lab,
+                              unsigned long long *__restrict__ cnt) {
+  unsigned long long c = 0;
+  for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < n;
+       v += (uint64_t)gridDim.x * blockDim.x)
+    c += (lab[v] == (uint32_t)v);
+  for (int o = 16; o; o >>= 1) c += __shfl_xor_sync(__activemask(), c, o);
+  if ((threadIdx.x & 31) == 0 && c) atomicAdd(cnt, c);
+}
+__global__ void k_gather(uint64_t n, const uint32_t *__restrict__ src, const uint32_t *__restrict__ idx,
+                         uint32_t *__restrict__ out) {
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n;
+       i += (uint64_t)gridDim.x * blockDim.x)
+    out[i] = src[idx[i]];
+}
+__global__ void k_iota(uint64_t n, uint32_t *__restrict__ out) {
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n;
+       i += (uint64_t)gridDim.x * blockDim.x)
+    out[i] = (uint32_t)i;
+}
+
+}  // namespace
+
+int labels_propagate(const Csr &g, uint32_t *lab, int max_rounds, cudaStream_t s,
+                     cudaMemPool_t pool, Counters &c, volatile int *host_flag, int *dev_flag) {
+  if (g.n == 0) return 0;
+  const uint32_t *col = static_cast<const uint32_t *>(g.col);
+  unsigned grid = grid_for(g.n, kBlock, kSMs * 32);
+  DevBuf rows(4 * (g.m / (kRowLimit + 1) + 1), s, pool), nr(4, s, pool);
+  CCG_CUDA(cudaMemsetAsync(nr.p, 0, 4, s));
+  k_rows_over<<<grid, kBlock, 0, s>>>(g.n, g.rp, kRowLimit, rows.as<uint32_t>(),
+                                      nr.as<unsigned int>());
+  CCG_LAUNCH_CHECK();
+  int rounds = 0;
+  const uint64_t round_bytes = 8 * (g.n + 1) + g.m * 4 + g.m * 4 + 2 * g.n * 4;
+  for (;;) {
+    if (rounds >= max_rounds) return -1;
+    CCG_CUDA(cudaMemsetAsync(dev_flag, 0, sizeof(int), s));
+    cudaEvent_t t0 = c.tic(s);
+    k_labels_round<<<grid, kBlock, 0, s>>>(g.n, g.rp, col, lab, dev_flag);
+    CCG_LAUNCH_CHECK();
+    k_labels_round_rows<<<kSMs * 4, kBlock, 0, s>>>(g.rp, col, rows.as<uint32_t>(),
+                                                    nr.as<unsigned int>(), lab, dev_flag);
+    CCG_LAUNCH_CHECK();
+    c.toc(s, "labels_round", t0, round_bytes);
+    CCG_CUDA(cudaMemcpyAsync((void *)host_flag, dev_flag, sizeof(int), cudaMemcpyDeviceToHost, s));
+    CCG_CUDA(cudaStreamSynchronize(s));
+    ++rounds;
+    c.add(2, round_bytes);
+    if (*host_flag == 0) break;
+  }
+  return rounds;
+}
+
+int shortcut_propagate(const Csr &g, uint32_t *lab, uint32_t hitters, int max_rounds,
+                       cudaStream_t s, cudaMemPool_t pool, Counters &c, volatile int *host_flag,
+                       int *dev_flag) {
+  if (g.n == 0) return 0;
+  const uint32_t *col = static_cast<const uint32_t *>(g.col);
+  unsigned grid = grid_for(g.n, kBlock, kSMs * 32);
+  DevBuf nfb(4 * g.n, s, pool), updb(4 * g.n, s, pool);
+  DevBuf rows(4 * (g.m / (kRowLimit + 1) + 1), s, pool), nr(4, s, pool);
+  DevBuf cnt, heavy;
+  if (hitters) {
+    cnt.alloc(4 * g.n, s, pool);
+    heavy.alloc(g.n, s, pool);
+    CCG_CUDA(cudaMemsetAsync(heavy.p, 0, g.n, s));
+  }
+  CCG_CUDA(cudaMemsetAsync(nr.p, 0, 4, s));
+  k_rows_over<<<grid, kBlock, 0, s>>>(g.n, g.rp, kRowLimit, rows.as<uint32_t>(),
+                                      nr.as<unsigned int>());
+  CCG_LAUNCH_CHECK();
+  uint32_t *f = lab, *nf = nfb.as<uint32_t>();
+  int rounds = 0;
+  for (;;) {
+    if (rounds >= max_rounds) return -1;
+    CCG_CUDA(cudaMemsetAsync(updb.p, 0xff, 4 * g.n, s));
+    k_sc_min<<<grid, kBlock, 0, s>>>(g.n, g.rp, col, f, nf, updb.as<uint32_t>());
+    CCG_LAUNCH_CHECK();
+    k_sc_min_rows<<<kSMs * 4, kBlock, 0, s>>>(g.rp, col, rows.as<uint32_t>(), nr.as<unsigned int>(),
+                                              f, nf, updb.as<uint32_t>());
+    CCG_LAUNCH_CHECK();
+    if (hitters) {
+      CCG_CUDA(cudaMemsetAsync(cnt.p, 0, 4 * g.n, s));
+      k_sc_count<<<grid, kBlock, 0, s>>>(g.n, nf, cnt.as<uint32_t>());
+      CCG_LAUNCH_CHECK();
+      k_sc_heavy<<<grid, kBlock, 0, s>>>(g.n, cnt.as<uint32_t>(), (uint32_t)(g.n / hitters),
+                                         heavy.as<uint8_t>());
+      CCG_LAUNCH_CHECK();
+      c.add(2, 12 * g.n);
+    }
+    CCG_CUDA(cudaMemsetAsync(dev_flag, 0, sizeof(int), s));
+    k_sc_jump<<<grid, kBlock, 0, s>>>(g.n, f, nf, updb.as<uint32_t>(),
+                                      hitters ? heavy.as<uint8_t>() : nullptr, dev_flag);
+    CCG_LAUNCH_CHECK();
+    CCG_CUDA(cudaMemcpyAsync((void *)host_flag, dev_flag, sizeof(int), cudaMemcpyDeviceToHost, s));
+    CCG_CUDA(cudaStreamSynchronize(s));
+    ++rounds;
+    // min sweep (offsets, ids, one label gather per edge, own r/w) + jump
+    // (own label, two gathers, write)
+    c.add(3, 8 * (g.n + 1) + g.m * 4 + g.m * 4 + 2 * g.n * 4 + 4 * g.n * 4 + 4 * g.n);
+    uint32_t *t = f;
+    f = nf;
+    nf = t;
+    if (*host_flag == 0) break;
+  }
+  if (f != lab) CCG_CUDA(cudaMemcpyAsync(lab, f, 4 * g.n, cudaMemcpyDeviceToDevice, s));
+  return rounds;
+}
+
+void compose_labels(const uint32_t *cl, const uint32_t *newid, const uint32_t *next,
+                    const uint32_t *rep, uint32_t *out, uint64_t n, cudaStream_t s, Counters &c) {
+  if (n == 0) return;
+  k_compose<<<grid_for(n, kBlock, kSMs * 32), kBlock, 0, s>>>(n, cl, newid, next, rep, out);
+  CCG_LAUNCH_CHECK();
+  c.add(1, 16 * n);
+}
+
+void canonicalize(uint32_t *lab, uint32_t *scratch, uint64_t n, cudaStream_t s, Counters &c) {
+  if (n == 0) return;
+  CCG_CUDA(cudaMemsetAsync(scratch, 0xff, 4 * n, s));
+  unsigned grid = grid_for(n, kBlock, kSMs * 32);
+  k_canon_min<<<grid, kBlock, 0, s>>>(n, lab, scratch);
+  CCG_LAUNCH_CHECK();
+  k_canon_apply<<<grid, kBlock, 0, s>>>(n, lab, scratch);
+  CCG_LAUNCH_CHECK();
+  c.add(2, 4 * n * 4);
+}
+
+void count_roots(const uint32_t *lab, uint64_t n, unsigned long long *d_count, cudaStream_t s,
+                 Counters &c) {
+  CCG_CUDA(cudaMemsetAsync(d_count, 0, 8, s));
+  if (n == 0) return;
+  k_count_roots<<<grid_for(n, kBlock, kSMs * 8), kBlock, 0, s>>>(n, lab, d_count);
+  CCG_LAUNCH_CHECK();
+  c.add(1, 4 * n);
+}
+
+void gather_u32(const uint32_t *src, const uint32_t *idx, uint32_t *out, uint64_t n,
+                cudaStream_t s, Counters &c) {
+  if (n == 0) return;
+  k_gather<<<grid_for(n, kBlock, kSMs * 32), kBlock, 0, s>>>(n, src, idx, out);
+  CCG_LAUNCH_CHECK();
+  c.add(1, 12 * n);
+}
+
+void iota_u32(uint32_t *out, uint64_t n, cudaStream_t s, Counters &c) {
+  if (n == 0) return;
+  k_iota<<<grid_for(n, kBlock, kSMs * 32), kBlock, 0, s>>>(n, out);
+  CCG_LAUNCH_CHECK();
+  c.add(1, 4 * n);
+}
+
+}  // namespace ccg

@@ -1,0 +1,491 @@
+// sortcsr.cu - prefix scans, a stable LSD radix sort of packed 64-bit edge keys,
+// and the quotient-graph (contraction) build.
+//
+// The reference builds contracted graphs with hash sets and message rounds:
+//   CAGBuilder::PerformLocalContraction   cag_builder.h:160-230 (unordered_set<HashedEdge>)
+//   CAGBuilder::BuildLocalContractionGraph cag_builder.h:577-667 (+ ips4o sort :669-674)
+//   DynamicContraction::FindExponentialConflictingEdges dynamic_contraction.h:251-290
+//   DynamicContraction::InsertAndClearEdges            dynamic_contraction.h:513-559
+// On one device the same quotient graph is: relabel every edge by its cluster
+// ids, keep the ones whose ids differ, pack (cu, cw) into one 64-bit key,
+// radix-sort, drop adjacent duplicates and rebuild the CSR.  The undirected
+// dedup key of the reference (edge_hash.h:30-42, min*n+max) becomes the
+// ordered pair key: both directions are kept, as the reference inserts both.
+#include "kernels.h"
+
+namespace ccg {
+namespace {
+
+constexpr int kScanItems = 8;
+constexpr int kScanTile = kBlock * kScanItems;  // 2048 elements per block
+
+__device__ __forceinline__ unsigned lane_id() { return threadIdx.x & 31; }
+
+// Exclusive block scan of one value per thread (blockDim == 256).
+template <class T>
+__device__ __forceinline__ T block_excl_scan(T x, T *sw, T &total) {
+  const unsigned lane = lane_id(), w = threadIdx.x >> 5;
+  T inc = x;
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    T y = __shfl_up_sync(0xffffffffu, inc, d);
+    if (lane >= (unsigned)d) inc += y;
+  }
+  if (lane == 31) sw[w] = inc;
+  __syncthreads();
+  if (w == 0) {
+    T s = lane < 8 ? sw[lane] : T(0);
+#pragma unroll
+    for (int d = 1; d < 8; d <<= 1) {
+      T y = __shfl_up_sync(0xffffffffu, s, d);
+      if (lane >= (unsigned)d) s += y;
+    }
+    if (lane < 8) sw[lane] = s;
+  }
+  __syncthreads();
+  T woff = w ? sw[w - 1] : T(0);
+  total = sw[7];
+  __syncthreads();
+  return woff + inc - x;
+}
+
+// ---- generic 3-phase exclusive scan over a predicate / value functor -------
+// Phase 1: per-tile sums.  Phase 2: scan of tile sums (recursive).  Phase 3:
+// per-tile scan plus tile offset, handed to a writer functor.
+
+template <class Get>
+__global__ void k_tile_sum(uint64_t n, Get get, uint32_t *__restrict__ tile_sums) {
+  __shared__ uint32_t sw[8];
+  uint64_t base = (uint64_t)blockIdx.x * kScanTile + threadIdx.x * kScanItems;
+  uint32_t s = 0;
+#pragma unroll
+  for (int i = 0; i < kScanItems; ++i)
+    if (base + i < n) s += get(base + i);
+  uint32_t total;
+  block_excl_scan<uint32_t>(s, sw, total);
+  if (threadIdx.x == 0) tile_sums[blockIdx.x] = total;
+}
+
+template <class Get, class Put>
+__global__ void k_tile_scan(uint64_t n, Get get, Put put, const uint32_t *__restrict__ tile_offs) {
+  __shared__ uint32_t sw[8];
+  uint64_t base = (uint64_t)blockIdx.x * kScanTile + threadIdx.x * kScanItems;
+  uint32_t vals[kScanItems];
+  uint32_t s = 0;
+#pragma unroll
+  for (int i = 0; i < kScanItems; ++i) {
+    vals[i] = (base + i < n) ? get(base + i) : 0u;
+    s += vals[i];
+  }
+  uint32_t total;
+  uint32_t run = block_excl_scan<uint32_t>(s, sw, total) + tile_offs[blockIdx.x];
+#pragma unroll
+  for (int i = 0; i < kScanItems; ++i) {
+    if (base + i < n) put(base + i, run, vals[i]);
+    run += vals[i];
+  }
+}
+
+struct GetArr {
+  const uint32_t *a;
+  __device__ uint32_t operator()(uint64_t i) const { return a[i]; }
+};
+struct PutArr {
+  uint32_t *o;
+  __device__ void operator()(uint64_t i, uint32_t excl, uint32_t) const { o[i] = excl; }
+};
+
+// In-place capable exclusive scan of uint32 -> uint32; *d_total (if given)
+// receives the sum.
+template <class Get, class Put>
+void scan_generic(uint64_t n, Get get, Put put, uint32_t *d_total, cudaStream_t s,
+                  cudaMemPool_t pool, Counters &c);
+
+__global__ void k_set_total(const uint32_t *tile_offs, const uint32_t *tile_sums, uint64_t nt,
+                            uint32_t *d_total) {
+  *d_total = tile_offs[nt - 1] + tile_sums[nt - 1];
+}
+
+template <class Get, class Put>
+void scan_generic(uint64_t n, Get get, Put put, uint32_t *d_total, cudaStream_t s,
+                  cudaMemPool_t pool, Counters &c) {
+  if (n == 0) {
+    if (d_total) CCG_CUDA(cudaMemsetAsync(d_total, 0, 4, s));
+    return;
+  }
+  uint64_t nt = (n + kScanTile - 1) / kScanTile;
+  DevBuf sums(4 * nt, s, pool), offs(4 * nt, s, pool);
+  k_tile_sum<<<(unsigned)nt, kBlock, 0, s>>>(n, get, sums.as<uint32_t>());
+  CCG_LAUNCH_CHECK();
+  if (nt == 1) {
+    CCG_CUDA(cudaMemsetAsync(offs.p, 0, 4, s));
+  } else {
+    scan_generic(nt, GetArr{sums.as<uint32_t>()}, PutArr{offs.as<uint32_t>()}, nullptr, s, pool, c);
+  }
+  k_tile_scan<<<(unsigned)nt, kBlock, 0, s>>>(n, get, put, offs.as<uint32_t>());
+  CCG_LAUNCH_CHECK();
+  if (d_total) {
+    k_set_total<<<1, 1, 0, s>>>(offs.as<uint32_t>(), sums.as<uint32_t>(), nt, d_total);
+    CCG_LAUNCH_CHECK();
+  }
+  c.add(3, 0);
+}
+
+// ---- radix sort --------------------------------------------------------------
+constexpr int kRadixBits = 8;
+constexpr int kRadix = 1 << kRadixBits;
+constexpr int kSortItems = 16;
+constexpr int kSortWarps = kBlock / 32;
+constexpr int kSortTile = kBlock * kSortItems;  // 4096 keys per block
+
+// counts[d * ntiles + tile] = keys of this tile with digit d
+__global__ void k_radix_hist(const uint64_t *__restrict__ keys, uint64_t n, int shift,
+                             uint32_t ntiles, uint32_t *__restrict__ counts) {
+  __shared__ uint32_t h[kSortWarps][kRadix];
+  for (int i = threadIdx.x; i < kSortWarps * kRadix; i += blockDim.x) (&h[0][0])[i] = 0;
+  __syncthreads();
+  const unsigned w = threadIdx.x >> 5, lane = lane_id();
+  uint64_t base = (uint64_t)blockIdx.x * kSortTile + (uint64_t)w * 32 * kSortItems;
+#pragma unroll 4
+  for (int i = 0; i < kSortItems; ++i) {
+    uint64_t idx = base + (uint64_t)i * 32 + lane;
+    if (idx < n) atomicAdd(&h[w][(keys[idx] >> shift) & (kRadix - 1)], 1u);
+  }
+  __syncthreads();
+  for (int d = threadIdx.x; d < kRadix; d += blockDim.x) {
+    uint32_t t = 0;
+#pragma unroll
+    for (int k = 0; k < kSortWarps; ++k) t += h[k][d];
+    counts[(uint64_t)d * ntiles + blockIdx.x] = t;
+  }
+}
+
+// Stable scatter: warps own contiguous sub-tiles, lanes take consecutive keys,
+// ranks inside a step come from __match_any_sync, so input order is kept for
+// equal digits.
+__global__ void k_radix_scatter(const uint64_t *__restrict__ keys, uint64_t *__restrict__ out,
+                                uint64_t n, int shift, uint32_t ntiles,
+                                const uint32_t *__restrict__ offs) {
+  __shared__ uint32_t wc[kSortWarps][kRadix];
+  __shared__ uint32_t gbase[kRadix];
+  for (int i = threadIdx.x; i < kSortWarps * kRadix; i += blockDim.x) (&wc[0][0])[i] = 0;
+  for (int d = threadIdx.x; d < kRadix; d += blockDim.x)
+    gbase[d] = offs[(uint64_t)d * ntiles + blockIdx.x];
+  __syncthreads();
+  const unsigned w = threadIdx.x >> 5, lane = lane_id();
+  const unsigned lt = (1u << lane) - 1u;
+  uint64_t base = (uint64_t)blockIdx.x * kSortTile + (uint64_t)w * 32 * kSortItems;
+  uint64_t k[kSortItems];
+  uint32_t rk[kSortItems];
+#pragma unroll
+  for (int i = 0; i < kSortItems; ++i) {
+    uint64_t idx = base + (uint64_t)i * 32 + lane;
+    bool valid = idx < n;
+    k[i] = valid ? keys[idx] : 0ull;
+    uint32_t d = valid ? (uint32_t)((k[i] >> shift) & (kRadix - 1)) : 0xffffu;
+    unsigned peers = __match_any_sync(0xffffffffu, d);
+    uint32_t before = __popc(peers & lt);
+    uint32_t basecnt = (d < kRadix) ? wc[w][d] : 0u;
+    __syncwarp();
+    if (d < kRadix && before == 0) wc[w][d] = basecnt + __popc(peers);
+    __syncwarp();
+    rk[i] = (d < kRadix) ? basecnt + before : 0xffffffffu;
+  }
+  __syncthreads();
+  for (int d = threadIdx.x; d < kRadix; d += blockDim.x) {
+    uint32_t run = 0;
+#pragma unroll
+    for (int q = 0; q < kSortWarps; ++q) {
+      uint32_t t = wc[q][d];
+      wc[q][d] = run;
+      run += t;
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int i = 0; i < kSortItems; ++i) {
+    if (rk[i] != 0xffffffffu) {
+      uint32_t d = (uint32_t)((k[i] >> shift) & (kRadix - 1));
+      out[gbase[d] + wc[w][d] + rk[i]] = k[i];
+    }
+  }
+}
+
+// ---- contraction -----------------------------------------------------------
+
+__device__ __forceinline__ bool edge_crosses(const PartMap &pm, bool part, uint32_t v, uint32_t w) {
+  return !part || pm.part(v) != pm.part(w);
+}
+
+// Emit key (cl[v] << b) | cl[w] for every kept edge; positions from one
+// warp-aggregated atomicAdd per warp step (the key order does not matter, the
+// sort follows).
+template <class T>
+__global__ void k_emit(uint64_t n, const uint64_t *__restrict__ rp, const T *__restrict__ col,
+                       const uint32_t *__restrict__ cl, PartMap pm, bool part, int b,
+                       uint64_t hub_limit, uint64_t *__restrict__ keys,
+                       unsigned long long *__restrict__ cnt) {
+  const unsigned lane = lane_id();
+  const uint64_t warp = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
+  const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+  // one warp per 32 consecutive vertices; the warp walks their edges jointly.
+  // Rows longer than hub_limit are left to k_emit_hubs.
+  for (uint64_t v0 = warp * 32; v0 < n; v0 += nwarps * 32) {
+    uint64_t v = v0 + lane;
+    uint64_t eb = 0, ee = 0;
+    uint32_t cv = 0;
+    if (v < n) {
+      eb = __ldg(rp + v);
+      ee = __ldg(rp + v + 1);
+      cv = cl[v];
+    }
+    uint64_t deg = ee - eb;
+    if (deg > hub_limit) deg = 0;
+    // maximum degree in this warp bounds the steps
+    uint64_t maxdeg = deg;
+#pragma unroll
+    for (int o = 16; o; o >>= 1) {
+      uint64_t y = __shfl_xor_sync(0xffffffffu, maxdeg, o);
+      maxdeg = y > maxdeg ? y : maxdeg;
+    }
+    for (uint64_t j = 0; j < maxdeg; ++j) {
+      bool keep = false;
+      uint64_t key = 0;
+      if (j < deg) {
+        uint32_t u = load_id(col, eb + j);
+        uint32_t cu = cl[u];
+        keep = cu != cv && edge_crosses(pm, part, (uint32_t)v, u);
+        key = ((uint64_t)cv << b) | cu;
+      }
+      unsigned m = __ballot_sync(0xffffffffu, keep);
+      if (m) {
+        unsigned long long pos0 = 0;
+        if (lane == 0) pos0 = atomicAdd(cnt, (unsigned long long)__popc(m));
+        pos0 = __shfl_sync(0xffffffffu, pos0, 0);
+        if (keep) keys[pos0 + __popc(m & ((1u << lane) - 1u))] = key;
+      }
+    }
+  }
+}
+
+// One warp per hub row (rows longer than the k_emit limit).
+template <class T>
+__global__ void k_emit_hubs(const uint64_t *__restrict__ rp, const T *__restrict__ col,
+                            const uint32_t *__restrict__ cl, PartMap pm, bool part, int b,
+                            const uint32_t *__restrict__ hubs,
+                            const unsigned int *__restrict__ d_nhubs,
+                            uint64_t *__restrict__ keys, unsigned long long *__restrict__ cnt) {
+  const unsigned lane = lane_id();
+  const uint64_t warp = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
+  const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+  const uint32_t nhubs = *d_nhubs;
+  for (uint64_t h = warp; h < nhubs; h += nwarps) {
+    uint32_t v = hubs[h];
+    uint64_t eb = __ldg(rp + v), ee = __ldg(rp + v + 1);
+    uint32_t cv = cl[v];
+    for (uint64_t e0 = eb; e0 < ee; e0 += 32) {
+      uint64_t e = e0 + lane;
+      bool keep = false;
+      uint64_t key = 0;
+      if (e < ee) {
+        uint32_t u = load_id(col, e);
+        uint32_t cu = cl[u];
+        keep = cu != cv && edge_crosses(pm, part, v, u);
+        key = ((uint64_t)cv << b) | cu;
+      }
+      unsigned m = __ballot_sync(0xffffffffu, keep);
+      if (m) {
+        unsigned long long pos0 = 0;
+        if (lane == 0) pos0 = atomicAdd(cnt, (unsigned long long)__popc(m));
+        pos0 = __shfl_sync(0xffffffffu, pos0, 0);
+        if (keep) keys[pos0 + __popc(m & ((1u << lane) - 1u))] = key;
+      }
+    }
+  }
+}
+
+// Rows longer than `limit` (hubs) are listed for the warp-per-row kernel.
+__global__ void k_list_hubs(uint64_t n, const uint64_t *__restrict__ rp, uint64_t limit,
+                            uint32_t *__restrict__ hubs, unsigned int *__restrict__ nh) {
+  for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < n;
+       v += (uint64_t)gridDim.x * blockDim.x) {
+    if (rp[v + 1] - rp[v] > limit) hubs[atomicAdd(nh, 1u)] = (uint32_t)v;
+  }
+}
+
+struct GetUniq {
+  const uint64_t *k;
+  __device__ uint32_t operator()(uint64_t i) const { return (i == 0 || k[i] != k[i - 1]) ? 1u : 0u; }
+};
+struct PutUniq {
+  const uint64_t *k;
+  uint64_t *o;
+  __device__ void operator()(uint64_t i, uint32_t excl, uint32_t f) const {
+    if (f) o[excl] = k[i];
+  }
+};
+struct GetFlag {
+  const uint32_t *f;
+  __device__ uint32_t operator()(uint64_t i) const { return f[i] ? 1u : 0u; }
+};
+struct PutNewId {
+  uint32_t *o;  // may alias the flag array: each index is read then written once
+  __device__ void operator()(uint64_t i, uint32_t excl, uint32_t f) const {
+    o[i] = f ? excl : kNone;
+  }
+};
+
+__global__ void k_mark_src(const uint64_t *__restrict__ uk, const uint32_t *__restrict__ d_u,
+                           int b, uint32_t *__restrict__ flag) {
+  uint32_t u = *d_u;
+  for (uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; e < u;
+       e += (uint64_t)gridDim.x * blockDim.x)
+    flag[uk[e] >> b] = 1u;
+}
+
+__global__ void k_build_csr(const uint64_t *__restrict__ uk, const uint32_t *__restrict__ d_u,
+                            int b, const uint32_t *__restrict__ newid, uint64_t *__restrict__ rp,
+                            uint32_t *__restrict__ col, const uint32_t *__restrict__ d_nv) {
+  uint32_t u = *d_u;
+  const uint64_t mask = (b == 64) ? ~0ull : ((1ull << b) - 1);
+  for (uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; e < u;
+       e += (uint64_t)gridDim.x * blockDim.x) {
+    uint64_t key = uk[e];
+    uint32_t s = (uint32_t)(key >> b);
+    if (e == 0 || (uint32_t)(uk[e - 1] >> b) != s) rp[newid[s]] = e;
+    col[e] = newid[(uint32_t)(key & mask)];
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) rp[*d_nv] = u;
+}
+
+__global__ void k_vid(uint64_t ncl, const uint32_t *__restrict__ newid,
+                      const uint32_t *__restrict__ vid_of_cluster, uint32_t *__restrict__ vid) {
+  for (uint64_t c = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; c < ncl;
+       c += (uint64_t)gridDim.x * blockDim.x) {
+    uint32_t id = newid[c];
+    if (id != kNone) vid[id] = vid_of_cluster ? vid_of_cluster[c] : (uint32_t)c;
+  }
+}
+
+int bits_for(uint64_t x) {  // bits needed to hold values < x
+  int b = 1;
+  while (b < 64 && (1ull << b) < x) ++b;
+  return b;
+}
+
+template <class T>
+void emit_keys(const Csr &g, const uint32_t *cl, const PartMap &pm, bool part, int b,
+               uint64_t *keys, unsigned long long *cnt, cudaStream_t s, cudaMemPool_t pool,
+               Counters &c) {
+  const T *col = static_cast<const T *>(g.col);
+  // k_emit walks up to max-degree steps per warp; rows above hub_limit go to
+  // the warp-per-row kernel so that one hub does not serialise 31 lanes.
+  const uint64_t hub_limit = 128;
+  DevBuf hubs(4 * (g.m / (hub_limit + 1) + 1), s, pool), nh(4, s, pool);
+  CCG_CUDA(cudaMemsetAsync(nh.p, 0, 4, s));
+  unsigned grid = grid_for(g.n, kBlock, kSMs * 32);
+  k_list_hubs<<<grid, kBlock, 0, s>>>(g.n, g.rp, hub_limit, hubs.as<uint32_t>(),
+                                      nh.as<unsigned int>());
+  CCG_LAUNCH_CHECK();
+  k_emit<T><<<grid, kBlock, 0, s>>>(g.n, g.rp, col, cl, pm, part, b, hub_limit, keys, cnt);
+  CCG_LAUNCH_CHECK();
+  k_emit_hubs<T><<<kSMs * 8, kBlock, 0, s>>>(g.rp, col, cl, pm, part, b, hubs.as<uint32_t>(),
+                                             nh.as<unsigned int>(), keys, cnt);
+  CCG_LAUNCH_CHECK();
+  // relabel + compact: offsets, neighbour id and its cluster per edge, own
+  // cluster per vertex (the emitted keys are counted at the sort)
+  c.add(3, 8 * (g.n + 1) + g.m * ((uint64_t)g.idb + 4) + 4 * g.n);
+}
+
+}  // namespace
+
+uint64_t *radix_sort_u64(uint64_t *keys, uint64_t *tmp, uint64_t n, int bits, cudaStream_t s,
+                         cudaMemPool_t pool, Counters &c) {
+  if (n <= 1) return keys;
+  if (n >= (1ull << 32)) throw Error(CC_ERR_UNSUPPORTED, "radix sort: more than 2^32 keys");
+  uint32_t ntiles = (uint32_t)((n + kSortTile - 1) / kSortTile);
+  DevBuf counts(4ull * kRadix * ntiles, s, pool);
+  uint64_t *src = keys, *dst = tmp;
+  for (int shift = 0; shift < bits; shift += kRadixBits) {
+    k_radix_hist<<<ntiles, kBlock, 0, s>>>(src, n, shift, ntiles, counts.as<uint32_t>());
+    CCG_LAUNCH_CHECK();
+    scan_generic((uint64_t)kRadix * ntiles, GetArr{counts.as<uint32_t>()},
+                 PutArr{counts.as<uint32_t>()}, nullptr, s, pool, c);
+    k_radix_scatter<<<ntiles, kBlock, 0, s>>>(src, dst, n, shift, ntiles, counts.as<uint32_t>());
+    CCG_LAUNCH_CHECK();
+    c.add(2, 8 * n * 3);  // hist read + scatter read + write
+    uint64_t *t = src;
+    src = dst;
+    dst = t;
+  }
+  return src;
+}
+
+void contract_graph(const Csr &g, const uint32_t *cl, uint64_t ncl,
+                    const uint32_t *vid_of_cluster, const PartMap *pm, Contracted &out,
+                    cudaStream_t s, cudaMemPool_t pool, Counters &c, uint32_t *host_mailbox) {
+  out = Contracted();
+  out.newid.alloc(4 * (ncl ? ncl : 1), s, pool);
+  if (g.m == 0 || g.n == 0) {
+    CCG_CUDA(cudaMemsetAsync(out.newid.p, 0xff, 4 * ncl, s));
+    out.rp.alloc(8, s, pool);
+    CCG_CUDA(cudaMemsetAsync(out.rp.p, 0, 8, s));
+    return;
+  }
+  if (ncl >= (1ull << 32) - 1) throw Error(CC_ERR_UNSUPPORTED, "contract: too many clusters");
+  const int b = bits_for(ncl);
+  PartMap p = pm ? *pm : PartMap(g.n, 1);
+  DevBuf keys(8 * g.m, s, pool);
+  DevBuf cnt(8, s, pool);
+  CCG_CUDA(cudaMemsetAsync(cnt.p, 0, 8, s));
+  if (g.idb == 8)
+    emit_keys<uint64_t>(g, cl, p, pm != nullptr, b, keys.as<uint64_t>(),
+                        cnt.as<unsigned long long>(), s, pool, c);
+  else
+    emit_keys<uint32_t>(g, cl, p, pm != nullptr, b, keys.as<uint64_t>(),
+                        cnt.as<unsigned long long>(), s, pool, c);
+  unsigned long long ne = 0;
+  CCG_CUDA(cudaMemcpyAsync(&ne, cnt.p, 8, cudaMemcpyDeviceToHost, s));
+  CCG_CUDA(cudaStreamSynchronize(s));
+  (void)host_mailbox;
+  if (ne == 0) {
+    CCG_CUDA(cudaMemsetAsync(out.newid.p, 0xff, 4 * ncl, s));
+    out.rp.alloc(8, s, pool);
+    CCG_CUDA(cudaMemsetAsync(out.rp.p, 0, 8, s));
+    return;
+  }
+  DevBuf tmp(8 * ne, s, pool);
+  uint64_t *sorted = radix_sort_u64(keys.as<uint64_t>(), tmp.as<uint64_t>(), ne, 2 * b, s, pool, c);
+  // unique keys into the other buffer
+  uint64_t *uk = (sorted == keys.as<uint64_t>()) ? tmp.as<uint64_t>() : keys.as<uint64_t>();
+  DevBuf d_u(4, s, pool), d_nv(4, s, pool);
+  scan_generic(ne, GetUniq{sorted}, PutUniq{sorted, uk}, d_u.as<uint32_t>(), s, pool, c);
+  c.add(0, 8 * ne + 8 * ne);  // dedup: read keys, write uniques (upper bound)
+  // source flags -> new ids (order preserving)
+  CCG_CUDA(cudaMemsetAsync(out.newid.p, 0, 4 * ncl, s));
+  k_mark_src<<<grid_for(ne, kBlock, kSMs * 16), kBlock, 0, s>>>(uk, d_u.as<uint32_t>(), b,
+                                                               out.newid.as<uint32_t>());
+  CCG_LAUNCH_CHECK();
+  scan_generic(ncl, GetFlag{out.newid.as<uint32_t>()}, PutNewId{out.newid.as<uint32_t>()},
+               d_nv.as<uint32_t>(), s, pool, c);
+  uint32_t uv[2];
+  CCG_CUDA(cudaMemcpyAsync(&uv[0], d_u.p, 4, cudaMemcpyDeviceToHost, s));
+  CCG_CUDA(cudaMemcpyAsync(&uv[1], d_nv.p, 4, cudaMemcpyDeviceToHost, s));
+  CCG_CUDA(cudaStreamSynchronize(s));
+  out.m = uv[0];
+  out.n = uv[1];
+  out.rp.alloc(8 * (out.n + 1), s, pool);
+  out.col.alloc(4 * out.m, s, pool);
+  out.vid.alloc(4 * (out.n ? out.n : 1), s, pool);
+  k_build_csr<<<grid_for(out.m, kBlock, kSMs * 16), kBlock, 0, s>>>(
+      uk, d_u.as<uint32_t>(), b, out.newid.as<uint32_t>(), out.rp.as<uint64_t>(),
+      out.col.as<uint32_t>(), d_nv.as<uint32_t>());
+  CCG_LAUNCH_CHECK();
+  k_vid<<<grid_for(ncl, kBlock, kSMs * 16), kBlock, 0, s>>>(ncl, out.newid.as<uint32_t>(),
+                                                           vid_of_cluster, out.vid.as<uint32_t>());
+  CCG_LAUNCH_CHECK();
+  // CSR rebuild: unique keys read, offsets + ids written, id map
+  c.add(4, 8 * out.m + 8 * (out.n + 1) + 4 * out.m + 8 * ncl);
+}
+
+}  // namespace ccg

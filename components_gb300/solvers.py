@@ -1,0 +1,178 @@
+"""The reference's solver classes over the C ABI.
+
+    comp = ExponentialContraction(conf, rank, size)
+    comp.FindComponents(G, labels)
+
+as in app/exp_contraction.cpp:104-105 (and all_reduce.cpp:97-98,
+local_contraction.cpp:114/142, shortcuts.cpp:117/145, labels.cpp:101).  On one
+GPU the `size` ranks become virtual ranks: contiguous vertex ranges of the one
+device-resident CSR (graph_io.h:308-313), so the partition-local steps of the
+algorithms keep their meaning.  `labels` is overwritten with canonical labels
+(minimum vertex id of the component) for every vertex.
+
+There is no CPU path: these classes call libccgpu and raise if it is missing
+or the call fails.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _lib
+from .config import Config
+from .graph import StaticGraph, _is_torch, _ptr
+
+
+class Context:
+    """A libccgpu context: one CUDA stream and one device memory pool."""
+
+    def __init__(self, device: int = 0, stream=None, profiling: bool = False):
+        self._h = C.c_void_p()
+        s = None
+        if stream is not None:
+            s = stream.cuda_stream if hasattr(stream, "cuda_stream") else int(stream)
+        _lib.check(_lib.gpu().cc_ctx_create(C.byref(self._h), device, s))
+        if profiling:
+            _lib.check(_lib.gpu().cc_ctx_set_profiling(self._h, 1))
+
+    @property
+    def handle(self):
+        return self._h
+
+    @property
+    def stream_handle(self) -> int:
+        return _lib.gpu().cc_ctx_stream(self._h) or 0
+
+    def set_profiling(self, on: bool) -> None:
+        _lib.check(_lib.gpu().cc_ctx_set_profiling(self._h, int(on)))
+
+    def run(self, g: StaticGraph, algo: int, cfg: _lib.cc_config, seed: int, labels) -> None:
+        csr = g.to_c()
+        where = _lib.CC_DEVICE if (_is_torch(labels) and labels.is_cuda) else _lib.CC_HOST
+        _lib.check(_lib.gpu().cc_ctx_run(self._h, C.byref(csr), algo, C.byref(cfg), seed,
+                                         _ptr(labels), where))
+
+    def stats(self) -> dict:
+        st = _lib.cc_stats()
+        _lib.check(_lib.gpu().cc_ctx_stats(self._h, C.byref(st)))
+        return st.as_dict()
+
+    def arena_bytes(self) -> int:
+        return int(_lib.gpu().cc_ctx_arena_bytes(self._h))
+
+    def close(self) -> None:
+        if self._h:
+            _lib.gpu().cc_ctx_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+_default_ctx: dict[int, Context] = {}
+
+
+def default_context() -> Context:
+    dev = 0
+    try:
+        import torch
+        if torch.cuda.is_available():
+            dev = torch.cuda.current_device()
+    except ImportError:
+        pass
+    if dev not in _default_ctx:
+        _default_ctx[dev] = Context(dev)
+    return _default_ctx[dev]
+
+
+def _check_labels(G: StaticGraph, labels) -> None:
+    n = G.n
+    if int(labels.shape[0]) < n:
+        raise ValueError(f"labels has {labels.shape[0]} entries, graph has {n} vertices")
+    isz = labels.element_size() if _is_torch(labels) else labels.itemsize
+    if isz != G.id_bytes:
+        raise ValueError(f"labels are {isz}-byte, graph ids are {G.id_bytes}-byte")
+    if not _is_torch(labels) and not labels.flags["C_CONTIGUOUS"]:
+        raise ValueError("labels must be contiguous")
+    if _is_torch(labels) and not labels.is_contiguous():
+        raise ValueError("labels must be contiguous")
+
+
+class _Solver:
+    ALGO = _lib.CC_EXP
+
+    def __init__(self, conf: Config, rank: int = 0, size: int = 1, context: Context | None = None):
+        if rank != 0:
+            raise ValueError("one process drives one GPU: rank must be 0 (size = virtual ranks)")
+        if size < 1:
+            raise ValueError("size must be >= 1")
+        self.config_ = conf
+        self.rank_ = rank
+        self.size_ = size
+        self.ctx = context
+        self.last_stats: dict = {}
+
+    def FindComponents(self, G: StaticGraph, labels) -> None:
+        _check_labels(G, labels)
+        ctx = self.ctx or default_context()
+        g = G.with_parts(self.size_) if G.num_parts != self.size_ else G
+        ctx.run(g, self.ALGO, self.config_.to_c(), int(self.config_.seed), labels)
+        self.last_stats = ctx.stats()
+
+    # driver statistics (exponential_contraction.h:325-335): no exchange on
+    # one device
+    def GetCommTime(self) -> float:
+        return 0.0
+
+    def GetSendVolume(self) -> int:
+        return 0
+
+    def GetReceiveVolume(self) -> int:
+        return 0
+
+
+class ExponentialContraction(_Solver):
+    """lib/components/exponential_contraction.h:40"""
+    ALGO = _lib.CC_EXP
+
+
+class LocalContraction(_Solver):
+    """lib/components/local_contraction.h:39"""
+    ALGO = _lib.CC_LOCAL
+
+
+class ShortcutPropagation(_Solver):
+    """lib/components/shortcut_propagation.h:38"""
+    ALGO = _lib.CC_SHORTCUTS
+
+
+class Propagation(_Solver):
+    """lib/components/propagation.h:38"""
+    ALGO = _lib.CC_LABELS
+
+
+class AllReduce(_Solver):
+    """lib/components/all_reduce.h:34 (AllReduce<GraphType>)"""
+    ALGO = _lib.CC_ALLREDUCE
+
+
+SOLVERS = {"exp": ExponentialContraction, "local": LocalContraction,
+           "shortcuts": ShortcutPropagation, "labels": Propagation, "allreduce": AllReduce}
+
+
+def find_components(G: StaticGraph, algo: str = "exp", conf: Config | None = None,
+                    context: Context | None = None):
+    """Convenience: labels (same kind and placement as G's ids) for G."""
+    conf = conf or Config()
+    if G.on_device:
+        import torch
+        dt = torch.int32 if G.id_bytes == 4 else torch.int64
+        labels = torch.empty(G.n, dtype=dt, device=G.row_ptr.device)
+    else:
+        labels = np.empty(G.n, np.uint32 if G.id_bytes == 4 else np.uint64)
+    SOLVERS[algo](conf, 0, G.num_parts, context).FindComponents(G, labels)
+    return labels

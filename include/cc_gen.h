@@ -1,0 +1,52 @@
+/*
+ * cc_gen.h - seeded synthetic graph generators (libccgen.so, host C++).
+ *
+ * The reference takes its inputs from KaGen (github.com/sebalamm/KaGen, an
+ * empty submodule in the reference tree) through IOUtility::LoadGraph
+ * (lib/io/io_utils.h:59-83: gnm_undirected, grid_2d, rhg, ...).  These
+ * generators produce the same graph families with the same parameters as
+ * symmetric CSR, from a counter-based hash of (seed, index), so every host
+ * builds the same graph for the same arguments.  Self-loops and duplicate
+ * edges are dropped; adjacency rows are sorted.
+ */
+#ifndef CC_GEN_H_
+#define CC_GEN_H_
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct cc_host_graph {
+  uint64_t n;         /* vertices */
+  uint64_t m_dir;     /* directed entries */
+  uint64_t *row_ptr;  /* n+1, malloc'ed */
+  void *col;          /* m_dir ids of id_bytes each, malloc'ed */
+  uint32_t id_bytes;  /* 4 or 8 */
+  uint32_t pad_;
+} cc_host_graph;
+
+/* Erdos-Renyi G(n, m): m endpoint pairs drawn uniformly (gnm_undirected). */
+int cc_gen_gnm(uint64_t n, uint64_t m, uint64_t seed, uint32_t id_bytes, cc_host_graph *out);
+
+/* 2D bond percolation on an X x Y lattice (grid_2d with -p): vertex id
+   y*X + x, each right/down lattice edge kept independently with
+   probability p; not periodic. */
+int cc_gen_grid(uint64_t X, uint64_t Y, double p, uint64_t seed, uint32_t id_bytes,
+                cc_host_graph *out);
+
+/* Random hyperbolic graph, threshold model (rhg): n points in a disk of
+   radius R, radial density alpha sinh(alpha r) with alpha = (gamma-1)/2,
+   edge iff hyperbolic distance <= R; R chosen for the expected average
+   degree avg_deg.  Vertex ids follow the angular order. */
+int cc_gen_rhg(uint64_t n, double avg_deg, double gamma, uint64_t seed, uint32_t id_bytes,
+               cc_host_graph *out);
+
+void cc_host_graph_free(cc_host_graph *g);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* CC_GEN_H_ */

@@ -1,0 +1,197 @@
+/*
+ * cc_gpu.h - C ABI of the GB300 connected-components library (libccgpu.so).
+ *
+ * This is the drop-in boundary for the connected-components (CC) solve of
+ * sebalamm/components.  The reference reaches that solve through a C++ class
+ * API used by its five drivers:
+ *
+ *     X comp(const Config &conf, PEID rank, PEID size);
+ *     comp.FindComponents(G, labels);
+ *
+ *   app/exp_contraction.cpp:104-105   ExponentialContraction
+ *   app/all_reduce.cpp:97-98          AllReduce<StaticGraph>
+ *   app/local_contraction.cpp:114,142 LocalContraction
+ *   app/shortcuts.cpp:117,145         ShortcutPropagation
+ *   app/labels.cpp:101                Propagation
+ *
+ * Here one call, cc_gpu_run(), replaces that pair.  The graph travels as a
+ * symmetric CSR (the reference's StaticGraph layout, lib/data_structures/
+ * static_graph.h:120-171, 423-437) and the labels come back canonical: every
+ * vertex gets the minimum vertex id of its component.  The reference's own
+ * labels are not canonical (exponential_contraction.h:872,887 labels
+ * unresolved vertices n+gid), so both sides are compared after
+ * canonicalisation.  The C++ class names are provided on top of this ABI by
+ * include/components_gb300.hpp.
+ *
+ * Errors are returned as an int status; the library never calls exit().  The
+ * reference has no status codes: it calls exit(1) or MPI_Finalize
+ * (io_utils.h:53-55, dynamic_contraction.h:437-438, comm_utils.h:58-60).
+ *
+ * Threading: one context (cc_ctx) owns one CUDA stream and one device arena;
+ * a context must not be used by two host threads at once.  cc_gpu_run() uses
+ * a per-thread default context on the current CUDA device.
+ */
+#ifndef CC_GPU_H_
+#define CC_GPU_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes -------------------------------------------------------- */
+enum {
+  CC_OK = 0,
+  CC_ERR_INVALID = 1,        /* bad argument, malformed CSR or config */
+  CC_ERR_OOM = 2,            /* device or pinned host allocation failed */
+  CC_ERR_CUDA = 3,           /* a CUDA runtime call failed */
+  CC_ERR_NO_CONVERGENCE = 4, /* an iterative loop hit its round cap */
+  CC_ERR_TIMEOUT = 5,        /* a bounded device-side wait gave up */
+  CC_ERR_UNSUPPORTED = 6,    /* option combination not provided */
+  CC_ERR_BUSY = 7            /* serving queue full / over the HBM budget */
+};
+
+/* where the caller's pointers live */
+enum { CC_HOST = 0, CC_DEVICE = 1 };
+
+/*
+ * Symmetric CSR of an undirected graph.  Vertex ids are 0..n-1; every
+ * undirected edge {u,w} appears as the two directed entries u->w and w->u
+ * (reference: StaticGraph built from symmetric generator edge lists,
+ * graph_io.h:68-160).  Self-loops are ignored.  num_parts is the number of
+ * virtual ranks P: vertex v belongs to the contiguous range of rank r with
+ * the reference's split  n/P + (r < n%P)  (graph_io.h:308-313).
+ */
+typedef struct cc_csr {
+  uint64_t n;               /* number of vertices */
+  uint64_t m_dir;           /* number of directed adjacency entries */
+  const uint64_t *row_ptr;  /* n+1 offsets into col */
+  const void *col;          /* m_dir neighbour ids, id_bytes each */
+  uint32_t id_bytes;        /* 4 (uint32 ids) or 8 (uint64 ids) */
+  uint32_t num_parts;       /* virtual ranks P >= 1 */
+  uint32_t where;           /* CC_HOST or CC_DEVICE for row_ptr and col */
+  uint32_t reserved;        /* must be 0 */
+} cc_csr;
+
+/* The five driver options of app/ (one solver class each). */
+typedef enum cc_algo {
+  CC_EXP = 0,       /* ExponentialContraction (exponential_contraction.h:40) */
+  CC_LOCAL = 1,     /* LocalContraction       (local_contraction.h:39)       */
+  CC_SHORTCUTS = 2, /* ShortcutPropagation    (shortcut_propagation.h:38)    */
+  CC_LABELS = 3,    /* Propagation            (propagation.h:38)             */
+  CC_ALLREDUCE = 4  /* AllReduce<G>           (all_reduce.h:34)              */
+} cc_algo;
+
+/*
+ * Mirror of the solver-relevant fields of Config (lib/config.h:29-87) with the
+ * defaults of ParseParameters (app/parse_parameters.h:30-100); fill it with
+ * cc_config_default().  I/O and generator fields stay on the host side.
+ */
+typedef struct cc_config {
+  double beta;                /* -beta      0.1  exponential shift rate      */
+  uint32_t seq;               /* -seq       1    sequential limit factor     */
+  uint32_t prop_iterations;   /* -pi        3    (accepted; unused upstream) */
+  uint32_t number_of_hitters; /* -heavy-hitters 0 shortcut request filter    */
+  uint32_t degree_threshold;  /* -hd-thres  16   hub threshold factor        */
+  uint32_t degree_limit;      /* -deg       100                              */
+  float hd_sf;                /* -hd-sf     0.5  neighbourhood sampling      */
+  uint8_t fixed_seq;          /* -fixed-seq                                  */
+  uint8_t contraction;        /* -contraction (two-level component graph)    */
+  uint8_t direct;             /* -direct                                     */
+  uint8_t single;             /* -single (one-level component graph)         */
+  uint8_t bfs;                /* -bfs (start-time gated decomposition)       */
+  uint8_t replicate;          /* -replicate (hub vertices)                   */
+  uint8_t regular;            /* -regular   accepted and ignored             */
+  uint8_t overalloc;          /* -overalloc accepted and ignored             */
+  uint8_t verbose;            /* -verbose                                    */
+  uint8_t pad_[3];
+} cc_config;
+
+#define CC_MAX_LEVELS 64
+#define CC_MAX_KSTATS 16
+
+/* Per-kernel timing (CUDA events on the context stream), filled when
+   profiling is on (cc_ctx_set_profiling). */
+typedef struct cc_kernel_stat {
+  char name[32];
+  uint32_t launches;
+  uint32_t pad_;
+  double ms;       /* summed device time of the launches */
+  uint64_t bytes;  /* summed algorithmic bytes of the launches */
+} cc_kernel_stat;
+
+/* Statistics of the last solve on a context (cc_gpu_stats / cc_ctx_stats). */
+typedef struct cc_stats {
+  uint32_t levels;                          /* contraction levels executed   */
+  uint32_t rounds_total;                    /* iterative rounds, all levels  */
+  uint32_t rounds[CC_MAX_LEVELS];           /* rounds per level              */
+  uint64_t level_vertices[CC_MAX_LEVELS];   /* vertices of each level graph  */
+  uint64_t level_edges[CC_MAX_LEVELS];      /* directed edges of each level  */
+  uint64_t bytes_algorithmic;               /* sum of algorithmic bytes      */
+  uint64_t kernel_launches;                 /* kernels launched by the solve */
+  uint64_t num_components;                  /* components incl. isolated     */
+  uint64_t h2d_bytes, d2h_bytes;            /* copies made for HOST buffers  */
+  double solve_ms;                          /* device time of the solve      */
+  double total_ms;                          /* incl. host<->device copies    */
+  /* driver compatibility: GetCommTime/GetSendVolume/GetReceiveVolume
+     (exponential_contraction.h:325-335).  No exchange happens on one
+     device, so they are always 0. */
+  double comm_time;
+  uint64_t send_volume, recv_volume;
+  uint32_t nkernels;                        /* entries used in kernels[]     */
+  uint32_t pad_;
+  cc_kernel_stat kernels[CC_MAX_KSTATS];
+} cc_stats;
+
+typedef struct cc_ctx cc_ctx;
+
+/* ---- single-graph solve -------------------------------------------------- */
+
+/* Fill *cfg with the ParseParameters defaults (parse_parameters.h:35-75). */
+void cc_config_default(cc_config *cfg);
+
+/*
+ * Solve CC of *g with the solver `algo` and write canonical labels (minimum
+ * vertex id of the component, id_bytes wide) to labels_out.  labels_out lives
+ * where g->where says (host or device).  seed is Config::seed.  Replaces
+ * X(conf, rank, size).FindComponents(G, labels) for one rank per GPU.
+ */
+int cc_gpu_run(const cc_csr *g, cc_algo algo, const cc_config *cfg,
+               uint64_t seed, void *labels_out);
+
+/* Statistics of the last cc_gpu_run() of this thread. */
+int cc_gpu_stats(cc_stats *out);
+
+/* Text of a status code, or of the last error of this thread for CC_ERR_CUDA. */
+const char *cc_gpu_strerror(int status);
+
+/* Validate a CSR (sizes, monotone offsets, ids < n, symmetry when check_sym);
+   runs on the host for CC_HOST graphs and on the device for CC_DEVICE. */
+int cc_csr_validate(const cc_csr *g, int check_sym);
+
+/* ---- contexts ------------------------------------------------------------ */
+
+/* Create a context on `device`.  stream may be NULL (the context creates a
+   non-blocking stream) or a cudaStream_t owned by the caller. */
+int cc_ctx_create(cc_ctx **out, int device, void *stream);
+int cc_ctx_destroy(cc_ctx *ctx);
+/* As cc_gpu_run on ctx's stream; labels_where says where labels_out lives. */
+int cc_ctx_run(cc_ctx *ctx, const cc_csr *g, cc_algo algo,
+               const cc_config *cfg, uint64_t seed, void *labels_out,
+               uint32_t labels_where);
+int cc_ctx_stats(cc_ctx *ctx, cc_stats *out);
+/* Device bytes the context holds in its arena (grows on demand, reused). */
+uint64_t cc_ctx_arena_bytes(cc_ctx *ctx);
+/* Per-kernel CUDA-event timing and a component count in cc_stats (off by
+   default; it adds event records and one counting pass per solve). */
+int cc_ctx_set_profiling(cc_ctx *ctx, int on);
+/* The cudaStream_t the context launches on. */
+void *cc_ctx_stream(cc_ctx *ctx);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* CC_GPU_H_ */

@@ -1,0 +1,164 @@
+"""GPU parity: canonical labels from every solver option, through the C ABI,
+equal the oracle's on the same seeded inputs (bit-exact; labels are integers).
+"""
+from __future__ import annotations
+
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+import components_gb300 as cc
+import oracle
+from components_gb300 import _lib
+from components_gb300.graph import StaticGraph
+
+from conftest import csr_from_rows
+
+pytestmark = pytest.mark.gpu
+ALGOS = ["exp", "local", "shortcuts", "labels", "allreduce"]
+GOLD = np.load(Path(__file__).with_name("golden") / "golden.npz")
+
+
+def gpu_labels(G: StaticGraph, algo: str, P: int = 1, where: str = "device", conf=None,
+               ctx=None):
+    import torch
+    conf = conf or cc.Config(seed=1001)
+    G = G.with_parts(P)
+    dt_t = torch.int32 if G.id_bytes == 4 else torch.int64
+    dt_n = np.uint32 if G.id_bytes == 4 else np.uint64
+    if where == "device":
+        D = G.to_device("cuda:0")
+        lab = torch.full((G.n,), -1, dtype=dt_t, device="cuda:0")
+        cc.SOLVERS[algo](conf, 0, P, ctx).FindComponents(D, lab)
+        return lab.cpu().numpy().view(dt_n).astype(np.uint64)
+    lab = np.full(G.n, 0xFFFFFFFF, dt_n)
+    cc.SOLVERS[algo](conf, 0, P, ctx).FindComponents(G, lab)
+    return lab.astype(np.uint64)
+
+
+def test_simple_graph_known_answer(cuda):
+    G = cc.from_edges(int(GOLD["simple_n"][0]), GOLD["simple_edges"])
+    for algo in ALGOS:
+        for P in (1, 2, 3):
+            for where in ("device", "host"):
+                got = gpu_labels(G, algo, P, where, cc.Config(seed=1001, sequential_limit=0))
+                assert np.array_equal(got, GOLD["simple_labels"]), (algo, P, where)
+
+
+@pytest.mark.parametrize("name", ["gnm_small", "gnm_sparse", "grid_16", "grid_40x25"])
+@pytest.mark.parametrize("algo", ALGOS)
+def test_golden_graphs(cuda, name, algo):
+    idb = int(GOLD[f"{name}_idb"][0])
+    G = StaticGraph(GOLD[f"{name}_rp"], GOLD[f"{name}_col"].astype(np.uint32 if idb == 4 else np.uint64))
+    for P in (1, 4, 16):
+        for seq in (0, 1):
+            got = gpu_labels(G, algo, P, "device", cc.Config(seed=1001, sequential_limit=seq))
+            assert np.array_equal(got, GOLD[f"{name}_labels"]), (name, algo, P, seq)
+
+
+@pytest.mark.parametrize("algo", ALGOS)
+def test_random_graphs_all_options(cuda, algo):
+    rng = np.random.default_rng(42)
+    for trial in range(12):
+        n = int(rng.integers(2, 3000))
+        m = int(rng.integers(0, 3 * n))
+        idb = 4 if trial % 2 else 8
+        G = cc.gen_gnm(n, m, seed=100 + trial, id_bytes=idb)
+        want = oracle.uf_labels(G)
+        P = int(rng.choice([1, 2, 5, 32]))
+        conf = cc.Config(seed=1001 + trial, sequential_limit=int(rng.integers(0, 3)),
+                         use_contraction=bool(trial % 3 == 0), use_bfs=bool(trial % 4 == 1),
+                         number_of_hitters=int(rng.choice([0, 0, 4])))
+        got = gpu_labels(G, algo, P, "device" if trial % 2 else "host", conf)
+        assert np.array_equal(got, want), (algo, trial, n, m, P)
+
+
+def test_exp_options_and_beta(cuda):
+    G = cc.gen_gnm(20000, 30000, seed=8, id_bytes=8)
+    want = oracle.uf_labels(G)
+    for kw in [dict(), dict(use_bfs=True), dict(single_level_contraction=True),
+               dict(use_contraction=True), dict(direct_contraction=True),
+               dict(replicate_high_degree=True), dict(beta=0.5), dict(beta=0.02),
+               dict(fixed_limit=True, sequential_limit=100), dict(sequential_limit=0)]:
+        conf = cc.Config(seed=1003, **kw)
+        for P in (3, 64):
+            assert np.array_equal(gpu_labels(G, "exp", P, "device", conf), want), (kw, P)
+
+
+def test_schedule_independence(cuda):
+    """Randomness changes the contraction schedule, never the partition."""
+    G = cc.gen_gnm(50000, 60000, seed=21, id_bytes=4)
+    want = oracle.uf_labels(G)
+    for seed in (1001, 1002, 1003, 5, 123456789):
+        for algo in ("exp", "local"):
+            got = gpu_labels(G, algo, 16, "device", cc.Config(seed=seed, sequential_limit=0))
+            assert np.array_equal(got, want), (algo, seed)
+
+
+def test_edge_cases(cuda):
+    cases = {
+        "single": csr_from_rows([[]]),
+        "isolated": csr_from_rows([[], [], [], []]),
+        "self_loops": csr_from_rows([[0, 1], [0, 1, 1], [2], [4], [3, 3]]),
+        "multi_edges": csr_from_rows([[1, 1, 1], [0, 0, 0, 2], [1]]),
+        "path": cc.from_edges(2000, [(i, i + 1) for i in range(1999)]),
+        "star_hub": cc.from_edges(5000, [(17, i) for i in range(5000) if i != 17]),
+        "two_hubs": cc.from_edges(3000, [(0, i) for i in range(1, 1500)]
+                                  + [(2999, i) for i in range(1500, 2999)]),
+        "cliques_bridge": cc.from_edges(
+            60, [(a, b) for a in range(30) for b in range(a + 1, 30)]
+            + [(a, b) for a in range(30, 60) for b in range(a + 1, 60)] + [(29, 30)]),
+        "u64_ids": cc.from_edges(10, [(0, 9), (3, 4), (4, 8)], id_bytes=8),
+    }
+    for name, G in cases.items():
+        want = oracle.uf_labels(G)
+        for algo in ALGOS:
+            for P in (1, 2, 7):
+                got = gpu_labels(G, algo, P, "device", cc.Config(seed=1001, sequential_limit=0))
+                assert np.array_equal(got, want), (name, algo, P)
+
+
+def test_empty_graph(cuda):
+    G = StaticGraph(np.zeros(1, np.uint64), np.zeros(0, np.uint32))
+    for algo in ALGOS:
+        lab = np.zeros(0, np.uint32)
+        cc.SOLVERS[algo](cc.Config(), 0, 1).FindComponents(G, lab)
+
+
+def test_invalid_ids_are_reported_not_faulted(cuda):
+    """An id >= n is caught by the kernels' own bounds checks (no access is
+    made) and returned as CC_ERR_INVALID; the context stays usable."""
+    bad = csr_from_rows([[1], [0, 9], [3], [2]])  # 9 >= n = 4
+    for algo in ALGOS:
+        with pytest.raises(_lib.CCError) as ei:
+            gpu_labels(bad, algo, 1, "device")
+        assert ei.value.status == _lib.CC_ERR_INVALID
+    good = cc.from_edges(4, [(0, 1), (2, 3)])
+    assert np.array_equal(gpu_labels(good, "exp", 1), [0, 0, 2, 2])
+
+
+def test_context_reuse_and_stats(cuda):
+    ctx = cc.Context(0, profiling=True)
+    G = cc.gen_grid(300, 200, 0.5, seed=3)
+    want = oracle.uf_labels(G)
+    for _ in range(3):
+        assert np.array_equal(gpu_labels(G, "exp", 1, "device", ctx=ctx), want)
+    st = ctx.stats()
+    assert st["num_components"] == len(np.unique(want))
+    assert st["kernel_launches"] > 0 and st["bytes_algorithmic"] > 0
+    assert "uf_hook" in st["kernels"]
+    arena = ctx.arena_bytes()
+    gpu_labels(G, "exp", 1, "device", ctx=ctx)
+    assert ctx.arena_bytes() == arena  # steady state: the pool is reused
+    ctx.close()
+
+
+def test_stream_interop(cuda):
+    """A context on a caller's torch stream."""
+    import torch
+    s = torch.cuda.Stream()
+    ctx = cc.Context(0, stream=s)
+    G = cc.gen_gnm(5000, 5000, seed=2, id_bytes=4)
+    assert np.array_equal(gpu_labels(G, "exp", 4, "device", ctx=ctx), oracle.uf_labels(G))
+    ctx.close()
