@@ -139,9 +139,9 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-def make_graph():
+def make_graph(side: int = GRID_X):
     import components_gb300 as cc
-    return cc.gen_grid(GRID_X, GRID_Y, GRID_P, seed=INPUT_SEED, id_bytes=4)
+    return cc.gen_grid(side, side, GRID_P, seed=INPUT_SEED, id_bytes=4)
 
 
 def cpu_reference_run(G, steps, warmup, sample_rows=None):
@@ -182,6 +182,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-steps", type=int, default=2)
     ap.add_argument("--no-check", action="store_true")
+    ap.add_argument("--grid", type=int, default=GRID_X,
+                    help="grid side (default 8192; smaller sides are for ncu captures)")
     args = ap.parse_args()
     rank, world, local = dist_env()
 
@@ -192,14 +194,14 @@ def main():
         import oracle
         oracle.build()
         ge.build()
-        G = make_graph()
+        G = make_graph(args.grid)
         gps, mean_s, threads, sample = cpu_reference_run(G, max(args.steps, 1), args.warmup)
         line = {
             "impl": "reference", "metric": METRIC, "value": gps, "unit": UNIT,
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": mean_s * 1e3, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "u64", "data": "synthetic",
-            "config": {"workload": "grid2d 8192x8192 p=0.5, exp_contraction", "n": G.n,
+            "config": {"workload": f"grid2d {args.grid}x{args.grid} p=0.5, exp_contraction", "n": G.n,
                        "m_dir": G.m, "ranks": threads, "beta": 0.1, "seq": 1},
             "cpu_baseline": {"value": gps, "unit": UNIT, "cores": threads, "kind": "port",
                              "sample": sample + "; oracle/cc_oracle.c restatement of "
@@ -222,7 +224,7 @@ def main():
     import components_gb300 as cc
     from components_gb300 import _lib
 
-    G = make_graph()
+    G = make_graph(args.grid)
     n, m = G.n, G.m
     conf = cc.Config(seed=ALGO_SEED)
     ctx = cc.Context(local)
@@ -332,7 +334,7 @@ def main():
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
-        "config": {"workload": "grid2d 8192x8192 p=0.5 (seed 1), exp_contraction, 1 rank",
+        "config": {"workload": f"grid2d {args.grid}x{args.grid} p=0.5 (seed 1), exp_contraction, 1 rank",
                    "n": n, "m_dir": m, "id_bytes": 4, "beta": 0.1, "seq": 1,
                    "algo_seed": ALGO_SEED, "parallelism": f"replicas x{world}",
                    "l2": "inputs larger than L2 (1.34 GB CSR+labels > 129 MB), no flush"},

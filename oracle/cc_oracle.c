@@ -258,17 +258,58 @@ static void graph_free(or_graph *g) {
   memset(g, 0, sizeof(*g));
 }
 
+static int n_threads(void) {
+#ifdef _OPENMP
+  return omp_get_max_threads();
+#else
+  return 1;
+#endif
+}
+static int thread_id(void) {
+#ifdef _OPENMP
+  return omp_get_thread_num();
+#else
+  return 0;
+#endif
+}
+
+static int keep_edge(u64 v, u64 w, const u64 *cl, int only_cut, u64 n, u64 P) {
+  if (only_cut && rank_of(v, n, P) == rank_of(w, n, P)) return 0;
+  return cl[v] != cl[w];
+}
+
 static void quotient(u64 n, const u64 *rp, const u64 *col, const u64 *cl, u64 ncl,
                      int only_cut, u64 P, or_graph *out) {
   int b = bits_for(ncl);
   u64 m = n ? rp[n] : 0, k = 0;
   u64 *keys = (u64 *)malloc(sizeof(u64) * (m ? m : 1));
-  for (u64 v = 0; v < n; ++v)
-    for (u64 e = rp[v]; e < rp[v + 1]; ++e) {
-      u64 w = col[e];
-      if (only_cut && rank_of(v, n, P) == rank_of(w, n, P)) continue;
-      if (cl[v] != cl[w]) keys[k++] = (cl[v] << b) | cl[w];
+  /* key emission in parallel, each thread over a contiguous vertex range (the
+     ranks of the reference do this step concurrently) */
+  int nt = n_threads(), used = 1;
+  u64 *cnt = (u64 *)calloc((size_t)nt + 1, sizeof(u64));
+#pragma omp parallel num_threads(nt)
+  {
+    int t = thread_id(), T = 1;
+#ifdef _OPENMP
+    T = omp_get_num_threads();
+#endif
+    u64 lo = n * (u64)t / (u64)T, hi = n * (u64)(t + 1) / (u64)T, c = 0;
+    for (u64 v = lo; v < hi; ++v)
+      for (u64 e = rp[v]; e < rp[v + 1]; ++e) c += keep_edge(v, col[e], cl, only_cut, n, P);
+    cnt[t + 1] = c;
+#pragma omp barrier
+#pragma omp single
+    {
+      for (int i = 0; i < T; ++i) cnt[i + 1] += cnt[i];
+      used = T;
     }
+    u64 pos = cnt[t];
+    for (u64 v = lo; v < hi; ++v)
+      for (u64 e = rp[v]; e < rp[v + 1]; ++e)
+        if (keep_edge(v, col[e], cl, only_cut, n, P)) keys[pos++] = (cl[v] << b) | cl[col[e]];
+  }
+  k = cnt[used];
+  free(cnt);
   radix_u64(keys, k, 2 * b);
   u64 u = 0;
   for (u64 i = 0; i < k; ++i)
@@ -445,7 +486,10 @@ int or_exp_contraction(u64 n, const u64 *rp, const u64 *col, u64 P, double beta,
   u64 *lab = (u64 *)malloc(sizeof(u64) * n);
   or_local_components(n, rp, col, P, lab);
   u64 *cv = (u64 *)malloc(sizeof(u64) * n);
-  for (u64 v = 0; v < n; ++v) {
+  long long vv;
+#pragma omp parallel for schedule(static)
+  for (vv = 0; vv < (long long)n; ++vv) {
+    u64 v = (u64)vv;
     int iface = 0;
     u64 r = rank_of(v, n, P);
     for (u64 e = rp[v]; e < rp[v + 1] && !iface; ++e) iface = rank_of(col[e], n, P) != r;
@@ -463,9 +507,10 @@ int or_exp_contraction(u64 n, const u64 *rp, const u64 *col, u64 P, double beta,
   u64 *sub = (u64 *)malloc(sizeof(u64) * (h.n ? h.n : 1));
   /* lcag labels are gids; its vertex order is gid order */
   levels(&R, h.n, h.rp, h.col, h.vid, 1, sub);
-  for (u64 v = 0; v < n; ++v) {
-    u64 id = h.newid[cv[v]];
-    raw_out[v] = id != OR_NONE ? sub[id] : cv[v];
+#pragma omp parallel for schedule(static)
+  for (vv = 0; vv < (long long)n; ++vv) {
+    u64 id = h.newid[cv[vv]];
+    raw_out[vv] = id != OR_NONE ? sub[id] : cv[vv];
   }
   if (rounds_out) *rounds_out = R.rounds_total;
   free(sub);
