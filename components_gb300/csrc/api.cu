@@ -27,26 +27,27 @@
 #include <algorithm>
 
 #include "../../include/cc_gpu_debug.h"
-#include "kernels.h"
+#include "ctx.h"
 
-struct cc_ctx {
-  int device = 0;
-  cudaStream_t stream = nullptr;
-  bool own_stream = false;
-  cudaMemPool_t pool = nullptr;
-  int *d_flag = nullptr;
-  int *d_err = nullptr;
-  int *h_flag = nullptr;  // pinned
-  uint64_t *d_geo = nullptr;
-  int geo_len = 0;
-  double geo_beta = -1.0;
-  bool prof = false;
-  cc_stats stats{};
-};
+namespace ccg {
+std::string &last_error() {
+  static thread_local std::string s;
+  return s;
+}
+
+void throw_on_kernel_error(cc_ctx *C, cudaStream_t s) {
+  int e = 0;
+  CCG_CUDA(cudaMemcpyAsync(&e, C->d_err, sizeof(int), cudaMemcpyDeviceToHost, s));
+  CCG_CUDA(cudaStreamSynchronize(s));
+  if (e == kErrBadOffsets) throw Error(CC_ERR_INVALID, "CSR offsets are not monotone or exceed m_dir");
+  if (e == kErrBadId) throw Error(CC_ERR_INVALID, "CSR holds a vertex id >= n");
+  if (e == kErrOverflow) throw Error(CC_ERR_INVALID, "CSR offsets disagree with m_dir");
+  if (e) throw Error(CC_ERR_INVALID, "CSR check failed");
+}
+}  // namespace ccg
 
 namespace {
 
-thread_local std::string g_last_error;
 thread_local std::map<int, std::unique_ptr<cc_ctx>> g_default_ctx;
 thread_local cc_stats g_last_stats{};
 
@@ -54,23 +55,8 @@ using ccg::Counters;
 using ccg::Csr;
 using ccg::DevBuf;
 using ccg::Error;
-
-template <class F>
-int guard(F &&f) {
-  try {
-    f();
-    return CC_OK;
-  } catch (const Error &e) {
-    g_last_error = e.what();
-    return e.status;
-  } catch (const std::bad_alloc &) {
-    g_last_error = "host allocation failed";
-    return CC_ERR_OOM;
-  } catch (const std::exception &e) {
-    g_last_error = e.what();
-    return CC_ERR_CUDA;
-  }
-}
+using ccg::guard;
+#define g_last_error (ccg::last_error())
 
 void ctx_init(cc_ctx *c, int device, void *stream) {
   c->device = device;
@@ -99,6 +85,8 @@ void ctx_free(cc_ctx *c) {
   if (!c) return;
   cudaSetDevice(c->device);
   if (c->stream) cudaStreamSynchronize(c->stream);
+  ccg::batch_cache_free(c->batch);
+  c->batch = nullptr;
   if (c->d_flag) cudaFree(c->d_flag);
   if (c->d_err) cudaFree(c->d_err);
   if (c->d_geo) cudaFree(c->d_geo);
@@ -139,15 +127,7 @@ struct Solver {
   uint32_t hub_degree = 32;    // rows above are processed one warp per row
   int max_levels = CC_MAX_LEVELS - 1;
 
-  void check_err() {
-    int e = 0;
-    CCG_CUDA(cudaMemcpyAsync(&e, C->d_err, sizeof(int), cudaMemcpyDeviceToHost, s));
-    CCG_CUDA(cudaStreamSynchronize(s));
-    if (e == ccg::kErrBadOffsets) throw Error(CC_ERR_INVALID, "CSR offsets are not monotone or exceed m_dir");
-    if (e == ccg::kErrBadId) throw Error(CC_ERR_INVALID, "CSR holds a vertex id >= n");
-    if (e == ccg::kErrOverflow) throw Error(CC_ERR_INVALID, "CSR offsets disagree with m_dir");
-    if (e) throw Error(CC_ERR_INVALID, "CSR check failed");
-  }
+  void check_err() { ccg::throw_on_kernel_error(C, s); }
 
   void note_level(uint32_t level, const Csr &G, int rounds) {
     if (level >= CC_MAX_LEVELS) return;

@@ -1,0 +1,57 @@
+// ctx.h - the context object behind cc_ctx* and the status guard shared by
+// the C ABI translation units (api.cu, batch.cu, serve.cu).
+#pragma once
+
+#include <memory>
+#include <string>
+
+#include "kernels.h"
+
+namespace ccg {
+struct BatchCache;  // batch.cu
+void batch_cache_free(BatchCache *c);
+}  // namespace ccg
+
+struct cc_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  cudaMemPool_t pool = nullptr;
+  int *d_flag = nullptr;
+  int *d_err = nullptr;
+  int *h_flag = nullptr;  // pinned
+  uint64_t *d_geo = nullptr;
+  int geo_len = 0;
+  double geo_beta = -1.0;
+  bool prof = false;
+  cc_stats stats{};
+  ccg::BatchCache *batch = nullptr;  // last recorded batch solve (CUDA graph)
+};
+
+namespace ccg {
+
+// Last error text of this thread (cc_gpu_strerror).
+std::string &last_error();
+
+template <class F>
+int guard(F &&f) {
+  try {
+    f();
+    return CC_OK;
+  } catch (const Error &e) {
+    last_error() = e.what();
+    return e.status;
+  } catch (const std::bad_alloc &) {
+    last_error() = "host allocation failed";
+    return CC_ERR_OOM;
+  } catch (const std::exception &e) {
+    last_error() = e.what();
+    return CC_ERR_CUDA;
+  }
+}
+
+// Read the context's error word after the stream drains; throw CC_ERR_INVALID
+// when a kernel recorded a bad offset or id.
+void throw_on_kernel_error(cc_ctx *C, cudaStream_t s);
+
+}  // namespace ccg

@@ -186,4 +186,77 @@ void cc_host_graph_free(cc_host_graph *g) {
   g->col = nullptr;
 }
 
+int cc_gen_batch(uint32_t k, double log2_nmin, double log2_nmax, double dmin, double dmax,
+                 uint64_t seed, cc_host_batch *out) {
+  if (!out || log2_nmin < 0 || log2_nmax < log2_nmin || log2_nmax > 31 || dmin < 0 || dmax < dmin)
+    return CC_ERR_INVALID;
+  std::memset(out, 0, sizeof(*out));
+  std::vector<uint64_t> n(k), m(k);
+  for (uint32_t i = 0; i < k; ++i) {
+    double ln = log2_nmin + (log2_nmax - log2_nmin) * unit(hash3(seed, i, 11));
+    n[i] = std::max<uint64_t>(1, (uint64_t)std::llround(std::exp2(ln)));
+    double d = dmin + (dmax - dmin) * unit(hash3(seed, i, 12));
+    m[i] = (uint64_t)std::llround((double)n[i] * d / 2.0);
+  }
+  std::vector<cc_host_graph> parts(k);
+  int bad = 0;
+  long long i;
+#pragma omp parallel for schedule(dynamic, 1) reduction(| : bad)
+  for (i = 0; i < (long long)k; ++i) {
+    // one graph: the G(n, m) generator on its own seed, single-threaded here
+    const uint64_t gs = hash3(seed, (uint64_t)i, 13), gn = n[i], gm = m[i];
+    const int b = bits_for(gn);
+    std::vector<uint64_t> keys;
+    keys.reserve(2 * gm);
+    for (uint64_t j = 0; j < gm; ++j) {
+      uint64_t u = below(hash3(gs, j, 1), gn), w = below(hash3(gs, j, 2), gn);
+      if (u == w) continue;
+      keys.push_back((u << b) | w);
+      keys.push_back((w << b) | u);
+    }
+    std::sort(keys.begin(), keys.end());
+    keys.erase(std::unique(keys.begin(), keys.end()), keys.end());
+    if (csr_from_keys(keys, b, gn, 4, &parts[i]) != CC_OK) bad |= 1;
+  }
+  if (bad) {
+    for (auto &p : parts) cc_host_graph_free(&p);
+    return CC_ERR_OOM;
+  }
+  out->k = k;
+  out->voff = static_cast<uint64_t *>(std::malloc(8 * (k + 1)));
+  std::vector<uint64_t> eoff(k + 1, 0);
+  out->voff[0] = 0;
+  for (uint32_t j = 0; j < k; ++j) {
+    out->voff[j + 1] = out->voff[j] + parts[j].n;
+    eoff[j + 1] = eoff[j] + parts[j].m_dir;
+  }
+  out->total_n = out->voff[k];
+  out->total_m = eoff[k];
+  out->row_ptr = static_cast<uint64_t *>(std::malloc(8 * (out->total_n + 1)));
+  out->col = static_cast<uint32_t *>(std::malloc(4 * (out->total_m ? out->total_m : 1)));
+  if (!out->voff || !out->row_ptr || !out->col) {
+    for (auto &p : parts) cc_host_graph_free(&p);
+    cc_host_batch_free(out);
+    return CC_ERR_OOM;
+  }
+#pragma omp parallel for schedule(dynamic, 4)
+  for (i = 0; i < (long long)k; ++i) {
+    const cc_host_graph &p = parts[i];
+    for (uint64_t v = 0; v < p.n; ++v) out->row_ptr[out->voff[i] + v] = eoff[i] + p.row_ptr[v];
+    if (p.m_dir) std::memcpy(out->col + eoff[i], p.col, 4 * p.m_dir);
+  }
+  out->row_ptr[out->total_n] = out->total_m;
+  for (auto &p : parts) cc_host_graph_free(&p);
+  return CC_OK;
+}
+
+void cc_host_batch_free(cc_host_batch *b) {
+  if (!b) return;
+  std::free(b->voff);
+  std::free(b->row_ptr);
+  std::free(b->col);
+  b->voff = b->row_ptr = nullptr;
+  b->col = nullptr;
+}
+
 }  // extern "C"

@@ -45,6 +45,23 @@ int cc_gen_rhg(uint64_t n, double avg_deg, double gamma, uint64_t seed, uint32_t
 
 void cc_host_graph_free(cc_host_graph *g);
 
+/* k independent G(n_i, m_i) graphs packed as a segmented CSR (cc_batch.h
+   layout: global row offsets, LOCAL uint32 neighbour ids).  Graph i draws
+   log2 n_i ~ U[log2_nmin, log2_nmax], average degree d_i ~ U[dmin, dmax],
+   m_i = round(n_i d_i / 2) endpoint pairs, all from hash(seed, i). */
+typedef struct cc_host_batch {
+  uint32_t k;
+  uint32_t pad_;
+  uint64_t total_n, total_m;
+  uint64_t *voff;     /* k+1 */
+  uint64_t *row_ptr;  /* total_n+1 */
+  uint32_t *col;      /* total_m */
+} cc_host_batch;
+
+int cc_gen_batch(uint32_t k, double log2_nmin, double log2_nmax, double dmin, double dmax,
+                 uint64_t seed, cc_host_batch *out);
+void cc_host_batch_free(cc_host_batch *b);
+
 #ifdef __cplusplus
 }
 #endif

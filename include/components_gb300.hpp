@@ -82,13 +82,9 @@ class Solver {
 
   // CSR already in hand: no adapter pass.
   void FindComponents(const HostCsr &g, std::vector<unsigned long long> &labels) {
-    const uint64_t n = g.GetNumberOfVertices();
-    if (labels.size() < n) labels.resize(n);
-    cc_csr c{n, (uint64_t)g.col.size(), g.row_ptr.data(), g.col.data(), 8, (uint32_t)size_,
-             CC_HOST, 0};
-    check(cc_gpu_run(&c, ALGO, &cfg_, seed_, labels.data()));
-    check(cc_gpu_stats(&stats_));
+    run_csr(g, labels);
   }
+  void FindComponents(HostCsr &g, std::vector<unsigned long long> &labels) { run_csr(g, labels); }
 
   // Reference graph types: the CSR is read through the StaticGraph accessors.
   template <class GraphType>
@@ -107,7 +103,7 @@ class Solver {
     for (uint64_t v = 0; v < n; ++v)
       if (h.row_ptr[v + 1] < h.row_ptr[v]) h.row_ptr[v + 1] = h.row_ptr[v];
     std::vector<unsigned long long> out(n);
-    FindComponents(h, out);
+    run_csr(h, out);
     if (labels.size() < n) labels.resize(n);
     for (uint64_t v : local) labels[v] = out[g.GetGlobalID(v)];
   }
@@ -118,6 +114,15 @@ class Solver {
   const cc_stats &GetStats() const { return stats_; }
 
  private:
+  void run_csr(const HostCsr &g, std::vector<unsigned long long> &labels) {
+    const uint64_t n = g.GetNumberOfVertices();
+    if (labels.size() < n) labels.resize(n);
+    cc_csr c{n, (uint64_t)g.col.size(), g.row_ptr.data(), g.col.data(), 8, (uint32_t)size_,
+             CC_HOST, 0};
+    check(cc_gpu_run(&c, ALGO, &cfg_, seed_, labels.data()));
+    check(cc_gpu_stats(&stats_));
+  }
+
   cc_config cfg_;
   uint64_t seed_;
   int size_;
