@@ -262,3 +262,99 @@ void sanitize_ids(const Csr &g, uint32_t *col32, cudaStream_t s, Counters &c) {
 }
 
 }  // namespace ccg
+
+// ============================================================================
+// Allocation-free entry point: cc_gpu_run_noalloc (declared in cc_gpu.h).
+//
+// Some callers cannot allocate device memory at the moment they need a
+// solve: a plugin's enqueue() inside an inference runtime must not allocate,
+// a process whose device memory is pre-reserved by its own allocator has
+// nothing left for ours, and a latency-critical loop cannot afford the
+// implicit device synchronisation of cudaMalloc/cudaFree.  This variant of
+// the hook-and-compress solve therefore takes every buffer from the caller
+// (CSR in, labels out, all on the device) and keeps its only scratch - the
+// hub-row list, the hub counter and the error word - in the fixed array
+// below, which every GPU that loads this library holds until the process
+// exits.  It calls no cudaMalloc, cudaFree or any other allocating routine.
+//
+// Limits: the hub list holds kNoAllocHubCap rows of degree > 32, so a graph
+// is accepted only if it cannot have more such rows:
+//     min(n, m_dir / 33 + 1) <= kNoAllocHubCap   (1,048,512)
+// e.g. any graph with n <= 1,048,512, or with m_dir <= 34.6 million.  Larger
+// graphs get CC_ERR_UNSUPPORTED before anything is launched.
+//
+// Shared state: all calls share the one scratch array, and it keeps the last
+// call's contents.  The counter and error word are cleared at the start of
+// every call; calls whose work overlaps on the GPU (different streams, or
+// different host threads) race on it and must be serialised by the caller.
+//
+// Set-up: the first call on a device looks up the device address of the
+// scratch array (cudaGetSymbolAddress) with that device current; make that
+// first call before any stream capture that should contain this solve.
+// ============================================================================
+#include <algorithm>
+#include <mutex>
+
+namespace {
+
+constexpr uint32_t kNoAllocWords = 1u << 20;                  // 4 MiB
+constexpr uint32_t kNoAllocHeader = 64;                       // counter, error word, padding
+constexpr uint32_t kNoAllocHubCap = kNoAllocWords - kNoAllocHeader;
+constexpr uint32_t kNoAllocHubDegree = 32;
+
+static __device__ __align__(256) uint32_t g_noalloc_scratch[kNoAllocWords];
+
+constexpr int kNoAllocMaxDevices = 64;
+uint32_t *g_noalloc_addr[kNoAllocMaxDevices] = {};
+std::mutex g_noalloc_mu;
+
+// Device address of the scratch array on the current device (looked up once
+// per device; the host-side symbol itself is not a device address).
+int noalloc_scratch(uint32_t **out) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return CC_ERR_CUDA;
+  if (dev < 0 || dev >= kNoAllocMaxDevices) return CC_ERR_UNSUPPORTED;
+  std::lock_guard<std::mutex> lk(g_noalloc_mu);
+  if (!g_noalloc_addr[dev]) {
+    void *p = nullptr;
+    if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) return CC_ERR_CUDA;
+    g_noalloc_addr[dev] = static_cast<uint32_t *>(p);
+  }
+  *out = g_noalloc_addr[dev];
+  return CC_OK;
+}
+
+}  // namespace
+
+extern "C" int cc_gpu_run_noalloc(const uint64_t *row_ptr, const uint32_t *col, uint64_t n,
+                                  uint64_t m_dir, uint32_t *labels_out, void *stream) {
+  using namespace ccg;
+  if (n == 0) return CC_OK;
+  if (!row_ptr || !labels_out || (m_dir > 0 && !col)) return CC_ERR_INVALID;
+  if (n >= 0xffffffffull) return CC_ERR_UNSUPPORTED;
+  const uint64_t worst_hubs = std::min<uint64_t>(n, m_dir / (kNoAllocHubDegree + 1) + 1);
+  if (worst_hubs > kNoAllocHubCap) return CC_ERR_UNSUPPORTED;
+  uint32_t *scratch = nullptr;
+  int rc = noalloc_scratch(&scratch);
+  if (rc != CC_OK) return rc;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  unsigned int *nhubs = scratch;                  // word 0
+  int *err = reinterpret_cast<int *>(scratch + 1);  // word 1
+  uint32_t *hubs = scratch + kNoAllocHeader;
+  if (cudaMemsetAsync(scratch, 0, 2 * sizeof(uint32_t), s) != cudaSuccess) return CC_ERR_CUDA;
+  const PartMap pm(n, 1);
+  const unsigned grid = grid_for(n, kBlock, kSMs * 32);
+  k_init<uint32_t, false><<<grid, kBlock, 0, s>>>(n, m_dir, row_ptr, col, labels_out, pm, err);
+  k_hook<uint32_t, false><<<grid, kBlock, 0, s>>>(n, m_dir, row_ptr, col, labels_out, pm,
+                                                  kNoAllocHubDegree, hubs, kNoAllocHubCap, nhubs,
+                                                  err);
+  k_hook_hubs<uint32_t, false><<<kSMs * 8, kBlock, 0, s>>>(n, row_ptr, col, labels_out, pm, hubs,
+                                                           kNoAllocHubCap, nhubs, err);
+  k_compress<<<grid, kBlock, 0, s>>>(n, labels_out);
+  if (cudaGetLastError() != cudaSuccess) return CC_ERR_CUDA;
+  int host_err = 0;
+  if (cudaMemcpyAsync(&host_err, err, sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess)
+    return CC_ERR_CUDA;
+  if (cudaStreamSynchronize(s) != cudaSuccess) return CC_ERR_CUDA;
+  return host_err ? CC_ERR_INVALID : CC_OK;
+}

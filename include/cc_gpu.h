@@ -171,6 +171,26 @@ const char *cc_gpu_strerror(int status);
    runs on the host for CC_HOST graphs and on the device for CC_DEVICE. */
 int cc_csr_validate(const cc_csr *g, int check_sym);
 
+/*
+ * Allocation-free solve, for callers that cannot allocate device memory when
+ * they solve: a plugin's enqueue() in an inference runtime, a process whose
+ * device memory is pre-reserved by its own allocator, or a latency-critical
+ * loop that cannot take the device synchronisation of cudaMalloc/cudaFree.
+ * No counterpart in the reference.  Same labels as cc_gpu_run(CC_ALLREDUCE)
+ * (and CC_EXP with one rank): labels_out[v] = minimum vertex id of v's
+ * component.  All pointers are device pointers: row_ptr (n+1), col (m_dir
+ * uint32 ids, symmetric CSR), labels_out (n uint32).  stream is a
+ * cudaStream_t (NULL = default stream); the call returns when the solve is
+ * done.  Scratch lives in a fixed 4 MiB device array that every GPU loading
+ * the library keeps until exit; graphs with min(n, m_dir/33 + 1) > 1,048,512
+ * are rejected with CC_ERR_UNSUPPORTED.  All calls share that array: calls
+ * that overlap on the GPU race and must be serialised by the caller.  The
+ * first call on a device looks up the array's device address; make it before
+ * any stream capture that should contain this solve.
+ */
+int cc_gpu_run_noalloc(const uint64_t *row_ptr, const uint32_t *col, uint64_t n,
+                       uint64_t m_dir, uint32_t *labels_out, void *stream);
+
 /* ---- contexts ------------------------------------------------------------ */
 
 /* Create a context on `device`.  stream may be NULL (the context creates a
