@@ -83,6 +83,14 @@ class cc_stats(C.Structure):
         }
 
 
+class cc_tuning(C.Structure):
+    _fields_ = [("hook_mode", C.c_uint32), ("tile_vertices", C.c_uint32),
+                ("tile_threads", C.c_uint32), ("hub_degree", C.c_uint32)]
+
+
+CC_HOOK_AUTO, CC_HOOK_GLOBAL, CC_HOOK_TILED = 0, 1, 2
+
+
 class cc_host_graph(C.Structure):
     _fields_ = [("n", C.c_uint64), ("m_dir", C.c_uint64), ("row_ptr", C.c_void_p),
                 ("col", C.c_void_p), ("id_bytes", C.c_uint32), ("pad_", C.c_uint32)]
@@ -106,6 +114,8 @@ GPU_SYMBOLS = {
     "cc_ctx_arena_bytes": (_U64, [_P]),
     "cc_ctx_set_profiling": (C.c_int, [_P, C.c_int]),
     "cc_ctx_stream": (_P, [_P]),
+    "cc_ctx_set_tuning": (C.c_int, [_P, C.POINTER(cc_tuning)]),
+    "cc_ctx_get_tuning": (C.c_int, [_P, C.POINTER(cc_tuning)]),
     "cc_debug_geo_table": (C.c_int, [C.c_double, _P, C.c_int]),
     "cc_debug_hash3": (_U64, [_U64, _U64, _U64]),
     "cc_debug_ldd": (C.c_int, [C.POINTER(cc_csr), _P, _U64, _U32, C.c_double, C.c_int, _P, _P]),

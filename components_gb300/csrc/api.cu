@@ -124,7 +124,7 @@ struct Solver {
   uint64_t seed;
   cc_stats &st;
   uint64_t limit = 0;          // sequential limit (edges for CC_EXP, vertices for CC_LOCAL)
-  uint32_t hub_degree = 32;    // rows above are processed one warp per row
+  ccg::UfTuning uf;            // hook-and-compress schedule (context tuning)
   int max_levels = CC_MAX_LEVELS - 1;
 
   void check_err() { ccg::throw_on_kernel_error(C, s); }
@@ -145,7 +145,7 @@ struct Solver {
   // AllReduce::FindComponents, exponential_contraction.h:908-922)
   void base_case(const Csr &G, const uint32_t *vid, uint32_t *out) {
     DevBuf par(4 * G.n, s, pool);
-    ccg::uf_components(G, par.as<uint32_t>(), nullptr, hub_degree, s, pool, c);
+    ccg::uf_components(G, par.as<uint32_t>(), nullptr, uf, s, pool, c);
     ccg::gather_u32(vid, par.as<uint32_t>(), out, G.n, s, c);
   }
 
@@ -221,7 +221,7 @@ struct Solver {
   // cut edge, numbered by that id.
   void local_then_cut_graph(const Csr &g, uint32_t P, uint32_t *lab, ccg::Contracted &G0) {
     ccg::PartMap pm(g.n, P);
-    ccg::uf_components(g, lab, &pm, hub_degree, s, pool, c);
+    ccg::uf_components(g, lab, &pm, uf, s, pool, c);
     check_err();  // the cut-edge pass reads the caller's ids again
     ccg::contract_graph(g, lab, g.n, nullptr, &pm, G0, s, pool, c, nullptr);
     note_level(0, g, 0);
@@ -245,7 +245,7 @@ struct Solver {
     switch (algo) {
       case CC_ALLREDUCE: {
         note_level(0, g, 0);
-        ccg::uf_components(g, lab, nullptr, hub_degree, s, pool, c);
+        ccg::uf_components(g, lab, nullptr, uf, s, pool, c);
         break;
       }
       case CC_EXP: {
@@ -255,7 +255,7 @@ struct Solver {
           // one rank: the local pass already is the whole solve, the component
           // graph has no edges (cag_builder.h:163-229)
           note_level(0, g, 0);
-          ccg::uf_components(g, lab, nullptr, hub_degree, s, pool, c);
+          ccg::uf_components(g, lab, nullptr, uf, s, pool, c);
           break;
         }
         ccg::Contracted G0;
@@ -430,6 +430,7 @@ int ctx_run(cc_ctx *C, const cc_csr *g, cc_algo algo, const cc_config *cfg_in, u
       lab = lab_d.as<uint32_t>();
     }
     Solver S{C, s, C->pool, c, cfg, seed, st};
+    S.uf = C->uf;
     S.run(algo, G, g->num_parts, lab);
     CCG_CUDA(cudaEventRecord(ev[2], s));
     DevBuf cnt(8, s, C->pool);
@@ -590,6 +591,29 @@ int cc_ctx_set_profiling(cc_ctx *ctx, int on) {
 
 void *cc_ctx_stream(cc_ctx *ctx) { return ctx ? (void *)ctx->stream : nullptr; }
 
+int cc_ctx_set_tuning(cc_ctx *ctx, const cc_tuning *t) {
+  if (!ctx || !t) return CC_ERR_INVALID;
+  if (t->hook_mode > CC_HOOK_TILED) return CC_ERR_INVALID;
+  if (t->tile_vertices > 56 * 1024 || (t->tile_threads && (t->tile_threads % 32 || t->tile_threads > 1024)))
+    return CC_ERR_INVALID;
+  ccg::UfTuning u;
+  u.mode = (int)t->hook_mode;
+  if (t->tile_vertices) u.tile_vertices = t->tile_vertices;
+  if (t->tile_threads) u.tile_threads = t->tile_threads;
+  if (t->hub_degree) u.hub_degree = t->hub_degree;
+  ctx->uf = u;
+  return CC_OK;
+}
+
+int cc_ctx_get_tuning(cc_ctx *ctx, cc_tuning *t) {
+  if (!ctx || !t) return CC_ERR_INVALID;
+  t->hook_mode = (uint32_t)ctx->uf.mode;
+  t->tile_vertices = ctx->uf.tile_vertices;
+  t->tile_threads = ctx->uf.tile_threads;
+  t->hub_degree = ctx->uf.hub_degree;
+  return CC_OK;
+}
+
 int cc_gpu_run(const cc_csr *g, cc_algo algo, const cc_config *cfg, uint64_t seed,
                void *labels_out) {
   cc_ctx *C = nullptr;
@@ -743,7 +767,7 @@ int cc_debug_local_components(const cc_csr *g, uint32_t *labels_out) {
     CCG_CUDA(cudaMemsetAsync(C->d_err, 0, sizeof(int), s));
     Counters c;
     ccg::PartMap pm(g->n, g->num_parts);
-    ccg::uf_components(G, labels_out, g->num_parts > 1 ? &pm : nullptr, 32, s, C->pool, c);
+    ccg::uf_components(G, labels_out, g->num_parts > 1 ? &pm : nullptr, C->uf, s, C->pool, c);
     int e = 0;
     CCG_CUDA(cudaMemcpyAsync(&e, C->d_err, sizeof(int), cudaMemcpyDeviceToHost, s));
     CCG_CUDA(cudaStreamSynchronize(s));

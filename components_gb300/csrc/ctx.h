@@ -24,6 +24,7 @@ struct cc_ctx {
   int geo_len = 0;
   double geo_beta = -1.0;
   bool prof = false;
+  ccg::UfTuning uf;  // hook-and-compress schedule (cc_ctx_set_tuning)
   cc_stats stats{};
   ccg::BatchCache *batch = nullptr;  // last recorded batch solve (CUDA graph)
 };

@@ -25,8 +25,15 @@ struct Csr {
 // edges whose endpoints lie in the same virtual rank are used, so parent[v] is
 // the minimum id of v's partition-local component
 // (exponential_contraction.h:391-411 FindLocalComponents).
+enum : int { kUfAuto = 0, kUfGlobal = 1, kUfTiled = 2 };
+struct UfTuning {
+  int mode = kUfAuto;            // auto: tiled when a sample shows < 50 % tile-crossing edges
+  uint32_t hub_degree = 32;      // rows above: one warp per row
+  uint32_t tile_vertices = 16384;  // vertices per CTA tile (4 bytes of shared memory each)
+  uint32_t tile_threads = 1024;
+};
 void uf_components(const Csr &g, uint32_t *parent, const PartMap *pm,
-                   uint32_t hub_degree, cudaStream_t s, cudaMemPool_t pool,
+                   const UfTuning &tu, cudaStream_t s, cudaMemPool_t pool,
                    Counters &c);
 
 // Write uint32 labels to an id_bytes-wide output array.

@@ -157,6 +157,176 @@ __global__ void k_compress(uint64_t n, uint32_t *p) {
   }
 }
 
+// ---- tiled pass ---------------------------------------------------------------
+// One CTA per tile of TILE consecutive vertices: the edges inside the tile are
+// united on a parent array in shared memory (chains resolve at shared-memory
+// latency instead of L2 latency), every vertex then stores the global id of
+// its tile-local root, and only the edges that leave the tile go to a global
+// list.  This is the reference's partition-local pass with the CTA as the
+// rank (FindLocalComponents, exponential_contraction.h:391-411).
+__device__ __forceinline__ uint32_t ts_find(volatile uint32_t *p, uint32_t v) {
+  uint32_t cur = p[v];
+  if (cur == v) return v;
+  uint32_t prev = v, next;
+  while (cur > (next = p[cur])) {
+    p[prev] = next;
+    prev = cur;
+    cur = next;
+  }
+  return cur;
+}
+__device__ __forceinline__ void ts_union(volatile uint32_t *p, uint32_t a, uint32_t b) {
+  uint32_t ra = ts_find(p, a), rb = ts_find(p, b);
+  while (ra != rb) {
+    if (ra < rb) {
+      uint32_t t = ra;
+      ra = rb;
+      rb = t;
+    }
+    uint32_t old = atomicCAS((uint32_t *)(p + ra), ra, rb);
+    if (old == ra) return;
+    ra = ts_find(p, old);
+    rb = ts_find(p, rb);
+  }
+}
+
+template <class T, bool PART>
+__global__ void __launch_bounds__(1024)
+    k_tile(uint64_t n, uint64_t m, const uint64_t *__restrict__ rp, const T *__restrict__ col,
+           uint32_t *__restrict__ p, PartMap pm, uint32_t tile, uint32_t hub_degree,
+           uint32_t *__restrict__ hubs, uint64_t hub_cap, unsigned int *__restrict__ nhubs,
+           uint2 *__restrict__ cut, uint64_t cut_cap, unsigned long long *__restrict__ ncut,
+           int *err) {
+  extern __shared__ uint32_t tile_parent[];
+  volatile uint32_t *s = tile_parent;
+  const unsigned lane = threadIdx.x & 31;
+  for (uint64_t t0 = (uint64_t)blockIdx.x * tile; t0 < n; t0 += (uint64_t)gridDim.x * tile) {
+    const uint32_t len = (uint32_t)min((uint64_t)tile, n - t0);
+    for (uint32_t i = threadIdx.x; i < len; i += blockDim.x) s[i] = i;
+    __syncthreads();
+    const uint32_t span = (len + blockDim.x - 1) / blockDim.x * blockDim.x;  // warp-uniform
+    for (uint32_t i = threadIdx.x; i < span; i += blockDim.x) {
+      const uint64_t v = t0 + i;
+      uint64_t b = 0, deg = 0;
+      uint32_t lo = 0;
+      if (i < len) {
+        Row r;
+        if (load_row(rp, v, m, err, r)) {
+          b = r.b;
+          deg = r.e - r.b;
+          if (deg > hub_degree) {
+            uint32_t slot = atomicAdd(nhubs, 1u);
+            if (slot < hub_cap) hubs[slot] = (uint32_t)v;
+            else set_err(err, kErrOverflow);
+            deg = 0;
+          }
+          if (PART) lo = part_lo(pm, (uint32_t)v);
+        }
+      }
+      uint64_t maxdeg = deg;
+#pragma unroll
+      for (int o = 16; o; o >>= 1) {
+        uint64_t y = __shfl_xor_sync(0xffffffffu, maxdeg, o);
+        maxdeg = y > maxdeg ? y : maxdeg;
+      }
+      for (uint64_t j = 0; j < maxdeg; ++j) {
+        bool emit = false;
+        uint32_t u = 0;
+        if (j < deg) {
+          uint64_t uu = (uint64_t)__ldg(col + b + j);
+          if (uu >= n) {
+            set_err(err, kErrBadId);
+          } else if (uu < v && (!PART || (uint32_t)uu >= lo)) {
+            u = (uint32_t)uu;
+            if (uu >= t0) ts_union(s, i, (uint32_t)(uu - t0));
+            else emit = true;
+          }
+        }
+        unsigned msk = __ballot_sync(0xffffffffu, emit);
+        if (msk) {
+          unsigned long long base = 0;
+          if (lane == (unsigned)(__ffs(msk) - 1)) base = atomicAdd(ncut, (unsigned long long)__popc(msk));
+          base = __shfl_sync(0xffffffffu, base, __ffs(msk) - 1);
+          if (emit) {
+            unsigned long long slot = base + __popc(msk & ((1u << lane) - 1u));
+            if (slot < cut_cap) cut[slot] = make_uint2((uint32_t)v, u);
+            else set_err(err, kErrOverflow);
+          }
+        }
+      }
+    }
+    __syncthreads();
+    for (uint32_t i = threadIdx.x; i < len; i += blockDim.x) {
+      uint32_t r = i, nx;
+      while ((nx = s[r]) != r) r = nx;
+      p[t0 + i] = (uint32_t)(t0 + r);
+    }
+    __syncthreads();
+  }
+}
+
+// Edges between tiles, on the global parent array of tile-local roots.
+__global__ void k_cut_union(const uint2 *__restrict__ cut, const unsigned long long *__restrict__ ncut,
+                            uint64_t cut_cap, uint32_t *p) {
+  uint64_t cnt = *ncut;
+  if (cnt > cut_cap) cnt = cut_cap;
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < cnt;
+       i += (uint64_t)gridDim.x * blockDim.x) {
+    uint2 e = cut[i];
+    uf_union(p, e.x, e.y);
+  }
+}
+
+// Hub rows of the tiled pass: one warp per row, every edge (no first-edge link
+// was made for them).
+template <class T, bool PART>
+__global__ void k_tile_hubs(uint64_t n, const uint64_t *__restrict__ rp, const T *__restrict__ col,
+                            uint32_t *p, PartMap pm, const uint32_t *__restrict__ hubs,
+                            uint64_t hub_cap, const unsigned int *__restrict__ nhubs, int *err) {
+  const unsigned lane = threadIdx.x & 31;
+  const uint64_t warp = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
+  const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+  uint64_t nh = *nhubs;
+  if (nh > hub_cap) nh = hub_cap;
+  for (uint64_t h = warp; h < nh; h += nwarps) {
+    uint32_t v = hubs[h];
+    uint64_t b = __ldg(rp + v), e = __ldg(rp + v + 1);  // checked by k_tile
+    uint32_t lo = PART ? part_lo(pm, v) : 0u;
+    for (uint64_t k = b + lane; k < e; k += 32) {
+      uint64_t u = (uint64_t)__ldg(col + k);
+      if (u >= n) {
+        set_err(err, kErrBadId);
+        continue;
+      }
+      if (u < v && (!PART || (uint32_t)u >= lo)) uf_union(p, v, (uint32_t)u);
+    }
+  }
+}
+
+// Share of sampled edges (u < v, same rank) that leave their tile.
+template <class T, bool PART>
+__global__ void k_cut_sample(uint64_t n, uint64_t m, const uint64_t *__restrict__ rp,
+                             const T *__restrict__ col, PartMap pm, uint32_t tile,
+                             uint32_t samples, unsigned long long *__restrict__ counts) {
+  unsigned long long tot = 0, cross = 0;
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < samples; i += gridDim.x * blockDim.x) {
+    uint64_t v = (uint64_t)i * n / samples;
+    uint64_t b = __ldg(rp + v), e = __ldg(rp + v + 1);
+    if (e < b || e > m) continue;
+    if (e - b > 64) e = b + 64;
+    uint64_t t0 = v / tile * tile;
+    uint32_t lo = PART ? part_lo(pm, (uint32_t)v) : 0u;
+    for (uint64_t k = b; k < e; ++k) {
+      uint64_t u = (uint64_t)__ldg(col + k);
+      if (u >= v || u < lo) continue;
+      ++tot;
+      cross += u < t0;
+    }
+  }
+  atomicAdd(counts, tot);
+  atomicAdd(counts + 1, cross);
+}
+
 template <class OUT>
 __global__ void k_widen(const uint32_t *__restrict__ in, OUT *__restrict__ out, uint64_t n) {
   for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < n;
@@ -219,20 +389,105 @@ void run_uf(const Csr &g, uint32_t *parent, const PartMap &pm, uint32_t hub_degr
   c.add(4, (8 * (g.n + 1) + g.n * si + 4 * g.n) + hook_bytes + 3 * g.n * 4);
 }
 
+template <class T, bool PART>
+void run_uf_tiled(const Csr &g, uint32_t *parent, const PartMap &pm, const UfTuning &tu,
+                  cudaStream_t s, cudaMemPool_t pool, Counters &c) {
+  const T *col = static_cast<const T *>(g.col);
+  const uint64_t si = (uint64_t)g.idb;
+  const uint32_t tile = tu.tile_vertices;
+  const int threads = (int)tu.tile_threads;
+  const size_t smem = 4ull * tile;
+  const void *fn = (const void *)k_tile<T, PART>;
+  if (smem > 48 * 1024)
+    CCG_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  int per_sm = 0;
+  CCG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, threads, smem));
+  if (per_sm < 1) throw Error(CC_ERR_INVALID, "tile does not fit in shared memory");
+  const uint64_t tiles = (g.n + tile - 1) / tile;
+  const unsigned grid = (unsigned)std::min<uint64_t>(tiles, (uint64_t)per_sm * kSMs);
+  const uint64_t hub_cap = g.m / (tu.hub_degree + 1) + 1;
+  const uint64_t cut_cap = g.m + 1;
+  DevBuf hubs(4 * hub_cap, s, pool), nh(4, s, pool), cut(8 * cut_cap, s, pool), ncut(8, s, pool);
+  CCG_CUDA(cudaMemsetAsync(nh.p, 0, 4, s));
+  CCG_CUDA(cudaMemsetAsync(ncut.p, 0, 8, s));
+  // tile pass: offsets, every id once, own parent written once (the parent
+  // chains stay in shared memory), cut edges counted at the union pass
+  const uint64_t tile_bytes = 8 * (g.n + 1) + g.m * si + 4 * g.n;
+  cudaEvent_t t0 = c.tic(s);
+  k_tile<T, PART><<<grid, threads, smem, s>>>(g.n, g.m, g.rp, col, parent, pm, tile, tu.hub_degree,
+                                              hubs.as<uint32_t>(), hub_cap, nh.as<unsigned int>(),
+                                              cut.as<uint2>(), cut_cap,
+                                              ncut.as<unsigned long long>(), g.err);
+  CCG_LAUNCH_CHECK();
+  c.toc(s, "uf_tile", t0, tile_bytes);
+  cudaEvent_t t1 = c.tic(s);
+  k_cut_union<<<kSMs * 16, kBlock, 0, s>>>(cut.as<uint2>(), ncut.as<unsigned long long>(), cut_cap,
+                                           parent);
+  CCG_LAUNCH_CHECK();
+  c.toc(s, "uf_cut_union", t1, 0);
+  cudaEvent_t t2 = c.tic(s);
+  k_tile_hubs<T, PART><<<kSMs * 8, kBlock, 0, s>>>(g.n, g.rp, col, parent, pm, hubs.as<uint32_t>(),
+                                                   hub_cap, nh.as<unsigned int>(), g.err);
+  CCG_LAUNCH_CHECK();
+  c.toc(s, "uf_hook_hubs", t2, 0);
+  cudaEvent_t t3 = c.tic(s);
+  k_compress<<<grid_for(g.n, kBlock, kSMs * 32), kBlock, 0, s>>>(g.n, parent);
+  CCG_LAUNCH_CHECK();
+  c.toc(s, "uf_compress", t3, 3 * g.n * 4);
+  c.add(4, tile_bytes + 3 * g.n * 4);
+}
+
+// Share of tile-crossing edges on a sample of 8192 rows (one small readback).
+template <class T, bool PART>
+double cut_share(const Csr &g, const PartMap &pm, uint32_t tile, cudaStream_t s,
+                 cudaMemPool_t pool, Counters &c) {
+  DevBuf cnt(16, s, pool);
+  CCG_CUDA(cudaMemsetAsync(cnt.p, 0, 16, s));
+  const uint32_t samples = (uint32_t)std::min<uint64_t>(g.n, 8192);
+  k_cut_sample<T, PART><<<(samples + 255) / 256, 256, 0, s>>>(
+      g.n, g.m, g.rp, static_cast<const T *>(g.col), pm, tile, samples,
+      cnt.as<unsigned long long>());
+  CCG_LAUNCH_CHECK();
+  unsigned long long h[2] = {0, 0};
+  CCG_CUDA(cudaMemcpyAsync(h, cnt.p, 16, cudaMemcpyDeviceToHost, s));
+  CCG_CUDA(cudaStreamSynchronize(s));
+  c.add(1, 0);
+  return h[0] ? (double)h[1] / (double)h[0] : 0.0;
+}
+
+template <class T, bool PART>
+void run_uf_mode(const Csr &g, uint32_t *parent, const PartMap &pm, const UfTuning &tu,
+                 cudaStream_t s, cudaMemPool_t pool, Counters &c) {
+  int mode = tu.mode;
+  if (mode == kUfAuto) {
+    // the tiled pass wins when most edges stay inside their tile (grids,
+    // geometric and angularly ordered graphs); random graphs stay global
+    mode = (g.n >= 4ull * tu.tile_vertices &&
+            cut_share<T, PART>(g, pm, tu.tile_vertices, s, pool, c) < 0.5)
+               ? kUfTiled
+               : kUfGlobal;
+  }
+  if (mode == kUfTiled) run_uf_tiled<T, PART>(g, parent, pm, tu, s, pool, c);
+  else run_uf<T, PART>(g, parent, pm, tu.hub_degree, s, pool, c);
+}
+
 }  // namespace
 
-void uf_components(const Csr &g, uint32_t *parent, const PartMap *pm, uint32_t hub_degree,
+void uf_components(const Csr &g, uint32_t *parent, const PartMap *pm, const UfTuning &tu_in,
                    cudaStream_t s, cudaMemPool_t pool, Counters &c) {
   if (g.n == 0) return;
-  if (hub_degree < 1) hub_degree = 1;
+  UfTuning tu = tu_in;
+  if (tu.hub_degree < 1) tu.hub_degree = 32;
+  if (tu.tile_vertices == 0) tu.tile_vertices = 16384;
+  if (tu.tile_threads == 0) tu.tile_threads = 1024;
   PartMap p = pm ? *pm : PartMap(g.n, 1);
   bool part = pm != nullptr && !(pm->rm == 0 && pm->q == g.n);
   if (g.idb == 8) {
-    if (part) run_uf<uint64_t, true>(g, parent, p, hub_degree, s, pool, c);
-    else run_uf<uint64_t, false>(g, parent, p, hub_degree, s, pool, c);
+    if (part) run_uf_mode<uint64_t, true>(g, parent, p, tu, s, pool, c);
+    else run_uf_mode<uint64_t, false>(g, parent, p, tu, s, pool, c);
   } else {
-    if (part) run_uf<uint32_t, true>(g, parent, p, hub_degree, s, pool, c);
-    else run_uf<uint32_t, false>(g, parent, p, hub_degree, s, pool, c);
+    if (part) run_uf_mode<uint32_t, true>(g, parent, p, tu, s, pool, c);
+    else run_uf_mode<uint32_t, false>(g, parent, p, tu, s, pool, c);
   }
 }
 

@@ -44,6 +44,18 @@ class Context:
     def stream_handle(self) -> int:
         return _lib.gpu().cc_ctx_stream(self._h) or 0
 
+    def set_tuning(self, hook_mode: int = 0, tile_vertices: int = 0, tile_threads: int = 0,
+                   hub_degree: int = 0) -> None:
+        """Hook-and-compress schedule (include/cc_gpu.h cc_tuning); 0 keeps a default."""
+        t = _lib.cc_tuning(hook_mode, tile_vertices, tile_threads, hub_degree)
+        _lib.check(_lib.gpu().cc_ctx_set_tuning(self._h, C.byref(t)))
+
+    def tuning(self) -> dict:
+        t = _lib.cc_tuning()
+        _lib.check(_lib.gpu().cc_ctx_get_tuning(self._h, C.byref(t)))
+        return {"hook_mode": t.hook_mode, "tile_vertices": t.tile_vertices,
+                "tile_threads": t.tile_threads, "hub_degree": t.hub_degree}
+
     def set_profiling(self, on: bool) -> None:
         _lib.check(_lib.gpu().cc_ctx_set_profiling(self._h, int(on)))
 

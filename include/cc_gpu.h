@@ -210,6 +210,20 @@ int cc_ctx_set_profiling(cc_ctx *ctx, int on);
 /* The cudaStream_t the context launches on. */
 void *cc_ctx_stream(cc_ctx *ctx);
 
+/* Schedule of the hook-and-compress pass (partition-local components, base
+   cases, CC_ALLREDUCE).  Zero fields keep the defaults. */
+enum { CC_HOOK_AUTO = 0, CC_HOOK_GLOBAL = 1, CC_HOOK_TILED = 2 };
+typedef struct cc_tuning {
+  uint32_t hook_mode;      /* CC_HOOK_*: auto picks tiled when a sample of rows
+                              shows < 50 % tile-crossing edges */
+  uint32_t tile_vertices;  /* vertices per CTA tile, 4 bytes of shared memory
+                              each (default 16384, at most 56K) */
+  uint32_t tile_threads;   /* CTA size of the tiled pass (default 1024) */
+  uint32_t hub_degree;     /* rows above go one warp per row (default 32) */
+} cc_tuning;
+int cc_ctx_set_tuning(cc_ctx *ctx, const cc_tuning *t);
+int cc_ctx_get_tuning(cc_ctx *ctx, cc_tuning *t);
+
 #ifdef __cplusplus
 }
 #endif

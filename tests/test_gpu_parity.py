@@ -147,7 +147,7 @@ def test_context_reuse_and_stats(cuda):
     st = ctx.stats()
     assert st["num_components"] == len(np.unique(want))
     assert st["kernel_launches"] > 0 and st["bytes_algorithmic"] > 0
-    assert "uf_hook" in st["kernels"]
+    assert "uf_hook" in st["kernels"] or "uf_tile" in st["kernels"]
     arena = ctx.arena_bytes()
     gpu_labels(G, "exp", 1, "device", ctx=ctx)
     assert ctx.arena_bytes() == arena  # steady state: the pool is reused
@@ -162,3 +162,22 @@ def test_stream_interop(cuda):
     G = cc.gen_gnm(5000, 5000, seed=2, id_bytes=4)
     assert np.array_equal(gpu_labels(G, "exp", 4, "device", ctx=ctx), oracle.uf_labels(G))
     ctx.close()
+
+
+@pytest.mark.parametrize("mode", [_lib.CC_HOOK_GLOBAL, _lib.CC_HOOK_TILED])
+def test_hook_modes_agree(cuda, mode):
+    """Global and tiled hook passes give the same labels, also with ranks,
+    hub rows, tiles smaller than a rank and ranks smaller than a tile."""
+    graphs = [cc.gen_grid(700, 500, 0.5, seed=6), cc.gen_gnm(60000, 80000, seed=6, id_bytes=8),
+              cc.from_edges(40000, [(5, i) for i in range(6, 40000, 3)] + [(i, i + 1) for i in range(0, 39999, 7)]),
+              cc.gen_grid(64, 2000, 0.7, seed=2)]
+    for tile in (1024, 16384):
+        ctx = cc.Context(0)
+        ctx.set_tuning(hook_mode=mode, tile_vertices=tile, tile_threads=256, hub_degree=16)
+        for G in graphs:
+            want = oracle.uf_labels(G)
+            for algo in ("allreduce", "exp"):
+                for P in (1, 3, 100):
+                    got = gpu_labels(G, algo, P, "device", cc.Config(seed=1001), ctx=ctx)
+                    assert np.array_equal(got, want), (mode, tile, G.n, algo, P)
+        ctx.close()
