@@ -184,6 +184,10 @@ def main():
     ap.add_argument("--no-check", action="store_true")
     ap.add_argument("--grid", type=int, default=GRID_X,
                     help="grid side (default 8192; smaller sides are for ncu captures)")
+    ap.add_argument("--hook-mode", type=int, default=0,
+                    help="hook schedule (cc_tuning.hook_mode: 0 auto, 1 global, 2 tiled)")
+    ap.add_argument("--tile", type=int, default=0, help="cc_tuning.tile_vertices (0 = default)")
+    ap.add_argument("--tile-threads", type=int, default=0, help="cc_tuning.tile_threads")
     args = ap.parse_args()
     rank, world, local = dist_env()
 
@@ -228,6 +232,7 @@ def main():
     n, m = G.n, G.m
     conf = cc.Config(seed=ALGO_SEED)
     ctx = cc.Context(local)
+    ctx.set_tuning(hook_mode=args.hook_mode, tile_vertices=args.tile, tile_threads=args.tile_threads)
     stream = torch.cuda.ExternalStream(ctx.stream_handle)
     D = G.to_device(f"cuda:{local}")
     lab = torch.empty(n, dtype=torch.int32, device=f"cuda:{local}")

@@ -132,6 +132,7 @@ GEN_SYMBOLS = {
     "cc_gen_grid": (C.c_int, [_U64, _U64, C.c_double, _U64, _U32, C.POINTER(cc_host_graph)]),
     "cc_gen_rhg": (C.c_int, [_U64, C.c_double, C.c_double, _U64, _U32, C.POINTER(cc_host_graph)]),
     "cc_host_graph_free": (None, [C.POINTER(cc_host_graph)]),
+    "cc_gen_rhg_radius": (C.c_double, [_U64, C.c_double, C.c_double]),
 }
 
 _gpu = None

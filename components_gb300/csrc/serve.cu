@@ -1,0 +1,557 @@
+// serve.cu - continuous-batching CC server (include/cc_serve.h).
+//
+// No counterpart in the reference.  One worker thread per server:
+//   admission  requests wait on the host in arrival order until their device
+//              bytes fit the HBM budget; then their CSR is copied to the device
+//              on the copy stream (an event marks the copy)
+//   batching   whenever one of the compute streams has finished its previous
+//              batch, every staged request (up to max_batch_graphs) is
+//              coalesced into one launch on it: graphs up to smem_max_n
+//              vertices are solved one CTA each (union-find in shared memory,
+//              CTAs pull graphs from a queue), larger ones by the grid-wide
+//              hook-and-compress; the stream first waits on the copy events
+//   completion a host callback after the batch marks its requests done
+//   collect    the client copies the labels back, which frees the request's
+//              device memory and budget
+// Copies of new requests overlap the batches already running, and two
+// compute streams let consecutive batches overlap on the device.
+#include <algorithm>
+#include <atomic>
+#include <chrono>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <memory>
+#include <mutex>
+#include <thread>
+#include <unordered_map>
+#include <vector>
+
+#include "../../include/cc_serve.h"
+#include "ctx.h"
+
+namespace ccg {
+struct Server;
+namespace {
+
+double now_s() {
+  using namespace std::chrono;
+  return duration<double>(steady_clock::now().time_since_epoch()).count();
+}
+
+struct GraphDesc {
+  const uint64_t *rp;  // local offsets (rp[0] == 0)
+  const void *col;     // local ids
+  uint32_t *labels;    // n labels, then the request's error word
+  uint64_t m;
+  uint32_t n;
+  uint32_t idb;
+};
+
+__device__ __forceinline__ uint32_t sv_find(volatile uint32_t *p, uint32_t v) {
+  uint32_t cur = p[v];
+  if (cur == v) return v;
+  uint32_t prev = v, next;
+  while (cur > (next = p[cur])) {
+    p[prev] = next;
+    prev = cur;
+    cur = next;
+  }
+  return cur;
+}
+__device__ __forceinline__ void sv_union(volatile uint32_t *p, uint32_t a, uint32_t b) {
+  uint32_t ra = sv_find(p, a), rb = sv_find(p, b);
+  while (ra != rb) {
+    if (ra < rb) {
+      uint32_t t = ra;
+      ra = rb;
+      rb = t;
+    }
+    uint32_t old = atomicCAS((uint32_t *)(p + ra), ra, rb);
+    if (old == ra) return;
+    ra = sv_find(p, old);
+    rb = sv_find(p, rb);
+  }
+}
+
+// One CTA per small graph of the batch; persistent CTAs pull descriptors.
+__global__ void k_serve_smem(const GraphDesc *__restrict__ descs, uint32_t count,
+                             unsigned int *__restrict__ queue) {
+  extern __shared__ uint32_t sp[];
+  __shared__ uint32_t item;
+  for (;;) {
+    if (threadIdx.x == 0) item = atomicAdd(queue, 1u);
+    __syncthreads();
+    const uint32_t it = item;
+    __syncthreads();
+    if (it >= count) return;
+    const GraphDesc d = descs[it];
+    int *err = reinterpret_cast<int *>(d.labels + d.n);
+    volatile uint32_t *p = sp;
+    for (uint32_t v = threadIdx.x; v < d.n; v += blockDim.x) p[v] = v;
+    __syncthreads();
+    for (uint32_t v = threadIdx.x; v < d.n; v += blockDim.x) {
+      uint64_t b = d.rp[v], e = d.rp[v + 1];
+      if (e < b || e > d.m) {
+        set_err(err, kErrBadOffsets);
+        continue;
+      }
+      for (uint64_t k = b; k < e; ++k) {
+        uint64_t u = d.idb == 8 ? static_cast<const uint64_t *>(d.col)[k]
+                                : static_cast<const uint32_t *>(d.col)[k];
+        if (u >= d.n) {
+          set_err(err, kErrBadId);
+          continue;
+        }
+        if (u < v) sv_union(p, v, (uint32_t)u);
+      }
+    }
+    __syncthreads();
+    for (uint32_t v = threadIdx.x; v < d.n; v += blockDim.x) {
+      uint32_t r = v, nx;
+      while ((nx = p[r]) != r) r = nx;
+      d.labels[v] = r;
+    }
+    __syncthreads();
+  }
+}
+
+enum ReqState { kWaiting = 0, kStaged = 1, kLaunched = 2, kDone = 3 };
+
+struct Req {
+  uint64_t id = 0;
+  cc_csr g{};
+  uint64_t need = 0;
+  double t_submit = 0, t_admit = 0, t_done = 0;
+  DevBuf rp, col, lab;  // lab: n labels + error word
+  cudaEvent_t copied = nullptr;
+  std::atomic<int> state{kWaiting};
+  uint32_t batch_id = 0, batch_size = 0;
+  bool tiled = false;  // large graph: tiled hook pass (estimated on the host)
+};
+
+struct Batch {
+  std::vector<Req *> reqs;
+  Server *srv = nullptr;
+  int stream = 0;
+};
+
+}  // namespace
+
+struct Server {
+  int device = 0;
+  cc_serve_config cfg{};
+  cudaMemPool_t pool = nullptr;
+  cudaStream_t copy_stream = nullptr, collect_stream = nullptr;
+  std::vector<cudaStream_t> streams;
+  std::vector<std::atomic<int>> busy;  // batches in flight per compute stream
+  std::vector<DevBuf> desc_dev, queue_dev;
+  std::vector<GraphDesc *> desc_host;  // pinned
+  std::mutex mu;
+  std::condition_variable cv_worker, cv_done;
+  std::deque<Req *> waiting, staged;
+  std::unordered_map<uint64_t, std::unique_ptr<Req>> reqs;
+  uint64_t next_id = 1, used = 0, peak = 0, batches = 0, submitted = 0, completed = 0,
+           collected = 0;
+  bool stop = false;
+  std::thread worker;
+  std::atomic<int> inflight{0};
+
+  explicit Server(size_t ns) : busy(ns) {}
+
+  static void CUDART_CB on_batch_done(void *arg) {
+    std::unique_ptr<Batch> b(static_cast<Batch *>(arg));
+    Server *s = b->srv;
+    double t = now_s();
+    {
+      std::lock_guard<std::mutex> lk(s->mu);
+      for (Req *r : b->reqs) {
+        r->t_done = t;
+        r->state = kDone;
+      }
+      s->completed += b->reqs.size();
+    }
+    s->busy[b->stream]--;
+    s->inflight--;
+    s->cv_done.notify_all();
+    s->cv_worker.notify_all();
+  }
+
+  uint64_t bytes_needed(const cc_csr &g) const {
+    uint64_t b = 8 * (g.n + 1) + (uint64_t)g.id_bytes * g.m_dir + 4 * (g.n + 1) + 3 * 256;
+    if (g.n > cfg.smem_max_n) b += 8 * (g.m_dir + 1) + 4 * (g.m_dir / 33 + 1) + 4096;  // hook scratch
+    return b;
+  }
+
+  // Share of sampled rows' edges (u < v) leaving a 16K-vertex tile, from the
+  // host CSR: decides the hook schedule of a large graph without a device
+  // round trip.
+  static bool prefers_tiles(const cc_csr &g) {
+    const uint64_t tile = 16384, samples = 256;
+    if (g.n < 4 * tile) return false;
+    uint64_t tot = 0, cross = 0;
+    for (uint64_t i = 0; i < samples; ++i) {
+      uint64_t v = i * g.n / samples;
+      for (uint64_t k = g.row_ptr[v]; k < g.row_ptr[v + 1] && k < g.row_ptr[v] + 64; ++k) {
+        uint64_t u = g.id_bytes == 8 ? static_cast<const uint64_t *>(g.col)[k]
+                                     : static_cast<const uint32_t *>(g.col)[k];
+        if (u >= v) continue;
+        ++tot;
+        cross += u < v / tile * tile;
+      }
+    }
+    return tot && cross * 2 < tot;
+  }
+
+  void stage(Req *r) {  // worker thread, no lock held
+    const cc_csr &g = r->g;
+    r->rp.alloc(8 * (g.n + 1), copy_stream, pool);
+    r->col.alloc((size_t)g.id_bytes * (g.m_dir ? g.m_dir : 1), copy_stream, pool);
+    r->lab.alloc(4 * (g.n + 1), copy_stream, pool);
+    CCG_CUDA(cudaMemcpyAsync(r->rp.p, g.row_ptr, 8 * (g.n + 1), cudaMemcpyHostToDevice, copy_stream));
+    if (g.m_dir)
+      CCG_CUDA(cudaMemcpyAsync(r->col.p, g.col, (size_t)g.id_bytes * g.m_dir,
+                               cudaMemcpyHostToDevice, copy_stream));
+    CCG_CUDA(cudaMemsetAsync(r->lab.as<uint32_t>() + g.n, 0, 4, copy_stream));
+    CCG_CUDA(cudaEventCreateWithFlags(&r->copied, cudaEventDisableTiming));
+    CCG_CUDA(cudaEventRecord(r->copied, copy_stream));
+    r->tiled = g.n > cfg.smem_max_n && prefers_tiles(g);
+  }
+
+  void launch(std::vector<Req *> &batch, int si) {  // worker thread, no lock held
+    cudaStream_t s = streams[si];
+    std::stable_partition(batch.begin(), batch.end(),
+                          [&](Req *r) { return r->g.n <= cfg.smem_max_n; });
+    GraphDesc *hd = desc_host[si];
+    uint32_t nsmall = 0;
+    for (size_t i = 0; i < batch.size(); ++i) {
+      Req *r = batch[i];
+      CCG_CUDA(cudaStreamWaitEvent(s, r->copied, 0));
+      hd[i] = GraphDesc{r->rp.as<uint64_t>(), r->col.p, r->lab.as<uint32_t>(), r->g.m_dir,
+                        (uint32_t)r->g.n, r->g.id_bytes};
+      if (r->g.n <= cfg.smem_max_n) ++nsmall;
+    }
+    Counters c;
+    if (nsmall) {
+      CCG_CUDA(cudaMemcpyAsync(desc_dev[si].p, hd, sizeof(GraphDesc) * nsmall,
+                               cudaMemcpyHostToDevice, s));
+      CCG_CUDA(cudaMemsetAsync(queue_dev[si].p, 0, 4, s));
+      const size_t smem = 4ull * cfg.smem_max_n;
+      if (smem > 48 * 1024)
+        CCG_CUDA(cudaFuncSetAttribute(k_serve_smem, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)smem));
+      int per_sm = 1;
+      CCG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_serve_smem, 256, smem));
+      unsigned grid = (unsigned)std::min<uint64_t>((uint64_t)std::max(per_sm, 1) * kSMs, nsmall);
+      k_serve_smem<<<grid, 256, smem, s>>>(desc_dev[si].as<GraphDesc>(), nsmall,
+                                           queue_dev[si].as<unsigned int>());
+      CCG_LAUNCH_CHECK();
+    }
+    for (size_t i = nsmall; i < batch.size(); ++i) {
+      Req *r = batch[i];
+      Csr G;
+      G.n = r->g.n;
+      G.m = r->g.m_dir;
+      G.rp = r->rp.as<uint64_t>();
+      G.col = r->col.p;
+      G.idb = (int)r->g.id_bytes;
+      G.err = reinterpret_cast<int *>(r->lab.as<uint32_t>() + r->g.n);
+      UfTuning tu;
+      tu.mode = r->tiled ? kUfTiled : kUfGlobal;
+      uf_components(G, r->lab.as<uint32_t>(), nullptr, tu, s, pool, c);
+    }
+    uint32_t bid;
+    {
+      std::lock_guard<std::mutex> lk(mu);
+      bid = (uint32_t)++batches;
+    }
+    for (Req *r : batch) {
+      r->batch_id = bid;
+      r->batch_size = (uint32_t)batch.size();
+      r->state = kLaunched;
+    }
+    Batch *b = new Batch{batch, this, si};
+    busy[si]++;
+    inflight++;
+    CCG_CUDA(cudaLaunchHostFunc(s, on_batch_done, b));
+  }
+
+  void loop() {
+    cudaSetDevice(device);
+    std::unique_lock<std::mutex> lk(mu);
+    for (;;) {
+      cv_worker.wait_for(lk, std::chrono::microseconds(500), [&] {
+        bool admit = !waiting.empty() && used + waiting.front()->need <= cfg.hbm_budget_bytes;
+        bool free_stream = false;
+        for (auto &b : busy) free_stream |= b.load() == 0;
+        return stop || admit || (!staged.empty() && free_stream);
+      });
+      if (stop && waiting.empty() && staged.empty()) break;
+      // admission, in arrival order, while the budget allows
+      while (!waiting.empty() && used + waiting.front()->need <= cfg.hbm_budget_bytes) {
+        Req *r = waiting.front();
+        waiting.pop_front();
+        used += r->need;
+        peak = std::max(peak, used);
+        r->t_admit = now_s();
+        lk.unlock();
+        try {
+          stage(r);
+        } catch (...) {
+          lk.lock();
+          used -= r->need;
+          r->t_done = now_s();
+          r->state = kDone;  // collect reports the failure through the error word
+          cv_done.notify_all();
+          continue;
+        }
+        lk.lock();
+        r->state = kStaged;
+        staged.push_back(r);
+      }
+      // batching: every free compute stream takes the staged requests
+      for (size_t si = 0; si < streams.size() && !staged.empty(); ++si) {
+        if (busy[si].load() > 0) continue;
+        std::vector<Req *> batch;
+        while (!staged.empty() && batch.size() < cfg.max_batch_graphs) {
+          batch.push_back(staged.front());
+          staged.pop_front();
+        }
+        lk.unlock();
+        try {
+          launch(batch, (int)si);
+        } catch (...) {
+          // leave the requests failed; their error word stays 0, so mark them
+          // done with a recorded error below
+          lk.lock();
+          for (Req *r : batch) {
+            r->t_done = now_s();
+            r->state = kDone;
+            r->batch_id = 0;
+          }
+          cv_done.notify_all();
+          continue;
+        }
+        lk.lock();
+      }
+    }
+  }
+};
+
+}  // namespace ccg
+
+struct cc_server {
+  std::unique_ptr<ccg::Server> s;
+};
+
+extern "C" {
+
+void cc_serve_config_default(cc_serve_config *c) {
+  if (!c) return;
+  std::memset(c, 0, sizeof(*c));
+  c->hbm_budget_bytes = 120ull << 30;
+  c->max_batch_graphs = 1024;
+  c->compute_streams = 2;
+  c->smem_max_n = 16384;
+}
+
+double cc_serve_now(void) { return ccg::now_s(); }
+
+int cc_serve_create(cc_server **out, int device, const cc_serve_config *cin) {
+  using namespace ccg;
+  if (!out) return CC_ERR_INVALID;
+  *out = nullptr;
+  cc_serve_config cfg;
+  if (cin) cfg = *cin;
+  else cc_serve_config_default(&cfg);
+  if (!cfg.max_batch_graphs || !cfg.compute_streams || cfg.compute_streams > 8 ||
+      cfg.smem_max_n == 0 || cfg.smem_max_n > 56 * 1024)
+    return CC_ERR_INVALID;
+  std::unique_ptr<cc_server> h(new cc_server());
+  int rc = guard([&] {
+    CCG_CUDA(cudaSetDevice(device));
+    h->s.reset(new Server(cfg.compute_streams));
+    Server &s = *h->s;
+    s.device = device;
+    s.cfg = cfg;
+    cudaMemPoolProps props;
+    std::memset(&props, 0, sizeof(props));
+    props.allocType = cudaMemAllocationTypePinned;
+    props.location.type = cudaMemLocationTypeDevice;
+    props.location.id = device;
+    CCG_CUDA(cudaMemPoolCreate(&s.pool, &props));
+    uint64_t thr = ~0ull;
+    CCG_CUDA(cudaMemPoolSetAttribute(s.pool, cudaMemPoolAttrReleaseThreshold, &thr));
+    CCG_CUDA(cudaStreamCreateWithFlags(&s.copy_stream, cudaStreamNonBlocking));
+    CCG_CUDA(cudaStreamCreateWithFlags(&s.collect_stream, cudaStreamNonBlocking));
+    s.streams.resize(cfg.compute_streams);
+    s.desc_dev.resize(cfg.compute_streams);
+    s.queue_dev.resize(cfg.compute_streams);
+    s.desc_host.resize(cfg.compute_streams, nullptr);
+    for (uint32_t i = 0; i < cfg.compute_streams; ++i) {
+      CCG_CUDA(cudaStreamCreateWithFlags(&s.streams[i], cudaStreamNonBlocking));
+      s.desc_dev[i].alloc(sizeof(GraphDesc) * cfg.max_batch_graphs, s.copy_stream, s.pool);
+      s.queue_dev[i].alloc(4, s.copy_stream, s.pool);
+      CCG_CUDA(cudaHostAlloc(&s.desc_host[i], sizeof(GraphDesc) * cfg.max_batch_graphs,
+                             cudaHostAllocDefault));
+    }
+    CCG_CUDA(cudaStreamSynchronize(s.copy_stream));
+    s.worker = std::thread([&s] { s.loop(); });
+  });
+  if (rc != CC_OK) return rc;
+  *out = h.release();
+  return CC_OK;
+}
+
+int cc_serve_destroy(cc_server *h) {
+  using namespace ccg;
+  if (!h) return CC_ERR_INVALID;
+  Server &s = *h->s;
+  {
+    std::lock_guard<std::mutex> lk(s.mu);
+    s.stop = true;
+  }
+  s.cv_worker.notify_all();
+  if (s.worker.joinable()) s.worker.join();
+  cudaSetDevice(s.device);
+  for (auto st : s.streams) cudaStreamSynchronize(st);
+  cudaStreamSynchronize(s.copy_stream);
+  while (s.inflight.load() > 0) std::this_thread::sleep_for(std::chrono::microseconds(100));
+  for (auto &kv : s.reqs) {
+    if (kv.second->copied) cudaEventDestroy(kv.second->copied);
+  }
+  s.reqs.clear();
+  s.desc_dev.clear();
+  s.queue_dev.clear();
+  cudaStreamSynchronize(s.copy_stream);
+  for (auto p : s.desc_host)
+    if (p) cudaFreeHost(p);
+  for (auto st : s.streams) cudaStreamDestroy(st);
+  cudaStreamDestroy(s.copy_stream);
+  cudaStreamDestroy(s.collect_stream);
+  cudaMemPoolDestroy(s.pool);
+  delete h;
+  return CC_OK;
+}
+
+int cc_serve_submit(cc_server *h, const cc_csr *g, uint64_t *ticket) {
+  using namespace ccg;
+  if (!h || !g || !ticket) return CC_ERR_INVALID;
+  if (g->where != CC_HOST || (g->id_bytes != 4 && g->id_bytes != 8) || g->reserved)
+    return CC_ERR_INVALID;
+  if (g->n == 0 || g->n >= 0xffffffffull) return CC_ERR_UNSUPPORTED;
+  if (!g->row_ptr || (g->m_dir && !g->col)) return CC_ERR_INVALID;
+  Server &s = *h->s;
+  std::unique_ptr<Req> r(new Req());
+  r->g = *g;
+  r->need = s.bytes_needed(*g);
+  if (r->need > s.cfg.hbm_budget_bytes) return CC_ERR_BUSY;
+  r->t_submit = now_s();
+  {
+    std::lock_guard<std::mutex> lk(s.mu);
+    r->id = s.next_id++;
+    *ticket = r->id;
+    s.waiting.push_back(r.get());
+    s.reqs[r->id] = std::move(r);
+    s.submitted++;
+  }
+  s.cv_worker.notify_all();
+  return CC_OK;
+}
+
+static int collect(cc_server *h, uint64_t ticket, void *labels_out, int *done, double timeout_s,
+                   bool block, cc_serve_ticket_info *info) {
+  using namespace ccg;
+  if (!h || !labels_out) return CC_ERR_INVALID;
+  Server &s = *h->s;
+  Req *r = nullptr;
+  {
+    std::unique_lock<std::mutex> lk(s.mu);
+    auto it = s.reqs.find(ticket);
+    if (it == s.reqs.end()) return CC_ERR_INVALID;
+    r = it->second.get();
+    if (r->state.load() != kDone) {
+      if (!block) {
+        if (done) *done = 0;
+        return CC_OK;
+      }
+      auto pred = [&] { return r->state.load() == kDone; };
+      if (timeout_s > 0) {
+        if (!s.cv_done.wait_for(lk, std::chrono::duration<double>(timeout_s), pred))
+          return CC_ERR_TIMEOUT;
+      } else {
+        s.cv_done.wait(lk, pred);
+      }
+    }
+  }
+  // done: copy the labels and the error word, then retire the request
+  int rc = guard([&] {
+    CCG_CUDA(cudaSetDevice(s.device));
+    const uint64_t n = r->g.n;
+    if (!r->lab.p) throw Error(CC_ERR_CUDA, "request failed before launch");
+    std::vector<uint32_t> tmp;
+    uint32_t *dst = static_cast<uint32_t *>(labels_out);
+    if (r->g.id_bytes == 8) {
+      tmp.resize(n);
+      dst = tmp.data();
+    }
+    int err = 0;
+    CCG_CUDA(cudaMemcpyAsync(dst, r->lab.p, 4 * n, cudaMemcpyDeviceToHost, s.collect_stream));
+    CCG_CUDA(cudaMemcpyAsync(&err, r->lab.as<uint32_t>() + n, 4, cudaMemcpyDeviceToHost,
+                             s.collect_stream));
+    CCG_CUDA(cudaStreamSynchronize(s.collect_stream));
+    if (r->g.id_bytes == 8) {
+      uint64_t *o = static_cast<uint64_t *>(labels_out);
+      for (uint64_t v = 0; v < n; ++v) o[v] = tmp[v];
+    }
+    if (err) throw Error(CC_ERR_INVALID, "CSR check failed in a served request");
+  });
+  if (info) {
+    info->submit_s = r->t_submit;
+    info->admit_s = r->t_admit;
+    info->done_s = r->t_done;
+    info->batch_id = r->batch_id;
+    info->batch_size = r->batch_size;
+  }
+  std::unique_ptr<Req> retired;
+  {
+    std::lock_guard<std::mutex> lk(s.mu);
+    auto it = s.reqs.find(ticket);
+    retired = std::move(it->second);
+    s.reqs.erase(it);
+    s.used -= retired->need;
+    s.collected++;
+  }
+  // CUDA calls outside the lock: the completion callbacks take it
+  if (retired->copied) cudaEventDestroy(retired->copied);
+  retired.reset();
+  s.cv_worker.notify_all();
+  if (done) *done = 1;
+  return rc;
+}
+
+int cc_serve_poll(cc_server *h, uint64_t ticket, void *labels_out, int *done,
+                  cc_serve_ticket_info *info) {
+  return collect(h, ticket, labels_out, done, 0.0, false, info);
+}
+
+int cc_serve_wait(cc_server *h, uint64_t ticket, void *labels_out, double timeout_s,
+                  cc_serve_ticket_info *info) {
+  return collect(h, ticket, labels_out, nullptr, timeout_s, true, info);
+}
+
+int cc_serve_get_stats(cc_server *h, cc_serve_stats *out) {
+  if (!h || !out) return CC_ERR_INVALID;
+  ccg::Server &s = *h->s;
+  std::lock_guard<std::mutex> lk(s.mu);
+  out->submitted = s.submitted;
+  out->completed = s.completed;
+  out->collected = s.collected;
+  out->batches = s.batches;
+  out->bytes_in_use = s.used;
+  out->peak_bytes_in_use = s.peak;
+  out->waiting = s.waiting.size();
+  return CC_OK;
+}
+
+}  // extern "C"

@@ -42,6 +42,8 @@ int cc_gen_grid(uint64_t X, uint64_t Y, double p, uint64_t seed, uint32_t id_byt
    degree avg_deg.  Vertex ids follow the angular order. */
 int cc_gen_rhg(uint64_t n, double avg_deg, double gamma, uint64_t seed, uint32_t id_bytes,
                cc_host_graph *out);
+/* The disk radius R that cc_gen_rhg uses for (n, avg_deg, gamma). */
+double cc_gen_rhg_radius(uint64_t n, double avg_deg, double gamma);
 
 void cc_host_graph_free(cc_host_graph *g);
 

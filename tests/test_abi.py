@@ -35,7 +35,9 @@ def _exported(lib: Path) -> set[str]:
 
 
 def test_gpu_library_exports_every_declared_symbol():
-    declared = _declared("cc_gpu.h") | _declared("cc_gpu_debug.h")
+    declared = set()
+    for h in ("cc_gpu.h", "cc_gpu_debug.h", "cc_batch.h", "cc_serve.h"):
+        declared |= _declared(h)
     exported = _exported(_lib.gpu_lib_path())
     missing = declared - exported
     assert not missing, missing
