@@ -174,6 +174,199 @@ def cpu_reference_run(G, steps, warmup, sample_rows=None):
     return m / mean / 1e9, mean, threads, sample
 
 
+def _timed_solves(solver, D, lab, steps, warmup, ctx):
+    for _ in range(warmup):
+        solver.FindComponents(D, lab)
+    ctx.set_profiling(True)
+    ms, kern = [], {}
+    for _ in range(steps):
+        solver.FindComponents(D, lab)
+        st = ctx.stats()
+        ms.append(st["solve_ms"])
+        for k, v in st["kernels"].items():
+            a = kern.setdefault(k, {"launches": 0, "ms": 0.0, "bytes": 0})
+            for f in a:
+                a[f] += v[f]
+    ctx.set_profiling(False)
+    return ms, kern, st
+
+
+def workload_single(args, name):
+    """G(2^20, 2^22) with 64-bit ids, or the 2^k-vertex RHG (d = 16, gamma = 2.6):
+    one JSON line per (algo option, virtual ranks)."""
+    import torch
+    import components_gb300 as cc
+    import oracle
+    t0 = time.time()
+    if name == "gnm":
+        G = cc.gen_gnm(1 << 20, 1 << 22, seed=INPUT_SEED, id_bytes=8)
+        desc = "G(n=2^20, m=2^22) uniform endpoints, u64 ids"
+    else:
+        G = cc.gen_rhg(1 << args.rhg_log2n, 16.0, 2.6, seed=INPUT_SEED, id_bytes=4)
+        desc = f"RHG n=2^{args.rhg_log2n}, d=16, gamma=2.6 (threshold model), u32 ids"
+    gen_s = time.time() - t0
+    want = oracle.uf_labels(G) if not args.no_check else None
+    D = G.to_device("cuda:0")
+    dt = torch.int32 if G.id_bytes == 4 else torch.int64
+    lab = torch.empty(G.n, dtype=dt, device="cuda:0")
+    peak, _ = peaks()
+    for algo, P, seq in [("exp", 1, 1), ("exp", 16, 1), ("exp", 16, 0), ("allreduce", 1, 1),
+                         ("shortcuts", 1, 1), ("local", 1, 1)]:
+        if name == "rhg" and algo in ("shortcuts", "local") and args.rhg_log2n > 24:
+            continue
+        ctx = cc.Context(0)
+        solver = cc.SOLVERS[algo](cc.Config(seed=ALGO_SEED, sequential_limit=seq), 0, P, ctx)
+        ms, kern, st = _timed_solves(solver, D, lab, args.steps, args.warmup, ctx)
+        ok = None
+        if want is not None:
+            got = lab.cpu().numpy().view(np.uint32 if G.id_bytes == 4 else np.uint64)
+            ok = bool(np.array_equal(got.astype(np.uint64), want))
+        med = statistics.median(ms)
+        top = max(kern.items(), key=lambda kv: kv[1]["ms"])
+        per_ms = top[1]["ms"] / top[1]["launches"]
+        ach = top[1]["bytes"] / top[1]["launches"] / (per_ms * 1e-3) / 1e9
+        print(json.dumps({
+            "workload": name, "graph": desc, "n": G.n, "m_dir": G.m, "algo": algo,
+            "virtual_ranks": P, "seq": seq, "metric": "Gedges/s per CC solve",
+            "value": G.m / (med * 1e-3) / 1e9, "unit": "Gedges/s", "solve_ms_median": med,
+            "levels": st["levels"], "rounds": st["rounds"], "level_edges": st["level_edges"],
+            "roofline": {"kernel": top[0], "achieved_GBs": ach, "frac": ach / peak,
+                         "ms_per_launch": per_ms},
+            "kernel_ms": {k: v["ms"] / args.steps for k, v in kern.items()},
+            "labels_match_oracle": ok, "gen_s": gen_s}), flush=True)
+        ctx.close()
+
+
+def workload_batch(args):
+    """4096 G(n, m) graphs, n log-uniform in [2^8, 2^18], degree uniform in
+    [0.5, 8]: one batched solve (CUDA-graph replay) against 4096 plain
+    cc_ctx_run launches on the same device-resident graphs."""
+    import torch
+    import components_gb300 as cc
+    from components_gb300 import batch as B
+    t0 = time.time()
+    bt = B.gen_batch(args.batch_k, 8, 18, 0.5, 8.0, seed=INPUT_SEED)
+    gen_s = time.time() - t0
+    D = bt.to_device("cuda:0")
+    ctx = cc.Context(0)
+    tune = B.autotune(D, ctx, reps=2)
+    lab = torch.empty(bt.total_n, dtype=torch.int32, device="cuda:0")
+    for _ in range(args.warmup):
+        B.batch_run(D, ctx, tune, lab)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        B.batch_run(D, ctx, tune, lab)
+    torch.cuda.synchronize()
+    batched_s = (time.perf_counter() - t0) / args.steps
+    batched = lab.cpu().numpy().view(np.uint32).copy()
+    # plain path: one cc_ctx_run per graph, inputs already on the device
+    v, r, c = bt.numpy()
+    graphs = []
+    for i in range(bt.k):
+        a, b = int(v[i]), int(v[i + 1])
+        rp = torch.from_numpy((r[a:b + 1] - r[a]).view(np.int64).copy()).to("cuda:0")
+        col = D.col[int(r[a]):int(r[b])]
+        graphs.append(cc.StaticGraph(rp, col))
+    plain_lab = torch.empty(bt.total_n, dtype=torch.int32, device="cuda:0")
+    solver = cc.ExponentialContraction(cc.Config(seed=ALGO_SEED), 0, 1, ctx)
+    for i in range(min(bt.k, 64)):
+        solver.FindComponents(graphs[i], plain_lab[int(v[i]):int(v[i + 1])])
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for i in range(bt.k):
+        solver.FindComponents(graphs[i], plain_lab[int(v[i]):int(v[i + 1])])
+    torch.cuda.synchronize()
+    plain_s = time.perf_counter() - t0
+    same = bool(np.array_equal(plain_lab.cpu().numpy().view(np.uint32), batched))
+    print(json.dumps({
+        "workload": "batch", "graphs": bt.k, "total_n": bt.total_n, "total_m": bt.total_m,
+        "metric": "graphs/s", "batched_graphs_per_s": bt.k / batched_s,
+        "plain_graphs_per_s": bt.k / plain_s, "speedup": plain_s / batched_s,
+        "batched_ms": batched_s * 1e3, "plain_ms": plain_s * 1e3,
+        "batched_gedges_per_s": bt.total_m / batched_s / 1e9,
+        "labels_bit_identical": same, "tuning": tune.as_dict(), "gen_s": gen_s}), flush=True)
+    ctx.close()
+
+
+def workload_serve(args):
+    """Poisson stream of CC requests (GNM / 2D grid p = 0.5 / RHG gamma = 2.6,
+    n log-uniform in [2^10, 2^22], degree uniform in [1, 16]) through the
+    continuous-batching server, against the plain path (one cc_gpu_run per
+    request with host buffers) on the same requests."""
+    import components_gb300 as cc
+    from components_gb300.serve import Server
+    rng = np.random.default_rng(INPUT_SEED)
+    pool = []
+    t0 = time.time()
+    for i in range(args.serve_pool):
+        kind = i % 3
+        n = int(2 ** rng.uniform(10, args.serve_log2n_max))
+        d = float(rng.uniform(1, 16))
+        if kind == 0:
+            pool.append(cc.gen_gnm(n, max(1, int(n * d / 2)), seed=1000 + i, id_bytes=4))
+        elif kind == 1:
+            side = max(2, int(round(np.sqrt(n))))
+            pool.append(cc.gen_grid(side, side, 0.5, seed=1000 + i))
+        else:
+            pool.append(cc.gen_rhg(n, d, 2.6, seed=1000 + i))
+    gen_s = time.time() - t0
+    reqs = [pool[int(j)] for j in rng.integers(0, len(pool), args.serve_requests)]
+    edges = sum(G.m for G in reqs)
+    # plain path, closed loop: one request after the other
+    plain = []
+    t0 = time.perf_counter()
+    for G in reqs:
+        plain.append(cc.find_components(G, "exp"))
+    plain_s = time.perf_counter() - t0
+    # served: capacity (closed loop), then an open-loop Poisson stream at 80 %
+    with Server(budget_bytes=120 << 30) as srv:
+        t0 = time.perf_counter()
+        ts = [srv.submit(G) for G in reqs]
+        for t in ts:
+            srv.wait(t)
+        cap_s = time.perf_counter() - t0
+        rate = 0.8 * len(reqs) / cap_s
+        gaps = rng.exponential(1.0 / rate, len(reqs))
+        results = [None] * len(reqs)
+        infos = [None] * len(reqs)
+        import threading
+        tickets = [None] * len(reqs)
+        submitted = threading.Event()
+
+        def producer():
+            t_next = time.perf_counter()
+            for i, G in enumerate(reqs):
+                t_next += gaps[i]
+                while time.perf_counter() < t_next:
+                    pass
+                tickets[i] = srv.submit(G)
+            submitted.set()
+
+        th = threading.Thread(target=producer)
+        t0 = time.perf_counter()
+        th.start()
+        for i in range(len(reqs)):
+            while tickets[i] is None:
+                time.sleep(0.0001)
+            results[i], infos[i] = srv.wait(tickets[i])
+        th.join()
+        served_s = time.perf_counter() - t0
+        st = srv.stats()
+    lat = np.array([(x["done_s"] - x["submit_s"]) * 1e3 for x in infos])
+    same = all(np.array_equal(a, b) for a, b in zip(results, plain))
+    print(json.dumps({
+        "workload": "serve", "requests": len(reqs), "pool_graphs": len(pool),
+        "edges_total": edges, "metric": "p50/p99 latency (ms) and graphs/s",
+        "arrival_rate_per_s": rate, "served_graphs_per_s": len(reqs) / served_s,
+        "capacity_graphs_per_s": len(reqs) / cap_s, "plain_graphs_per_s": len(reqs) / plain_s,
+        "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+        "batches": st["batches"], "peak_hbm_bytes": st["peak_bytes_in_use"],
+        "labels_same_alone_and_in_mix": same, "gen_s": gen_s,
+        "sample": f"{len(reqs)} requests drawn from {len(pool)} seeded graphs, "
+                  f"n log-uniform in [2^10, 2^{args.serve_log2n_max}]"}), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -188,8 +381,27 @@ def main():
                     help="hook schedule (cc_tuning.hook_mode: 0 auto, 1 global, 2 tiled)")
     ap.add_argument("--tile", type=int, default=0, help="cc_tuning.tile_vertices (0 = default)")
     ap.add_argument("--tile-threads", type=int, default=0, help="cc_tuning.tile_threads")
+    ap.add_argument("--workload", default="grid", choices=["grid", "gnm", "rhg", "batch", "serve"],
+                    help="grid (the headline line); the others print their own lines")
+    ap.add_argument("--rhg-log2n", type=int, default=26)
+    ap.add_argument("--batch-k", type=int, default=4096)
+    ap.add_argument("--serve-requests", type=int, default=600)
+    ap.add_argument("--serve-pool", type=int, default=24)
+    ap.add_argument("--serve-log2n-max", type=float, default=22)
     args = ap.parse_args()
     rank, world, local = dist_env()
+    if args.workload != "grid" and args.impl == "ours":
+        import __graft_entry__ as ge
+        ge.build()
+        import torch
+        torch.cuda.set_device(0)
+        if args.workload in ("gnm", "rhg"):
+            workload_single(args, args.workload)
+        elif args.workload == "batch":
+            workload_batch(args)
+        else:
+            workload_serve(args)
+        return 0
 
     if args.impl == "reference":
         if rank != 0:

@@ -190,78 +190,131 @@ __device__ __forceinline__ void ts_union(volatile uint32_t *p, uint32_t a, uint3
   }
 }
 
+// The tile kernel: 32-bit offsets inside the tile, a plain per-thread edge
+// loop, tile-crossing edges staged in shared memory (flushed with one global
+// atomic per tile) with their near endpoint replaced by its tile-local root,
+// and the tile-local roots listed for the final roots-only compression.
+constexpr int kCutStage = 2048;  // staged cut edges per tile (16 KB)
+constexpr int kRootStage = 2048;
+
 template <class T, bool PART>
 __global__ void __launch_bounds__(1024)
-    k_tile(uint64_t n, uint64_t m, const uint64_t *__restrict__ rp, const T *__restrict__ col,
-           uint32_t *__restrict__ p, PartMap pm, uint32_t tile, uint32_t hub_degree,
-           uint32_t *__restrict__ hubs, uint64_t hub_cap, unsigned int *__restrict__ nhubs,
-           uint2 *__restrict__ cut, uint64_t cut_cap, unsigned long long *__restrict__ ncut,
-           int *err) {
+    k_tile2(uint64_t n, uint64_t m, const uint64_t *__restrict__ rp, const T *__restrict__ col,
+            uint32_t *__restrict__ p, PartMap pm, uint32_t tile, uint32_t hub_degree,
+            uint32_t *__restrict__ hubs, uint64_t hub_cap, unsigned int *__restrict__ nhubs,
+            uint2 *__restrict__ cut, uint64_t cut_cap, unsigned long long *__restrict__ ncut,
+            uint32_t *__restrict__ roots, unsigned long long *__restrict__ nroots, int *err) {
   extern __shared__ uint32_t tile_parent[];
+  __shared__ uint2 cstage[kCutStage];
+  __shared__ uint32_t rstage[kRootStage];
+  __shared__ unsigned int ccount, rcount;
+  __shared__ unsigned long long cbase, rbase;
   volatile uint32_t *s = tile_parent;
-  const unsigned lane = threadIdx.x & 31;
   for (uint64_t t0 = (uint64_t)blockIdx.x * tile; t0 < n; t0 += (uint64_t)gridDim.x * tile) {
     const uint32_t len = (uint32_t)min((uint64_t)tile, n - t0);
     for (uint32_t i = threadIdx.x; i < len; i += blockDim.x) s[i] = i;
+    if (threadIdx.x == 0) {
+      ccount = 0;
+      rcount = 0;
+    }
     __syncthreads();
-    const uint32_t span = (len + blockDim.x - 1) / blockDim.x * blockDim.x;  // warp-uniform
-    for (uint32_t i = threadIdx.x; i < span; i += blockDim.x) {
+    for (uint32_t i = threadIdx.x; i < len; i += blockDim.x) {
       const uint64_t v = t0 + i;
-      uint64_t b = 0, deg = 0;
-      uint32_t lo = 0;
-      if (i < len) {
-        Row r;
-        if (load_row(rp, v, m, err, r)) {
-          b = r.b;
-          deg = r.e - r.b;
-          if (deg > hub_degree) {
-            uint32_t slot = atomicAdd(nhubs, 1u);
-            if (slot < hub_cap) hubs[slot] = (uint32_t)v;
-            else set_err(err, kErrOverflow);
-            deg = 0;
-          }
-          if (PART) lo = part_lo(pm, (uint32_t)v);
-        }
+      const uint64_t b = __ldg(rp + v), e = __ldg(rp + v + 1);
+      if (e < b || e > m) {
+        set_err(err, kErrBadOffsets);
+        continue;
       }
-      uint64_t maxdeg = deg;
-#pragma unroll
-      for (int o = 16; o; o >>= 1) {
-        uint64_t y = __shfl_xor_sync(0xffffffffu, maxdeg, o);
-        maxdeg = y > maxdeg ? y : maxdeg;
+      if (e - b > hub_degree) {
+        uint32_t slot = atomicAdd(nhubs, 1u);
+        if (slot < hub_cap) hubs[slot] = (uint32_t)v;
+        else set_err(err, kErrOverflow);
+        continue;
       }
-      for (uint64_t j = 0; j < maxdeg; ++j) {
-        bool emit = false;
-        uint32_t u = 0;
-        if (j < deg) {
-          uint64_t uu = (uint64_t)__ldg(col + b + j);
-          if (uu >= n) {
-            set_err(err, kErrBadId);
-          } else if (uu < v && (!PART || (uint32_t)uu >= lo)) {
-            u = (uint32_t)uu;
-            if (uu >= t0) ts_union(s, i, (uint32_t)(uu - t0));
-            else emit = true;
-          }
+      const uint32_t lo = PART ? part_lo(pm, (uint32_t)v) : 0u;
+      const uint32_t vv = (uint32_t)v, tt = (uint32_t)t0;
+      const uint32_t deg = (uint32_t)(e - b);
+      const T *row = col + b;
+      for (uint32_t j = 0; j < deg; ++j) {
+        const uint64_t uu = (uint64_t)__ldg(row + j);
+        if (uu >= n) {
+          set_err(err, kErrBadId);
+          continue;
         }
-        unsigned msk = __ballot_sync(0xffffffffu, emit);
-        if (msk) {
-          unsigned long long base = 0;
-          if (lane == (unsigned)(__ffs(msk) - 1)) base = atomicAdd(ncut, (unsigned long long)__popc(msk));
-          base = __shfl_sync(0xffffffffu, base, __ffs(msk) - 1);
-          if (emit) {
-            unsigned long long slot = base + __popc(msk & ((1u << lane) - 1u));
-            if (slot < cut_cap) cut[slot] = make_uint2((uint32_t)v, u);
+        const uint32_t u = (uint32_t)uu;
+        if (u >= vv || (PART && u < lo)) continue;  // each undirected edge once, same rank
+        if (u >= tt) {
+          ts_union(s, i, u - tt);
+        } else {
+          unsigned int slot = atomicAdd(&ccount, 1u);
+          if (slot < kCutStage) {
+            cstage[slot] = make_uint2(i, u);  // near end as a tile index for now
+          } else {
+            unsigned long long g = atomicAdd(ncut, 1ull);
+            if (g < cut_cap) cut[g] = make_uint2(vv, u);
             else set_err(err, kErrOverflow);
           }
         }
       }
     }
     __syncthreads();
+    // every vertex stores the global id of its tile-local root; roots are listed
     for (uint32_t i = threadIdx.x; i < len; i += blockDim.x) {
       uint32_t r = i, nx;
       while ((nx = s[r]) != r) r = nx;
       p[t0 + i] = (uint32_t)(t0 + r);
+      if (r == i) {
+        unsigned int slot = atomicAdd(&rcount, 1u);
+        if (slot < kRootStage) {
+          rstage[slot] = (uint32_t)(t0 + i);
+        } else {
+          unsigned long long g = atomicAdd(nroots, 1ull);
+          roots[g] = (uint32_t)(t0 + i);  // at most n roots: the list holds n
+        }
+      }
     }
     __syncthreads();
+    const unsigned int nc = min(ccount, (unsigned int)kCutStage);
+    const unsigned int nr = min(rcount, (unsigned int)kRootStage);
+    if (threadIdx.x == 0) {
+      cbase = nc ? atomicAdd(ncut, (unsigned long long)nc) : 0ull;
+      rbase = nr ? atomicAdd(nroots, (unsigned long long)nr) : 0ull;
+    }
+    __syncthreads();
+    for (uint32_t k = threadIdx.x; k < nc; k += blockDim.x) {
+      uint2 c = cstage[k];
+      uint32_t r = c.x, nx;
+      while ((nx = s[r]) != r) r = nx;  // near end -> its tile-local root
+      unsigned long long g = cbase + k;
+      if (g < cut_cap) cut[g] = make_uint2((uint32_t)(t0 + r), c.y);
+      else set_err(err, kErrOverflow);
+    }
+    for (uint32_t k = threadIdx.x; k < nr; k += blockDim.x) roots[rbase + k] = rstage[k];
+    __syncthreads();
+  }
+}
+
+// Roots-only compression: every tile-local root points at its final root.
+__global__ void k_roots_compress(const uint32_t *__restrict__ roots,
+                                 const unsigned long long *__restrict__ nroots, uint32_t *p) {
+  const uint64_t cnt = *nroots;
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < cnt;
+       i += (uint64_t)gridDim.x * blockDim.x) {
+    const uint32_t v = roots[i];
+    uint32_t r = ld_cg(p + v), nx;
+    if (r == v) continue;
+    while ((nx = ld_cg(p + r)) != r) r = nx;
+    st_cg(p + v, r);
+  }
+}
+
+// Every vertex points at a tile-local root (or at a final root): two hops.
+__global__ void k_two_hop(uint64_t n, uint32_t *p) {
+  for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < n;
+       v += (uint64_t)gridDim.x * blockDim.x) {
+    const uint32_t a = p[v];
+    const uint32_t r = ld_cg(p + a);
+    if (r != a) p[v] = r;
   }
 }
 
@@ -396,10 +449,9 @@ void run_uf_tiled(const Csr &g, uint32_t *parent, const PartMap &pm, const UfTun
   const uint64_t si = (uint64_t)g.idb;
   const uint32_t tile = tu.tile_vertices;
   const int threads = (int)tu.tile_threads;
-  const size_t smem = 4ull * tile;
-  const void *fn = (const void *)k_tile<T, PART>;
-  if (smem > 48 * 1024)
-    CCG_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  const size_t smem = 4ull * tile;  // dynamic: the tile's parent array
+  const void *fn = (const void *)k_tile2<T, PART>;
+  CCG_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   int per_sm = 0;
   CCG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, threads, smem));
   if (per_sm < 1) throw Error(CC_ERR_INVALID, "tile does not fit in shared memory");
@@ -407,22 +459,23 @@ void run_uf_tiled(const Csr &g, uint32_t *parent, const PartMap &pm, const UfTun
   const unsigned grid = (unsigned)std::min<uint64_t>(tiles, (uint64_t)per_sm * kSMs);
   const uint64_t hub_cap = g.m / (tu.hub_degree + 1) + 1;
   const uint64_t cut_cap = g.m + 1;
-  DevBuf hubs(4 * hub_cap, s, pool), nh(4, s, pool), cut(8 * cut_cap, s, pool), ncut(8, s, pool);
+  DevBuf hubs(4 * hub_cap, s, pool), nh(4, s, pool), cut(8 * cut_cap, s, pool), cnt(16, s, pool);
+  DevBuf roots(4 * g.n, s, pool);
   CCG_CUDA(cudaMemsetAsync(nh.p, 0, 4, s));
-  CCG_CUDA(cudaMemsetAsync(ncut.p, 0, 8, s));
+  CCG_CUDA(cudaMemsetAsync(cnt.p, 0, 16, s));
+  unsigned long long *ncut = cnt.as<unsigned long long>(), *nroots = ncut + 1;
   // tile pass: offsets, every id once, own parent written once (the parent
-  // chains stay in shared memory), cut edges counted at the union pass
+  // chains stay in shared memory); cut edges and roots are counted where read
   const uint64_t tile_bytes = 8 * (g.n + 1) + g.m * si + 4 * g.n;
   cudaEvent_t t0 = c.tic(s);
-  k_tile<T, PART><<<grid, threads, smem, s>>>(g.n, g.m, g.rp, col, parent, pm, tile, tu.hub_degree,
-                                              hubs.as<uint32_t>(), hub_cap, nh.as<unsigned int>(),
-                                              cut.as<uint2>(), cut_cap,
-                                              ncut.as<unsigned long long>(), g.err);
+  k_tile2<T, PART><<<grid, threads, smem, s>>>(g.n, g.m, g.rp, col, parent, pm, tile,
+                                               tu.hub_degree, hubs.as<uint32_t>(), hub_cap,
+                                               nh.as<unsigned int>(), cut.as<uint2>(), cut_cap,
+                                               ncut, roots.as<uint32_t>(), nroots, g.err);
   CCG_LAUNCH_CHECK();
   c.toc(s, "uf_tile", t0, tile_bytes);
   cudaEvent_t t1 = c.tic(s);
-  k_cut_union<<<kSMs * 16, kBlock, 0, s>>>(cut.as<uint2>(), ncut.as<unsigned long long>(), cut_cap,
-                                           parent);
+  k_cut_union<<<kSMs * 16, kBlock, 0, s>>>(cut.as<uint2>(), ncut, cut_cap, parent);
   CCG_LAUNCH_CHECK();
   c.toc(s, "uf_cut_union", t1, 0);
   cudaEvent_t t2 = c.tic(s);
@@ -431,10 +484,14 @@ void run_uf_tiled(const Csr &g, uint32_t *parent, const PartMap &pm, const UfTun
   CCG_LAUNCH_CHECK();
   c.toc(s, "uf_hook_hubs", t2, 0);
   cudaEvent_t t3 = c.tic(s);
-  k_compress<<<grid_for(g.n, kBlock, kSMs * 32), kBlock, 0, s>>>(g.n, parent);
+  k_roots_compress<<<kSMs * 16, kBlock, 0, s>>>(roots.as<uint32_t>(), nroots, parent);
   CCG_LAUNCH_CHECK();
-  c.toc(s, "uf_compress", t3, 3 * g.n * 4);
-  c.add(4, tile_bytes + 3 * g.n * 4);
+  c.toc(s, "uf_roots_compress", t3, 0);
+  cudaEvent_t t4 = c.tic(s);
+  k_two_hop<<<grid_for(g.n, kBlock, kSMs * 32), kBlock, 0, s>>>(g.n, parent);
+  CCG_LAUNCH_CHECK();
+  c.toc(s, "uf_two_hop", t4, 3 * g.n * 4);
+  c.add(5, tile_bytes + 3 * g.n * 4);
 }
 
 // Share of tile-crossing edges on a sample of 8192 rows (one small readback).
