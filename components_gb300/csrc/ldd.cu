@@ -240,11 +240,14 @@ int ldd_decompose(const Csr &g, const uint32_t *vid, uint64_t seed, uint32_t lev
     uint32_t maxdev = 0;
     CCG_CUDA(cudaMemcpyAsync(&maxdev, mx.p, 4, cudaMemcpyDeviceToHost, s));
     CCG_CUDA(cudaStreamSynchronize(s));
+    cudaEvent_t t0 = c.tic(s);
     for (uint32_t t = 0; t <= maxdev; ++t) {
       k_ldd_gated<<<grid, kBlock, 0, s>>>(g.n, g.rp, col, key, t);
       CCG_LAUNCH_CHECK();
       ++rounds;
     }
+    c.toc(s, "ldd_gated_all_rounds", t0,
+          8 * (g.n + 1) + g.m * 4 + g.m * 8 + (uint64_t)rounds * g.n * 8);
     // every vertex is final once; every edge pushed once
     c.add(rounds, 8 * (g.n + 1) + g.m * 4 + g.m * 8 + (uint64_t)rounds * g.n * 8);
   } else {
@@ -257,11 +260,13 @@ int ldd_decompose(const Csr &g, const uint32_t *vid, uint64_t seed, uint32_t lev
       if (rounds >= max_rounds) return -1;
       *host_flag = 0;
       CCG_CUDA(cudaMemsetAsync(dev_flag, 0, sizeof(int), s));
+      cudaEvent_t t0 = c.tic(s);
       k_ldd_round<<<grid, kBlock, 0, s>>>(g.n, g.rp, col, key, dev_flag);
       CCG_LAUNCH_CHECK();
       k_ldd_round_hubs<<<kSMs * 4, kBlock, 0, s>>>(g.rp, col, hubs.as<uint32_t>(),
                                                    nh.as<unsigned int>(), key, dev_flag);
       CCG_LAUNCH_CHECK();
+      c.toc(s, "ldd_round", t0, round_bytes);
       CCG_CUDA(cudaMemcpyAsync((void *)host_flag, dev_flag, sizeof(int), cudaMemcpyDeviceToHost, s));
       CCG_CUDA(cudaStreamSynchronize(s));
       ++rounds;

@@ -250,6 +250,7 @@ int shortcut_propagate(const Csr &g, uint32_t *lab, uint32_t hitters, int max_ro
   for (;;) {
     if (rounds >= max_rounds) return -1;
     CCG_CUDA(cudaMemsetAsync(updb.p, 0xff, 4 * g.n, s));
+    cudaEvent_t t0 = c.tic(s);
     k_sc_min<<<grid, kBlock, 0, s>>>(g.n, g.rp, col, f, nf, updb.as<uint32_t>());
     CCG_LAUNCH_CHECK();
     k_sc_min_rows<<<kSMs * 4, kBlock, 0, s>>>(g.rp, col, rows.as<uint32_t>(), nr.as<unsigned int>(),
@@ -268,6 +269,7 @@ int shortcut_propagate(const Csr &g, uint32_t *lab, uint32_t hitters, int max_ro
     k_sc_jump<<<grid, kBlock, 0, s>>>(g.n, f, nf, updb.as<uint32_t>(),
                                       hitters ? heavy.as<uint8_t>() : nullptr, dev_flag);
     CCG_LAUNCH_CHECK();
+    c.toc(s, "shortcut_round", t0, 8 * (g.n + 1) + g.m * 4 + g.m * 4 + 2 * g.n * 4 + 4 * g.n * 4 + 4 * g.n);
     CCG_CUDA(cudaMemcpyAsync((void *)host_flag, dev_flag, sizeof(int), cudaMemcpyDeviceToHost, s));
     CCG_CUDA(cudaStreamSynchronize(s));
     ++rounds;

@@ -309,6 +309,12 @@ struct Server {
         r->state = kStaged;
         staged.push_back(r);
       }
+      // batching window: let more requests arrive unless the batch is full
+      if (!staged.empty() && cfg.batch_window_us && staged.size() < cfg.max_batch_graphs &&
+          (now_s() - staged.front()->t_admit) * 1e6 < cfg.batch_window_us && !stop) {
+        cv_worker.wait_for(lk, std::chrono::microseconds(50));
+        continue;
+      }
       // batching: every free compute stream takes the staged requests
       for (size_t si = 0; si < streams.size() && !staged.empty(); ++si) {
         if (busy[si].load() > 0) continue;

@@ -21,7 +21,7 @@ from .graph import StaticGraph
 class cc_serve_config(C.Structure):
     _fields_ = [("hbm_budget_bytes", C.c_uint64), ("max_batch_graphs", C.c_uint32),
                 ("compute_streams", C.c_uint32), ("smem_max_n", C.c_uint32),
-                ("reserved", C.c_uint32)]
+                ("batch_window_us", C.c_uint32)]
 
 
 class cc_serve_ticket_info(C.Structure):
@@ -71,7 +71,7 @@ def now() -> float:
 
 class Server:
     def __init__(self, device: int = 0, budget_bytes: int | None = None, max_batch: int = 0,
-                 streams: int = 0, smem_max_n: int = 0):
+                 streams: int = 0, smem_max_n: int = 0, window_us: int = 0):
         _bind()
         cfg = cc_serve_config()
         _lib.gpu().cc_serve_config_default(C.byref(cfg))
@@ -83,6 +83,7 @@ class Server:
             cfg.compute_streams = streams
         if smem_max_n:
             cfg.smem_max_n = smem_max_n
+        cfg.batch_window_us = window_us
         self._h = C.c_void_p()
         _lib.check(_lib.gpu().cc_serve_create(C.byref(self._h), device, C.byref(cfg)))
         self._graphs: dict[int, StaticGraph] = {}
@@ -113,8 +114,10 @@ class Server:
     def wait(self, t: int, timeout_s: float = 0.0):
         out = self._out(t)
         info = cc_serve_ticket_info()
-        _lib.check(_lib.gpu().cc_serve_wait(self._h, t, out.ctypes.data, timeout_s, C.byref(info)))
-        n = self._graphs.pop(t).n
+        rc = _lib.gpu().cc_serve_wait(self._h, t, out.ctypes.data, timeout_s, C.byref(info))
+        if rc != _lib.CC_ERR_TIMEOUT:  # any other outcome retires the ticket
+            n = self._graphs.pop(t).n
+        _lib.check(rc)
         return out[:n], info.as_dict()
 
     def stats(self) -> dict:

@@ -32,7 +32,9 @@ typedef struct cc_serve_config {
   uint32_t max_batch_graphs;   /* graphs coalesced into one launch (default 1024) */
   uint32_t compute_streams;    /* batches in flight at once (default 2) */
   uint32_t smem_max_n;         /* graphs up to this many vertices go one CTA each (default 16384) */
-  uint32_t reserved;
+  uint32_t batch_window_us;    /* a free stream waits up to this long after the oldest staged
+                                  request for more to coalesce, unless the batch is full
+                                  (default 0: launch at once) */
 } cc_serve_config;
 
 typedef struct cc_serve_ticket_info {

@@ -42,7 +42,7 @@ def test_results_alone_and_in_the_mix(cuda):
     alone = [cc.find_components(G, "exp") for G in graphs]
     for G, a in zip(graphs[:12], alone[:12]):
         assert np.array_equal(a.astype(np.uint64), oracle.uf_labels(G))
-    with Server(max_batch=16) as srv:
+    with Server(max_batch=16, window_us=3000) as srv:
         tickets = {}
         rng = np.random.default_rng(2)
 
