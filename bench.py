@@ -222,16 +222,18 @@ def workload_single(args, name):
             got = lab.cpu().numpy().view(np.uint32 if G.id_bytes == 4 else np.uint64)
             ok = bool(np.array_equal(got.astype(np.uint64), want))
         med = statistics.median(ms)
-        top = max(kern.items(), key=lambda kv: kv[1]["ms"])
-        per_ms = top[1]["ms"] / top[1]["launches"]
-        ach = top[1]["bytes"] / top[1]["launches"] / (per_ms * 1e-3) / 1e9
+        roof = None
+        if kern:
+            top = max(kern.items(), key=lambda kv: kv[1]["ms"])
+            per_ms = top[1]["ms"] / top[1]["launches"]
+            ach = top[1]["bytes"] / top[1]["launches"] / (per_ms * 1e-3) / 1e9
+            roof = {"kernel": top[0], "achieved_GBs": ach, "frac": ach / peak, "ms_per_launch": per_ms}
         print(json.dumps({
             "workload": name, "graph": desc, "n": G.n, "m_dir": G.m, "algo": algo,
             "virtual_ranks": P, "seq": seq, "metric": "Gedges/s per CC solve",
             "value": G.m / (med * 1e-3) / 1e9, "unit": "Gedges/s", "solve_ms_median": med,
             "levels": st["levels"], "rounds": st["rounds"], "level_edges": st["level_edges"],
-            "roofline": {"kernel": top[0], "achieved_GBs": ach, "frac": ach / peak,
-                         "ms_per_launch": per_ms},
+            "roofline": roof,
             "kernel_ms": {k: v["ms"] / args.steps for k, v in kern.items()},
             "labels_match_oracle": ok, "gen_s": gen_s}), flush=True)
         ctx.close()

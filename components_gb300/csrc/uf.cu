@@ -16,7 +16,11 @@
 //
 // The kernels read the caller's CSR directly, so every offset and id is
 // checked: a bad one is recorded in the error word and skipped.
+#include <cooperative_groups.h>
+
 #include "kernels.h"
+
+namespace cg = cooperative_groups;
 
 namespace ccg {
 namespace {
@@ -195,6 +199,14 @@ __device__ __forceinline__ void ts_union(volatile uint32_t *p, uint32_t a, uint3
 // atomic per tile) with their near endpoint replaced by its tile-local root,
 // and the tile-local roots listed for the final roots-only compression.
 constexpr int kCutStage = 2048;  // staged cut edges per tile (16 KB)
+
+// Slot from a shared counter, one atomic per group of converged lanes.
+__device__ __forceinline__ unsigned int agg_inc(unsigned int *ctr) {
+  cg::coalesced_group g = cg::coalesced_threads();
+  unsigned int base = 0;
+  if (g.thread_rank() == 0) base = atomicAdd(ctr, g.size());
+  return g.shfl(base, 0) + g.thread_rank();
+}
 constexpr int kRootStage = 2048;
 
 template <class T, bool PART>
@@ -246,7 +258,7 @@ __global__ void __launch_bounds__(1024)
         if (u >= tt) {
           ts_union(s, i, u - tt);
         } else {
-          unsigned int slot = atomicAdd(&ccount, 1u);
+          unsigned int slot = agg_inc(&ccount);
           if (slot < kCutStage) {
             cstage[slot] = make_uint2(i, u);  // near end as a tile index for now
           } else {
@@ -264,7 +276,7 @@ __global__ void __launch_bounds__(1024)
       while ((nx = s[r]) != r) r = nx;
       p[t0 + i] = (uint32_t)(t0 + r);
       if (r == i) {
-        unsigned int slot = atomicAdd(&rcount, 1u);
+        unsigned int slot = agg_inc(&rcount);
         if (slot < kRootStage) {
           rstage[slot] = (uint32_t)(t0 + i);
         } else {
