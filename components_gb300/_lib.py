@@ -88,7 +88,7 @@ class cc_tuning(C.Structure):
                 ("tile_threads", C.c_uint32), ("hub_degree", C.c_uint32)]
 
 
-CC_HOOK_AUTO, CC_HOOK_GLOBAL, CC_HOOK_TILED = 0, 1, 2
+CC_HOOK_AUTO, CC_HOOK_GLOBAL, CC_HOOK_TILED, CC_HOOK_SAMPLED = 0, 1, 2, 3
 
 
 class cc_host_graph(C.Structure):

@@ -25,9 +25,9 @@ struct Csr {
 // edges whose endpoints lie in the same virtual rank are used, so parent[v] is
 // the minimum id of v's partition-local component
 // (exponential_contraction.h:391-411 FindLocalComponents).
-enum : int { kUfAuto = 0, kUfGlobal = 1, kUfTiled = 2 };
+enum : int { kUfAuto = 0, kUfGlobal = 1, kUfTiled = 2, kUfSampled = 3 };
 struct UfTuning {
-  int mode = kUfAuto;            // auto: tiled when a sample shows < 50 % tile-crossing edges
+  int mode = kUfAuto;  // auto: tiled when a sample shows < 50 % tile-crossing edges, else sampled
   uint32_t hub_degree = 32;      // rows above: one warp per row
   uint32_t tile_vertices = 16384;  // vertices per CTA tile (4 bytes of shared memory each)
   uint32_t tile_threads = 1024;

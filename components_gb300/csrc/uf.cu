@@ -16,11 +16,10 @@
 //
 // The kernels read the caller's CSR directly, so every offset and id is
 // checked: a bad one is recorded in the error word and skipped.
-#include <cooperative_groups.h>
+#include <algorithm>
+#include <vector>
 
 #include "kernels.h"
-
-namespace cg = cooperative_groups;
 
 namespace ccg {
 namespace {
@@ -161,6 +160,102 @@ __global__ void k_compress(uint64_t n, uint32_t *p) {
   }
 }
 
+// ---- sampled linking (Afforest: Sutton, Ben-Nun, Barak, IPDPS 2018) ------------
+// Link every vertex to its r-th neighbour for r < kAffRounds, compress, find
+// the most frequent root L on a sample, then only vertices outside L's tree
+// process their remaining edges.  An edge skipped by an endpoint inside L is
+// either processed from its other endpoint or joins two vertices that are
+// already connected, so the components are exact.  On graphs with a giant
+// component most edges are never touched; without one it costs two light
+// passes.
+constexpr uint32_t kAffRounds = 2;
+
+__device__ __forceinline__ bool same_part(const PartMap &pm, uint32_t v, uint32_t u) {
+  return pm.part(v) == pm.part(u);
+}
+
+template <class T, bool PART>
+__global__ void k_aff_link(uint64_t n, uint64_t m, const uint64_t *__restrict__ rp,
+                           const T *__restrict__ col, uint32_t *p, PartMap pm, uint32_t r, int *err) {
+  for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < n;
+       v += (uint64_t)gridDim.x * blockDim.x) {
+    Row row;
+    if (!load_row(rp, v, m, err, row) || row.e - row.b <= r) continue;
+    uint64_t u = (uint64_t)__ldg(col + row.b + r);
+    if (u >= n) {
+      set_err(err, kErrBadId);
+      continue;
+    }
+    if (!PART || same_part(pm, (uint32_t)v, (uint32_t)u)) uf_union(p, (uint32_t)v, (uint32_t)u);
+  }
+}
+
+__global__ void k_aff_sample(uint64_t n, const uint32_t *p, uint32_t samples, uint64_t salt,
+                             uint32_t *__restrict__ out) {
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < samples; i += gridDim.x * blockDim.x) {
+    uint32_t r = (uint32_t)(mix64(salt + i) % n), nx;
+    while ((nx = ld_cg(p + r)) != r) r = nx;
+    out[i] = r;
+  }
+}
+
+template <class T, bool PART>
+__global__ void k_aff_rest(uint64_t n, uint64_t m, const uint64_t *__restrict__ rp,
+                           const T *__restrict__ col, uint32_t *p, PartMap pm, uint32_t L,
+                           uint32_t hub_degree, uint32_t *__restrict__ hubs, uint64_t hub_cap,
+                           unsigned int *__restrict__ nhubs, int *err) {
+  for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < n;
+       v += (uint64_t)gridDim.x * blockDim.x) {
+    Row row;
+    if (!load_row(rp, v, m, err, row) || row.e - row.b <= kAffRounds) continue;
+    if (uf_find(p, (uint32_t)v) == L) continue;
+    if (row.e - row.b > hub_degree) {
+      uint32_t slot = atomicAdd(nhubs, 1u);
+      if (slot < hub_cap) hubs[slot] = (uint32_t)v;
+      else set_err(err, kErrOverflow);
+      continue;
+    }
+    for (uint64_t k = row.b + kAffRounds; k < row.e; ++k) {
+      uint64_t u = (uint64_t)__ldg(col + k);
+      if (u >= n) {
+        set_err(err, kErrBadId);
+        continue;
+      }
+      if (!PART || same_part(pm, (uint32_t)v, (uint32_t)u)) uf_union(p, (uint32_t)v, (uint32_t)u);
+    }
+  }
+}
+
+template <class T, bool PART>
+__global__ void k_aff_rest_hubs(uint64_t n, const uint64_t *__restrict__ rp,
+                                const T *__restrict__ col, uint32_t *p, PartMap pm,
+                                const uint32_t *__restrict__ hubs, uint64_t hub_cap,
+                                const unsigned int *__restrict__ nhubs, int *err) {
+  const unsigned lane = threadIdx.x & 31;
+  const uint64_t warp = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
+  const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+  uint64_t nh = *nhubs;
+  if (nh > hub_cap) nh = hub_cap;
+  for (uint64_t h = warp; h < nh; h += nwarps) {
+    uint32_t v = hubs[h];
+    uint64_t b = __ldg(rp + v), e = __ldg(rp + v + 1);  // checked by k_aff_rest
+    for (uint64_t k = b + kAffRounds + lane; k < e; k += 32) {
+      uint64_t u = (uint64_t)__ldg(col + k);
+      if (u >= n) {
+        set_err(err, kErrBadId);
+        continue;
+      }
+      if (!PART || same_part(pm, v, (uint32_t)u)) uf_union(p, v, (uint32_t)u);
+    }
+  }
+}
+
+__global__ void k_iota_parent(uint64_t n, uint32_t *p) {
+  for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < n;
+       v += (uint64_t)gridDim.x * blockDim.x)
+    p[v] = (uint32_t)v;
+}
+
 // ---- tiled pass ---------------------------------------------------------------
 // One CTA per tile of TILE consecutive vertices: the edges inside the tile are
 // united on a parent array in shared memory (chains resolve at shared-memory
@@ -200,13 +295,6 @@ __device__ __forceinline__ void ts_union(volatile uint32_t *p, uint32_t a, uint3
 // and the tile-local roots listed for the final roots-only compression.
 constexpr int kCutStage = 2048;  // staged cut edges per tile (16 KB)
 
-// Slot from a shared counter, one atomic per group of converged lanes.
-__device__ __forceinline__ unsigned int agg_inc(unsigned int *ctr) {
-  cg::coalesced_group g = cg::coalesced_threads();
-  unsigned int base = 0;
-  if (g.thread_rank() == 0) base = atomicAdd(ctr, g.size());
-  return g.shfl(base, 0) + g.thread_rank();
-}
 constexpr int kRootStage = 2048;
 
 template <class T, bool PART>
@@ -230,58 +318,86 @@ __global__ void __launch_bounds__(1024)
       rcount = 0;
     }
     __syncthreads();
-    for (uint32_t i = threadIdx.x; i < len; i += blockDim.x) {
+    const unsigned lane = threadIdx.x & 31;
+    const uint32_t span = (len + blockDim.x - 1) / blockDim.x * blockDim.x;  // warp-uniform
+    for (uint32_t i = threadIdx.x; i < span; i += blockDim.x) {
       const uint64_t v = t0 + i;
-      const uint64_t b = __ldg(rp + v), e = __ldg(rp + v + 1);
-      if (e < b || e > m) {
-        set_err(err, kErrBadOffsets);
-        continue;
-      }
-      if (e - b > hub_degree) {
-        uint32_t slot = atomicAdd(nhubs, 1u);
-        if (slot < hub_cap) hubs[slot] = (uint32_t)v;
-        else set_err(err, kErrOverflow);
-        continue;
-      }
-      const uint32_t lo = PART ? part_lo(pm, (uint32_t)v) : 0u;
-      const uint32_t vv = (uint32_t)v, tt = (uint32_t)t0;
-      const uint32_t deg = (uint32_t)(e - b);
-      const T *row = col + b;
-      for (uint32_t j = 0; j < deg; ++j) {
-        const uint64_t uu = (uint64_t)__ldg(row + j);
-        if (uu >= n) {
-          set_err(err, kErrBadId);
-          continue;
-        }
-        const uint32_t u = (uint32_t)uu;
-        if (u >= vv || (PART && u < lo)) continue;  // each undirected edge once, same rank
-        if (u >= tt) {
-          ts_union(s, i, u - tt);
+      uint64_t b = 0;
+      uint32_t deg = 0, lo = 0;
+      if (i < len) {
+        const uint64_t rb = __ldg(rp + v), re = __ldg(rp + v + 1);
+        if (re < rb || re > m) {
+          set_err(err, kErrBadOffsets);
+        } else if (re - rb > hub_degree) {
+          uint32_t slot = atomicAdd(nhubs, 1u);
+          if (slot < hub_cap) hubs[slot] = (uint32_t)v;
+          else set_err(err, kErrOverflow);
         } else {
-          unsigned int slot = agg_inc(&ccount);
-          if (slot < kCutStage) {
-            cstage[slot] = make_uint2(i, u);  // near end as a tile index for now
-          } else {
-            unsigned long long g = atomicAdd(ncut, 1ull);
-            if (g < cut_cap) cut[g] = make_uint2(vv, u);
-            else set_err(err, kErrOverflow);
+          b = rb;
+          deg = (uint32_t)(re - rb);
+          if (PART) lo = part_lo(pm, (uint32_t)v);
+        }
+      }
+      // every lane walks the warp's longest row so the ballots below see the
+      // whole warp (rows above hub_degree were queued instead)
+      const uint32_t maxdeg = __reduce_max_sync(0xffffffffu, deg);
+      const uint32_t vv = (uint32_t)v, tt = (uint32_t)t0;
+      for (uint32_t j = 0; j < maxdeg; ++j) {
+        bool emit = false;
+        uint32_t u = 0;
+        if (j < deg) {
+          const uint64_t uu = (uint64_t)__ldg(col + b + j);
+          if (uu >= n) {
+            set_err(err, kErrBadId);
+          } else if ((uint32_t)uu < vv && (!PART || (uint32_t)uu >= lo)) {
+            u = (uint32_t)uu;
+            if (u >= tt) ts_union(s, i, u - tt);
+            else emit = true;  // each undirected edge once, from its larger end
+          }
+        }
+        const unsigned msk = __ballot_sync(0xffffffffu, emit);
+        if (msk) {
+          const int leader = __ffs(msk) - 1;
+          unsigned int base = 0;
+          if ((int)lane == leader) base = atomicAdd(&ccount, (unsigned)__popc(msk));
+          base = __shfl_sync(0xffffffffu, base, leader);
+          if (emit) {
+            const unsigned int slot = base + __popc(msk & ((1u << lane) - 1u));
+            if (slot < kCutStage) {
+              cstage[slot] = make_uint2(i, u);  // near end as a tile index for now
+            } else {
+              unsigned long long g = atomicAdd(ncut, 1ull);
+              if (g < cut_cap) cut[g] = make_uint2(vv, u);
+              else set_err(err, kErrOverflow);
+            }
           }
         }
       }
     }
     __syncthreads();
     // every vertex stores the global id of its tile-local root; roots are listed
-    for (uint32_t i = threadIdx.x; i < len; i += blockDim.x) {
-      uint32_t r = i, nx;
-      while ((nx = s[r]) != r) r = nx;
-      p[t0 + i] = (uint32_t)(t0 + r);
-      if (r == i) {
-        unsigned int slot = agg_inc(&rcount);
-        if (slot < kRootStage) {
-          rstage[slot] = (uint32_t)(t0 + i);
-        } else {
-          unsigned long long g = atomicAdd(nroots, 1ull);
-          roots[g] = (uint32_t)(t0 + i);  // at most n roots: the list holds n
+    for (uint32_t i = threadIdx.x; i < span; i += blockDim.x) {
+      bool is_root = false;
+      if (i < len) {
+        uint32_t r = i, nx;
+        while ((nx = s[r]) != r) r = nx;
+        p[t0 + i] = (uint32_t)(t0 + r);
+        is_root = r == i;
+      }
+      const unsigned msk = __ballot_sync(0xffffffffu, is_root);
+      if (msk) {
+        const int leader = __ffs(msk) - 1;
+        unsigned int base = 0;
+        if ((int)lane == leader) base = atomicAdd(&rcount, (unsigned)__popc(msk));
+        base = __shfl_sync(0xffffffffu, base, leader);
+        if (is_root) {
+          const unsigned int slot = base + __popc(msk & ((1u << lane) - 1u));
+          if (slot < kRootStage) {
+            rstage[slot] = (uint32_t)(t0 + i);
+          } else {
+            unsigned long long g = atomicAdd(nroots, 1ull);
+            roots[g] = (uint32_t)(t0 + i);  // at most n roots: the list holds n
+          }
         }
       }
     }
@@ -525,18 +641,81 @@ double cut_share(const Csr &g, const PartMap &pm, uint32_t tile, cudaStream_t s,
 }
 
 template <class T, bool PART>
+void run_uf_afforest(const Csr &g, uint32_t *parent, const PartMap &pm, uint32_t hub_degree,
+                     cudaStream_t s, cudaMemPool_t pool, Counters &c) {
+  const T *col = static_cast<const T *>(g.col);
+  const uint64_t si = (uint64_t)g.idb;
+  const unsigned grid = grid_for(g.n, kBlock, kSMs * 32);
+  k_iota_parent<<<grid, kBlock, 0, s>>>(g.n, parent);
+  CCG_LAUNCH_CHECK();
+  // each link round: offsets, one id, one union (two parent gathers)
+  const uint64_t link_bytes = 8 * (g.n + 1) + g.n * si + 2 * g.n * 4;
+  for (uint32_t r = 0; r < kAffRounds; ++r) {
+    cudaEvent_t t0 = c.tic(s);
+    k_aff_link<T, PART><<<grid, kBlock, 0, s>>>(g.n, g.m, g.rp, col, parent, pm, r, g.err);
+    CCG_LAUNCH_CHECK();
+    c.toc(s, "uf_sample_link", t0, link_bytes);
+  }
+  k_compress<<<grid, kBlock, 0, s>>>(g.n, parent);
+  CCG_LAUNCH_CHECK();
+  // most frequent root of a sample = the giant component, if there is one
+  const uint32_t samples = (uint32_t)std::min<uint64_t>(g.n, 1024);
+  DevBuf smp(4 * samples, s, pool);
+  k_aff_sample<<<(samples + 255) / 256, 256, 0, s>>>(g.n, parent, samples, 0x5eedull,
+                                                     smp.as<uint32_t>());
+  CCG_LAUNCH_CHECK();
+  std::vector<uint32_t> h(samples);
+  CCG_CUDA(cudaMemcpyAsync(h.data(), smp.p, 4 * samples, cudaMemcpyDeviceToHost, s));
+  CCG_CUDA(cudaStreamSynchronize(s));
+  std::sort(h.begin(), h.end());
+  uint32_t L = h.empty() ? kNone : h[0];
+  size_t best = 0;
+  for (size_t i = 0; i < h.size();) {
+    size_t j = i;
+    while (j < h.size() && h[j] == h[i]) ++j;
+    if (j - i > best) {
+      best = j - i;
+      L = h[i];
+    }
+    i = j;
+  }
+  const uint64_t hub_cap = g.m / (hub_degree + 1) + 1;
+  DevBuf hubs(4 * hub_cap, s, pool), nh(4, s, pool);
+  CCG_CUDA(cudaMemsetAsync(nh.p, 0, 4, s));
+  // remaining pass: offsets, own root, and the ids + unions of the rows
+  // outside the giant component (counted as the full edge stream)
+  const uint64_t rest_bytes = 8 * (g.n + 1) + g.m * si + g.m * 4 + 2 * g.n * 4;
+  cudaEvent_t t1 = c.tic(s);
+  k_aff_rest<T, PART><<<grid, kBlock, 0, s>>>(g.n, g.m, g.rp, col, parent, pm, L, hub_degree,
+                                              hubs.as<uint32_t>(), hub_cap, nh.as<unsigned int>(),
+                                              g.err);
+  CCG_LAUNCH_CHECK();
+  c.toc(s, "uf_sample_rest", t1, rest_bytes);
+  k_aff_rest_hubs<T, PART><<<kSMs * 8, kBlock, 0, s>>>(g.n, g.rp, col, parent, pm,
+                                                       hubs.as<uint32_t>(), hub_cap,
+                                                       nh.as<unsigned int>(), g.err);
+  CCG_LAUNCH_CHECK();
+  cudaEvent_t t2 = c.tic(s);
+  k_compress<<<grid, kBlock, 0, s>>>(g.n, parent);
+  CCG_LAUNCH_CHECK();
+  c.toc(s, "uf_compress", t2, 3 * g.n * 4);
+  c.add(8, 4 * g.n + kAffRounds * link_bytes + rest_bytes + 6 * g.n * 4);
+}
+
+template <class T, bool PART>
 void run_uf_mode(const Csr &g, uint32_t *parent, const PartMap &pm, const UfTuning &tu,
                  cudaStream_t s, cudaMemPool_t pool, Counters &c) {
   int mode = tu.mode;
   if (mode == kUfAuto) {
     // the tiled pass wins when most edges stay inside their tile (grids,
-    // geometric and angularly ordered graphs); random graphs stay global
+    // geometric and angularly ordered graphs); otherwise sampled linking
     mode = (g.n >= 4ull * tu.tile_vertices &&
             cut_share<T, PART>(g, pm, tu.tile_vertices, s, pool, c) < 0.5)
                ? kUfTiled
-               : kUfGlobal;
+               : kUfSampled;
   }
   if (mode == kUfTiled) run_uf_tiled<T, PART>(g, parent, pm, tu, s, pool, c);
+  else if (mode == kUfSampled) run_uf_afforest<T, PART>(g, parent, pm, tu.hub_degree, s, pool, c);
   else run_uf<T, PART>(g, parent, pm, tu.hub_degree, s, pool, c);
 }
 

@@ -212,10 +212,14 @@ void *cc_ctx_stream(cc_ctx *ctx);
 
 /* Schedule of the hook-and-compress pass (partition-local components, base
    cases, CC_ALLREDUCE).  Zero fields keep the defaults. */
-enum { CC_HOOK_AUTO = 0, CC_HOOK_GLOBAL = 1, CC_HOOK_TILED = 2 };
+enum { CC_HOOK_AUTO = 0, CC_HOOK_GLOBAL = 1, CC_HOOK_TILED = 2, CC_HOOK_SAMPLED = 3 };
 typedef struct cc_tuning {
-  uint32_t hook_mode;      /* CC_HOOK_*: auto picks tiled when a sample of rows
-                              shows < 50 % tile-crossing edges */
+  uint32_t hook_mode;      /* CC_HOOK_*: GLOBAL links every edge (thread per
+                              vertex); TILED unites each CTA tile in shared
+                              memory first; SAMPLED links two neighbours per
+                              vertex, then only rows outside the largest
+                              component; AUTO picks TILED when a sample of rows
+                              shows < 50 % tile-crossing edges, else SAMPLED */
   uint32_t tile_vertices;  /* vertices per CTA tile, 4 bytes of shared memory
                               each (default 16384, at most 56K) */
   uint32_t tile_threads;   /* CTA size of the tiled pass (default 1024) */

@@ -164,7 +164,7 @@ def test_stream_interop(cuda):
     ctx.close()
 
 
-@pytest.mark.parametrize("mode", [_lib.CC_HOOK_GLOBAL, _lib.CC_HOOK_TILED])
+@pytest.mark.parametrize("mode", [_lib.CC_HOOK_GLOBAL, _lib.CC_HOOK_TILED, _lib.CC_HOOK_SAMPLED])
 def test_hook_modes_agree(cuda, mode):
     """Global and tiled hook passes give the same labels, also with ranks,
     hub rows, tiles smaller than a rank and ranks smaller than a tile."""
