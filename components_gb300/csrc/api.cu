@@ -79,6 +79,7 @@ void ctx_init(cc_ctx *c, int device, void *stream) {
   CCG_CUDA(cudaMalloc(&c->d_err, sizeof(int)));
   CCG_CUDA(cudaMalloc(&c->d_geo, sizeof(uint64_t) * ccg::kGeoMax));
   CCG_CUDA(cudaHostAlloc(&c->h_flag, sizeof(int), cudaHostAllocDefault));
+  CCG_CUDA(cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking));
 }
 
 void ctx_free(cc_ctx *c) {
@@ -92,6 +93,10 @@ void ctx_free(cc_ctx *c) {
   if (c->d_geo) cudaFree(c->d_geo);
   if (c->h_flag) cudaFreeHost(c->h_flag);
   if (c->pool) cudaMemPoolDestroy(c->pool);
+  if (c->copy_stream) {
+    cudaStreamSynchronize(c->copy_stream);
+    cudaStreamDestroy(c->copy_stream);
+  }
   if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
 }
 
@@ -125,6 +130,7 @@ struct Solver {
   cc_stats &st;
   uint64_t limit = 0;          // sequential limit (edges for CC_EXP, vertices for CC_LOCAL)
   ccg::UfTuning uf;            // hook-and-compress schedule (context tuning)
+  const ccg::HostSource *hs = nullptr;  // streamed host input (tiled pass only)
   int max_levels = CC_MAX_LEVELS - 1;
 
   void check_err() { ccg::throw_on_kernel_error(C, s); }
@@ -245,7 +251,7 @@ struct Solver {
     switch (algo) {
       case CC_ALLREDUCE: {
         note_level(0, g, 0);
-        ccg::uf_components(g, lab, nullptr, uf, s, pool, c);
+        ccg::uf_components(g, lab, nullptr, uf, s, pool, c, hs);
         break;
       }
       case CC_EXP: {
@@ -255,7 +261,7 @@ struct Solver {
           // one rank: the local pass already is the whole solve, the component
           // graph has no edges (cag_builder.h:163-229)
           note_level(0, g, 0);
-          ccg::uf_components(g, lab, nullptr, uf, s, pool, c);
+          ccg::uf_components(g, lab, nullptr, uf, s, pool, c, hs);
           break;
         }
         ccg::Contracted G0;
@@ -406,11 +412,31 @@ int ctx_run(cc_ctx *C, const cc_csr *g, cc_algo algo, const cc_config *cfg_in, u
     G.m = m;
     G.idb = idb;
     G.err = C->d_err;
+    // Host input that suits the tiled pass (a sample of rows keeps most edges
+    // inside their tile) is copied chunk by chunk while the tile kernel works
+    // on the chunks already on the device.
+    ccg::HostSource hsrc{g->row_ptr, g->col, C->copy_stream};
+    bool streamed = false;
+    if (g->where == CC_HOST && n > 0 && m > 0 &&
+        (algo == CC_ALLREDUCE || (algo == CC_EXP && g->num_parts == 1)) &&
+        (C->uf.mode == ccg::kUfTiled ||
+         (C->uf.mode == ccg::kUfAuto && n >= 4ull * C->uf.tile_vertices &&
+          ccg::host_cut_share(g->row_ptr, g->col, idb, n, m, C->uf.tile_vertices) < 0.5)))
+      streamed = true;
     if (g->where == CC_HOST) {
       rp_d.alloc(8 * (n + 1), s, C->pool);
       col_d.alloc((size_t)idb * (m ? m : 1), s, C->pool);
-      if (n) CCG_CUDA(cudaMemcpyAsync(rp_d.p, g->row_ptr, 8 * (n + 1), cudaMemcpyHostToDevice, s));
-      if (m) CCG_CUDA(cudaMemcpyAsync(col_d.p, g->col, (size_t)idb * m, cudaMemcpyHostToDevice, s));
+      if (streamed) {
+        // the copy stream may only write the buffers once they are allocated
+        cudaEvent_t ev;
+        CCG_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+        CCG_CUDA(cudaEventRecord(ev, s));
+        CCG_CUDA(cudaStreamWaitEvent(C->copy_stream, ev, 0));
+        cudaEventDestroy(ev);
+      } else {
+        if (n) CCG_CUDA(cudaMemcpyAsync(rp_d.p, g->row_ptr, 8 * (n + 1), cudaMemcpyHostToDevice, s));
+        if (m) CCG_CUDA(cudaMemcpyAsync(col_d.p, g->col, (size_t)idb * m, cudaMemcpyHostToDevice, s));
+      }
       st.h2d_bytes = n ? 8 * (n + 1) + (uint64_t)idb * m : 0;
       G.rp = rp_d.as<uint64_t>();
       G.col = col_d.p;
@@ -431,6 +457,7 @@ int ctx_run(cc_ctx *C, const cc_csr *g, cc_algo algo, const cc_config *cfg_in, u
     }
     Solver S{C, s, C->pool, c, cfg, seed, st};
     S.uf = C->uf;
+    if (streamed) S.hs = &hsrc;
     S.run(algo, G, g->num_parts, lab);
     CCG_CUDA(cudaEventRecord(ev[2], s));
     DevBuf cnt(8, s, C->pool);

@@ -15,6 +15,7 @@ void batch_cache_free(BatchCache *c);
 struct cc_ctx {
   int device = 0;
   cudaStream_t stream = nullptr;
+  cudaStream_t copy_stream = nullptr;  // host-to-device chunks overlapping the tile pass
   bool own_stream = false;
   cudaMemPool_t pool = nullptr;
   int *d_flag = nullptr;

@@ -32,9 +32,20 @@ struct UfTuning {
   uint32_t tile_vertices = 16384;  // vertices per CTA tile (4 bytes of shared memory each)
   uint32_t tile_threads = 1024;
 };
+// Host source of a caller graph whose device buffers are still empty: the
+// tiled pass copies tile-aligned chunks on `copy` and overlaps them with the
+// tile kernel (rp/col of the Csr are the destination device buffers).
+struct HostSource {
+  const uint64_t *rp;
+  const void *col;
+  cudaStream_t copy;
+};
 void uf_components(const Csr &g, uint32_t *parent, const PartMap *pm,
                    const UfTuning &tu, cudaStream_t s, cudaMemPool_t pool,
-                   Counters &c);
+                   Counters &c, const HostSource *hs = nullptr);
+// Share of sampled edges (u < v) that leave their tile, from a host CSR.
+double host_cut_share(const uint64_t *rp, const void *col, int idb, uint64_t n, uint64_t m,
+                      uint32_t tile);
 
 // Write uint32 labels to an id_bytes-wide output array.
 void widen_labels(const uint32_t *in, void *out, int out_bytes, uint64_t n,

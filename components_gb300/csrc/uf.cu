@@ -299,7 +299,8 @@ constexpr int kRootStage = 2048;
 
 template <class T, bool PART>
 __global__ void __launch_bounds__(1024)
-    k_tile2(uint64_t n, uint64_t m, const uint64_t *__restrict__ rp, const T *__restrict__ col,
+    k_tile2(uint64_t n, uint64_t m, uint64_t v_begin, uint64_t v_end,
+            const uint64_t *__restrict__ rp, const T *__restrict__ col,
             uint32_t *__restrict__ p, PartMap pm, uint32_t tile, uint32_t hub_degree,
             uint32_t *__restrict__ hubs, uint64_t hub_cap, unsigned int *__restrict__ nhubs,
             uint2 *__restrict__ cut, uint64_t cut_cap, unsigned long long *__restrict__ ncut,
@@ -310,8 +311,9 @@ __global__ void __launch_bounds__(1024)
   __shared__ unsigned int ccount, rcount;
   __shared__ unsigned long long cbase, rbase;
   volatile uint32_t *s = tile_parent;
-  for (uint64_t t0 = (uint64_t)blockIdx.x * tile; t0 < n; t0 += (uint64_t)gridDim.x * tile) {
-    const uint32_t len = (uint32_t)min((uint64_t)tile, n - t0);
+  for (uint64_t t0 = v_begin + (uint64_t)blockIdx.x * tile; t0 < v_end;
+       t0 += (uint64_t)gridDim.x * tile) {
+    const uint32_t len = (uint32_t)min((uint64_t)tile, v_end - t0);
     for (uint32_t i = threadIdx.x; i < len; i += blockDim.x) s[i] = i;
     if (threadIdx.x == 0) {
       ccount = 0;
@@ -572,7 +574,7 @@ void run_uf(const Csr &g, uint32_t *parent, const PartMap &pm, uint32_t hub_degr
 
 template <class T, bool PART>
 void run_uf_tiled(const Csr &g, uint32_t *parent, const PartMap &pm, const UfTuning &tu,
-                  cudaStream_t s, cudaMemPool_t pool, Counters &c) {
+                  cudaStream_t s, cudaMemPool_t pool, Counters &c, const HostSource *hs) {
   const T *col = static_cast<const T *>(g.col);
   const uint64_t si = (uint64_t)g.idb;
   const uint32_t tile = tu.tile_vertices;
@@ -596,12 +598,42 @@ void run_uf_tiled(const Csr &g, uint32_t *parent, const PartMap &pm, const UfTun
   // chains stay in shared memory); cut edges and roots are counted where read
   const uint64_t tile_bytes = 8 * (g.n + 1) + g.m * si + 4 * g.n;
   cudaEvent_t t0 = c.tic(s);
-  k_tile2<T, PART><<<grid, threads, smem, s>>>(g.n, g.m, g.rp, col, parent, pm, tile,
-                                               tu.hub_degree, hubs.as<uint32_t>(), hub_cap,
-                                               nh.as<unsigned int>(), cut.as<uint2>(), cut_cap,
-                                               ncut, roots.as<uint32_t>(), nroots, g.err);
-  CCG_LAUNCH_CHECK();
-  c.toc(s, "uf_tile", t0, tile_bytes);
+  if (!hs) {
+    k_tile2<T, PART><<<grid, threads, smem, s>>>(g.n, g.m, 0, g.n, g.rp, col, parent, pm, tile,
+                                                 tu.hub_degree, hubs.as<uint32_t>(), hub_cap,
+                                                 nh.as<unsigned int>(), cut.as<uint2>(), cut_cap,
+                                                 ncut, roots.as<uint32_t>(), nroots, g.err);
+    CCG_LAUNCH_CHECK();
+  } else {
+    // Copy tile-aligned chunks of the caller's host CSR on the copy stream and
+    // run each chunk's tiles as soon as its slice is on the device: the tile
+    // pass overlaps the host-to-device transfer.
+    const uint64_t chunk = (uint64_t)grid * tile;  // one full wave of CTAs
+    for (uint64_t v0 = 0; v0 < g.n; v0 += chunk) {
+      const uint64_t v1 = std::min<uint64_t>(g.n, v0 + chunk);
+      const uint64_t e0 = hs->rp[v0], e1 = hs->rp[v1];
+      if (e1 < e0 || e1 > g.m) throw Error(CC_ERR_INVALID, "CSR offsets are not monotone or exceed m_dir");
+      CCG_CUDA(cudaMemcpyAsync(const_cast<uint64_t *>(g.rp) + v0, hs->rp + v0, 8 * (v1 - v0 + 1),
+                               cudaMemcpyHostToDevice, hs->copy));
+      if (e1 > e0)
+        CCG_CUDA(cudaMemcpyAsync(static_cast<char *>(const_cast<void *>(g.col)) + si * e0,
+                                 static_cast<const char *>(hs->col) + si * e0, si * (e1 - e0),
+                                 cudaMemcpyHostToDevice, hs->copy));
+      cudaEvent_t ev;
+      CCG_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+      CCG_CUDA(cudaEventRecord(ev, hs->copy));
+      CCG_CUDA(cudaStreamWaitEvent(s, ev, 0));
+      cudaEventDestroy(ev);
+      const unsigned cgrid = (unsigned)std::min<uint64_t>((v1 - v0 + tile - 1) / tile, grid);
+      k_tile2<T, PART><<<cgrid, threads, smem, s>>>(g.n, g.m, v0, v1, g.rp, col, parent, pm, tile,
+                                                    tu.hub_degree, hubs.as<uint32_t>(), hub_cap,
+                                                    nh.as<unsigned int>(), cut.as<uint2>(),
+                                                    cut_cap, ncut, roots.as<uint32_t>(), nroots,
+                                                    g.err);
+      CCG_LAUNCH_CHECK();
+    }
+  }
+  c.toc(s, hs ? "uf_tile_streamed" : "uf_tile", t0, tile_bytes);
   cudaEvent_t t1 = c.tic(s);
   k_cut_union<<<kSMs * 16, kBlock, 0, s>>>(cut.as<uint2>(), ncut, cut_cap, parent);
   CCG_LAUNCH_CHECK();
@@ -704,7 +736,11 @@ void run_uf_afforest(const Csr &g, uint32_t *parent, const PartMap &pm, uint32_t
 
 template <class T, bool PART>
 void run_uf_mode(const Csr &g, uint32_t *parent, const PartMap &pm, const UfTuning &tu,
-                 cudaStream_t s, cudaMemPool_t pool, Counters &c) {
+                 cudaStream_t s, cudaMemPool_t pool, Counters &c, const HostSource *hs) {
+  if (hs) {  // the caller decided on the host that the tiled pass fits this graph
+    run_uf_tiled<T, PART>(g, parent, pm, tu, s, pool, c, hs);
+    return;
+  }
   int mode = tu.mode;
   if (mode == kUfAuto) {
     // the tiled pass wins when most edges stay inside their tile (grids,
@@ -714,7 +750,7 @@ void run_uf_mode(const Csr &g, uint32_t *parent, const PartMap &pm, const UfTuni
                ? kUfTiled
                : kUfSampled;
   }
-  if (mode == kUfTiled) run_uf_tiled<T, PART>(g, parent, pm, tu, s, pool, c);
+  if (mode == kUfTiled) run_uf_tiled<T, PART>(g, parent, pm, tu, s, pool, c, nullptr);
   else if (mode == kUfSampled) run_uf_afforest<T, PART>(g, parent, pm, tu.hub_degree, s, pool, c);
   else run_uf<T, PART>(g, parent, pm, tu.hub_degree, s, pool, c);
 }
@@ -722,7 +758,7 @@ void run_uf_mode(const Csr &g, uint32_t *parent, const PartMap &pm, const UfTuni
 }  // namespace
 
 void uf_components(const Csr &g, uint32_t *parent, const PartMap *pm, const UfTuning &tu_in,
-                   cudaStream_t s, cudaMemPool_t pool, Counters &c) {
+                   cudaStream_t s, cudaMemPool_t pool, Counters &c, const HostSource *hs) {
   if (g.n == 0) return;
   UfTuning tu = tu_in;
   if (tu.hub_degree < 1) tu.hub_degree = 32;
@@ -731,12 +767,31 @@ void uf_components(const Csr &g, uint32_t *parent, const PartMap *pm, const UfTu
   PartMap p = pm ? *pm : PartMap(g.n, 1);
   bool part = pm != nullptr && !(pm->rm == 0 && pm->q == g.n);
   if (g.idb == 8) {
-    if (part) run_uf_mode<uint64_t, true>(g, parent, p, tu, s, pool, c);
-    else run_uf_mode<uint64_t, false>(g, parent, p, tu, s, pool, c);
+    if (part) run_uf_mode<uint64_t, true>(g, parent, p, tu, s, pool, c, hs);
+    else run_uf_mode<uint64_t, false>(g, parent, p, tu, s, pool, c, hs);
   } else {
-    if (part) run_uf_mode<uint32_t, true>(g, parent, p, tu, s, pool, c);
-    else run_uf_mode<uint32_t, false>(g, parent, p, tu, s, pool, c);
+    if (part) run_uf_mode<uint32_t, true>(g, parent, p, tu, s, pool, c, hs);
+    else run_uf_mode<uint32_t, false>(g, parent, p, tu, s, pool, c, hs);
   }
+}
+
+double host_cut_share(const uint64_t *rp, const void *col, int idb, uint64_t n, uint64_t m,
+                      uint32_t tile) {
+  const uint64_t samples = std::min<uint64_t>(n, 8192);
+  uint64_t tot = 0, cross = 0;
+  for (uint64_t i = 0; i < samples; ++i) {
+    const uint64_t v = i * n / samples, t0 = v / tile * tile;
+    const uint64_t b = rp[v], e = rp[v + 1];
+    if (e < b || e > m) continue;  // malformed rows are reported by the kernels
+    for (uint64_t k = b; k < e && k < b + 64; ++k) {
+      const uint64_t u = idb == 8 ? static_cast<const uint64_t *>(col)[k]
+                                  : static_cast<const uint32_t *>(col)[k];
+      if (u >= v) continue;
+      ++tot;
+      cross += u < t0;
+    }
+  }
+  return tot ? (double)cross / (double)tot : 0.0;
 }
 
 void widen_labels(const uint32_t *in, void *out, int out_bytes, uint64_t n, cudaStream_t s,

@@ -147,7 +147,7 @@ def test_context_reuse_and_stats(cuda):
     st = ctx.stats()
     assert st["num_components"] == len(np.unique(want))
     assert st["kernel_launches"] > 0 and st["bytes_algorithmic"] > 0
-    assert "uf_hook" in st["kernels"] or "uf_tile" in st["kernels"]
+    assert any(k.startswith("uf_") for k in st["kernels"])  # hook pass timed
     arena = ctx.arena_bytes()
     gpu_labels(G, "exp", 1, "device", ctx=ctx)
     assert ctx.arena_bytes() == arena  # steady state: the pool is reused
