@@ -227,7 +227,13 @@ def workload_single(args, name):
             top = max(kern.items(), key=lambda kv: kv[1]["ms"])
             per_ms = top[1]["ms"] / top[1]["launches"]
             ach = top[1]["bytes"] / top[1]["launches"] / (per_ms * 1e-3) / 1e9
-            roof = {"kernel": top[0], "achieved_GBs": ach, "frac": ach / peak, "ms_per_launch": per_ms}
+            roof = {"kernel": top[0], "achieved_GBs": ach, "frac": ach / peak, "ms_per_launch": per_ms,
+                    "per_kernel": {k: {"launches": v["launches"] // args.steps,
+                                       "ms_per_launch": v["ms"] / v["launches"],
+                                       "frac": (v["bytes"] / v["launches"]
+                                                / (v["ms"] / v["launches"] * 1e-3) / 1e9 / peak)
+                                       if v["bytes"] and v["ms"] > 0 else None}
+                                   for k, v in kern.items()}}
         print(json.dumps({
             "workload": name, "graph": desc, "n": G.n, "m_dir": G.m, "algo": algo,
             "virtual_ranks": P, "seq": seq, "metric": "Gedges/s per CC solve",

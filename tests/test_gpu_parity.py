@@ -181,3 +181,24 @@ def test_hook_modes_agree(cuda, mode):
                     got = gpu_labels(G, algo, P, "device", cc.Config(seed=1001), ctx=ctx)
                     assert np.array_equal(got, want), (mode, tile, G.n, algo, P)
         ctx.close()
+
+
+def test_streamed_host_input(cuda):
+    """Host CSR copied in tile-aligned chunks under the tile pass: same labels
+    for pageable and pinned buffers, both id widths, many chunks."""
+    import torch
+    for idb in (4, 8):
+        G = cc.gen_grid(1100, 900, 0.55, seed=12, id_bytes=idb)
+        want = oracle.uf_labels(G)
+        for tile in (0, 1024):
+            ctx = cc.Context(0)
+            ctx.set_tuning(hook_mode=_lib.CC_HOOK_TILED, tile_vertices=tile, tile_threads=256)
+            for algo in ("exp", "allreduce"):
+                assert np.array_equal(gpu_labels(G, algo, 1, "host", ctx=ctx), want), (idb, tile, algo)
+            Pn = G.pinned()
+            dt = torch.int32 if idb == 4 else torch.int64
+            lab = torch.empty(G.n, dtype=dt).pin_memory()
+            cc.ExponentialContraction(cc.Config(seed=1001), 0, 1, ctx).FindComponents(Pn, lab)
+            got = lab.numpy().view(np.uint32 if idb == 4 else np.uint64).astype(np.uint64)
+            assert np.array_equal(got, want), (idb, tile, "pinned")
+            ctx.close()
