@@ -621,7 +621,8 @@ void *cc_ctx_stream(cc_ctx *ctx) { return ctx ? (void *)ctx->stream : nullptr; }
 int cc_ctx_set_tuning(cc_ctx *ctx, const cc_tuning *t) {
   if (!ctx || !t) return CC_ERR_INVALID;
   if (t->hook_mode > CC_HOOK_SAMPLED) return CC_ERR_INVALID;
-  if (t->tile_vertices > 56 * 1024 || (t->tile_threads && (t->tile_threads % 32 || t->tile_threads > 1024)))
+  if ((t->tile_vertices && (t->tile_vertices < 32 || t->tile_vertices > 65536)) ||
+      (t->tile_threads && (t->tile_threads % 32 || t->tile_threads > 1024)))
     return CC_ERR_INVALID;
   ccg::UfTuning u;
   u.mode = (int)t->hook_mode;

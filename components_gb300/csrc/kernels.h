@@ -29,7 +29,7 @@ enum : int { kUfAuto = 0, kUfGlobal = 1, kUfTiled = 2, kUfSampled = 3 };
 struct UfTuning {
   int mode = kUfAuto;  // auto: tiled when a sample shows < 50 % tile-crossing edges, else sampled
   uint32_t hub_degree = 32;      // rows above: one warp per row
-  uint32_t tile_vertices = 16384;  // vertices per CTA tile (4 bytes of shared memory each)
+  uint32_t tile_vertices = 32768;  // vertices per CTA tile (2 bytes of shared memory each)
   uint32_t tile_threads = 1024;
 };
 // Host source of a caller graph whose device buffers are still empty: the

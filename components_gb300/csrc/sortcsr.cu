@@ -132,6 +132,7 @@ void scan_generic(uint64_t n, Get get, Put put, uint32_t *d_total, cudaStream_t 
 }
 
 // ---- radix sort --------------------------------------------------------------
+constexpr uint64_t kEmitPiece = 4096;  // edges per hub work item of the emit pass
 constexpr int kRadixBits = 8;
 constexpr int kRadix = 1 << kRadixBits;
 constexpr int kSortItems = 16;
@@ -268,23 +269,27 @@ __global__ void k_emit(uint64_t n, const uint64_t *__restrict__ rp, const T *__r
   }
 }
 
-// One warp per hub row (rows longer than the k_emit limit).
+// One warp per piece of a hub row (rows longer than the k_emit limit):
+// kEmitPiece edges each, so the longest row is spread over many warps.
 template <class T>
 __global__ void k_emit_hubs(const uint64_t *__restrict__ rp, const T *__restrict__ col,
                             const uint32_t *__restrict__ cl, PartMap pm, bool part, int b,
-                            const uint32_t *__restrict__ hubs,
-                            const unsigned int *__restrict__ d_nhubs,
+                            const uint2 *__restrict__ items, uint64_t cap,
+                            const unsigned int *__restrict__ d_nitems,
                             uint64_t *__restrict__ keys, unsigned long long *__restrict__ cnt) {
   const unsigned lane = lane_id();
   const uint64_t warp = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
   const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
-  const uint32_t nhubs = *d_nhubs;
-  for (uint64_t h = warp; h < nhubs; h += nwarps) {
-    uint32_t v = hubs[h];
-    uint64_t eb = __ldg(rp + v), ee = __ldg(rp + v + 1);
-    uint32_t cv = cl[v];
+  const uint64_t nitems = min((uint64_t)*d_nitems, cap);
+  for (uint64_t h = warp; h < nitems; h += nwarps) {
+    const uint2 it = items[h];
+    const uint32_t v = it.x;
+    const uint64_t re = __ldg(rp + v + 1);
+    const uint64_t eb = __ldg(rp + v) + (uint64_t)it.y * kEmitPiece;
+    const uint64_t ee = min(re, eb + kEmitPiece);
+    const uint32_t cv = cl[v];
     for (uint64_t e0 = eb; e0 < ee; e0 += 32) {
-      uint64_t e = e0 + lane;
+      const uint64_t e = e0 + lane;
       bool keep = false;
       uint64_t key = 0;
       if (e < ee) {
@@ -306,10 +311,16 @@ __global__ void k_emit_hubs(const uint64_t *__restrict__ rp, const T *__restrict
 
 // Rows longer than `limit` (hubs) are listed for the warp-per-row kernel.
 __global__ void k_list_hubs(uint64_t n, const uint64_t *__restrict__ rp, uint64_t limit,
-                            uint32_t *__restrict__ hubs, unsigned int *__restrict__ nh) {
+                            uint2 *__restrict__ items, uint64_t cap, unsigned int *__restrict__ nh) {
   for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < n;
        v += (uint64_t)gridDim.x * blockDim.x) {
-    if (rp[v + 1] - rp[v] > limit) hubs[atomicAdd(nh, 1u)] = (uint32_t)v;
+    const uint64_t d = rp[v + 1] - rp[v];
+    if (d <= limit) continue;
+    // a long row becomes ceil(d / kEmitPiece) warp-sized work items
+    const uint32_t np = (uint32_t)((d + kEmitPiece - 1) / kEmitPiece);
+    const unsigned int slot = atomicAdd(nh, np);
+    for (uint32_t q = 0; q < np && (uint64_t)slot + q < cap; ++q)
+      items[slot + q] = make_uint2((uint32_t)v, q);
   }
 }
 
@@ -381,17 +392,20 @@ void emit_keys(const Csr &g, const uint32_t *cl, const PartMap &pm, bool part, i
   // k_emit walks up to max-degree steps per warp; rows above hub_limit go to
   // the warp-per-row kernel so that one hub does not serialise 31 lanes.
   const uint64_t hub_limit = 128;
-  DevBuf hubs(4 * (g.m / (hub_limit + 1) + 1), s, pool), nh(4, s, pool);
+  const uint64_t cap = g.m / (hub_limit + 1) + g.m / kEmitPiece + 2;
+  DevBuf hubs(8 * cap, s, pool), nh(4, s, pool);
   CCG_CUDA(cudaMemsetAsync(nh.p, 0, 4, s));
   unsigned grid = grid_for(g.n, kBlock, kSMs * 32);
-  k_list_hubs<<<grid, kBlock, 0, s>>>(g.n, g.rp, hub_limit, hubs.as<uint32_t>(),
+  cudaEvent_t t0 = c.tic(s);
+  k_list_hubs<<<grid, kBlock, 0, s>>>(g.n, g.rp, hub_limit, hubs.as<uint2>(), cap,
                                       nh.as<unsigned int>());
   CCG_LAUNCH_CHECK();
   k_emit<T><<<grid, kBlock, 0, s>>>(g.n, g.rp, col, cl, pm, part, b, hub_limit, keys, cnt);
   CCG_LAUNCH_CHECK();
-  k_emit_hubs<T><<<kSMs * 8, kBlock, 0, s>>>(g.rp, col, cl, pm, part, b, hubs.as<uint32_t>(),
+  k_emit_hubs<T><<<kSMs * 8, kBlock, 0, s>>>(g.rp, col, cl, pm, part, b, hubs.as<uint2>(), cap,
                                              nh.as<unsigned int>(), keys, cnt);
   CCG_LAUNCH_CHECK();
+  c.toc(s, "contract_emit", t0, 8 * (g.n + 1) + g.m * ((uint64_t)g.idb + 4) + 4 * g.n);
   // relabel + compact: offsets, neighbour id and its cluster per edge, own
   // cluster per vertex (the emitted keys are counted at the sort)
   c.add(3, 8 * (g.n + 1) + g.m * ((uint64_t)g.idb + 4) + 4 * g.n);
@@ -455,7 +469,10 @@ void contract_graph(const Csr &g, const uint32_t *cl, uint64_t ncl,
     return;
   }
   DevBuf tmp(8 * ne, s, pool);
+  cudaEvent_t ts = c.tic(s);
   uint64_t *sorted = radix_sort_u64(keys.as<uint64_t>(), tmp.as<uint64_t>(), ne, 2 * b, s, pool, c);
+  c.toc(s, "contract_sort", ts, 24 * ne * (uint64_t)((2 * b + 7) / 8));
+  cudaEvent_t td = c.tic(s);
   // unique keys into the other buffer
   uint64_t *uk = (sorted == keys.as<uint64_t>()) ? tmp.as<uint64_t>() : keys.as<uint64_t>();
   DevBuf d_u(4, s, pool), d_nv(4, s, pool);
@@ -468,6 +485,7 @@ void contract_graph(const Csr &g, const uint32_t *cl, uint64_t ncl,
   CCG_LAUNCH_CHECK();
   scan_generic(ncl, GetFlag{out.newid.as<uint32_t>()}, PutNewId{out.newid.as<uint32_t>()},
                d_nv.as<uint32_t>(), s, pool, c);
+  c.toc(s, "contract_dedup", td, 16 * ne + 8 * ncl);
   uint32_t uv[2];
   CCG_CUDA(cudaMemcpyAsync(&uv[0], d_u.p, 4, cudaMemcpyDeviceToHost, s));
   CCG_CUDA(cudaMemcpyAsync(&uv[1], d_nv.p, 4, cudaMemcpyDeviceToHost, s));
@@ -477,6 +495,7 @@ void contract_graph(const Csr &g, const uint32_t *cl, uint64_t ncl,
   out.rp.alloc(8 * (out.n + 1), s, pool);
   out.col.alloc(4 * out.m, s, pool);
   out.vid.alloc(4 * (out.n ? out.n : 1), s, pool);
+  cudaEvent_t tb = c.tic(s);
   k_build_csr<<<grid_for(out.m, kBlock, kSMs * 16), kBlock, 0, s>>>(
       uk, d_u.as<uint32_t>(), b, out.newid.as<uint32_t>(), out.rp.as<uint64_t>(),
       out.col.as<uint32_t>(), d_nv.as<uint32_t>());
@@ -485,6 +504,7 @@ void contract_graph(const Csr &g, const uint32_t *cl, uint64_t ncl,
                                                            vid_of_cluster, out.vid.as<uint32_t>());
   CCG_LAUNCH_CHECK();
   // CSR rebuild: unique keys read, offsets + ids written, id map
+  c.toc(s, "contract_csr", tb, 8 * out.m + 8 * (out.n + 1) + 4 * out.m + 8 * ncl);
   c.add(4, 8 * out.m + 8 * (out.n + 1) + 4 * out.m + 8 * ncl);
 }
 

@@ -152,12 +152,35 @@ __global__ void k_hook_hubs(uint64_t n, const uint64_t *__restrict__ rp,
 __global__ void k_compress(uint64_t n, uint32_t *p) {
   for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < n;
        v += (uint64_t)gridDim.x * blockDim.x) {
-    uint32_t r = p[v];
-    if (r == (uint32_t)v) continue;
-    uint32_t nx;
+    const uint32_t r0 = p[v];
+    if (r0 == (uint32_t)v) continue;
+    uint32_t r = r0, nx;
     while ((nx = ld_cg(p + r)) != r) r = nx;
-    p[v] = r;
+    if (r != r0) p[v] = r;  // most vertices already point at their root
   }
+}
+
+// Hub rows are split into pieces of kPiece edges, one warp per piece, so that
+// one row of a million edges is spread over hundreds of warps.
+constexpr uint32_t kPiece = 2048;
+struct HubList {
+  uint2 *items;  // (row, piece index)
+  uint64_t cap;
+  unsigned int *count;
+};
+// Pieces needed for hub rows of a graph with m edges and rows above hub_degree.
+inline uint64_t hub_list_cap(uint64_t m, uint32_t hub_degree) {
+  return m / ((uint64_t)hub_degree + 1) + m / kPiece + 2;
+}
+__device__ __forceinline__ void queue_hub(const HubList &hl, uint32_t v, uint64_t len, int *err) {
+  const uint32_t np = (uint32_t)((len + kPiece - 1) / kPiece);
+  if (np == 0) return;
+  const unsigned int slot = atomicAdd(hl.count, np);
+  if ((uint64_t)slot + np > hl.cap) {
+    set_err(err, kErrOverflow);
+    return;
+  }
+  for (uint32_t q = 0; q < np; ++q) hl.items[slot + q] = make_uint2(v, q);
 }
 
 // ---- sampled linking (Afforest: Sutton, Ben-Nun, Barak, IPDPS 2018) ------------
@@ -174,19 +197,24 @@ __device__ __forceinline__ bool same_part(const PartMap &pm, uint32_t v, uint32_
   return pm.part(v) == pm.part(u);
 }
 
+// Both sampled neighbours of a row in one pass: they share the row's first
+// sector of ids, so the second costs no extra DRAM traffic.
 template <class T, bool PART>
 __global__ void k_aff_link(uint64_t n, uint64_t m, const uint64_t *__restrict__ rp,
-                           const T *__restrict__ col, uint32_t *p, PartMap pm, uint32_t r, int *err) {
+                           const T *__restrict__ col, uint32_t *p, PartMap pm, int *err) {
   for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < n;
        v += (uint64_t)gridDim.x * blockDim.x) {
     Row row;
-    if (!load_row(rp, v, m, err, row) || row.e - row.b <= r) continue;
-    uint64_t u = (uint64_t)__ldg(col + row.b + r);
-    if (u >= n) {
-      set_err(err, kErrBadId);
-      continue;
+    if (!load_row(rp, v, m, err, row)) continue;
+    const uint32_t k = (uint32_t)min(row.e - row.b, (uint64_t)kAffRounds);
+    for (uint32_t r = 0; r < k; ++r) {
+      const uint64_t u = (uint64_t)__ldg(col + row.b + r);
+      if (u >= n) {
+        set_err(err, kErrBadId);
+        continue;
+      }
+      if (!PART || same_part(pm, (uint32_t)v, (uint32_t)u)) uf_union(p, (uint32_t)v, (uint32_t)u);
     }
-    if (!PART || same_part(pm, (uint32_t)v, (uint32_t)u)) uf_union(p, (uint32_t)v, (uint32_t)u);
   }
 }
 
@@ -202,19 +230,19 @@ __global__ void k_aff_sample(uint64_t n, const uint32_t *p, uint32_t samples, ui
 template <class T, bool PART>
 __global__ void k_aff_rest(uint64_t n, uint64_t m, const uint64_t *__restrict__ rp,
                            const T *__restrict__ col, uint32_t *p, PartMap pm, uint32_t L,
-                           uint32_t hub_degree, uint32_t *__restrict__ hubs, uint64_t hub_cap,
-                           unsigned int *__restrict__ nhubs, int *err) {
+                           uint32_t hub_degree, HubList hl, int *err,
+                           unsigned long long *__restrict__ edges_read) {
+  uint32_t work = 0;  // neighbour ids this thread reads (for the byte count)
   for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < n;
        v += (uint64_t)gridDim.x * blockDim.x) {
     Row row;
     if (!load_row(rp, v, m, err, row) || row.e - row.b <= kAffRounds) continue;
     if (uf_find(p, (uint32_t)v) == L) continue;
     if (row.e - row.b > hub_degree) {
-      uint32_t slot = atomicAdd(nhubs, 1u);
-      if (slot < hub_cap) hubs[slot] = (uint32_t)v;
-      else set_err(err, kErrOverflow);
+      queue_hub(hl, (uint32_t)v, row.e - row.b - kAffRounds, err);
       continue;
     }
+    work += (uint32_t)(row.e - row.b - kAffRounds);
     for (uint64_t k = row.b + kAffRounds; k < row.e; ++k) {
       uint64_t u = (uint64_t)__ldg(col + k);
       if (u >= n) {
@@ -224,28 +252,45 @@ __global__ void k_aff_rest(uint64_t n, uint64_t m, const uint64_t *__restrict__ 
       if (!PART || same_part(pm, (uint32_t)v, (uint32_t)u)) uf_union(p, (uint32_t)v, (uint32_t)u);
     }
   }
+  if (edges_read) {  // every thread of the warp reaches this point
+    work = __reduce_add_sync(0xffffffffu, work);
+    if ((threadIdx.x & 31) == 0 && work) atomicAdd(edges_read, (unsigned long long)work);
+  }
 }
 
-template <class T, bool PART>
-__global__ void k_aff_rest_hubs(uint64_t n, const uint64_t *__restrict__ rp,
-                                const T *__restrict__ col, uint32_t *p, PartMap pm,
-                                const uint32_t *__restrict__ hubs, uint64_t hub_cap,
-                                const unsigned int *__restrict__ nhubs, int *err) {
+// One warp per hub piece: edges [skip + y*kPiece, skip + (y+1)*kPiece) of row
+// x.  LESS: only edges to smaller ids (hook/tile passes, each undirected edge
+// once); otherwise every edge (the sampled pass skips rows inside the giant
+// component, so an edge may be seen from its larger end only).
+template <class T, bool PART, bool LESS>
+__global__ void k_hub_pieces(uint64_t n, uint64_t m, const uint64_t *__restrict__ rp,
+                             const T *__restrict__ col, uint32_t *p, PartMap pm, uint32_t skip,
+                             HubList hl, int *err) {
   const unsigned lane = threadIdx.x & 31;
   const uint64_t warp = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
   const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
-  uint64_t nh = *nhubs;
-  if (nh > hub_cap) nh = hub_cap;
-  for (uint64_t h = warp; h < nh; h += nwarps) {
-    uint32_t v = hubs[h];
-    uint64_t b = __ldg(rp + v), e = __ldg(rp + v + 1);  // checked by k_aff_rest
-    for (uint64_t k = b + kAffRounds + lane; k < e; k += 32) {
-      uint64_t u = (uint64_t)__ldg(col + k);
+  uint64_t cnt = *hl.count;
+  if (cnt > hl.cap) cnt = hl.cap;  // an overflow was recorded; unwritten items are skipped below
+  for (uint64_t h = warp; h < cnt; h += nwarps) {
+    const uint2 it = hl.items[h];
+    const uint32_t v = it.x;
+    if (v >= n) continue;
+    const uint64_t rb = __ldg(rp + v), re = __ldg(rp + v + 1);
+    if (re < rb || re > m) continue;  // recorded by the pass that queued the row
+    const uint64_t b = rb + skip + (uint64_t)it.y * kPiece;
+    const uint64_t e = min(re, b + kPiece);
+    const uint32_t lo = PART ? part_lo(pm, v) : 0u;
+    for (uint64_t k = b + lane; k < e; k += 32) {
+      const uint64_t u = (uint64_t)__ldg(col + k);
       if (u >= n) {
         set_err(err, kErrBadId);
         continue;
       }
-      if (!PART || same_part(pm, v, (uint32_t)u)) uf_union(p, v, (uint32_t)u);
+      if (LESS) {
+        if (u < v && (!PART || (uint32_t)u >= lo)) uf_union(p, v, (uint32_t)u);
+      } else {
+        if (!PART || same_part(pm, v, (uint32_t)u)) uf_union(p, v, (uint32_t)u);
+      }
     }
   }
 }
@@ -263,188 +308,191 @@ __global__ void k_iota_parent(uint64_t n, uint32_t *p) {
 // its tile-local root, and only the edges that leave the tile go to a global
 // list.  This is the reference's partition-local pass with the CTA as the
 // rank (FindLocalComponents, exponential_contraction.h:391-411).
-__device__ __forceinline__ uint32_t ts_find(volatile uint32_t *p, uint32_t v) {
+// Shared-memory parent entries are 16 bits wide when the tile has at most
+// 65536 vertices (twice the tile for the same shared memory) and 32 bits
+// otherwise.
+__device__ __forceinline__ uint32_t ts_cas(uint16_t *a, uint32_t c, uint32_t v) {
+  return atomicCAS(reinterpret_cast<unsigned short *>(a), (unsigned short)c, (unsigned short)v);
+}
+__device__ __forceinline__ uint32_t ts_cas(uint32_t *a, uint32_t c, uint32_t v) {
+  return atomicCAS(reinterpret_cast<unsigned int *>(a), c, v);
+}
+template <class PT>
+__device__ __forceinline__ uint32_t tw_find(volatile PT *p, uint32_t v) {
   uint32_t cur = p[v];
   if (cur == v) return v;
   uint32_t prev = v, next;
   while (cur > (next = p[cur])) {
-    p[prev] = next;
+    p[prev] = (PT)next;
     prev = cur;
     cur = next;
   }
   return cur;
 }
-__device__ __forceinline__ void ts_union(volatile uint32_t *p, uint32_t a, uint32_t b) {
-  uint32_t ra = ts_find(p, a), rb = ts_find(p, b);
+template <class PT>
+__device__ __forceinline__ void tw_union(volatile PT *p, uint32_t a, uint32_t b) {
+  uint32_t ra = tw_find(p, a), rb = tw_find(p, b);
   while (ra != rb) {
     if (ra < rb) {
       uint32_t t = ra;
       ra = rb;
       rb = t;
     }
-    uint32_t old = atomicCAS((uint32_t *)(p + ra), ra, rb);
+    const uint32_t old = ts_cas(const_cast<PT *>(p + ra), ra, rb);
     if (old == ra) return;
-    ra = ts_find(p, old);
-    rb = ts_find(p, rb);
+    ra = tw_find(p, old);
+    rb = tw_find(p, rb);
   }
 }
 
-// The tile kernel: 32-bit offsets inside the tile, a plain per-thread edge
-// loop, tile-crossing edges staged in shared memory (flushed with one global
-// atomic per tile) with their near endpoint replaced by its tile-local root,
-// and the tile-local roots listed for the final roots-only compression.
-constexpr int kCutStage = 2048;  // staged cut edges per tile (16 KB)
+__device__ __forceinline__ uint64_t shfl64(uint64_t x, int src) {
+  const uint32_t lo = __shfl_sync(0xffffffffu, (uint32_t)x, src);
+  const uint32_t hi = __shfl_sync(0xffffffffu, (uint32_t)(x >> 32), src);
+  return ((uint64_t)hi << 32) | lo;
+}
 
-constexpr int kRootStage = 2048;
+// The tile kernel.  Warps take 32 consecutive rows at a time and walk the
+// rows' edges as one flattened, coalesced stream (lane k reads edge k of the
+// 32 rows' concatenated adjacency; its row comes from a binary search over
+// the warp's degree prefix sums).  Edges inside the tile go to a per-warp
+// queue in shared memory and are united 32 at a time, so every lane of a
+// union step has work.  Edges leaving the tile are staged in shared memory
+// (one global atomic per tile) and written out with their near end replaced
+// by its tile-local root; when the stage is full they go straight to the
+// global list with the raw near end.  Every vertex finally stores the global
+// id of its tile-local root.
+constexpr uint32_t kUnionQueue = 64;  // per warp: < 32 pending + up to 32 new
+constexpr uint32_t kTileMax = 65536;  // queue entries pack two 16-bit tile indices
 
-template <class T, bool PART>
+template <class PT>
+size_t tile_smem_bytes(uint32_t tile, uint32_t threads, uint32_t stage) {
+  return (size_t)tile * sizeof(PT) + (size_t)(threads / 32) * kUnionQueue * 4 + (size_t)stage * 8;
+}
+
+template <class T, bool PART, class PT>
 __global__ void __launch_bounds__(1024)
-    k_tile2(uint64_t n, uint64_t m, uint64_t v_begin, uint64_t v_end,
+    k_tile3(uint64_t n, uint64_t m, uint64_t v_begin, uint64_t v_end,
             const uint64_t *__restrict__ rp, const T *__restrict__ col,
-            uint32_t *__restrict__ p, PartMap pm, uint32_t tile, uint32_t hub_degree,
-            uint32_t *__restrict__ hubs, uint64_t hub_cap, unsigned int *__restrict__ nhubs,
-            uint2 *__restrict__ cut, uint64_t cut_cap, unsigned long long *__restrict__ ncut,
-            uint32_t *__restrict__ roots, unsigned long long *__restrict__ nroots, int *err) {
-  extern __shared__ uint32_t tile_parent[];
-  __shared__ uint2 cstage[kCutStage];
-  __shared__ uint32_t rstage[kRootStage];
-  __shared__ unsigned int ccount, rcount;
-  __shared__ unsigned long long cbase, rbase;
-  volatile uint32_t *s = tile_parent;
+            uint32_t *__restrict__ p, PartMap pm, uint32_t tile, uint32_t stage_cap,
+            uint32_t hub_degree, HubList hl, uint2 *__restrict__ cut, uint64_t cut_cap,
+            unsigned long long *__restrict__ ncut, int *err) {
+  extern __shared__ __align__(16) unsigned char tile_smem[];
+  // layout: cut stage (8-byte entries), union queues, tile parents
+  uint2 *cstage = reinterpret_cast<uint2 *>(tile_smem);
+  uint32_t *queues = reinterpret_cast<uint32_t *>(cstage + stage_cap);
+  volatile PT *s = reinterpret_cast<volatile PT *>(queues + (blockDim.x / 32) * kUnionQueue);
+  __shared__ unsigned int ccount;
+  __shared__ unsigned long long cbase;
+  const unsigned lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  const unsigned lt = (1u << lane) - 1u;
+  uint32_t *q = queues + wid * kUnionQueue;
   for (uint64_t t0 = v_begin + (uint64_t)blockIdx.x * tile; t0 < v_end;
        t0 += (uint64_t)gridDim.x * tile) {
     const uint32_t len = (uint32_t)min((uint64_t)tile, v_end - t0);
-    for (uint32_t i = threadIdx.x; i < len; i += blockDim.x) s[i] = i;
-    if (threadIdx.x == 0) {
-      ccount = 0;
-      rcount = 0;
-    }
+    const uint32_t tt = (uint32_t)t0;
+    for (uint32_t i = threadIdx.x; i < len; i += blockDim.x) s[i] = (PT)i;
+    if (threadIdx.x == 0) ccount = 0;
     __syncthreads();
-    const unsigned lane = threadIdx.x & 31;
-    const uint32_t span = (len + blockDim.x - 1) / blockDim.x * blockDim.x;  // warp-uniform
-    for (uint32_t i = threadIdx.x; i < span; i += blockDim.x) {
-      const uint64_t v = t0 + i;
-      uint64_t b = 0;
+    uint32_t qn = 0;  // warp-uniform queue fill
+    for (uint32_t g0 = wid * 32; g0 < len; g0 += nw * 32) {
+      const uint32_t i = g0 + lane;
+      uint64_t rb = 0;
       uint32_t deg = 0, lo = 0;
       if (i < len) {
-        const uint64_t rb = __ldg(rp + v), re = __ldg(rp + v + 1);
+        const uint64_t v = t0 + i;
+        rb = __ldg(rp + v);
+        const uint64_t re = __ldg(rp + v + 1);
         if (re < rb || re > m) {
           set_err(err, kErrBadOffsets);
         } else if (re - rb > hub_degree) {
-          uint32_t slot = atomicAdd(nhubs, 1u);
-          if (slot < hub_cap) hubs[slot] = (uint32_t)v;
-          else set_err(err, kErrOverflow);
+          queue_hub(hl, (uint32_t)v, re - rb, err);
         } else {
-          b = rb;
           deg = (uint32_t)(re - rb);
           if (PART) lo = part_lo(pm, (uint32_t)v);
         }
       }
-      // every lane walks the warp's longest row so the ballots below see the
-      // whole warp (rows above hub_degree were queued instead)
-      const uint32_t maxdeg = __reduce_max_sync(0xffffffffu, deg);
-      const uint32_t vv = (uint32_t)v, tt = (uint32_t)t0;
-      for (uint32_t j = 0; j < maxdeg; ++j) {
-        bool emit = false;
+      uint32_t inc = deg;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t t = __shfl_up_sync(0xffffffffu, inc, o);
+        if ((int)lane >= o) inc += t;
+      }
+      const uint32_t total = __shfl_sync(0xffffffffu, inc, 31);
+      const uint32_t off = inc - deg;
+      for (uint32_t f0 = 0; f0 < total; f0 += 32) {
+        const uint32_t f = f0 + lane;
+        int r = 0;  // the last lane whose row starts at or before f
+#pragma unroll
+        for (int step = 16; step; step >>= 1) {
+          const uint32_t o = __shfl_sync(0xffffffffu, off, r + step);
+          if (o <= f) r += step;
+        }
+        const uint32_t ro = __shfl_sync(0xffffffffu, off, r);
+        const uint64_t rbr = shfl64(rb, r);
+        const uint32_t lor = PART ? __shfl_sync(0xffffffffu, lo, r) : 0u;
+        const uint32_t vi = g0 + (uint32_t)r, vv = tt + vi;
+        bool uni = false, emit = false;
         uint32_t u = 0;
-        if (j < deg) {
-          const uint64_t uu = (uint64_t)__ldg(col + b + j);
+        if (f < total) {
+          const uint64_t uu = (uint64_t)__ldg(col + rbr + (f - ro));
           if (uu >= n) {
             set_err(err, kErrBadId);
-          } else if ((uint32_t)uu < vv && (!PART || (uint32_t)uu >= lo)) {
-            u = (uint32_t)uu;
-            if (u >= tt) ts_union(s, i, u - tt);
-            else emit = true;  // each undirected edge once, from its larger end
+          } else if ((uint32_t)uu < vv && (!PART || (uint32_t)uu >= lor)) {
+            u = (uint32_t)uu;  // each undirected edge once, from its larger end
+            if (u >= tt) uni = true;
+            else emit = true;
           }
         }
-        const unsigned msk = __ballot_sync(0xffffffffu, emit);
-        if (msk) {
-          const int leader = __ffs(msk) - 1;
+        const unsigned um = __ballot_sync(0xffffffffu, uni);
+        if (uni) q[qn + __popc(um & lt)] = vi | ((u - tt) << 16);
+        qn += __popc(um);
+        if (qn >= 32) {  // a full union step: the newest 32 entries
+          __syncwarp();
+          const uint32_t w = q[qn - 32 + lane];
+          tw_union(s, w & 0xffffu, w >> 16);
+          qn -= 32;
+          __syncwarp();
+        }
+        const unsigned em = __ballot_sync(0xffffffffu, emit);
+        if (em) {
           unsigned int base = 0;
-          if ((int)lane == leader) base = atomicAdd(&ccount, (unsigned)__popc(msk));
-          base = __shfl_sync(0xffffffffu, base, leader);
-          if (emit) {
-            const unsigned int slot = base + __popc(msk & ((1u << lane) - 1u));
-            if (slot < kCutStage) {
-              cstage[slot] = make_uint2(i, u);  // near end as a tile index for now
-            } else {
-              unsigned long long g = atomicAdd(ncut, 1ull);
-              if (g < cut_cap) cut[g] = make_uint2(vv, u);
+          if (lane == (unsigned)(__ffs(em) - 1)) base = atomicAdd(&ccount, (unsigned)__popc(em));
+          base = __shfl_sync(0xffffffffu, base, __ffs(em) - 1);
+          const unsigned int slot = base + __popc(em & lt);
+          const bool over = emit && slot >= stage_cap;
+          if (emit && !over) cstage[slot] = make_uint2(vi, u);  // near end as a tile index for now
+          const unsigned om = __ballot_sync(0xffffffffu, over);
+          if (om) {
+            unsigned long long gb = 0;
+            if (lane == (unsigned)(__ffs(om) - 1)) gb = atomicAdd(ncut, (unsigned long long)__popc(om));
+            gb = __shfl_sync(0xffffffffu, gb, __ffs(om) - 1);
+            if (over) {
+              const unsigned long long gs = gb + __popc(om & lt);
+              if (gs < cut_cap) cut[gs] = make_uint2(vv, u);
               else set_err(err, kErrOverflow);
             }
           }
         }
       }
     }
-    __syncthreads();
-    // every vertex stores the global id of its tile-local root; roots are listed
-    for (uint32_t i = threadIdx.x; i < span; i += blockDim.x) {
-      bool is_root = false;
-      if (i < len) {
-        uint32_t r = i, nx;
-        while ((nx = s[r]) != r) r = nx;
-        p[t0 + i] = (uint32_t)(t0 + r);
-        is_root = r == i;
-      }
-      const unsigned msk = __ballot_sync(0xffffffffu, is_root);
-      if (msk) {
-        const int leader = __ffs(msk) - 1;
-        unsigned int base = 0;
-        if ((int)lane == leader) base = atomicAdd(&rcount, (unsigned)__popc(msk));
-        base = __shfl_sync(0xffffffffu, base, leader);
-        if (is_root) {
-          const unsigned int slot = base + __popc(msk & ((1u << lane) - 1u));
-          if (slot < kRootStage) {
-            rstage[slot] = (uint32_t)(t0 + i);
-          } else {
-            unsigned long long g = atomicAdd(nroots, 1ull);
-            roots[g] = (uint32_t)(t0 + i);  // at most n roots: the list holds n
-          }
-        }
-      }
+    __syncwarp();
+    if (lane < qn) {  // the queue's remainder
+      const uint32_t w = q[lane];
+      tw_union(s, w & 0xffffu, w >> 16);
     }
     __syncthreads();
-    const unsigned int nc = min(ccount, (unsigned int)kCutStage);
-    const unsigned int nr = min(rcount, (unsigned int)kRootStage);
-    if (threadIdx.x == 0) {
-      cbase = nc ? atomicAdd(ncut, (unsigned long long)nc) : 0ull;
-      rbase = nr ? atomicAdd(nroots, (unsigned long long)nr) : 0ull;
-    }
+    // every vertex stores the global id of its tile-local root
+    for (uint32_t i = threadIdx.x; i < len; i += blockDim.x) p[t0 + i] = tt + tw_find(s, i);
+    const unsigned int nc = min(ccount, stage_cap);
+    if (threadIdx.x == 0) cbase = nc ? atomicAdd(ncut, (unsigned long long)nc) : 0ull;
     __syncthreads();
     for (uint32_t k = threadIdx.x; k < nc; k += blockDim.x) {
-      uint2 c = cstage[k];
-      uint32_t r = c.x, nx;
-      while ((nx = s[r]) != r) r = nx;  // near end -> its tile-local root
-      unsigned long long g = cbase + k;
-      if (g < cut_cap) cut[g] = make_uint2((uint32_t)(t0 + r), c.y);
+      const uint2 c = cstage[k];
+      const unsigned long long g = cbase + k;
+      if (g < cut_cap) cut[g] = make_uint2(tt + tw_find(s, c.x), c.y);
       else set_err(err, kErrOverflow);
     }
-    for (uint32_t k = threadIdx.x; k < nr; k += blockDim.x) roots[rbase + k] = rstage[k];
     __syncthreads();
-  }
-}
-
-// Roots-only compression: every tile-local root points at its final root.
-__global__ void k_roots_compress(const uint32_t *__restrict__ roots,
-                                 const unsigned long long *__restrict__ nroots, uint32_t *p) {
-  const uint64_t cnt = *nroots;
-  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < cnt;
-       i += (uint64_t)gridDim.x * blockDim.x) {
-    const uint32_t v = roots[i];
-    uint32_t r = ld_cg(p + v), nx;
-    if (r == v) continue;
-    while ((nx = ld_cg(p + r)) != r) r = nx;
-    st_cg(p + v, r);
-  }
-}
-
-// Every vertex points at a tile-local root (or at a final root): two hops.
-__global__ void k_two_hop(uint64_t n, uint32_t *p) {
-  for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < n;
-       v += (uint64_t)gridDim.x * blockDim.x) {
-    const uint32_t a = p[v];
-    const uint32_t r = ld_cg(p + a);
-    if (r != a) p[v] = r;
   }
 }
 
@@ -457,32 +505,6 @@ __global__ void k_cut_union(const uint2 *__restrict__ cut, const unsigned long l
        i += (uint64_t)gridDim.x * blockDim.x) {
     uint2 e = cut[i];
     uf_union(p, e.x, e.y);
-  }
-}
-
-// Hub rows of the tiled pass: one warp per row, every edge (no first-edge link
-// was made for them).
-template <class T, bool PART>
-__global__ void k_tile_hubs(uint64_t n, const uint64_t *__restrict__ rp, const T *__restrict__ col,
-                            uint32_t *p, PartMap pm, const uint32_t *__restrict__ hubs,
-                            uint64_t hub_cap, const unsigned int *__restrict__ nhubs, int *err) {
-  const unsigned lane = threadIdx.x & 31;
-  const uint64_t warp = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
-  const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
-  uint64_t nh = *nhubs;
-  if (nh > hub_cap) nh = hub_cap;
-  for (uint64_t h = warp; h < nh; h += nwarps) {
-    uint32_t v = hubs[h];
-    uint64_t b = __ldg(rp + v), e = __ldg(rp + v + 1);  // checked by k_tile
-    uint32_t lo = PART ? part_lo(pm, v) : 0u;
-    for (uint64_t k = b + lane; k < e; k += 32) {
-      uint64_t u = (uint64_t)__ldg(col + k);
-      if (u >= n) {
-        set_err(err, kErrBadId);
-        continue;
-      }
-      if (u < v && (!PART || (uint32_t)u >= lo)) uf_union(p, v, (uint32_t)u);
-    }
   }
 }
 
@@ -579,30 +601,44 @@ void run_uf_tiled(const Csr &g, uint32_t *parent, const PartMap &pm, const UfTun
   const uint64_t si = (uint64_t)g.idb;
   const uint32_t tile = tu.tile_vertices;
   const int threads = (int)tu.tile_threads;
-  const size_t smem = 4ull * tile;  // dynamic: the tile's parent array
-  const void *fn = (const void *)k_tile2<T, PART>;
+  if (tile < 32 || tile > kTileMax) throw Error(CC_ERR_INVALID, "tile_vertices must lie in [32, 65536]");
+  if (threads < 32 || threads > 1024 || threads % 32)
+    throw Error(CC_ERR_INVALID, "tile_threads must be a multiple of 32 up to 1024");
+  // shared memory: two CTAs per SM when the tile leaves room for a cut stage
+  // of at least 256 edges, else one; the stage takes what is left (<= 8192)
+  int dev = 0, sm_smem = 0, blk_smem = 0;
+  CCG_CUDA(cudaGetDevice(&dev));
+  CCG_CUDA(cudaDeviceGetAttribute(&sm_smem, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev));
+  CCG_CUDA(cudaDeviceGetAttribute(&blk_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+  const size_t fixed = tile_smem_bytes<uint16_t>(tile, (uint32_t)threads, 0);
+  const size_t reserve = 1024 + 64;  // per-CTA system reserve + static shared memory
+  size_t room = (size_t)sm_smem / 2 > reserve + fixed ? (size_t)sm_smem / 2 - reserve - fixed : 0;
+  if (room < 256 * 8) room = (size_t)blk_smem > 64 + fixed ? (size_t)blk_smem - 64 - fixed : 0;
+  const uint32_t stage = (uint32_t)std::min<size_t>(room / 8, 8192);
+  if (stage < 64) throw Error(CC_ERR_INVALID, "tile does not fit in shared memory");
+  const size_t smem = tile_smem_bytes<uint16_t>(tile, (uint32_t)threads, stage);
+  const void *fn = (const void *)k_tile3<T, PART, uint16_t>;
   CCG_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   int per_sm = 0;
   CCG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, threads, smem));
   if (per_sm < 1) throw Error(CC_ERR_INVALID, "tile does not fit in shared memory");
   const uint64_t tiles = (g.n + tile - 1) / tile;
   const unsigned grid = (unsigned)std::min<uint64_t>(tiles, (uint64_t)per_sm * kSMs);
-  const uint64_t hub_cap = g.m / (tu.hub_degree + 1) + 1;
+  const uint64_t hub_cap = hub_list_cap(g.m, tu.hub_degree);
   const uint64_t cut_cap = g.m + 1;
-  DevBuf hubs(4 * hub_cap, s, pool), nh(4, s, pool), cut(8 * cut_cap, s, pool), cnt(16, s, pool);
-  DevBuf roots(4 * g.n, s, pool);
+  DevBuf hubs(8 * hub_cap, s, pool), nh(4, s, pool), cut(8 * cut_cap, s, pool), cnt(8, s, pool);
+  const HubList hl{hubs.as<uint2>(), hub_cap, nh.as<unsigned int>()};
   CCG_CUDA(cudaMemsetAsync(nh.p, 0, 4, s));
-  CCG_CUDA(cudaMemsetAsync(cnt.p, 0, 16, s));
-  unsigned long long *ncut = cnt.as<unsigned long long>(), *nroots = ncut + 1;
+  CCG_CUDA(cudaMemsetAsync(cnt.p, 0, 8, s));
+  unsigned long long *ncut = cnt.as<unsigned long long>();
   // tile pass: offsets, every id once, own parent written once (the parent
-  // chains stay in shared memory); cut edges and roots are counted where read
+  // chains stay in shared memory); cut edges are counted where read
   const uint64_t tile_bytes = 8 * (g.n + 1) + g.m * si + 4 * g.n;
   cudaEvent_t t0 = c.tic(s);
   if (!hs) {
-    k_tile2<T, PART><<<grid, threads, smem, s>>>(g.n, g.m, 0, g.n, g.rp, col, parent, pm, tile,
-                                                 tu.hub_degree, hubs.as<uint32_t>(), hub_cap,
-                                                 nh.as<unsigned int>(), cut.as<uint2>(), cut_cap,
-                                                 ncut, roots.as<uint32_t>(), nroots, g.err);
+    k_tile3<T, PART, uint16_t><<<grid, threads, smem, s>>>(g.n, g.m, 0, g.n, g.rp, col, parent,
+                                                           pm, tile, stage, tu.hub_degree, hl,
+                                                           cut.as<uint2>(), cut_cap, ncut, g.err);
     CCG_LAUNCH_CHECK();
   } else {
     // Copy tile-aligned chunks of the caller's host CSR on the copy stream and
@@ -625,11 +661,10 @@ void run_uf_tiled(const Csr &g, uint32_t *parent, const PartMap &pm, const UfTun
       CCG_CUDA(cudaStreamWaitEvent(s, ev, 0));
       cudaEventDestroy(ev);
       const unsigned cgrid = (unsigned)std::min<uint64_t>((v1 - v0 + tile - 1) / tile, grid);
-      k_tile2<T, PART><<<cgrid, threads, smem, s>>>(g.n, g.m, v0, v1, g.rp, col, parent, pm, tile,
-                                                    tu.hub_degree, hubs.as<uint32_t>(), hub_cap,
-                                                    nh.as<unsigned int>(), cut.as<uint2>(),
-                                                    cut_cap, ncut, roots.as<uint32_t>(), nroots,
-                                                    g.err);
+      k_tile3<T, PART, uint16_t><<<cgrid, threads, smem, s>>>(g.n, g.m, v0, v1, g.rp, col,
+                                                              parent, pm, tile, stage,
+                                                              tu.hub_degree, hl, cut.as<uint2>(),
+                                                              cut_cap, ncut, g.err);
       CCG_LAUNCH_CHECK();
     }
   }
@@ -639,19 +674,17 @@ void run_uf_tiled(const Csr &g, uint32_t *parent, const PartMap &pm, const UfTun
   CCG_LAUNCH_CHECK();
   c.toc(s, "uf_cut_union", t1, 0);
   cudaEvent_t t2 = c.tic(s);
-  k_tile_hubs<T, PART><<<kSMs * 8, kBlock, 0, s>>>(g.n, g.rp, col, parent, pm, hubs.as<uint32_t>(),
-                                                   hub_cap, nh.as<unsigned int>(), g.err);
+  k_hub_pieces<T, PART, true><<<kSMs * 8, kBlock, 0, s>>>(g.n, g.m, g.rp, col, parent, pm, 0u,
+                                                          hl, g.err);
   CCG_LAUNCH_CHECK();
   c.toc(s, "uf_hook_hubs", t2, 0);
+  // every vertex points at a tile-local root or at a final root: full
+  // compression, writing only the entries that change
   cudaEvent_t t3 = c.tic(s);
-  k_roots_compress<<<kSMs * 16, kBlock, 0, s>>>(roots.as<uint32_t>(), nroots, parent);
+  k_compress<<<grid_for(g.n, kBlock, kSMs * 32), kBlock, 0, s>>>(g.n, parent);
   CCG_LAUNCH_CHECK();
-  c.toc(s, "uf_roots_compress", t3, 0);
-  cudaEvent_t t4 = c.tic(s);
-  k_two_hop<<<grid_for(g.n, kBlock, kSMs * 32), kBlock, 0, s>>>(g.n, parent);
-  CCG_LAUNCH_CHECK();
-  c.toc(s, "uf_two_hop", t4, 3 * g.n * 4);
-  c.add(5, tile_bytes + 3 * g.n * 4);
+  c.toc(s, "uf_compress", t3, 3 * g.n * 4);
+  c.add(4, tile_bytes + 3 * g.n * 4);
 }
 
 // Share of tile-crossing edges on a sample of 8192 rows (one small readback).
@@ -680,14 +713,12 @@ void run_uf_afforest(const Csr &g, uint32_t *parent, const PartMap &pm, uint32_t
   const unsigned grid = grid_for(g.n, kBlock, kSMs * 32);
   k_iota_parent<<<grid, kBlock, 0, s>>>(g.n, parent);
   CCG_LAUNCH_CHECK();
-  // each link round: offsets, one id, one union (two parent gathers)
-  const uint64_t link_bytes = 8 * (g.n + 1) + g.n * si + 2 * g.n * 4;
-  for (uint32_t r = 0; r < kAffRounds; ++r) {
-    cudaEvent_t t0 = c.tic(s);
-    k_aff_link<T, PART><<<grid, kBlock, 0, s>>>(g.n, g.m, g.rp, col, parent, pm, r, g.err);
-    CCG_LAUNCH_CHECK();
-    c.toc(s, "uf_sample_link", t0, link_bytes);
-  }
+  // link pass: offsets, kAffRounds ids and unions (two parent gathers each)
+  const uint64_t link_bytes = 8 * (g.n + 1) + kAffRounds * g.n * (si + 2 * 4);
+  cudaEvent_t t0 = c.tic(s);
+  k_aff_link<T, PART><<<grid, kBlock, 0, s>>>(g.n, g.m, g.rp, col, parent, pm, g.err);
+  CCG_LAUNCH_CHECK();
+  c.toc(s, "uf_sample_link", t0, link_bytes);
   k_compress<<<grid, kBlock, 0, s>>>(g.n, parent);
   CCG_LAUNCH_CHECK();
   // most frequent root of a sample = the giant component, if there is one
@@ -711,27 +742,39 @@ void run_uf_afforest(const Csr &g, uint32_t *parent, const PartMap &pm, uint32_t
     }
     i = j;
   }
-  const uint64_t hub_cap = g.m / (hub_degree + 1) + 1;
-  DevBuf hubs(4 * hub_cap, s, pool), nh(4, s, pool);
+  const uint64_t hub_cap = hub_list_cap(g.m, hub_degree);
+  DevBuf hubs(8 * hub_cap, s, pool), nh(4, s, pool);
   CCG_CUDA(cudaMemsetAsync(nh.p, 0, 4, s));
-  // remaining pass: offsets, own root, and the ids + unions of the rows
-  // outside the giant component (counted as the full edge stream)
-  const uint64_t rest_bytes = 8 * (g.n + 1) + g.m * si + g.m * 4 + 2 * g.n * 4;
+  const HubList hl{hubs.as<uint2>(), hub_cap, nh.as<unsigned int>()};
+  // remaining pass: every row's offsets and root; then, for the rows outside
+  // the giant component, one id and one root gather per remaining edge.  The
+  // edge part is counted on the device while profiling and left out otherwise.
+  uint64_t rest_bytes = 8 * (g.n + 1) + 4 * g.n;
+  DevBuf ecount(8, s, pool);
+  if (c.prof) CCG_CUDA(cudaMemsetAsync(ecount.p, 0, 8, s));
   cudaEvent_t t1 = c.tic(s);
-  k_aff_rest<T, PART><<<grid, kBlock, 0, s>>>(g.n, g.m, g.rp, col, parent, pm, L, hub_degree,
-                                              hubs.as<uint32_t>(), hub_cap, nh.as<unsigned int>(),
-                                              g.err);
+  k_aff_rest<T, PART><<<grid, kBlock, 0, s>>>(
+      g.n, g.m, g.rp, col, parent, pm, L, hub_degree, hl, g.err,
+      c.prof ? ecount.as<unsigned long long>() : nullptr);
   CCG_LAUNCH_CHECK();
   c.toc(s, "uf_sample_rest", t1, rest_bytes);
-  k_aff_rest_hubs<T, PART><<<kSMs * 8, kBlock, 0, s>>>(g.n, g.rp, col, parent, pm,
-                                                       hubs.as<uint32_t>(), hub_cap,
-                                                       nh.as<unsigned int>(), g.err);
+  if (c.prof && !c.recs.empty()) {
+    unsigned long long edges = 0;
+    CCG_CUDA(cudaMemcpyAsync(&edges, ecount.p, 8, cudaMemcpyDeviceToHost, s));
+    CCG_CUDA(cudaStreamSynchronize(s));
+    rest_bytes += edges * (si + 4);
+    c.recs.back().bytes = rest_bytes;
+  }
+  cudaEvent_t th = c.tic(s);
+  k_hub_pieces<T, PART, false><<<kSMs * 8, kBlock, 0, s>>>(g.n, g.m, g.rp, col, parent, pm,
+                                                           kAffRounds, hl, g.err);
   CCG_LAUNCH_CHECK();
+  c.toc(s, "uf_sample_hubs", th, 0);
   cudaEvent_t t2 = c.tic(s);
   k_compress<<<grid, kBlock, 0, s>>>(g.n, parent);
   CCG_LAUNCH_CHECK();
   c.toc(s, "uf_compress", t2, 3 * g.n * 4);
-  c.add(8, 4 * g.n + kAffRounds * link_bytes + rest_bytes + 6 * g.n * 4);
+  c.add(7, 4 * g.n + link_bytes + rest_bytes + 6 * g.n * 4);
 }
 
 template <class T, bool PART>

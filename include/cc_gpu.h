@@ -220,10 +220,11 @@ typedef struct cc_tuning {
                               vertex, then only rows outside the largest
                               component; AUTO picks TILED when a sample of rows
                               shows < 50 % tile-crossing edges, else SAMPLED */
-  uint32_t tile_vertices;  /* vertices per CTA tile, 4 bytes of shared memory
-                              each (default 16384, at most 56K) */
+  uint32_t tile_vertices;  /* vertices per CTA tile, 2 bytes of shared memory
+                              each (default 32768, 32 to 65536) */
   uint32_t tile_threads;   /* CTA size of the tiled pass (default 1024) */
-  uint32_t hub_degree;     /* rows above go one warp per row (default 32) */
+  uint32_t hub_degree;     /* rows above are split into pieces of 2048 edges,
+                              one warp per piece (default 32) */
 } cc_tuning;
 int cc_ctx_set_tuning(cc_ctx *ctx, const cc_tuning *t);
 int cc_ctx_get_tuning(cc_ctx *ctx, cc_tuning *t);
