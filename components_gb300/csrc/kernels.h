@@ -27,7 +27,7 @@ struct Csr {
 // (exponential_contraction.h:391-411 FindLocalComponents).
 enum : int { kUfAuto = 0, kUfGlobal = 1, kUfTiled = 2, kUfSampled = 3 };
 struct UfTuning {
-  int mode = kUfAuto;  // auto: tiled when a sample shows < 50 % tile-crossing edges, else sampled
+  int mode = kUfAuto;  // auto: tiled when a row sample suits it (host_tiles_suit), else sampled
   uint32_t hub_degree = 32;      // rows above: one warp per row
   uint32_t tile_vertices = 32768;  // vertices per CTA tile (2 bytes of shared memory each)
   uint32_t tile_threads = 1024;
@@ -43,9 +43,11 @@ struct HostSource {
 void uf_components(const Csr &g, uint32_t *parent, const PartMap *pm,
                    const UfTuning &tu, cudaStream_t s, cudaMemPool_t pool,
                    Counters &c, const HostSource *hs = nullptr);
-// Share of sampled edges (u < v) that leave their tile, from a host CSR.
-double host_cut_share(const uint64_t *rp, const void *col, int idb, uint64_t n, uint64_t m,
-                      uint32_t tile);
+// Whether the tiled pass suits a host CSR: on a sample of 8192 rows, fewer than
+// half of the edges (u < v) leave their tile and fewer than a tenth lie in
+// rows above hub_degree.
+bool host_tiles_suit(const uint64_t *rp, const void *col, int idb, uint64_t n, uint64_t m,
+                     uint32_t tile, uint32_t hub_degree);
 
 // Write uint32 labels to an id_bytes-wide output array.
 void widen_labels(const uint32_t *in, void *out, int out_bytes, uint64_t n,

@@ -179,28 +179,18 @@ struct Server {
 
   uint64_t bytes_needed(const cc_csr &g) const {
     uint64_t b = 8 * (g.n + 1) + (uint64_t)g.id_bytes * g.m_dir + 4 * (g.n + 1) + 3 * 256;
-    if (g.n > cfg.smem_max_n) b += 8 * (g.m_dir + 1) + 4 * (g.m_dir / 33 + 1) + 4096;  // hook scratch
+    if (g.n > cfg.smem_max_n)  // hook scratch: cut list and hub pieces
+      b += 8 * (g.m_dir + 1) + 8 * (g.m_dir / 33 + g.m_dir / 2048 + 2) + 8192;
     return b;
   }
 
-  // Share of sampled rows' edges (u < v) leaving a 16K-vertex tile, from the
-  // host CSR: decides the hook schedule of a large graph without a device
-  // round trip.
+  // Hook schedule of a large graph, decided on the host CSR without a device
+  // round trip: the tiled pass when a row sample suits it, else sampled linking.
   static bool prefers_tiles(const cc_csr &g) {
-    const uint64_t tile = 16384, samples = 256;
-    if (g.n < 4 * tile) return false;
-    uint64_t tot = 0, cross = 0;
-    for (uint64_t i = 0; i < samples; ++i) {
-      uint64_t v = i * g.n / samples;
-      for (uint64_t k = g.row_ptr[v]; k < g.row_ptr[v + 1] && k < g.row_ptr[v] + 64; ++k) {
-        uint64_t u = g.id_bytes == 8 ? static_cast<const uint64_t *>(g.col)[k]
-                                     : static_cast<const uint32_t *>(g.col)[k];
-        if (u >= v) continue;
-        ++tot;
-        cross += u < v / tile * tile;
-      }
-    }
-    return tot && cross * 2 < tot;
+    const UfTuning tu;
+    if (g.n < 4ull * tu.tile_vertices) return false;
+    return host_tiles_suit(g.row_ptr, g.col, (int)g.id_bytes, g.n, g.m_dir, tu.tile_vertices,
+                           tu.hub_degree);
   }
 
   void stage(Req *r) {  // worker thread, no lock held
@@ -257,7 +247,7 @@ struct Server {
       G.idb = (int)r->g.id_bytes;
       G.err = reinterpret_cast<int *>(r->lab.as<uint32_t>() + r->g.n);
       UfTuning tu;
-      tu.mode = r->tiled ? kUfTiled : kUfGlobal;
+      tu.mode = r->tiled ? kUfTiled : kUfSampled;
       uf_components(G, r->lab.as<uint32_t>(), nullptr, tu, s, pool, c);
     }
     uint32_t bid;

@@ -160,6 +160,40 @@ __global__ void k_compress(uint64_t n, uint32_t *p) {
   }
 }
 
+// Full compression with four chains per thread, walked in lockstep so that
+// their dependent loads are in flight together (the chains are latency-bound;
+// p[x] < x for every non-root, so each chain ends).  Only changed entries are
+// written.
+__global__ void k_compress4(uint64_t n, uint32_t *p) {
+  const uint64_t nq = (n + 3) / 4;
+  for (uint64_t qi = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; qi < nq;
+       qi += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t v0 = qi * 4;
+    uint32_t r0[4], r[4];
+    bool act[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const bool in = v0 + k < n;
+      r0[k] = in ? p[v0 + k] : 0u;
+      r[k] = r0[k];
+      act[k] = in && r0[k] != (uint32_t)(v0 + k);
+    }
+    while (act[0] || act[1] || act[2] || act[3]) {
+      uint32_t nx[4];
+#pragma unroll
+      for (int k = 0; k < 4; ++k) nx[k] = act[k] ? ld_cg(p + r[k]) : r[k];
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        if (nx[k] == r[k]) act[k] = false;
+        else r[k] = nx[k];
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+      if (v0 + k < n && r[k] != r0[k]) p[v0 + k] = r[k];
+  }
+}
+
 // Hub rows are split into pieces of kPiece edges, one warp per piece, so that
 // one row of a million edges is spread over hundreds of warps.
 constexpr uint32_t kPiece = 2048;
@@ -496,29 +530,92 @@ __global__ void __launch_bounds__(1024)
   }
 }
 
-// Edges between tiles, on the global parent array of tile-local roots.
+// Edges between tiles, on the global parent array of tile-local roots.  Each
+// thread takes four edges and finds their eight roots in lockstep (path
+// halving as in uf_find), then links them one edge at a time.
 __global__ void k_cut_union(const uint2 *__restrict__ cut, const unsigned long long *__restrict__ ncut,
                             uint64_t cut_cap, uint32_t *p) {
   uint64_t cnt = *ncut;
   if (cnt > cut_cap) cnt = cut_cap;
-  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < cnt;
-       i += (uint64_t)gridDim.x * blockDim.x) {
-    uint2 e = cut[i];
-    uf_union(p, e.x, e.y);
+  const uint64_t nq = (cnt + 3) / 4;
+  for (uint64_t qi = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; qi < nq;
+       qi += (uint64_t)gridDim.x * blockDim.x) {
+    uint32_t prev[8], cur[8];
+    bool act[8];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const uint64_t e = qi * 4 + k;
+      const uint2 x = e < cnt ? cut[e] : make_uint2(0u, 0u);
+      prev[2 * k] = x.x;
+      prev[2 * k + 1] = x.y;
+    }
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      cur[j] = ld_cg(p + prev[j]);
+      act[j] = cur[j] != prev[j];
+    }
+    bool any = true;
+    while (any) {
+      uint32_t nx[8];
+#pragma unroll
+      for (int j = 0; j < 8; ++j) nx[j] = act[j] ? ld_cg(p + cur[j]) : cur[j];
+      any = false;
+#pragma unroll
+      for (int j = 0; j < 8; ++j) {
+        if (act[j] && cur[j] > nx[j]) {
+          st_cg(p + prev[j], nx[j]);  // path halving
+          prev[j] = cur[j];
+          cur[j] = nx[j];
+          any = true;
+        } else {
+          act[j] = false;
+        }
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      if (qi * 4 + k >= cnt) continue;
+      uint32_t ra = cur[2 * k], rb = cur[2 * k + 1];
+      while (ra != rb) {
+        if (ra < rb) {
+          const uint32_t t = ra;
+          ra = rb;
+          rb = t;
+        }
+        const uint32_t old = atomicCAS(p + ra, ra, rb);
+        if (old == ra) break;
+        ra = uf_find(p, old);
+        rb = uf_find(p, rb);
+      }
+    }
   }
 }
 
-// Share of sampled edges (u < v, same rank) that leave their tile.
+// Row i of a stratified sample: a hashed position inside stratum i, so that
+// a sample stride never aliases with a regular structure of the ids (grid rows).
+__host__ __device__ __forceinline__ uint64_t sample_row(uint64_t i, uint64_t samples, uint64_t n) {
+  const uint64_t lo = i * n / samples, hi = (i + 1) * n / samples;
+  return hi > lo ? lo + mix64(0x9e3779b97f4a7c15ull ^ i) % (hi - lo) : lo;
+}
+
+// Sampled edges (u < v, same rank): total, edges leaving their tile, and edges
+// of hub rows (about half of a hub row's entries are u < v).  Both kinds are
+// left to global unions by the tiled pass.
 template <class T, bool PART>
 __global__ void k_cut_sample(uint64_t n, uint64_t m, const uint64_t *__restrict__ rp,
                              const T *__restrict__ col, PartMap pm, uint32_t tile,
-                             uint32_t samples, unsigned long long *__restrict__ counts) {
-  unsigned long long tot = 0, cross = 0;
+                             uint32_t hub_degree, uint32_t samples,
+                             unsigned long long *__restrict__ counts) {
+  unsigned long long tot = 0, cross = 0, hub = 0;
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < samples; i += gridDim.x * blockDim.x) {
-    uint64_t v = (uint64_t)i * n / samples;
+    uint64_t v = sample_row(i, samples, n);
     uint64_t b = __ldg(rp + v), e = __ldg(rp + v + 1);
     if (e < b || e > m) continue;
-    if (e - b > 64) e = b + 64;
+    if (e - b > hub_degree) {
+      tot += (e - b) / 2;
+      hub += (e - b) / 2;
+      continue;
+    }
     uint64_t t0 = v / tile * tile;
     uint32_t lo = PART ? part_lo(pm, (uint32_t)v) : 0u;
     for (uint64_t k = b; k < e; ++k) {
@@ -530,6 +627,7 @@ __global__ void k_cut_sample(uint64_t n, uint64_t m, const uint64_t *__restrict_
   }
   atomicAdd(counts, tot);
   atomicAdd(counts + 1, cross);
+  atomicAdd(counts + 2, hub);
 }
 
 template <class OUT>
@@ -588,7 +686,7 @@ void run_uf(const Csr &g, uint32_t *parent, const PartMap &pm, uint32_t hub_degr
   CCG_LAUNCH_CHECK();
   c.toc(s, "uf_hook_hubs", t2, 0);
   cudaEvent_t t3 = c.tic(s);
-  k_compress<<<grid, kBlock, 0, s>>>(g.n, parent);
+  k_compress4<<<grid_for((g.n + 3) / 4, kBlock, kSMs * 16), kBlock, 0, s>>>(g.n, parent);
   CCG_LAUNCH_CHECK();
   c.toc(s, "uf_compress", t3, 3 * g.n * 4);
   c.add(4, (8 * (g.n + 1) + g.n * si + 4 * g.n) + hook_bytes + 3 * g.n * 4);
@@ -670,7 +768,7 @@ void run_uf_tiled(const Csr &g, uint32_t *parent, const PartMap &pm, const UfTun
   }
   c.toc(s, hs ? "uf_tile_streamed" : "uf_tile", t0, tile_bytes);
   cudaEvent_t t1 = c.tic(s);
-  k_cut_union<<<kSMs * 16, kBlock, 0, s>>>(cut.as<uint2>(), ncut, cut_cap, parent);
+  k_cut_union<<<kSMs * 8, kBlock, 0, s>>>(cut.as<uint2>(), ncut, cut_cap, parent);
   CCG_LAUNCH_CHECK();
   c.toc(s, "uf_cut_union", t1, 0);
   cudaEvent_t t2 = c.tic(s);
@@ -681,28 +779,36 @@ void run_uf_tiled(const Csr &g, uint32_t *parent, const PartMap &pm, const UfTun
   // every vertex points at a tile-local root or at a final root: full
   // compression, writing only the entries that change
   cudaEvent_t t3 = c.tic(s);
-  k_compress<<<grid_for(g.n, kBlock, kSMs * 32), kBlock, 0, s>>>(g.n, parent);
+  k_compress4<<<grid_for((g.n + 3) / 4, kBlock, kSMs * 16), kBlock, 0, s>>>(g.n, parent);
   CCG_LAUNCH_CHECK();
   c.toc(s, "uf_compress", t3, 3 * g.n * 4);
   c.add(4, tile_bytes + 3 * g.n * 4);
 }
 
-// Share of tile-crossing edges on a sample of 8192 rows (one small readback).
+// The tiled pass suits a graph when a sample of rows shows fewer than half of
+// the edges leaving their tile and fewer than a tenth in hub rows (hub edges
+// contend on a few global roots; the sampled pass skips most of them).
+inline bool tiles_fit(uint64_t tot, uint64_t cross, uint64_t hub) {
+  return tot == 0 || (2 * cross < tot && 10 * hub < tot);
+}
+
+// The decision above on a sample of 8192 rows of a device graph (one small
+// readback).
 template <class T, bool PART>
-double cut_share(const Csr &g, const PartMap &pm, uint32_t tile, cudaStream_t s,
-                 cudaMemPool_t pool, Counters &c) {
-  DevBuf cnt(16, s, pool);
-  CCG_CUDA(cudaMemsetAsync(cnt.p, 0, 16, s));
+bool tiles_suit(const Csr &g, const PartMap &pm, uint32_t tile, uint32_t hub_degree,
+                cudaStream_t s, cudaMemPool_t pool, Counters &c) {
+  DevBuf cnt(24, s, pool);
+  CCG_CUDA(cudaMemsetAsync(cnt.p, 0, 24, s));
   const uint32_t samples = (uint32_t)std::min<uint64_t>(g.n, 8192);
   k_cut_sample<T, PART><<<(samples + 255) / 256, 256, 0, s>>>(
-      g.n, g.m, g.rp, static_cast<const T *>(g.col), pm, tile, samples,
+      g.n, g.m, g.rp, static_cast<const T *>(g.col), pm, tile, hub_degree, samples,
       cnt.as<unsigned long long>());
   CCG_LAUNCH_CHECK();
-  unsigned long long h[2] = {0, 0};
-  CCG_CUDA(cudaMemcpyAsync(h, cnt.p, 16, cudaMemcpyDeviceToHost, s));
+  unsigned long long h[3] = {0, 0, 0};
+  CCG_CUDA(cudaMemcpyAsync(h, cnt.p, 24, cudaMemcpyDeviceToHost, s));
   CCG_CUDA(cudaStreamSynchronize(s));
   c.add(1, 0);
-  return h[0] ? (double)h[1] / (double)h[0] : 0.0;
+  return tiles_fit(h[0], h[1], h[2]);
 }
 
 template <class T, bool PART>
@@ -719,7 +825,7 @@ void run_uf_afforest(const Csr &g, uint32_t *parent, const PartMap &pm, uint32_t
   k_aff_link<T, PART><<<grid, kBlock, 0, s>>>(g.n, g.m, g.rp, col, parent, pm, g.err);
   CCG_LAUNCH_CHECK();
   c.toc(s, "uf_sample_link", t0, link_bytes);
-  k_compress<<<grid, kBlock, 0, s>>>(g.n, parent);
+  k_compress4<<<grid_for((g.n + 3) / 4, kBlock, kSMs * 16), kBlock, 0, s>>>(g.n, parent);
   CCG_LAUNCH_CHECK();
   // most frequent root of a sample = the giant component, if there is one
   const uint32_t samples = (uint32_t)std::min<uint64_t>(g.n, 1024);
@@ -771,7 +877,7 @@ void run_uf_afforest(const Csr &g, uint32_t *parent, const PartMap &pm, uint32_t
   CCG_LAUNCH_CHECK();
   c.toc(s, "uf_sample_hubs", th, 0);
   cudaEvent_t t2 = c.tic(s);
-  k_compress<<<grid, kBlock, 0, s>>>(g.n, parent);
+  k_compress4<<<grid_for((g.n + 3) / 4, kBlock, kSMs * 16), kBlock, 0, s>>>(g.n, parent);
   CCG_LAUNCH_CHECK();
   c.toc(s, "uf_compress", t2, 3 * g.n * 4);
   c.add(7, 4 * g.n + link_bytes + rest_bytes + 6 * g.n * 4);
@@ -789,7 +895,7 @@ void run_uf_mode(const Csr &g, uint32_t *parent, const PartMap &pm, const UfTuni
     // the tiled pass wins when most edges stay inside their tile (grids,
     // geometric and angularly ordered graphs); otherwise sampled linking
     mode = (g.n >= 4ull * tu.tile_vertices &&
-            cut_share<T, PART>(g, pm, tu.tile_vertices, s, pool, c) < 0.5)
+            tiles_suit<T, PART>(g, pm, tu.tile_vertices, tu.hub_degree, s, pool, c))
                ? kUfTiled
                : kUfSampled;
   }
@@ -818,15 +924,20 @@ void uf_components(const Csr &g, uint32_t *parent, const PartMap *pm, const UfTu
   }
 }
 
-double host_cut_share(const uint64_t *rp, const void *col, int idb, uint64_t n, uint64_t m,
-                      uint32_t tile) {
+bool host_tiles_suit(const uint64_t *rp, const void *col, int idb, uint64_t n, uint64_t m,
+                     uint32_t tile, uint32_t hub_degree) {
   const uint64_t samples = std::min<uint64_t>(n, 8192);
-  uint64_t tot = 0, cross = 0;
+  uint64_t tot = 0, cross = 0, hub = 0;
   for (uint64_t i = 0; i < samples; ++i) {
-    const uint64_t v = i * n / samples, t0 = v / tile * tile;
+    const uint64_t v = sample_row(i, samples, n), t0 = v / tile * tile;
     const uint64_t b = rp[v], e = rp[v + 1];
     if (e < b || e > m) continue;  // malformed rows are reported by the kernels
-    for (uint64_t k = b; k < e && k < b + 64; ++k) {
+    if (e - b > hub_degree) {
+      tot += (e - b) / 2;
+      hub += (e - b) / 2;
+      continue;
+    }
+    for (uint64_t k = b; k < e; ++k) {
       const uint64_t u = idb == 8 ? static_cast<const uint64_t *>(col)[k]
                                   : static_cast<const uint32_t *>(col)[k];
       if (u >= v) continue;
@@ -834,7 +945,7 @@ double host_cut_share(const uint64_t *rp, const void *col, int idb, uint64_t n, 
       cross += u < t0;
     }
   }
-  return tot ? (double)cross / (double)tot : 0.0;
+  return tiles_fit(tot, cross, hub);
 }
 
 void widen_labels(const uint32_t *in, void *out, int out_bytes, uint64_t n, cudaStream_t s,

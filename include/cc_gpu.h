@@ -219,7 +219,8 @@ typedef struct cc_tuning {
                               memory first; SAMPLED links two neighbours per
                               vertex, then only rows outside the largest
                               component; AUTO picks TILED when a sample of rows
-                              shows < 50 % tile-crossing edges, else SAMPLED */
+                              shows < 50 % tile-crossing edges and < 10 % of
+                              edges in hub rows, else SAMPLED */
   uint32_t tile_vertices;  /* vertices per CTA tile, 2 bytes of shared memory
                               each (default 32768, 32 to 65536) */
   uint32_t tile_threads;   /* CTA size of the tiled pass (default 1024) */
