@@ -148,49 +148,15 @@ __global__ void k_hook_hubs(uint64_t n, const uint64_t *__restrict__ rp,
   }
 }
 
-// Full compression: parent[v] <- root.  Runs after every link is made.
+// Full compression: parent[v] <- root.  Runs after every link is made; the
+// chain walks halve the paths they pass.
 __global__ void k_compress(uint64_t n, uint32_t *p) {
   for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < n;
        v += (uint64_t)gridDim.x * blockDim.x) {
     const uint32_t r0 = p[v];
     if (r0 == (uint32_t)v) continue;
-    uint32_t r = r0, nx;
-    while ((nx = ld_cg(p + r)) != r) r = nx;
+    const uint32_t r = uf_find(p, r0);  // path halving helps the chains other threads walk
     if (r != r0) p[v] = r;  // most vertices already point at their root
-  }
-}
-
-// Full compression with four chains per thread, walked in lockstep so that
-// their dependent loads are in flight together (the chains are latency-bound;
-// p[x] < x for every non-root, so each chain ends).  Only changed entries are
-// written.
-__global__ void k_compress4(uint64_t n, uint32_t *p) {
-  const uint64_t nq = (n + 3) / 4;
-  for (uint64_t qi = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; qi < nq;
-       qi += (uint64_t)gridDim.x * blockDim.x) {
-    const uint64_t v0 = qi * 4;
-    uint32_t r0[4], r[4];
-    bool act[4];
-#pragma unroll
-    for (int k = 0; k < 4; ++k) {
-      const bool in = v0 + k < n;
-      r0[k] = in ? p[v0 + k] : 0u;
-      r[k] = r0[k];
-      act[k] = in && r0[k] != (uint32_t)(v0 + k);
-    }
-    while (act[0] || act[1] || act[2] || act[3]) {
-      uint32_t nx[4];
-#pragma unroll
-      for (int k = 0; k < 4; ++k) nx[k] = act[k] ? ld_cg(p + r[k]) : r[k];
-#pragma unroll
-      for (int k = 0; k < 4; ++k) {
-        if (nx[k] == r[k]) act[k] = false;
-        else r[k] = nx[k];
-      }
-    }
-#pragma unroll
-    for (int k = 0; k < 4; ++k)
-      if (v0 + k < n && r[k] != r0[k]) p[v0 + k] = r[k];
   }
 }
 
@@ -231,31 +197,36 @@ __device__ __forceinline__ bool same_part(const PartMap &pm, uint32_t v, uint32_
   return pm.part(v) == pm.part(u);
 }
 
-// Both sampled neighbours of a row in one pass: they share the row's first
-// sector of ids, so the second costs no extra DRAM traffic.
 template <class T, bool PART>
 __global__ void k_aff_link(uint64_t n, uint64_t m, const uint64_t *__restrict__ rp,
-                           const T *__restrict__ col, uint32_t *p, PartMap pm, int *err) {
+                           const T *__restrict__ col, uint32_t *p, PartMap pm, uint32_t r, int *err) {
   for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < n;
        v += (uint64_t)gridDim.x * blockDim.x) {
     Row row;
-    if (!load_row(rp, v, m, err, row)) continue;
-    const uint32_t k = (uint32_t)min(row.e - row.b, (uint64_t)kAffRounds);
-    for (uint32_t r = 0; r < k; ++r) {
-      const uint64_t u = (uint64_t)__ldg(col + row.b + r);
-      if (u >= n) {
-        set_err(err, kErrBadId);
-        continue;
-      }
-      if (!PART || same_part(pm, (uint32_t)v, (uint32_t)u)) uf_union(p, (uint32_t)v, (uint32_t)u);
+    if (!load_row(rp, v, m, err, row) || row.e - row.b <= r) continue;
+    const uint64_t u = (uint64_t)__ldg(col + row.b + r);
+    if (u >= n) {
+      set_err(err, kErrBadId);
+      continue;
     }
+    if (!PART || same_part(pm, (uint32_t)v, (uint32_t)u)) uf_union(p, (uint32_t)v, (uint32_t)u);
   }
 }
 
-__global__ void k_aff_sample(uint64_t n, const uint32_t *p, uint32_t samples, uint64_t salt,
-                             uint32_t *__restrict__ out) {
+// `per` sampled roots for each of `nparts` partitions (nparts = 1: the whole
+// graph): a partition's most frequent root is its giant local component.
+__global__ void k_aff_sample(uint64_t n, const uint32_t *p, PartMap pm, uint32_t nparts,
+                             uint32_t per, uint64_t salt, uint32_t *__restrict__ out) {
+  const uint32_t samples = nparts * per;
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < samples; i += gridDim.x * blockDim.x) {
-    uint32_t r = (uint32_t)(mix64(salt + i) % n), nx;
+    const uint64_t h = mix64(salt + i);
+    uint64_t lo = 0, len = n;
+    if (nparts > 1) {
+      const uint32_t q = i / per;
+      lo = q < pm.rm ? (uint64_t)q * (pm.q + 1) : (uint64_t)pm.big + (uint64_t)(q - pm.rm) * pm.q;
+      len = q < pm.rm ? pm.q + 1 : pm.q;
+    }
+    uint32_t r = (uint32_t)(lo + h % len), nx;
     while ((nx = ld_cg(p + r)) != r) r = nx;
     out[i] = r;
   }
@@ -263,7 +234,8 @@ __global__ void k_aff_sample(uint64_t n, const uint32_t *p, uint32_t samples, ui
 
 template <class T, bool PART>
 __global__ void k_aff_rest(uint64_t n, uint64_t m, const uint64_t *__restrict__ rp,
-                           const T *__restrict__ col, uint32_t *p, PartMap pm, uint32_t L,
+                           const T *__restrict__ col, uint32_t *p, PartMap pm,
+                           const uint32_t *__restrict__ Ls, uint32_t nparts,
                            uint32_t hub_degree, HubList hl, int *err,
                            unsigned long long *__restrict__ edges_read) {
   uint32_t work = 0;  // neighbour ids this thread reads (for the byte count)
@@ -271,6 +243,7 @@ __global__ void k_aff_rest(uint64_t n, uint64_t m, const uint64_t *__restrict__ 
        v += (uint64_t)gridDim.x * blockDim.x) {
     Row row;
     if (!load_row(rp, v, m, err, row) || row.e - row.b <= kAffRounds) continue;
+    const uint32_t L = nparts > 1 ? Ls[pm.part((uint32_t)v)] : Ls[0];
     if (uf_find(p, (uint32_t)v) == L) continue;
     if (row.e - row.b > hub_degree) {
       queue_hub(hl, (uint32_t)v, row.e - row.b - kAffRounds, err);
@@ -404,7 +377,7 @@ size_t tile_smem_bytes(uint32_t tile, uint32_t threads, uint32_t stage) {
 }
 
 template <class T, bool PART, class PT>
-__global__ void __launch_bounds__(1024)
+__global__ void __launch_bounds__(1024, 2)
     k_tile3(uint64_t n, uint64_t m, uint64_t v_begin, uint64_t v_end,
             const uint64_t *__restrict__ rp, const T *__restrict__ col,
             uint32_t *__restrict__ p, PartMap pm, uint32_t tile, uint32_t stage_cap,
@@ -428,14 +401,24 @@ __global__ void __launch_bounds__(1024)
     if (threadIdx.x == 0) ccount = 0;
     __syncthreads();
     uint32_t qn = 0;  // warp-uniform queue fill
+    // offsets of the warp's first rows; every group prefetches the next
+    // group's offsets, so their latency hides behind this group's edges
+    uint64_t nrb = 0, nre = 0;
+    if (wid * 32 + lane < len) {
+      nrb = __ldg(rp + t0 + wid * 32 + lane);
+      nre = __ldg(rp + t0 + wid * 32 + lane + 1);
+    }
     for (uint32_t g0 = wid * 32; g0 < len; g0 += nw * 32) {
       const uint32_t i = g0 + lane;
-      uint64_t rb = 0;
+      uint64_t rb = nrb;
+      const uint64_t re = nre;
+      if (i + nw * 32 < len) {
+        nrb = __ldg(rp + t0 + i + nw * 32);
+        nre = __ldg(rp + t0 + i + nw * 32 + 1);
+      }
       uint32_t deg = 0, lo = 0;
       if (i < len) {
         const uint64_t v = t0 + i;
-        rb = __ldg(rp + v);
-        const uint64_t re = __ldg(rp + v + 1);
         if (re < rb || re > m) {
           set_err(err, kErrBadOffsets);
         } else if (re - rb > hub_degree) {
@@ -530,64 +513,15 @@ __global__ void __launch_bounds__(1024)
   }
 }
 
-// Edges between tiles, on the global parent array of tile-local roots.  Each
-// thread takes four edges and finds their eight roots in lockstep (path
-// halving as in uf_find), then links them one edge at a time.
+// Edges between tiles, on the global parent array of tile-local roots.
 __global__ void k_cut_union(const uint2 *__restrict__ cut, const unsigned long long *__restrict__ ncut,
                             uint64_t cut_cap, uint32_t *p) {
   uint64_t cnt = *ncut;
   if (cnt > cut_cap) cnt = cut_cap;
-  const uint64_t nq = (cnt + 3) / 4;
-  for (uint64_t qi = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; qi < nq;
-       qi += (uint64_t)gridDim.x * blockDim.x) {
-    uint32_t prev[8], cur[8];
-    bool act[8];
-#pragma unroll
-    for (int k = 0; k < 4; ++k) {
-      const uint64_t e = qi * 4 + k;
-      const uint2 x = e < cnt ? cut[e] : make_uint2(0u, 0u);
-      prev[2 * k] = x.x;
-      prev[2 * k + 1] = x.y;
-    }
-#pragma unroll
-    for (int j = 0; j < 8; ++j) {
-      cur[j] = ld_cg(p + prev[j]);
-      act[j] = cur[j] != prev[j];
-    }
-    bool any = true;
-    while (any) {
-      uint32_t nx[8];
-#pragma unroll
-      for (int j = 0; j < 8; ++j) nx[j] = act[j] ? ld_cg(p + cur[j]) : cur[j];
-      any = false;
-#pragma unroll
-      for (int j = 0; j < 8; ++j) {
-        if (act[j] && cur[j] > nx[j]) {
-          st_cg(p + prev[j], nx[j]);  // path halving
-          prev[j] = cur[j];
-          cur[j] = nx[j];
-          any = true;
-        } else {
-          act[j] = false;
-        }
-      }
-    }
-#pragma unroll
-    for (int k = 0; k < 4; ++k) {
-      if (qi * 4 + k >= cnt) continue;
-      uint32_t ra = cur[2 * k], rb = cur[2 * k + 1];
-      while (ra != rb) {
-        if (ra < rb) {
-          const uint32_t t = ra;
-          ra = rb;
-          rb = t;
-        }
-        const uint32_t old = atomicCAS(p + ra, ra, rb);
-        if (old == ra) break;
-        ra = uf_find(p, old);
-        rb = uf_find(p, rb);
-      }
-    }
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < cnt;
+       i += (uint64_t)gridDim.x * blockDim.x) {
+    const uint2 e = cut[i];
+    uf_union(p, e.x, e.y);
   }
 }
 
@@ -686,7 +620,7 @@ void run_uf(const Csr &g, uint32_t *parent, const PartMap &pm, uint32_t hub_degr
   CCG_LAUNCH_CHECK();
   c.toc(s, "uf_hook_hubs", t2, 0);
   cudaEvent_t t3 = c.tic(s);
-  k_compress4<<<grid_for((g.n + 3) / 4, kBlock, kSMs * 16), kBlock, 0, s>>>(g.n, parent);
+  k_compress<<<grid_for(g.n, kBlock, kSMs * 32), kBlock, 0, s>>>(g.n, parent);
   CCG_LAUNCH_CHECK();
   c.toc(s, "uf_compress", t3, 3 * g.n * 4);
   c.add(4, (8 * (g.n + 1) + g.n * si + 4 * g.n) + hook_bytes + 3 * g.n * 4);
@@ -768,7 +702,7 @@ void run_uf_tiled(const Csr &g, uint32_t *parent, const PartMap &pm, const UfTun
   }
   c.toc(s, hs ? "uf_tile_streamed" : "uf_tile", t0, tile_bytes);
   cudaEvent_t t1 = c.tic(s);
-  k_cut_union<<<kSMs * 8, kBlock, 0, s>>>(cut.as<uint2>(), ncut, cut_cap, parent);
+  k_cut_union<<<kSMs * 16, kBlock, 0, s>>>(cut.as<uint2>(), ncut, cut_cap, parent);
   CCG_LAUNCH_CHECK();
   c.toc(s, "uf_cut_union", t1, 0);
   cudaEvent_t t2 = c.tic(s);
@@ -779,7 +713,7 @@ void run_uf_tiled(const Csr &g, uint32_t *parent, const PartMap &pm, const UfTun
   // every vertex points at a tile-local root or at a final root: full
   // compression, writing only the entries that change
   cudaEvent_t t3 = c.tic(s);
-  k_compress4<<<grid_for((g.n + 3) / 4, kBlock, kSMs * 16), kBlock, 0, s>>>(g.n, parent);
+  k_compress<<<grid_for(g.n, kBlock, kSMs * 32), kBlock, 0, s>>>(g.n, parent);
   CCG_LAUNCH_CHECK();
   c.toc(s, "uf_compress", t3, 3 * g.n * 4);
   c.add(4, tile_bytes + 3 * g.n * 4);
@@ -819,35 +753,50 @@ void run_uf_afforest(const Csr &g, uint32_t *parent, const PartMap &pm, uint32_t
   const unsigned grid = grid_for(g.n, kBlock, kSMs * 32);
   k_iota_parent<<<grid, kBlock, 0, s>>>(g.n, parent);
   CCG_LAUNCH_CHECK();
-  // link pass: offsets, kAffRounds ids and unions (two parent gathers each)
-  const uint64_t link_bytes = 8 * (g.n + 1) + kAffRounds * g.n * (si + 2 * 4);
-  cudaEvent_t t0 = c.tic(s);
-  k_aff_link<T, PART><<<grid, kBlock, 0, s>>>(g.n, g.m, g.rp, col, parent, pm, g.err);
+  // each link round: offsets, one id, one union (two parent gathers); the
+  // rounds stay separate launches (one round's links all land before the
+  // next round's finds, which keeps the trees shallow)
+  const uint64_t link_bytes = 8 * (g.n + 1) + g.n * (si + 2 * 4);
+  for (uint32_t r = 0; r < kAffRounds; ++r) {
+    cudaEvent_t t0 = c.tic(s);
+    k_aff_link<T, PART><<<grid, kBlock, 0, s>>>(g.n, g.m, g.rp, col, parent, pm, r, g.err);
+    CCG_LAUNCH_CHECK();
+    c.toc(s, "uf_sample_link", t0, link_bytes);
+  }
+  k_compress<<<grid_for(g.n, kBlock, kSMs * 32), kBlock, 0, s>>>(g.n, parent);
   CCG_LAUNCH_CHECK();
-  c.toc(s, "uf_sample_link", t0, link_bytes);
-  k_compress4<<<grid_for((g.n + 3) / 4, kBlock, kSMs * 16), kBlock, 0, s>>>(g.n, parent);
-  CCG_LAUNCH_CHECK();
-  // most frequent root of a sample = the giant component, if there is one
-  const uint32_t samples = (uint32_t)std::min<uint64_t>(g.n, 1024);
-  DevBuf smp(4 * samples, s, pool);
-  k_aff_sample<<<(samples + 255) / 256, 256, 0, s>>>(g.n, parent, samples, 0x5eedull,
+  // most frequent root of a sample = the giant component, if there is one;
+  // with virtual ranks (up to 4096) one per rank, as each rank has its own
+  // giant local component
+  uint32_t P = 1;
+  if (PART) P = pm.q ? pm.rm + (uint32_t)((g.n - pm.big) / pm.q) : (uint32_t)g.n;
+  const uint32_t nparts = (PART && P > 1 && P <= 4096) ? P : 1;
+  const uint32_t per = nparts > 1 ? 64u : (uint32_t)std::min<uint64_t>(g.n, 1024);
+  const uint32_t samples = nparts * per;
+  DevBuf smp(4 * samples, s, pool), dL(4 * nparts, s, pool);
+  k_aff_sample<<<(samples + 255) / 256, 256, 0, s>>>(g.n, parent, pm, nparts, per, 0x5eedull,
                                                      smp.as<uint32_t>());
   CCG_LAUNCH_CHECK();
-  std::vector<uint32_t> h(samples);
+  std::vector<uint32_t> h(samples), Ls(nparts);
   CCG_CUDA(cudaMemcpyAsync(h.data(), smp.p, 4 * samples, cudaMemcpyDeviceToHost, s));
   CCG_CUDA(cudaStreamSynchronize(s));
-  std::sort(h.begin(), h.end());
-  uint32_t L = h.empty() ? kNone : h[0];
-  size_t best = 0;
-  for (size_t i = 0; i < h.size();) {
-    size_t j = i;
-    while (j < h.size() && h[j] == h[i]) ++j;
-    if (j - i > best) {
-      best = j - i;
-      L = h[i];
+  for (uint32_t q = 0; q < nparts; ++q) {
+    auto b = h.begin() + (size_t)q * per, e = b + per;
+    std::sort(b, e);
+    uint32_t L = per ? *b : kNone;
+    size_t best = 0;
+    for (auto i = b; i != e;) {
+      auto j = i;
+      while (j != e && *j == *i) ++j;
+      if ((size_t)(j - i) > best) {
+        best = (size_t)(j - i);
+        L = *i;
+      }
+      i = j;
     }
-    i = j;
+    Ls[q] = L;
   }
+  CCG_CUDA(cudaMemcpyAsync(dL.p, Ls.data(), 4 * nparts, cudaMemcpyHostToDevice, s));
   const uint64_t hub_cap = hub_list_cap(g.m, hub_degree);
   DevBuf hubs(8 * hub_cap, s, pool), nh(4, s, pool);
   CCG_CUDA(cudaMemsetAsync(nh.p, 0, 4, s));
@@ -860,7 +809,7 @@ void run_uf_afforest(const Csr &g, uint32_t *parent, const PartMap &pm, uint32_t
   if (c.prof) CCG_CUDA(cudaMemsetAsync(ecount.p, 0, 8, s));
   cudaEvent_t t1 = c.tic(s);
   k_aff_rest<T, PART><<<grid, kBlock, 0, s>>>(
-      g.n, g.m, g.rp, col, parent, pm, L, hub_degree, hl, g.err,
+      g.n, g.m, g.rp, col, parent, pm, dL.as<uint32_t>(), nparts, hub_degree, hl, g.err,
       c.prof ? ecount.as<unsigned long long>() : nullptr);
   CCG_LAUNCH_CHECK();
   c.toc(s, "uf_sample_rest", t1, rest_bytes);
@@ -877,10 +826,10 @@ void run_uf_afforest(const Csr &g, uint32_t *parent, const PartMap &pm, uint32_t
   CCG_LAUNCH_CHECK();
   c.toc(s, "uf_sample_hubs", th, 0);
   cudaEvent_t t2 = c.tic(s);
-  k_compress4<<<grid_for((g.n + 3) / 4, kBlock, kSMs * 16), kBlock, 0, s>>>(g.n, parent);
+  k_compress<<<grid_for(g.n, kBlock, kSMs * 32), kBlock, 0, s>>>(g.n, parent);
   CCG_LAUNCH_CHECK();
   c.toc(s, "uf_compress", t2, 3 * g.n * 4);
-  c.add(7, 4 * g.n + link_bytes + rest_bytes + 6 * g.n * 4);
+  c.add(6 + kAffRounds, 4 * g.n + kAffRounds * link_bytes + rest_bytes + 6 * g.n * 4);
 }
 
 template <class T, bool PART>
