@@ -148,14 +148,16 @@ __global__ void k_hook_hubs(uint64_t n, const uint64_t *__restrict__ rp,
   }
 }
 
-// Full compression: parent[v] <- root.  Runs after every link is made; the
-// chain walks halve the paths they pass.
+// Full compression: parent[v] <- root.  Runs after every link is made.  The
+// walks do not halve paths: a halving store into p[x] could land after x's
+// own thread wrote its root and leave x pointing at an inner node.
 __global__ void k_compress(uint64_t n, uint32_t *p) {
   for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < n;
        v += (uint64_t)gridDim.x * blockDim.x) {
     const uint32_t r0 = p[v];
     if (r0 == (uint32_t)v) continue;
-    const uint32_t r = uf_find(p, r0);  // path halving helps the chains other threads walk
+    uint32_t r = r0, nx;
+    while ((nx = ld_cg(p + r)) != r) r = nx;
     if (r != r0) p[v] = r;  // most vertices already point at their root
   }
 }
