@@ -338,6 +338,10 @@ __device__ __forceinline__ uint32_t tw_find(volatile PT *p, uint32_t v) {
   }
   return cur;
 }
+// Union of a and b; afterwards both endpoints point straight at the common
+// root they saw (an ancestor of both, never a root that could still be CAS'ed:
+// an endpoint different from that root has a parent already), so the next
+// edges of a and b start next to the root.
 template <class PT>
 __device__ __forceinline__ void tw_union(volatile PT *p, uint32_t a, uint32_t b) {
   uint32_t ra = tw_find(p, a), rb = tw_find(p, b);
@@ -348,10 +352,15 @@ __device__ __forceinline__ void tw_union(volatile PT *p, uint32_t a, uint32_t b)
       rb = t;
     }
     const uint32_t old = ts_cas(const_cast<PT *>(p + ra), ra, rb);
-    if (old == ra) return;
+    if (old == ra) {
+      ra = rb;
+      break;
+    }
     ra = tw_find(p, old);
     rb = tw_find(p, rb);
   }
+  if (a != ra) p[a] = (PT)ra;
+  if (b != ra) p[b] = (PT)ra;
 }
 
 __device__ __forceinline__ uint64_t shfl64(uint64_t x, int src) {
@@ -403,24 +412,14 @@ __global__ void __launch_bounds__(1024, 2)
     if (threadIdx.x == 0) ccount = 0;
     __syncthreads();
     uint32_t qn = 0;  // warp-uniform queue fill
-    // offsets of the warp's first rows; every group prefetches the next
-    // group's offsets, so their latency hides behind this group's edges
-    uint64_t nrb = 0, nre = 0;
-    if (wid * 32 + lane < len) {
-      nrb = __ldg(rp + t0 + wid * 32 + lane);
-      nre = __ldg(rp + t0 + wid * 32 + lane + 1);
-    }
     for (uint32_t g0 = wid * 32; g0 < len; g0 += nw * 32) {
       const uint32_t i = g0 + lane;
-      uint64_t rb = nrb;
-      const uint64_t re = nre;
-      if (i + nw * 32 < len) {
-        nrb = __ldg(rp + t0 + i + nw * 32);
-        nre = __ldg(rp + t0 + i + nw * 32 + 1);
-      }
+      uint64_t rb = 0;
       uint32_t deg = 0, lo = 0;
       if (i < len) {
         const uint64_t v = t0 + i;
+        rb = __ldg(rp + v);
+        const uint64_t re = __ldg(rp + v + 1);
         if (re < rb || re > m) {
           set_err(err, kErrBadOffsets);
         } else if (re - rb > hub_degree) {
@@ -430,33 +429,17 @@ __global__ void __launch_bounds__(1024, 2)
           if (PART) lo = part_lo(pm, (uint32_t)v);
         }
       }
-      uint32_t inc = deg;
-#pragma unroll
-      for (int o = 1; o < 32; o <<= 1) {
-        const uint32_t t = __shfl_up_sync(0xffffffffu, inc, o);
-        if ((int)lane >= o) inc += t;
-      }
-      const uint32_t total = __shfl_sync(0xffffffffu, inc, 31);
-      const uint32_t off = inc - deg;
-      for (uint32_t f0 = 0; f0 < total; f0 += 32) {
-        const uint32_t f = f0 + lane;
-        int r = 0;  // the last lane whose row starts at or before f
-#pragma unroll
-        for (int step = 16; step; step >>= 1) {
-          const uint32_t o = __shfl_sync(0xffffffffu, off, r + step);
-          if (o <= f) r += step;
-        }
-        const uint32_t ro = __shfl_sync(0xffffffffu, off, r);
-        const uint64_t rbr = shfl64(rb, r);
-        const uint32_t lor = PART ? __shfl_sync(0xffffffffu, lo, r) : 0u;
-        const uint32_t vi = g0 + (uint32_t)r, vv = tt + vi;
+      // One edge (v, uu) per lane, all lanes together: an in-tile edge to a
+      // smaller id goes to the warp's union queue (32 queued entries make a
+      // union step), an edge to an earlier tile to the cut stage.
+      auto edge = [&](bool valid, uint64_t uu, uint32_t vi, uint32_t lov) {
+        const uint32_t vv = tt + vi;
         bool uni = false, emit = false;
         uint32_t u = 0;
-        if (f < total) {
-          const uint64_t uu = (uint64_t)__ldg(col + rbr + (f - ro));
+        if (valid) {
           if (uu >= n) {
             set_err(err, kErrBadId);
-          } else if ((uint32_t)uu < vv && (!PART || (uint32_t)uu >= lor)) {
+          } else if ((uint32_t)uu < vv && (!PART || (uint32_t)uu >= lov)) {
             u = (uint32_t)uu;  // each undirected edge once, from its larger end
             if (u >= tt) uni = true;
             else emit = true;
@@ -491,6 +474,40 @@ __global__ void __launch_bounds__(1024, 2)
               else set_err(err, kErrOverflow);
             }
           }
+        }
+      };
+      const uint32_t maxdeg = __reduce_max_sync(0xffffffffu, deg);
+      const uint32_t total = __reduce_add_sync(0xffffffffu, deg);
+      if (maxdeg <= 2 * ((total + 31) / 32) + 1) {
+        // even degrees: lane = row, maxdeg steps, the ids of 32 neighbouring
+        // rows are adjacent in memory
+        for (uint32_t j = 0; j < maxdeg; ++j) {
+          const bool valid = j < deg;
+          edge(valid, valid ? (uint64_t)__ldg(col + rb + j) : 0ull, i, lo);
+        }
+      } else {
+        // skewed degrees: the 32 rows' edges as one flattened stream, lane k
+        // reads entry k; its row is the last lane whose prefix sum is <= k
+        uint32_t inc = deg;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+          const uint32_t t = __shfl_up_sync(0xffffffffu, inc, o);
+          if ((int)lane >= o) inc += t;
+        }
+        const uint32_t off = inc - deg;
+        for (uint32_t f0 = 0; f0 < total; f0 += 32) {
+          const uint32_t f = f0 + lane;
+          int r = 0;
+#pragma unroll
+          for (int step = 16; step; step >>= 1) {
+            const uint32_t o = __shfl_sync(0xffffffffu, off, r + step);
+            if (o <= f) r += step;
+          }
+          const uint32_t ro = __shfl_sync(0xffffffffu, off, r);
+          const uint64_t rbr = shfl64(rb, r);
+          const uint32_t lor = PART ? __shfl_sync(0xffffffffu, lo, r) : 0u;
+          const bool valid = f < total;
+          edge(valid, valid ? (uint64_t)__ldg(col + rbr + (f - ro)) : 0ull, g0 + (uint32_t)r, lor);
         }
       }
     }
