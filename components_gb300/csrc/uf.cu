@@ -148,9 +148,11 @@ __global__ void k_hook_hubs(uint64_t n, const uint64_t *__restrict__ rp,
   }
 }
 
-// Full compression: parent[v] <- root.  Runs after every link is made.  The
-// walks do not halve paths: a halving store into p[x] could land after x's
-// own thread wrote its root and leave x pointing at an inner node.
+// Full compression: parent[v] <- root.  Runs after every link is made, so the
+// roots no longer change: every node of the walked path is set to the root
+// (any store is the final value; a halving store of an inner node could land
+// after that node's own thread wrote its root and is never made).  Vertices
+// that share a path (a tile's vertices and their tile root) find it short.
 __global__ void k_compress(uint64_t n, uint32_t *p) {
   for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < n;
        v += (uint64_t)gridDim.x * blockDim.x) {
@@ -158,7 +160,9 @@ __global__ void k_compress(uint64_t n, uint32_t *p) {
     if (r0 == (uint32_t)v) continue;
     uint32_t r = r0, nx;
     while ((nx = ld_cg(p + r)) != r) r = nx;
-    if (r != r0) p[v] = r;  // most vertices already point at their root
+    if (r == r0) continue;  // most vertices already point at their root
+    p[v] = r;
+    for (uint32_t x = r0; (nx = ld_cg(p + x)) != r; x = nx) st_cg(p + x, r);
   }
 }
 
@@ -240,13 +244,15 @@ __global__ void k_aff_rest(uint64_t n, uint64_t m, const uint64_t *__restrict__ 
                            const uint32_t *__restrict__ Ls, uint32_t nparts,
                            uint32_t hub_degree, HubList hl, int *err,
                            unsigned long long *__restrict__ edges_read) {
-  uint32_t work = 0;  // neighbour ids this thread reads (for the byte count)
+  uint32_t work = 0, rows = 0;  // neighbour ids and offset pairs this thread reads
   for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < n;
        v += (uint64_t)gridDim.x * blockDim.x) {
-    Row row;
-    if (!load_row(rp, v, m, err, row) || row.e - row.b <= kAffRounds) continue;
+    // the root first: rows inside the giant component never read their offsets
     const uint32_t L = nparts > 1 ? Ls[pm.part((uint32_t)v)] : Ls[0];
     if (uf_find(p, (uint32_t)v) == L) continue;
+    ++rows;
+    Row row;
+    if (!load_row(rp, v, m, err, row) || row.e - row.b <= kAffRounds) continue;
     if (row.e - row.b > hub_degree) {
       queue_hub(hl, (uint32_t)v, row.e - row.b - kAffRounds, err);
       continue;
@@ -263,7 +269,11 @@ __global__ void k_aff_rest(uint64_t n, uint64_t m, const uint64_t *__restrict__ 
   }
   if (edges_read) {  // every thread of the warp reaches this point
     work = __reduce_add_sync(0xffffffffu, work);
-    if ((threadIdx.x & 31) == 0 && work) atomicAdd(edges_read, (unsigned long long)work);
+    rows = __reduce_add_sync(0xffffffffu, rows);
+    if ((threadIdx.x & 31) == 0) {
+      if (work) atomicAdd(edges_read, (unsigned long long)work);
+      if (rows) atomicAdd(edges_read + 1, (unsigned long long)rows);
+    }
   }
 }
 
@@ -387,7 +397,11 @@ size_t tile_smem_bytes(uint32_t tile, uint32_t threads, uint32_t stage) {
   return (size_t)tile * sizeof(PT) + (size_t)(threads / 32) * kUnionQueue * 4 + (size_t)stage * 8;
 }
 
-template <class T, bool PART, class PT>
+// LINK = 0: every edge to a smaller id (the tiled hook pass; rows above
+// hub_degree are queued as hub pieces).  LINK = k > 0: the first k entries of
+// every row in either direction (the link rounds of sampled linking, which
+// stay inside their tile on geometric and angularly ordered graphs).
+template <class T, bool PART, class PT, int LINK>
 __global__ void __launch_bounds__(1024, 2)
     k_tile3(uint64_t n, uint64_t m, uint64_t v_begin, uint64_t v_end,
             const uint64_t *__restrict__ rp, const T *__restrict__ col,
@@ -422,10 +436,10 @@ __global__ void __launch_bounds__(1024, 2)
         const uint64_t re = __ldg(rp + v + 1);
         if (re < rb || re > m) {
           set_err(err, kErrBadOffsets);
-        } else if (re - rb > hub_degree) {
+        } else if (!LINK && re - rb > hub_degree) {
           queue_hub(hl, (uint32_t)v, re - rb, err);
         } else {
-          deg = (uint32_t)(re - rb);
+          deg = LINK ? (uint32_t)min(re - rb, (uint64_t)LINK) : (uint32_t)(re - rb);
           if (PART) lo = part_lo(pm, (uint32_t)v);
         }
       }
@@ -439,6 +453,12 @@ __global__ void __launch_bounds__(1024, 2)
         if (valid) {
           if (uu >= n) {
             set_err(err, kErrBadId);
+          } else if (LINK) {
+            if ((uint32_t)uu != vv && (!PART || same_part(pm, vv, (uint32_t)uu))) {
+              u = (uint32_t)uu;
+              if (u >= tt && u - tt < len) uni = true;
+              else emit = true;  // a cut edge in either direction
+            }
           } else if ((uint32_t)uu < vv && (!PART || (uint32_t)uu >= lov)) {
             u = (uint32_t)uu;  // each undirected edge once, from its larger end
             if (u >= tt) uni = true;
@@ -532,7 +552,10 @@ __global__ void __launch_bounds__(1024, 2)
   }
 }
 
-// Edges between tiles, on the global parent array of tile-local roots.
+// Edges between tiles, on the global parent array of tile-local roots.  After
+// each union both endpoints point at the common root they saw (an ancestor of
+// both; an endpoint other than that root already has a parent, so no CAS can
+// target it): the many cut edges of one tile root then start next to the root.
 __global__ void k_cut_union(const uint2 *__restrict__ cut, const unsigned long long *__restrict__ ncut,
                             uint64_t cut_cap, uint32_t *p) {
   uint64_t cnt = *ncut;
@@ -540,7 +563,23 @@ __global__ void k_cut_union(const uint2 *__restrict__ cut, const unsigned long l
   for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < cnt;
        i += (uint64_t)gridDim.x * blockDim.x) {
     const uint2 e = cut[i];
-    uf_union(p, e.x, e.y);
+    uint32_t ra = uf_find(p, e.x), rb = uf_find(p, e.y);
+    while (ra != rb) {
+      if (ra < rb) {
+        const uint32_t t = ra;
+        ra = rb;
+        rb = t;
+      }
+      const uint32_t old = atomicCAS(p + ra, ra, rb);
+      if (old == ra) {
+        ra = rb;
+        break;
+      }
+      ra = uf_find(p, old);
+      rb = uf_find(p, rb);
+    }
+    if (e.x != ra) st_cg(p + e.x, ra);
+    if (e.y != ra) st_cg(p + e.y, ra);
   }
 }
 
@@ -645,36 +684,54 @@ void run_uf(const Csr &g, uint32_t *parent, const PartMap &pm, uint32_t hub_degr
   c.add(4, (8 * (g.n + 1) + g.n * si + 4 * g.n) + hook_bytes + 3 * g.n * 4);
 }
 
+// Launch shape of the tile kernel: two CTAs per SM when the tile leaves room
+// for a cut stage of at least 256 edges, else one; the stage takes what is
+// left of the shared memory (at most 8192 edges).
+struct TileShape {
+  uint32_t tile = 0, stage = 0;
+  int threads = 0;
+  size_t smem = 0;
+  unsigned grid = 0;
+};
+template <class T, bool PART, int LINK>
+TileShape tile_shape(uint64_t n, const UfTuning &tu) {
+  TileShape t;
+  t.tile = tu.tile_vertices;
+  t.threads = (int)tu.tile_threads;
+  if (t.tile < 32 || t.tile > kTileMax) throw Error(CC_ERR_INVALID, "tile_vertices must lie in [32, 65536]");
+  if (t.threads < 32 || t.threads > 1024 || t.threads % 32)
+    throw Error(CC_ERR_INVALID, "tile_threads must be a multiple of 32 up to 1024");
+  int dev = 0, sm_smem = 0, blk_smem = 0;
+  CCG_CUDA(cudaGetDevice(&dev));
+  CCG_CUDA(cudaDeviceGetAttribute(&sm_smem, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev));
+  CCG_CUDA(cudaDeviceGetAttribute(&blk_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+  const size_t fixed = tile_smem_bytes<uint16_t>(t.tile, (uint32_t)t.threads, 0);
+  const size_t reserve = 1024 + 64;  // per-CTA system reserve + static shared memory
+  size_t room = (size_t)sm_smem / 2 > reserve + fixed ? (size_t)sm_smem / 2 - reserve - fixed : 0;
+  if (room < 256 * 8) room = (size_t)blk_smem > 64 + fixed ? (size_t)blk_smem - 64 - fixed : 0;
+  t.stage = (uint32_t)std::min<size_t>(room / 8, 8192);
+  if (t.stage < 64) throw Error(CC_ERR_INVALID, "tile does not fit in shared memory");
+  t.smem = tile_smem_bytes<uint16_t>(t.tile, (uint32_t)t.threads, t.stage);
+  const void *fn = (const void *)k_tile3<T, PART, uint16_t, LINK>;
+  CCG_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)t.smem));
+  int per_sm = 0;
+  CCG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, t.threads, t.smem));
+  if (per_sm < 1) throw Error(CC_ERR_INVALID, "tile does not fit in shared memory");
+  const uint64_t tiles = (n + t.tile - 1) / t.tile;
+  t.grid = (unsigned)std::min<uint64_t>(tiles, (uint64_t)per_sm * kSMs);
+  return t;
+}
+
 template <class T, bool PART>
 void run_uf_tiled(const Csr &g, uint32_t *parent, const PartMap &pm, const UfTuning &tu,
                   cudaStream_t s, cudaMemPool_t pool, Counters &c, const HostSource *hs) {
   const T *col = static_cast<const T *>(g.col);
   const uint64_t si = (uint64_t)g.idb;
-  const uint32_t tile = tu.tile_vertices;
-  const int threads = (int)tu.tile_threads;
-  if (tile < 32 || tile > kTileMax) throw Error(CC_ERR_INVALID, "tile_vertices must lie in [32, 65536]");
-  if (threads < 32 || threads > 1024 || threads % 32)
-    throw Error(CC_ERR_INVALID, "tile_threads must be a multiple of 32 up to 1024");
-  // shared memory: two CTAs per SM when the tile leaves room for a cut stage
-  // of at least 256 edges, else one; the stage takes what is left (<= 8192)
-  int dev = 0, sm_smem = 0, blk_smem = 0;
-  CCG_CUDA(cudaGetDevice(&dev));
-  CCG_CUDA(cudaDeviceGetAttribute(&sm_smem, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev));
-  CCG_CUDA(cudaDeviceGetAttribute(&blk_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
-  const size_t fixed = tile_smem_bytes<uint16_t>(tile, (uint32_t)threads, 0);
-  const size_t reserve = 1024 + 64;  // per-CTA system reserve + static shared memory
-  size_t room = (size_t)sm_smem / 2 > reserve + fixed ? (size_t)sm_smem / 2 - reserve - fixed : 0;
-  if (room < 256 * 8) room = (size_t)blk_smem > 64 + fixed ? (size_t)blk_smem - 64 - fixed : 0;
-  const uint32_t stage = (uint32_t)std::min<size_t>(room / 8, 8192);
-  if (stage < 64) throw Error(CC_ERR_INVALID, "tile does not fit in shared memory");
-  const size_t smem = tile_smem_bytes<uint16_t>(tile, (uint32_t)threads, stage);
-  const void *fn = (const void *)k_tile3<T, PART, uint16_t>;
-  CCG_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  int per_sm = 0;
-  CCG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, threads, smem));
-  if (per_sm < 1) throw Error(CC_ERR_INVALID, "tile does not fit in shared memory");
-  const uint64_t tiles = (g.n + tile - 1) / tile;
-  const unsigned grid = (unsigned)std::min<uint64_t>(tiles, (uint64_t)per_sm * kSMs);
+  const TileShape ts = tile_shape<T, PART, 0>(g.n, tu);
+  const uint32_t tile = ts.tile, stage = ts.stage;
+  const int threads = ts.threads;
+  const size_t smem = ts.smem;
+  const unsigned grid = ts.grid;
   const uint64_t hub_cap = hub_list_cap(g.m, tu.hub_degree);
   const uint64_t cut_cap = g.m + 1;
   DevBuf hubs(8 * hub_cap, s, pool), nh(4, s, pool), cut(8 * cut_cap, s, pool), cnt(8, s, pool);
@@ -687,7 +744,7 @@ void run_uf_tiled(const Csr &g, uint32_t *parent, const PartMap &pm, const UfTun
   const uint64_t tile_bytes = 8 * (g.n + 1) + g.m * si + 4 * g.n;
   cudaEvent_t t0 = c.tic(s);
   if (!hs) {
-    k_tile3<T, PART, uint16_t><<<grid, threads, smem, s>>>(g.n, g.m, 0, g.n, g.rp, col, parent,
+    k_tile3<T, PART, uint16_t, 0><<<grid, threads, smem, s>>>(g.n, g.m, 0, g.n, g.rp, col, parent,
                                                            pm, tile, stage, tu.hub_degree, hl,
                                                            cut.as<uint2>(), cut_cap, ncut, g.err);
     CCG_LAUNCH_CHECK();
@@ -712,7 +769,7 @@ void run_uf_tiled(const Csr &g, uint32_t *parent, const PartMap &pm, const UfTun
       CCG_CUDA(cudaStreamWaitEvent(s, ev, 0));
       cudaEventDestroy(ev);
       const unsigned cgrid = (unsigned)std::min<uint64_t>((v1 - v0 + tile - 1) / tile, grid);
-      k_tile3<T, PART, uint16_t><<<cgrid, threads, smem, s>>>(g.n, g.m, v0, v1, g.rp, col,
+      k_tile3<T, PART, uint16_t, 0><<<cgrid, threads, smem, s>>>(g.n, g.m, v0, v1, g.rp, col,
                                                               parent, pm, tile, stage,
                                                               tu.hub_degree, hl, cut.as<uint2>(),
                                                               cut_cap, ncut, g.err);
@@ -765,22 +822,49 @@ bool tiles_suit(const Csr &g, const PartMap &pm, uint32_t tile, uint32_t hub_deg
 }
 
 template <class T, bool PART>
-void run_uf_afforest(const Csr &g, uint32_t *parent, const PartMap &pm, uint32_t hub_degree,
+void run_uf_afforest(const Csr &g, uint32_t *parent, const PartMap &pm, const UfTuning &tu,
                      cudaStream_t s, cudaMemPool_t pool, Counters &c) {
   const T *col = static_cast<const T *>(g.col);
   const uint64_t si = (uint64_t)g.idb;
+  const uint32_t hub_degree = tu.hub_degree;
   const unsigned grid = grid_for(g.n, kBlock, kSMs * 32);
-  k_iota_parent<<<grid, kBlock, 0, s>>>(g.n, parent);
-  CCG_LAUNCH_CHECK();
-  // each link round: offsets, one id, one union (two parent gathers); the
-  // rounds stay separate launches (one round's links all land before the
-  // next round's finds, which keeps the trees shallow)
-  const uint64_t link_bytes = 8 * (g.n + 1) + g.n * (si + 2 * 4);
-  for (uint32_t r = 0; r < kAffRounds; ++r) {
+  uint64_t link_bytes = 0;
+  if (g.n >= 4ull * tu.tile_vertices) {
+    // link rounds as one tiled pass: the first kAffRounds entries of every
+    // row, united in shared memory when they stay in the tile (most do on
+    // geometric and angularly ordered graphs), the others as cut edges
+    const TileShape ts = tile_shape<T, PART, (int)kAffRounds>(g.n, tu);
+    const uint64_t cut_cap = std::min<uint64_t>(g.m, kAffRounds * g.n) + 1;
+    DevBuf cut(8 * cut_cap, s, pool), cnt(8, s, pool);
+    CCG_CUDA(cudaMemsetAsync(cnt.p, 0, 8, s));
+    const HubList none{nullptr, 0, nullptr};  // no row is queued in link mode
+    // offsets, one sector of ids per row (the first kAffRounds entries), own parent
+    link_bytes = 8 * (g.n + 1) + g.n * 32 + 4 * g.n;
     cudaEvent_t t0 = c.tic(s);
-    k_aff_link<T, PART><<<grid, kBlock, 0, s>>>(g.n, g.m, g.rp, col, parent, pm, r, g.err);
+    k_tile3<T, PART, uint16_t, (int)kAffRounds><<<ts.grid, ts.threads, ts.smem, s>>>(
+        g.n, g.m, 0, g.n, g.rp, col, parent, pm, ts.tile, ts.stage, hub_degree, none,
+        cut.as<uint2>(), cut_cap, cnt.as<unsigned long long>(), g.err);
     CCG_LAUNCH_CHECK();
-    c.toc(s, "uf_sample_link", t0, link_bytes);
+    c.toc(s, "uf_sample_link_tiled", t0, link_bytes);
+    cudaEvent_t t1 = c.tic(s);
+    k_cut_union<<<kSMs * 16, kBlock, 0, s>>>(cut.as<uint2>(), cnt.as<unsigned long long>(),
+                                             cut_cap, parent);
+    CCG_LAUNCH_CHECK();
+    c.toc(s, "uf_cut_union", t1, 0);
+  } else {
+    k_iota_parent<<<grid, kBlock, 0, s>>>(g.n, parent);
+    CCG_LAUNCH_CHECK();
+    // each link round: offsets, one id, one union (two parent gathers); the
+    // rounds stay separate launches (one round's links all land before the
+    // next round's finds, which keeps the trees shallow)
+    const uint64_t round_bytes = 8 * (g.n + 1) + g.n * (si + 2 * 4);
+    for (uint32_t r = 0; r < kAffRounds; ++r) {
+      cudaEvent_t t0 = c.tic(s);
+      k_aff_link<T, PART><<<grid, kBlock, 0, s>>>(g.n, g.m, g.rp, col, parent, pm, r, g.err);
+      CCG_LAUNCH_CHECK();
+      c.toc(s, "uf_sample_link", t0, round_bytes);
+    }
+    link_bytes = kAffRounds * round_bytes;
   }
   k_compress<<<grid_for(g.n, kBlock, kSMs * 32), kBlock, 0, s>>>(g.n, parent);
   CCG_LAUNCH_CHECK();
@@ -820,12 +904,12 @@ void run_uf_afforest(const Csr &g, uint32_t *parent, const PartMap &pm, uint32_t
   DevBuf hubs(8 * hub_cap, s, pool), nh(4, s, pool);
   CCG_CUDA(cudaMemsetAsync(nh.p, 0, 4, s));
   const HubList hl{hubs.as<uint2>(), hub_cap, nh.as<unsigned int>()};
-  // remaining pass: every row's offsets and root; then, for the rows outside
-  // the giant component, one id and one root gather per remaining edge.  The
+  // remaining pass: every row's root; then, for the rows outside the giant
+  // component, offsets and one id and one root gather per remaining edge.  The
   // edge part is counted on the device while profiling and left out otherwise.
-  uint64_t rest_bytes = 8 * (g.n + 1) + 4 * g.n;
-  DevBuf ecount(8, s, pool);
-  if (c.prof) CCG_CUDA(cudaMemsetAsync(ecount.p, 0, 8, s));
+  uint64_t rest_bytes = 4 * g.n;
+  DevBuf ecount(16, s, pool);
+  if (c.prof) CCG_CUDA(cudaMemsetAsync(ecount.p, 0, 16, s));
   cudaEvent_t t1 = c.tic(s);
   k_aff_rest<T, PART><<<grid, kBlock, 0, s>>>(
       g.n, g.m, g.rp, col, parent, pm, dL.as<uint32_t>(), nparts, hub_degree, hl, g.err,
@@ -833,10 +917,10 @@ void run_uf_afforest(const Csr &g, uint32_t *parent, const PartMap &pm, uint32_t
   CCG_LAUNCH_CHECK();
   c.toc(s, "uf_sample_rest", t1, rest_bytes);
   if (c.prof && !c.recs.empty()) {
-    unsigned long long edges = 0;
-    CCG_CUDA(cudaMemcpyAsync(&edges, ecount.p, 8, cudaMemcpyDeviceToHost, s));
+    unsigned long long cnt[2] = {0, 0};  // ids read, rows whose offsets were read
+    CCG_CUDA(cudaMemcpyAsync(cnt, ecount.p, 16, cudaMemcpyDeviceToHost, s));
     CCG_CUDA(cudaStreamSynchronize(s));
-    rest_bytes += edges * (si + 4);
+    rest_bytes += cnt[0] * (si + 4) + cnt[1] * 16;
     c.recs.back().bytes = rest_bytes;
   }
   cudaEvent_t th = c.tic(s);
@@ -848,7 +932,7 @@ void run_uf_afforest(const Csr &g, uint32_t *parent, const PartMap &pm, uint32_t
   k_compress<<<grid_for(g.n, kBlock, kSMs * 32), kBlock, 0, s>>>(g.n, parent);
   CCG_LAUNCH_CHECK();
   c.toc(s, "uf_compress", t2, 3 * g.n * 4);
-  c.add(6 + kAffRounds, 4 * g.n + kAffRounds * link_bytes + rest_bytes + 6 * g.n * 4);
+  c.add(6 + kAffRounds, link_bytes + rest_bytes + 6 * g.n * 4);
 }
 
 template <class T, bool PART>
@@ -868,7 +952,7 @@ void run_uf_mode(const Csr &g, uint32_t *parent, const PartMap &pm, const UfTuni
                : kUfSampled;
   }
   if (mode == kUfTiled) run_uf_tiled<T, PART>(g, parent, pm, tu, s, pool, c, nullptr);
-  else if (mode == kUfSampled) run_uf_afforest<T, PART>(g, parent, pm, tu.hub_degree, s, pool, c);
+  else if (mode == kUfSampled) run_uf_afforest<T, PART>(g, parent, pm, tu, s, pool, c);
   else run_uf<T, PART>(g, parent, pm, tu.hub_degree, s, pool, c);
 }
 
