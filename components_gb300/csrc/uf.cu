@@ -148,11 +148,10 @@ __global__ void k_hook_hubs(uint64_t n, const uint64_t *__restrict__ rp,
   }
 }
 
-// Full compression: parent[v] <- root.  Runs after every link is made, so the
-// roots no longer change: every node of the walked path is set to the root
-// (any store is the final value; a halving store of an inner node could land
-// after that node's own thread wrote its root and is never made).  Vertices
-// that share a path (a tile's vertices and their tile root) find it short.
+// Full compression: parent[v] <- root.  Runs after every link is made.  Only
+// v's own entry is written: a halving store into p[x] could land after x's own
+// thread wrote its root (and leave x at an inner node), and writing the root
+// along the whole path was measured slower (store traffic on shared paths).
 __global__ void k_compress(uint64_t n, uint32_t *p) {
   for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < n;
        v += (uint64_t)gridDim.x * blockDim.x) {
@@ -160,9 +159,7 @@ __global__ void k_compress(uint64_t n, uint32_t *p) {
     if (r0 == (uint32_t)v) continue;
     uint32_t r = r0, nx;
     while ((nx = ld_cg(p + r)) != r) r = nx;
-    if (r == r0) continue;  // most vertices already point at their root
-    p[v] = r;
-    for (uint32_t x = r0; (nx = ld_cg(p + x)) != r; x = nx) st_cg(p + x, r);
+    if (r != r0) p[v] = r;  // most vertices already point at their root
   }
 }
 
@@ -552,10 +549,18 @@ __global__ void __launch_bounds__(1024, 2)
   }
 }
 
+// Root of v by loads only: many cut edges share a few endpoints (a tile root,
+// a hub), and stores into those hot entries would serialise in L2.
+__device__ __forceinline__ uint32_t uf_root(const uint32_t *p, uint32_t v) {
+  uint32_t r = v, nx;
+  while ((nx = ld_cg(p + r)) != r) r = nx;
+  return r;
+}
+
 // Edges between tiles, on the global parent array of tile-local roots.  After
-// each union both endpoints point at the common root they saw (an ancestor of
-// both; an endpoint other than that root already has a parent, so no CAS can
-// target it): the many cut edges of one tile root then start next to the root.
+// each union an endpoint whose parent is not yet the common root it saw is
+// pointed at it (an ancestor of both; an endpoint other than that root already
+// has a parent, so no CAS can target it).
 __global__ void k_cut_union(const uint2 *__restrict__ cut, const unsigned long long *__restrict__ ncut,
                             uint64_t cut_cap, uint32_t *p) {
   uint64_t cnt = *ncut;
@@ -563,7 +568,7 @@ __global__ void k_cut_union(const uint2 *__restrict__ cut, const unsigned long l
   for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < cnt;
        i += (uint64_t)gridDim.x * blockDim.x) {
     const uint2 e = cut[i];
-    uint32_t ra = uf_find(p, e.x), rb = uf_find(p, e.y);
+    uint32_t ra = uf_root(p, e.x), rb = uf_root(p, e.y);
     while (ra != rb) {
       if (ra < rb) {
         const uint32_t t = ra;
@@ -575,11 +580,11 @@ __global__ void k_cut_union(const uint2 *__restrict__ cut, const unsigned long l
         ra = rb;
         break;
       }
-      ra = uf_find(p, old);
-      rb = uf_find(p, rb);
+      ra = uf_root(p, old);
+      rb = uf_root(p, rb);
     }
-    if (e.x != ra) st_cg(p + e.x, ra);
-    if (e.y != ra) st_cg(p + e.y, ra);
+    if (e.x != ra && ld_cg(p + e.x) != ra) st_cg(p + e.x, ra);
+    if (e.y != ra && ld_cg(p + e.y) != ra) st_cg(p + e.y, ra);
   }
 }
 
@@ -592,17 +597,25 @@ __host__ __device__ __forceinline__ uint64_t sample_row(uint64_t i, uint64_t sam
 
 // Sampled edges (u < v, same rank): total, edges leaving their tile, and edges
 // of hub rows (about half of a hub row's entries are u < v).  Both kinds are
-// left to global unions by the tiled pass.
+// left to global unions by the tiled pass.  Also the rows' first kAffRounds
+// entries (the sampled-linking edges): total and leaving the tile.
 template <class T, bool PART>
 __global__ void k_cut_sample(uint64_t n, uint64_t m, const uint64_t *__restrict__ rp,
                              const T *__restrict__ col, PartMap pm, uint32_t tile,
                              uint32_t hub_degree, uint32_t samples,
                              unsigned long long *__restrict__ counts) {
-  unsigned long long tot = 0, cross = 0, hub = 0;
+  unsigned long long tot = 0, cross = 0, hub = 0, ltot = 0, lcross = 0;
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < samples; i += gridDim.x * blockDim.x) {
     uint64_t v = sample_row(i, samples, n);
     uint64_t b = __ldg(rp + v), e = __ldg(rp + v + 1);
     if (e < b || e > m) continue;
+    // the sampled-linking entries (the first kAffRounds of the row)
+    for (uint64_t k = b; k < e && k < b + kAffRounds; ++k) {
+      const uint64_t u = (uint64_t)__ldg(col + k);
+      if (u >= n || u == v) continue;
+      ++ltot;
+      lcross += u / tile != v / tile;
+    }
     if (e - b > hub_degree) {
       tot += (e - b) / 2;
       hub += (e - b) / 2;
@@ -620,6 +633,8 @@ __global__ void k_cut_sample(uint64_t n, uint64_t m, const uint64_t *__restrict_
   atomicAdd(counts, tot);
   atomicAdd(counts + 1, cross);
   atomicAdd(counts + 2, hub);
+  atomicAdd(counts + 3, ltot);
+  atomicAdd(counts + 4, lcross);
 }
 
 template <class OUT>
@@ -802,34 +817,41 @@ inline bool tiles_fit(uint64_t tot, uint64_t cross, uint64_t hub) {
   return tot == 0 || (2 * cross < tot && 10 * hub < tot);
 }
 
-// The decision above on a sample of 8192 rows of a device graph (one small
-// readback).
+// Both decisions on a sample of 8192 rows of a device graph (one small
+// readback): the tiled pass, and whether the link rounds of sampled linking
+// run as a tiled pass (at least three quarters of their edges in the tile).
+struct Shares {
+  bool tiles = false, link_tiles = false;
+};
 template <class T, bool PART>
-bool tiles_suit(const Csr &g, const PartMap &pm, uint32_t tile, uint32_t hub_degree,
-                cudaStream_t s, cudaMemPool_t pool, Counters &c) {
-  DevBuf cnt(24, s, pool);
-  CCG_CUDA(cudaMemsetAsync(cnt.p, 0, 24, s));
+Shares sample_shares(const Csr &g, const PartMap &pm, uint32_t tile, uint32_t hub_degree,
+                     cudaStream_t s, cudaMemPool_t pool, Counters &c) {
+  DevBuf cnt(40, s, pool);
+  CCG_CUDA(cudaMemsetAsync(cnt.p, 0, 40, s));
   const uint32_t samples = (uint32_t)std::min<uint64_t>(g.n, 8192);
   k_cut_sample<T, PART><<<(samples + 255) / 256, 256, 0, s>>>(
       g.n, g.m, g.rp, static_cast<const T *>(g.col), pm, tile, hub_degree, samples,
       cnt.as<unsigned long long>());
   CCG_LAUNCH_CHECK();
-  unsigned long long h[3] = {0, 0, 0};
-  CCG_CUDA(cudaMemcpyAsync(h, cnt.p, 24, cudaMemcpyDeviceToHost, s));
+  unsigned long long h[5] = {0, 0, 0, 0, 0};
+  CCG_CUDA(cudaMemcpyAsync(h, cnt.p, 40, cudaMemcpyDeviceToHost, s));
   CCG_CUDA(cudaStreamSynchronize(s));
   c.add(1, 0);
-  return tiles_fit(h[0], h[1], h[2]);
+  Shares r;
+  r.tiles = tiles_fit(h[0], h[1], h[2]);
+  r.link_tiles = h[3] > 0 && 4 * h[4] < h[3];
+  return r;
 }
 
 template <class T, bool PART>
 void run_uf_afforest(const Csr &g, uint32_t *parent, const PartMap &pm, const UfTuning &tu,
-                     cudaStream_t s, cudaMemPool_t pool, Counters &c) {
+                     bool link_tiles, cudaStream_t s, cudaMemPool_t pool, Counters &c) {
   const T *col = static_cast<const T *>(g.col);
   const uint64_t si = (uint64_t)g.idb;
   const uint32_t hub_degree = tu.hub_degree;
   const unsigned grid = grid_for(g.n, kBlock, kSMs * 32);
   uint64_t link_bytes = 0;
-  if (g.n >= 4ull * tu.tile_vertices) {
+  if (link_tiles) {
     // link rounds as one tiled pass: the first kAffRounds entries of every
     // row, united in shared memory when they stay in the tile (most do on
     // geometric and angularly ordered graphs), the others as cut edges
@@ -943,16 +965,15 @@ void run_uf_mode(const Csr &g, uint32_t *parent, const PartMap &pm, const UfTuni
     return;
   }
   int mode = tu.mode;
-  if (mode == kUfAuto) {
-    // the tiled pass wins when most edges stay inside their tile (grids,
-    // geometric and angularly ordered graphs); otherwise sampled linking
-    mode = (g.n >= 4ull * tu.tile_vertices &&
-            tiles_suit<T, PART>(g, pm, tu.tile_vertices, tu.hub_degree, s, pool, c))
-               ? kUfTiled
-               : kUfSampled;
-  }
+  const bool big = g.n >= 4ull * tu.tile_vertices;
+  Shares sh;
+  if (big && (mode == kUfAuto || mode == kUfSampled))
+    sh = sample_shares<T, PART>(g, pm, tu.tile_vertices, tu.hub_degree, s, pool, c);
+  // the tiled pass wins when most edges stay inside their tile and few lie in
+  // hub rows (grids, geometric graphs); otherwise sampled linking
+  if (mode == kUfAuto) mode = (big && sh.tiles) ? kUfTiled : kUfSampled;
   if (mode == kUfTiled) run_uf_tiled<T, PART>(g, parent, pm, tu, s, pool, c, nullptr);
-  else if (mode == kUfSampled) run_uf_afforest<T, PART>(g, parent, pm, tu, s, pool, c);
+  else if (mode == kUfSampled) run_uf_afforest<T, PART>(g, parent, pm, tu, sh.link_tiles, s, pool, c);
   else run_uf<T, PART>(g, parent, pm, tu.hub_degree, s, pool, c);
 }
 

@@ -166,11 +166,13 @@ def test_stream_interop(cuda):
 
 @pytest.mark.parametrize("mode", [_lib.CC_HOOK_GLOBAL, _lib.CC_HOOK_TILED, _lib.CC_HOOK_SAMPLED])
 def test_hook_modes_agree(cuda, mode):
-    """Global and tiled hook passes give the same labels, also with ranks,
-    hub rows, tiles smaller than a rank and ranks smaller than a tile."""
+    """Global, tiled and sampled hook passes give the same labels, also with
+    ranks, hub rows, tiles smaller than a rank and ranks smaller than a tile,
+    and with link rounds run as a tiled pass (grids, the angularly ordered
+    hyperbolic graph) or as global rounds (G(n, m), the star)."""
     graphs = [cc.gen_grid(700, 500, 0.5, seed=6), cc.gen_gnm(60000, 80000, seed=6, id_bytes=8),
               cc.from_edges(40000, [(5, i) for i in range(6, 40000, 3)] + [(i, i + 1) for i in range(0, 39999, 7)]),
-              cc.gen_grid(64, 2000, 0.7, seed=2)]
+              cc.gen_grid(64, 2000, 0.7, seed=2), cc.gen_rhg(1 << 17, 16.0, 2.6, seed=3)]
     for tile in (1024, 16384):
         ctx = cc.Context(0)
         ctx.set_tuning(hook_mode=mode, tile_vertices=tile, tile_threads=256, hub_degree=16)
