@@ -31,6 +31,7 @@ struct UfTuning {
   uint32_t hub_degree = 32;      // rows above: one warp per row
   uint32_t tile_vertices = 32768;  // vertices per CTA tile (2 bytes of shared memory each)
   uint32_t tile_threads = 1024;
+  int link_tiles = -1;  // sampled linking: link rounds tiled (1) or global (0); -1 decide from a row sample
 };
 // Host source of a caller graph whose device buffers are still empty: the
 // tiled pass copies tile-aligned chunks on `copy` and overlaps them with the
@@ -48,6 +49,10 @@ void uf_components(const Csr &g, uint32_t *parent, const PartMap *pm,
 // rows above hub_degree.
 bool host_tiles_suit(const uint64_t *rp, const void *col, int idb, uint64_t n, uint64_t m,
                      uint32_t tile, uint32_t hub_degree);
+// Whether the link rounds of sampled linking stay in their tile (at least three
+// quarters of the sampled rows' first entries), from a host CSR.
+bool host_link_tiles(const uint64_t *rp, const void *col, int idb, uint64_t n, uint64_t m,
+                     uint32_t tile);
 
 // Write uint32 labels to an id_bytes-wide output array.
 void widen_labels(const uint32_t *in, void *out, int out_bytes, uint64_t n,

@@ -127,7 +127,8 @@ struct Req {
   cudaEvent_t copied = nullptr;
   std::atomic<int> state{kWaiting};
   uint32_t batch_id = 0, batch_size = 0;
-  bool tiled = false;  // large graph: tiled hook pass (estimated on the host)
+  bool tiled = false;       // large graph: tiled hook pass (estimated on the host)
+  bool link_tiles = false;  // large graph, sampled linking: tiled link rounds
 };
 
 struct Batch {
@@ -206,6 +207,9 @@ struct Server {
     CCG_CUDA(cudaEventCreateWithFlags(&r->copied, cudaEventDisableTiming));
     CCG_CUDA(cudaEventRecord(r->copied, copy_stream));
     r->tiled = g.n > cfg.smem_max_n && prefers_tiles(g);
+    r->link_tiles = g.n > cfg.smem_max_n && !r->tiled &&
+                    host_link_tiles(g.row_ptr, g.col, (int)g.id_bytes, g.n, g.m_dir,
+                                    UfTuning().tile_vertices);
   }
 
   void launch(std::vector<Req *> &batch, int si) {  // worker thread, no lock held
@@ -248,6 +252,7 @@ struct Server {
       G.err = reinterpret_cast<int *>(r->lab.as<uint32_t>() + r->g.n);
       UfTuning tu;
       tu.mode = r->tiled ? kUfTiled : kUfSampled;
+      tu.link_tiles = r->link_tiles ? 1 : 0;  // decided on the host: no device round trip
       uf_components(G, r->lab.as<uint32_t>(), nullptr, tu, s, pool, c);
     }
     uint32_t bid;

@@ -235,6 +235,57 @@ __global__ void k_aff_sample(uint64_t n, const uint32_t *p, PartMap pm, uint32_t
   }
 }
 
+// Most frequent value among the `per` (<= kModeBlock) samples of block q
+// (ties: the smallest value): a bitonic sort in shared memory, each run's
+// length by a binary search for its end, then a block-wide maximum of
+// (length, ~value).
+constexpr int kModeBlock = 1024;
+__global__ void __launch_bounds__(kModeBlock) k_aff_mode(const uint32_t *__restrict__ smp, uint32_t per,
+                                                        uint32_t *__restrict__ Ls) {
+  __shared__ uint32_t a[kModeBlock];
+  __shared__ unsigned long long best[kModeBlock / 32];
+  const uint32_t i = threadIdx.x;
+  a[i] = i < per ? smp[(uint64_t)blockIdx.x * per + i] : 0xffffffffu;
+  __syncthreads();
+  for (uint32_t k = 2; k <= kModeBlock; k <<= 1) {
+    for (uint32_t j = k >> 1; j > 0; j >>= 1) {
+      const uint32_t ixj = i ^ j;
+      if (ixj > i) {
+        const uint32_t x = a[i], y = a[ixj];
+        if ((i & k) == 0 ? x > y : x < y) {
+          a[i] = y;
+          a[ixj] = x;
+        }
+      }
+      __syncthreads();
+    }
+  }
+  unsigned long long key = 0;
+  if (i < per && (i == 0 || a[i] != a[i - 1])) {
+    uint32_t lo = i, hi = per;  // first index past the run of a[i]
+    while (hi - lo > 1) {
+      const uint32_t mid = (lo + hi) / 2;
+      if (a[mid] == a[i]) lo = mid;
+      else hi = mid;
+    }
+    key = ((unsigned long long)(lo + 1 - i) << 32) | (0xffffffffu - a[i]);
+  }
+  for (int o = 16; o; o >>= 1) {
+    const unsigned long long y = __shfl_xor_sync(0xffffffffu, key, o);
+    key = y > key ? y : key;
+  }
+  if ((i & 31) == 0) best[i >> 5] = key;
+  __syncthreads();
+  if (i < 32) {
+    key = best[i];
+    for (int o = 16; o; o >>= 1) {
+      const unsigned long long y = __shfl_xor_sync(0xffffffffu, key, o);
+      key = y > key ? y : key;
+    }
+    if (i == 0) Ls[blockIdx.x] = key ? 0xffffffffu - (uint32_t)key : kNone;
+  }
+}
+
 template <class T, bool PART>
 __global__ void k_aff_rest(uint64_t n, uint64_t m, const uint64_t *__restrict__ rp,
                            const T *__restrict__ col, uint32_t *p, PartMap pm,
@@ -549,18 +600,12 @@ __global__ void __launch_bounds__(1024, 2)
   }
 }
 
-// Root of v by loads only: many cut edges share a few endpoints (a tile root,
-// a hub), and stores into those hot entries would serialise in L2.
-__device__ __forceinline__ uint32_t uf_root(const uint32_t *p, uint32_t v) {
-  uint32_t r = v, nx;
-  while ((nx = ld_cg(p + r)) != r) r = nx;
-  return r;
-}
-
 // Edges between tiles, on the global parent array of tile-local roots.  After
 // each union an endpoint whose parent is not yet the common root it saw is
 // pointed at it (an ancestor of both; an endpoint other than that root already
-// has a parent, so no CAS can target it).
+// has a parent, so no CAS can target it).  The store is skipped when the entry
+// already holds the root: many cut edges share a few endpoints (a tile root, a
+// hub), and repeated stores into those hot entries serialise in L2.
 __global__ void k_cut_union(const uint2 *__restrict__ cut, const unsigned long long *__restrict__ ncut,
                             uint64_t cut_cap, uint32_t *p) {
   uint64_t cnt = *ncut;
@@ -568,7 +613,7 @@ __global__ void k_cut_union(const uint2 *__restrict__ cut, const unsigned long l
   for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < cnt;
        i += (uint64_t)gridDim.x * blockDim.x) {
     const uint2 e = cut[i];
-    uint32_t ra = uf_root(p, e.x), rb = uf_root(p, e.y);
+    uint32_t ra = uf_find(p, e.x), rb = uf_find(p, e.y);
     while (ra != rb) {
       if (ra < rb) {
         const uint32_t t = ra;
@@ -580,8 +625,8 @@ __global__ void k_cut_union(const uint2 *__restrict__ cut, const unsigned long l
         ra = rb;
         break;
       }
-      ra = uf_root(p, old);
-      rb = uf_root(p, rb);
+      ra = uf_find(p, old);
+      rb = uf_find(p, rb);
     }
     if (e.x != ra && ld_cg(p + e.x) != ra) st_cg(p + e.x, ra);
     if (e.y != ra && ld_cg(p + e.y) != ra) st_cg(p + e.y, ra);
@@ -902,26 +947,9 @@ void run_uf_afforest(const Csr &g, uint32_t *parent, const PartMap &pm, const Uf
   k_aff_sample<<<(samples + 255) / 256, 256, 0, s>>>(g.n, parent, pm, nparts, per, 0x5eedull,
                                                      smp.as<uint32_t>());
   CCG_LAUNCH_CHECK();
-  std::vector<uint32_t> h(samples), Ls(nparts);
-  CCG_CUDA(cudaMemcpyAsync(h.data(), smp.p, 4 * samples, cudaMemcpyDeviceToHost, s));
-  CCG_CUDA(cudaStreamSynchronize(s));
-  for (uint32_t q = 0; q < nparts; ++q) {
-    auto b = h.begin() + (size_t)q * per, e = b + per;
-    std::sort(b, e);
-    uint32_t L = per ? *b : kNone;
-    size_t best = 0;
-    for (auto i = b; i != e;) {
-      auto j = i;
-      while (j != e && *j == *i) ++j;
-      if ((size_t)(j - i) > best) {
-        best = (size_t)(j - i);
-        L = *i;
-      }
-      i = j;
-    }
-    Ls[q] = L;
-  }
-  CCG_CUDA(cudaMemcpyAsync(dL.p, Ls.data(), 4 * nparts, cudaMemcpyHostToDevice, s));
+  // the mode of each partition's samples, on the device (no host round trip)
+  k_aff_mode<<<nparts, kModeBlock, 0, s>>>(smp.as<uint32_t>(), per, dL.as<uint32_t>());
+  CCG_LAUNCH_CHECK();
   const uint64_t hub_cap = hub_list_cap(g.m, hub_degree);
   DevBuf hubs(8 * hub_cap, s, pool), nh(4, s, pool);
   CCG_CUDA(cudaMemsetAsync(nh.p, 0, 4, s));
@@ -954,7 +982,7 @@ void run_uf_afforest(const Csr &g, uint32_t *parent, const PartMap &pm, const Uf
   k_compress<<<grid_for(g.n, kBlock, kSMs * 32), kBlock, 0, s>>>(g.n, parent);
   CCG_LAUNCH_CHECK();
   c.toc(s, "uf_compress", t2, 3 * g.n * 4);
-  c.add(6 + kAffRounds, link_bytes + rest_bytes + 6 * g.n * 4);
+  c.add((link_tiles ? 2 : 1 + kAffRounds) + 6, link_bytes + rest_bytes + 6 * g.n * 4);
 }
 
 template <class T, bool PART>
@@ -967,8 +995,9 @@ void run_uf_mode(const Csr &g, uint32_t *parent, const PartMap &pm, const UfTuni
   int mode = tu.mode;
   const bool big = g.n >= 4ull * tu.tile_vertices;
   Shares sh;
-  if (big && (mode == kUfAuto || mode == kUfSampled))
+  if (big && (mode == kUfAuto || (mode == kUfSampled && tu.link_tiles < 0)))
     sh = sample_shares<T, PART>(g, pm, tu.tile_vertices, tu.hub_degree, s, pool, c);
+  if (tu.link_tiles >= 0) sh.link_tiles = big && tu.link_tiles > 0;
   // the tiled pass wins when most edges stay inside their tile and few lie in
   // hub rows (grids, geometric graphs); otherwise sampled linking
   if (mode == kUfAuto) mode = (big && sh.tiles) ? kUfTiled : kUfSampled;
@@ -1019,6 +1048,25 @@ bool host_tiles_suit(const uint64_t *rp, const void *col, int idb, uint64_t n, u
     }
   }
   return tiles_fit(tot, cross, hub);
+}
+
+bool host_link_tiles(const uint64_t *rp, const void *col, int idb, uint64_t n, uint64_t m,
+                     uint32_t tile) {
+  const uint64_t samples = std::min<uint64_t>(n, 8192);
+  uint64_t tot = 0, cross = 0;
+  for (uint64_t i = 0; i < samples; ++i) {
+    const uint64_t v = sample_row(i, samples, n);
+    const uint64_t b = rp[v], e = rp[v + 1];
+    if (e < b || e > m) continue;
+    for (uint64_t k = b; k < e && k < b + kAffRounds; ++k) {
+      const uint64_t u = idb == 8 ? static_cast<const uint64_t *>(col)[k]
+                                  : static_cast<const uint32_t *>(col)[k];
+      if (u >= n || u == v) continue;
+      ++tot;
+      cross += u / tile != v / tile;
+    }
+  }
+  return tot > 0 && 4 * cross < tot;
 }
 
 void widen_labels(const uint32_t *in, void *out, int out_bytes, uint64_t n, cudaStream_t s,
