@@ -50,7 +50,7 @@ void uf_components(const Csr &g, uint32_t *parent, const PartMap *pm,
 bool host_tiles_suit(const uint64_t *rp, const void *col, int idb, uint64_t n, uint64_t m,
                      uint32_t tile, uint32_t hub_degree);
 // Whether the link rounds of sampled linking stay in their tile (at least three
-// quarters of the sampled rows' first entries), from a host CSR.
+// quarters of the sampled rows' link-round entries), from a host CSR.
 bool host_link_tiles(const uint64_t *rp, const void *col, int idb, uint64_t n, uint64_t m,
                      uint32_t tile);
 

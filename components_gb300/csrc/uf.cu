@@ -187,7 +187,7 @@ __device__ __forceinline__ void queue_hub(const HubList &hl, uint32_t v, uint64_
 }
 
 // ---- sampled linking (Afforest: Sutton, Ben-Nun, Barak, IPDPS 2018) ------------
-// Link every vertex to its r-th neighbour for r < kAffRounds, compress, find
+// Link every vertex to kAffRounds of its neighbours, compress, find
 // the most frequent root L on a sample, then only vertices outside L's tree
 // process their remaining edges.  An edge skipped by an endpoint inside L is
 // either processed from its other endpoint or joins two vertices that are
@@ -195,6 +195,19 @@ __device__ __forceinline__ void queue_hub(const HubList &hl, uint32_t v, uint64_
 // component most edges are never touched; without one it costs two light
 // passes.
 constexpr uint32_t kAffRounds = 2;
+
+// Entry of a row of d entries that link round r uses (r < min(d, kAffRounds);
+// the positions are distinct): spread through the row rather than its first
+// entries, because rows are sorted and every row's first entries would point
+// at the same few small ids.
+__host__ __device__ __forceinline__ uint64_t link_pos(uint64_t d, uint32_t r) {
+  return d * (2 * r + 1) / (2 * kAffRounds);
+}
+__host__ __device__ __forceinline__ bool is_link_pos(uint64_t d, uint64_t j) {
+  for (uint32_t r = 0; r < kAffRounds && r < d; ++r)
+    if (link_pos(d, r) == j) return true;
+  return false;
+}
 
 __device__ __forceinline__ bool same_part(const PartMap &pm, uint32_t v, uint32_t u) {
   return pm.part(v) == pm.part(u);
@@ -207,7 +220,7 @@ __global__ void k_aff_link(uint64_t n, uint64_t m, const uint64_t *__restrict__ 
        v += (uint64_t)gridDim.x * blockDim.x) {
     Row row;
     if (!load_row(rp, v, m, err, row) || row.e - row.b <= r) continue;
-    const uint64_t u = (uint64_t)__ldg(col + row.b + r);
+    const uint64_t u = (uint64_t)__ldg(col + row.b + link_pos(row.e - row.b, r));
     if (u >= n) {
       set_err(err, kErrBadId);
       continue;
@@ -302,11 +315,12 @@ __global__ void k_aff_rest(uint64_t n, uint64_t m, const uint64_t *__restrict__ 
     Row row;
     if (!load_row(rp, v, m, err, row) || row.e - row.b <= kAffRounds) continue;
     if (row.e - row.b > hub_degree) {
-      queue_hub(hl, (uint32_t)v, row.e - row.b - kAffRounds, err);
+      queue_hub(hl, (uint32_t)v, row.e - row.b, err);
       continue;
     }
     work += (uint32_t)(row.e - row.b - kAffRounds);
-    for (uint64_t k = row.b + kAffRounds; k < row.e; ++k) {
+    for (uint64_t k = row.b; k < row.e; ++k) {
+      if (is_link_pos(row.e - row.b, k - row.b)) continue;  // linked already
       uint64_t u = (uint64_t)__ldg(col + k);
       if (u >= n) {
         set_err(err, kErrBadId);
@@ -325,14 +339,14 @@ __global__ void k_aff_rest(uint64_t n, uint64_t m, const uint64_t *__restrict__ 
   }
 }
 
-// One warp per hub piece: edges [skip + y*kPiece, skip + (y+1)*kPiece) of row
-// x.  LESS: only edges to smaller ids (hook/tile passes, each undirected edge
-// once); otherwise every edge (the sampled pass skips rows inside the giant
-// component, so an edge may be seen from its larger end only).
+// One warp per hub piece: edges [y*kPiece, (y+1)*kPiece) of row x.  LESS:
+// only edges to smaller ids (hook/tile passes, each undirected edge once);
+// otherwise every edge but the row's link-round entries (the sampled pass skips
+// rows inside the giant component, so an edge may be seen from one end only).
 template <class T, bool PART, bool LESS>
 __global__ void k_hub_pieces(uint64_t n, uint64_t m, const uint64_t *__restrict__ rp,
-                             const T *__restrict__ col, uint32_t *p, PartMap pm, uint32_t skip,
-                             HubList hl, int *err) {
+                             const T *__restrict__ col, uint32_t *p, PartMap pm, HubList hl,
+                             int *err) {
   const unsigned lane = threadIdx.x & 31;
   const uint64_t warp = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
   const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
@@ -344,7 +358,7 @@ __global__ void k_hub_pieces(uint64_t n, uint64_t m, const uint64_t *__restrict_
     if (v >= n) continue;
     const uint64_t rb = __ldg(rp + v), re = __ldg(rp + v + 1);
     if (re < rb || re > m) continue;  // recorded by the pass that queued the row
-    const uint64_t b = rb + skip + (uint64_t)it.y * kPiece;
+    const uint64_t b = rb + (uint64_t)it.y * kPiece;
     const uint64_t e = min(re, b + kPiece);
     const uint32_t lo = PART ? part_lo(pm, v) : 0u;
     for (uint64_t k = b + lane; k < e; k += 32) {
@@ -355,7 +369,7 @@ __global__ void k_hub_pieces(uint64_t n, uint64_t m, const uint64_t *__restrict_
       }
       if (LESS) {
         if (u < v && (!PART || (uint32_t)u >= lo)) uf_union(p, v, (uint32_t)u);
-      } else {
+      } else if (!is_link_pos(re - rb, k - rb)) {  // the link rounds took those
         if (!PART || same_part(pm, v, (uint32_t)u)) uf_union(p, v, (uint32_t)u);
       }
     }
@@ -446,9 +460,10 @@ size_t tile_smem_bytes(uint32_t tile, uint32_t threads, uint32_t stage) {
 }
 
 // LINK = 0: every edge to a smaller id (the tiled hook pass; rows above
-// hub_degree are queued as hub pieces).  LINK = k > 0: the first k entries of
-// every row in either direction (the link rounds of sampled linking, which
-// stay inside their tile on geometric and angularly ordered graphs).
+// hub_degree are queued as hub pieces).  LINK = k > 0: the k link-round entries
+// of every row (link_pos) in either direction (the link rounds of sampled
+// linking, which stay inside their tile on geometric and angularly ordered
+// graphs).
 template <class T, bool PART, class PT, int LINK>
 __global__ void __launch_bounds__(1024, 2)
     k_tile3(uint64_t n, uint64_t m, uint64_t v_begin, uint64_t v_end,
@@ -476,12 +491,13 @@ __global__ void __launch_bounds__(1024, 2)
     uint32_t qn = 0;  // warp-uniform queue fill
     for (uint32_t g0 = wid * 32; g0 < len; g0 += nw * 32) {
       const uint32_t i = g0 + lane;
-      uint64_t rb = 0;
+      uint64_t rb = 0, rl = 0;  // row start; row length (link mode)
       uint32_t deg = 0, lo = 0;
       if (i < len) {
         const uint64_t v = t0 + i;
         rb = __ldg(rp + v);
         const uint64_t re = __ldg(rp + v + 1);
+        if (LINK) rl = re - rb;
         if (re < rb || re > m) {
           set_err(err, kErrBadOffsets);
         } else if (!LINK && re - rb > hub_degree) {
@@ -551,7 +567,8 @@ __global__ void __launch_bounds__(1024, 2)
         // rows are adjacent in memory
         for (uint32_t j = 0; j < maxdeg; ++j) {
           const bool valid = j < deg;
-          edge(valid, valid ? (uint64_t)__ldg(col + rb + j) : 0ull, i, lo);
+          const uint64_t k = rb + (LINK ? link_pos(rl, j) : j);
+          edge(valid, valid ? (uint64_t)__ldg(col + k) : 0ull, i, lo);
         }
       } else {
         // skewed degrees: the 32 rows' edges as one flattened stream, lane k
@@ -642,8 +659,8 @@ __host__ __device__ __forceinline__ uint64_t sample_row(uint64_t i, uint64_t sam
 
 // Sampled edges (u < v, same rank): total, edges leaving their tile, and edges
 // of hub rows (about half of a hub row's entries are u < v).  Both kinds are
-// left to global unions by the tiled pass.  Also the rows' first kAffRounds
-// entries (the sampled-linking edges): total and leaving the tile.
+// left to global unions by the tiled pass.  Also the rows' link-round entries
+// (the sampled-linking edges): total and leaving the tile.
 template <class T, bool PART>
 __global__ void k_cut_sample(uint64_t n, uint64_t m, const uint64_t *__restrict__ rp,
                              const T *__restrict__ col, PartMap pm, uint32_t tile,
@@ -654,9 +671,9 @@ __global__ void k_cut_sample(uint64_t n, uint64_t m, const uint64_t *__restrict_
     uint64_t v = sample_row(i, samples, n);
     uint64_t b = __ldg(rp + v), e = __ldg(rp + v + 1);
     if (e < b || e > m) continue;
-    // the sampled-linking entries (the first kAffRounds of the row)
-    for (uint64_t k = b; k < e && k < b + kAffRounds; ++k) {
-      const uint64_t u = (uint64_t)__ldg(col + k);
+    // the link-round entries of the row
+    for (uint32_t r = 0; r < kAffRounds && r < e - b; ++r) {
+      const uint64_t u = (uint64_t)__ldg(col + b + link_pos(e - b, r));
       if (u >= n || u == v) continue;
       ++ltot;
       lcross += u / tile != v / tile;
@@ -842,7 +859,7 @@ void run_uf_tiled(const Csr &g, uint32_t *parent, const PartMap &pm, const UfTun
   CCG_LAUNCH_CHECK();
   c.toc(s, "uf_cut_union", t1, 0);
   cudaEvent_t t2 = c.tic(s);
-  k_hub_pieces<T, PART, true><<<kSMs * 8, kBlock, 0, s>>>(g.n, g.m, g.rp, col, parent, pm, 0u,
+  k_hub_pieces<T, PART, true><<<kSMs * 8, kBlock, 0, s>>>(g.n, g.m, g.rp, col, parent, pm,
                                                           hl, g.err);
   CCG_LAUNCH_CHECK();
   c.toc(s, "uf_hook_hubs", t2, 0);
@@ -897,16 +914,16 @@ void run_uf_afforest(const Csr &g, uint32_t *parent, const PartMap &pm, const Uf
   const unsigned grid = grid_for(g.n, kBlock, kSMs * 32);
   uint64_t link_bytes = 0;
   if (link_tiles) {
-    // link rounds as one tiled pass: the first kAffRounds entries of every
-    // row, united in shared memory when they stay in the tile (most do on
+    // link rounds as one tiled pass: the link-round entries of every row,
+    // united in shared memory when they stay in the tile (most do on
     // geometric and angularly ordered graphs), the others as cut edges
     const TileShape ts = tile_shape<T, PART, (int)kAffRounds>(g.n, tu);
     const uint64_t cut_cap = std::min<uint64_t>(g.m, kAffRounds * g.n) + 1;
     DevBuf cut(8 * cut_cap, s, pool), cnt(8, s, pool);
     CCG_CUDA(cudaMemsetAsync(cnt.p, 0, 8, s));
     const HubList none{nullptr, 0, nullptr};  // no row is queued in link mode
-    // offsets, one sector of ids per row (the first kAffRounds entries), own parent
-    link_bytes = 8 * (g.n + 1) + g.n * 32 + 4 * g.n;
+    // offsets, the link-round ids, own parent
+    link_bytes = 8 * (g.n + 1) + kAffRounds * g.n * si + 4 * g.n;
     cudaEvent_t t0 = c.tic(s);
     k_tile3<T, PART, uint16_t, (int)kAffRounds><<<ts.grid, ts.threads, ts.smem, s>>>(
         g.n, g.m, 0, g.n, g.rp, col, parent, pm, ts.tile, ts.stage, hub_degree, none,
@@ -974,8 +991,8 @@ void run_uf_afforest(const Csr &g, uint32_t *parent, const PartMap &pm, const Uf
     c.recs.back().bytes = rest_bytes;
   }
   cudaEvent_t th = c.tic(s);
-  k_hub_pieces<T, PART, false><<<kSMs * 8, kBlock, 0, s>>>(g.n, g.m, g.rp, col, parent, pm,
-                                                           kAffRounds, hl, g.err);
+  k_hub_pieces<T, PART, false><<<kSMs * 8, kBlock, 0, s>>>(g.n, g.m, g.rp, col, parent, pm, hl,
+                                                           g.err);
   CCG_LAUNCH_CHECK();
   c.toc(s, "uf_sample_hubs", th, 0);
   cudaEvent_t t2 = c.tic(s);
@@ -1058,7 +1075,8 @@ bool host_link_tiles(const uint64_t *rp, const void *col, int idb, uint64_t n, u
     const uint64_t v = sample_row(i, samples, n);
     const uint64_t b = rp[v], e = rp[v + 1];
     if (e < b || e > m) continue;
-    for (uint64_t k = b; k < e && k < b + kAffRounds; ++k) {
+    for (uint32_t r = 0; r < kAffRounds && r < e - b; ++r) {
+      const uint64_t k = b + link_pos(e - b, r);
       const uint64_t u = idb == 8 ? static_cast<const uint64_t *>(col)[k]
                                   : static_cast<const uint32_t *>(col)[k];
       if (u >= n || u == v) continue;
