@@ -196,12 +196,14 @@ __device__ __forceinline__ void queue_hub(const HubList &hl, uint32_t v, uint64_
 // passes.
 constexpr uint32_t kAffRounds = 2;
 
-// Entry of a row of d entries that link round r uses (r < min(d, kAffRounds);
-// the positions are distinct): spread through the row rather than its first
-// entries, because rows are sorted and every row's first entries would point
-// at the same few small ids.
+// Entry of a row of d entries that link round r uses (r < min(d, kAffRounds)):
+// the row's first entries.  On sorted rows these are the smallest neighbour
+// ids, which on hyperbolic graphs are often hubs: the link rounds then already
+// join the giant component (entries spread through the row were measured to
+// leave it in pieces, and the remaining pass then does most of the work).
 __host__ __device__ __forceinline__ uint64_t link_pos(uint64_t d, uint32_t r) {
-  return d * (2 * r + 1) / (2 * kAffRounds);
+  (void)d;
+  return r;
 }
 __host__ __device__ __forceinline__ bool is_link_pos(uint64_t d, uint64_t j) {
   for (uint32_t r = 0; r < kAffRounds && r < d; ++r)
@@ -510,7 +512,12 @@ __global__ void __launch_bounds__(1024, 2)
       // One edge (v, uu) per lane, all lanes together: an in-tile edge to a
       // smaller id goes to the warp's union queue (32 queued entries make a
       // union step), an edge to an earlier tile to the cut stage.
-      auto edge = [&](bool valid, uint64_t uu, uint32_t vi, uint32_t lov) {
+      // hook: the lane's row may link itself under its first in-tile smaller
+      // neighbour with one CAS (no finds) while it is still a root; a link
+      // under a non-root keeps parents smaller than children, so the forest
+      // stays acyclic.  Only the row-per-lane loop hooks.
+      bool hooked = false;
+      auto edge = [&](bool valid, uint64_t uu, uint32_t vi, uint32_t lov, bool may_hook) {
         const uint32_t vv = tt + vi;
         bool uni = false, emit = false;
         uint32_t u = 0;
@@ -525,8 +532,14 @@ __global__ void __launch_bounds__(1024, 2)
             }
           } else if ((uint32_t)uu < vv && (!PART || (uint32_t)uu >= lov)) {
             u = (uint32_t)uu;  // each undirected edge once, from its larger end
-            if (u >= tt) uni = true;
-            else emit = true;
+            if (u < tt) {
+              emit = true;
+            } else if (may_hook && !hooked) {
+              hooked = true;
+              uni = ts_cas(const_cast<PT *>(s + vi), vi, u - tt) != vi;  // hooked, or queue
+            } else {
+              uni = true;
+            }
           }
         }
         const unsigned um = __ballot_sync(0xffffffffu, uni);
@@ -568,7 +581,7 @@ __global__ void __launch_bounds__(1024, 2)
         for (uint32_t j = 0; j < maxdeg; ++j) {
           const bool valid = j < deg;
           const uint64_t k = rb + (LINK ? link_pos(rl, j) : j);
-          edge(valid, valid ? (uint64_t)__ldg(col + k) : 0ull, i, lo);
+          edge(valid, valid ? (uint64_t)__ldg(col + k) : 0ull, i, lo, !LINK);
         }
       } else {
         // skewed degrees: the 32 rows' edges as one flattened stream, lane k
@@ -592,7 +605,8 @@ __global__ void __launch_bounds__(1024, 2)
           const uint64_t rbr = shfl64(rb, r);
           const uint32_t lor = PART ? __shfl_sync(0xffffffffu, lo, r) : 0u;
           const bool valid = f < total;
-          edge(valid, valid ? (uint64_t)__ldg(col + rbr + (f - ro)) : 0ull, g0 + (uint32_t)r, lor);
+          edge(valid, valid ? (uint64_t)__ldg(col + rbr + (f - ro)) : 0ull, g0 + (uint32_t)r, lor,
+               false);
         }
       }
     }
