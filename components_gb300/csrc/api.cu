@@ -456,6 +456,9 @@ int ctx_run(cc_ctx *C, const cc_csr *g, cc_algo algo, const cc_config *cfg_in, u
       lab_d.alloc(4 * (n ? n : 1), s, C->pool);
       lab = lab_d.as<uint32_t>();
     }
+    // streamed uint32 host labels leave chunk by chunk under the final pass
+    const bool labels_streamed = streamed && labels_where == CC_HOST && idb == 4 && n > 0;
+    if (labels_streamed) hsrc.labels_out = labels_out;
     Solver S{C, s, C->pool, c, cfg, seed, st};
     S.uf = C->uf;
     if (streamed) S.hs = &hsrc;
@@ -463,7 +466,9 @@ int ctx_run(cc_ctx *C, const cc_csr *g, cc_algo algo, const cc_config *cfg_in, u
     CCG_CUDA(cudaEventRecord(ev[2], s));
     DevBuf cnt(8, s, C->pool);
     if (C->prof) ccg::count_roots(lab, n, cnt.as<unsigned long long>(), s, c);
-    if (n) {
+    if (labels_streamed) {
+      st.d2h_bytes = 4 * n;  // copied by the final pass
+    } else if (n) {
       if (labels_where == CC_DEVICE) {
         if (lab != labels_out) ccg::widen_labels(lab, labels_out, idb, n, s, c);
       } else {

@@ -40,6 +40,8 @@ struct HostSource {
   const uint64_t *rp;
   const void *col;
   cudaStream_t copy;
+  void *labels_out = nullptr;  // host uint32 labels: each chunk is copied out on `copy`
+                               // as soon as the final compression has finished it
 };
 void uf_components(const Csr &g, uint32_t *parent, const PartMap *pm,
                    const UfTuning &tu, cudaStream_t s, cudaMemPool_t pool,

@@ -254,11 +254,9 @@ __global__ void k_emit(uint64_t n, const uint64_t *__restrict__ rp, const T *__r
       uint64_t key = 0;
       if (j < deg) {
         uint32_t u = load_id(col, eb + j);
-        if (edge_crosses(pm, part, (uint32_t)v, u)) {  // the rank test first: no gather for
-          const uint32_t cu = cl[u];                    // edges inside a rank
-          keep = cu != cv;
-          key = ((uint64_t)cv << b) | cu;
-        }
+        uint32_t cu = cl[u];
+        keep = cu != cv && edge_crosses(pm, part, (uint32_t)v, u);
+        key = ((uint64_t)cv << b) | cu;
       }
       unsigned m = __ballot_sync(0xffffffffu, keep);
       if (m) {
@@ -296,11 +294,9 @@ __global__ void k_emit_hubs(const uint64_t *__restrict__ rp, const T *__restrict
       uint64_t key = 0;
       if (e < ee) {
         uint32_t u = load_id(col, e);
-        if (edge_crosses(pm, part, v, u)) {
-          const uint32_t cu = cl[u];
-          keep = cu != cv;
-          key = ((uint64_t)cv << b) | cu;
-        }
+        uint32_t cu = cl[u];
+        keep = cu != cv && edge_crosses(pm, part, v, u);
+        key = ((uint64_t)cv << b) | cu;
       }
       unsigned m = __ballot_sync(0xffffffffu, keep);
       if (m) {

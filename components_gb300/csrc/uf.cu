@@ -152,8 +152,8 @@ __global__ void k_hook_hubs(uint64_t n, const uint64_t *__restrict__ rp,
 // v's own entry is written: a halving store into p[x] could land after x's own
 // thread wrote its root (and leave x at an inner node), and writing the root
 // along the whole path was measured slower (store traffic on shared paths).
-__global__ void k_compress(uint64_t n, uint32_t *p) {
-  for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < n;
+__global__ void k_compress(uint64_t n, uint32_t *p, uint64_t v_begin = 0) {
+  for (uint64_t v = v_begin + blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < n;
        v += (uint64_t)gridDim.x * blockDim.x) {
     const uint32_t r0 = p[v];
     if (r0 == (uint32_t)v) continue;
@@ -880,9 +880,41 @@ void run_uf_tiled(const Csr &g, uint32_t *parent, const PartMap &pm, const UfTun
   // every vertex points at a tile-local root or at a final root: full
   // compression, writing only the entries that change
   cudaEvent_t t3 = c.tic(s);
-  k_compress<<<grid_for(g.n, kBlock, kSMs * 32), kBlock, 0, s>>>(g.n, parent);
-  CCG_LAUNCH_CHECK();
-  c.toc(s, "uf_compress", t3, 3 * g.n * 4);
+  if (hs && hs->labels_out) {
+    // host labels: compress in chunks and copy each chunk out on the copy
+    // stream as soon as it is final (a chunk's entries are written only by its
+    // own launch), so the device-to-host copy overlaps the later chunks.  All
+    // launches are queued first: a copy into pageable memory blocks the host.
+    constexpr int kOutChunks = 8;
+    const uint64_t step = ((g.n + kOutChunks - 1) / kOutChunks + 1023) / 1024 * 1024;
+    cudaEvent_t done[kOutChunks];
+    int nch = 0;
+    for (uint64_t a = 0; a < g.n; a += step, ++nch) {
+      const uint64_t b = std::min<uint64_t>(g.n, a + step);
+      k_compress<<<grid_for(b - a, kBlock, kSMs * 32), kBlock, 0, s>>>(b, parent, a);
+      CCG_LAUNCH_CHECK();
+      CCG_CUDA(cudaEventCreateWithFlags(&done[nch], cudaEventDisableTiming));
+      CCG_CUDA(cudaEventRecord(done[nch], s));
+    }
+    c.toc(s, "uf_compress", t3, 3 * g.n * 4);
+    for (int k = 0; k < nch; ++k) {
+      const uint64_t a = (uint64_t)k * step, b = std::min<uint64_t>(g.n, a + step);
+      CCG_CUDA(cudaStreamWaitEvent(hs->copy, done[k], 0));
+      CCG_CUDA(cudaMemcpyAsync(static_cast<uint32_t *>(hs->labels_out) + a, parent + a,
+                               4 * (b - a), cudaMemcpyDeviceToHost, hs->copy));
+      cudaEventDestroy(done[k]);
+    }
+    cudaEvent_t copied;  // the caller's stream ends after the last copy
+    CCG_CUDA(cudaEventCreateWithFlags(&copied, cudaEventDisableTiming));
+    CCG_CUDA(cudaEventRecord(copied, hs->copy));
+    CCG_CUDA(cudaStreamWaitEvent(s, copied, 0));
+    cudaEventDestroy(copied);
+    c.add(nch - 1, 0);
+  } else {
+    k_compress<<<grid_for(g.n, kBlock, kSMs * 32), kBlock, 0, s>>>(g.n, parent);
+    CCG_LAUNCH_CHECK();
+    c.toc(s, "uf_compress", t3, 3 * g.n * 4);
+  }
   c.add(4, tile_bytes + 3 * g.n * 4);
 }
 
