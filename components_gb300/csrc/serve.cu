@@ -127,6 +127,8 @@ struct Req {
   cudaEvent_t copied = nullptr;
   std::atomic<int> state{kWaiting};
   uint32_t batch_id = 0, batch_size = 0;
+  bool failed = false;    // could not be launched (collect reports CC_ERR_CUDA)
+  bool enqueued = false;  // its completion callback is queued on a stream
   bool tiled = false;       // large graph: tiled hook pass (estimated on the host)
   bool link_tiles = false;  // large graph, sampled linking: tiled link rounds
 };
@@ -212,63 +214,103 @@ struct Server {
                                     UfTuning().tile_vertices);
   }
 
+  // A request that could not be launched: done, reported as failed by collect.
+  void fail(Req *r) {
+    {
+      std::lock_guard<std::mutex> lk(mu);
+      r->failed = true;
+      r->batch_id = 0;
+      r->t_done = now_s();
+      r->state = kDone;
+    }
+    cv_done.notify_all();
+  }
+
+  // Completion of `reqs` once stream s reaches this point (a host callback).
+  void enqueue_done(std::vector<Req *> reqs, int si, cudaStream_t s) {
+    Batch *b = new Batch{std::move(reqs), this, si};
+    busy[si]++;
+    inflight++;
+    for (Req *r : b->reqs) r->enqueued = true;
+    if (cudaLaunchHostFunc(s, on_batch_done, b) != cudaSuccess) {
+      busy[si]--;
+      inflight--;
+      for (Req *r : b->reqs) fail(r);
+      delete b;
+    }
+  }
+
+  // One launch sequence on compute stream si: the small graphs (one CTA each in
+  // shared memory) complete together as soon as their kernel ends; every large
+  // graph completes on its own after its hook pass, so small requests never
+  // wait behind a large one in the same launch.  Never throws: a request whose
+  // part cannot be launched is failed alone.
   void launch(std::vector<Req *> &batch, int si) {  // worker thread, no lock held
     cudaStream_t s = streams[si];
     std::stable_partition(batch.begin(), batch.end(),
                           [&](Req *r) { return r->g.n <= cfg.smem_max_n; });
+    {
+      std::lock_guard<std::mutex> lk(mu);
+      const uint32_t bid = (uint32_t)++batches;
+      for (Req *r : batch) {
+        r->batch_id = bid;
+        r->batch_size = (uint32_t)batch.size();
+        r->state = kLaunched;
+      }
+    }
     GraphDesc *hd = desc_host[si];
     uint32_t nsmall = 0;
-    for (size_t i = 0; i < batch.size(); ++i) {
-      Req *r = batch[i];
-      CCG_CUDA(cudaStreamWaitEvent(s, r->copied, 0));
-      hd[i] = GraphDesc{r->rp.as<uint64_t>(), r->col.p, r->lab.as<uint32_t>(), r->g.m_dir,
-                        (uint32_t)r->g.n, r->g.id_bytes};
+    for (Req *r : batch)
       if (r->g.n <= cfg.smem_max_n) ++nsmall;
-    }
     Counters c;
     if (nsmall) {
-      CCG_CUDA(cudaMemcpyAsync(desc_dev[si].p, hd, sizeof(GraphDesc) * nsmall,
-                               cudaMemcpyHostToDevice, s));
-      CCG_CUDA(cudaMemsetAsync(queue_dev[si].p, 0, 4, s));
-      const size_t smem = 4ull * cfg.smem_max_n;
-      if (smem > 48 * 1024)
-        CCG_CUDA(cudaFuncSetAttribute(k_serve_smem, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      (int)smem));
-      int per_sm = 1;
-      CCG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_serve_smem, 256, smem));
-      unsigned grid = (unsigned)std::min<uint64_t>((uint64_t)std::max(per_sm, 1) * kSMs, nsmall);
-      k_serve_smem<<<grid, 256, smem, s>>>(desc_dev[si].as<GraphDesc>(), nsmall,
-                                           queue_dev[si].as<unsigned int>());
-      CCG_LAUNCH_CHECK();
+      std::vector<Req *> small(batch.begin(), batch.begin() + nsmall);
+      try {
+        for (uint32_t i = 0; i < nsmall; ++i) {
+          Req *r = batch[i];
+          CCG_CUDA(cudaStreamWaitEvent(s, r->copied, 0));
+          hd[i] = GraphDesc{r->rp.as<uint64_t>(), r->col.p, r->lab.as<uint32_t>(), r->g.m_dir,
+                            (uint32_t)r->g.n, r->g.id_bytes};
+        }
+        CCG_CUDA(cudaMemcpyAsync(desc_dev[si].p, hd, sizeof(GraphDesc) * nsmall,
+                                 cudaMemcpyHostToDevice, s));
+        CCG_CUDA(cudaMemsetAsync(queue_dev[si].p, 0, 4, s));
+        const size_t smem = 4ull * cfg.smem_max_n;
+        if (smem > 48 * 1024)
+          CCG_CUDA(cudaFuncSetAttribute(k_serve_smem, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)smem));
+        int per_sm = 1;
+        CCG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_serve_smem, 256, smem));
+        unsigned grid = (unsigned)std::min<uint64_t>((uint64_t)std::max(per_sm, 1) * kSMs, nsmall);
+        k_serve_smem<<<grid, 256, smem, s>>>(desc_dev[si].as<GraphDesc>(), nsmall,
+                                             queue_dev[si].as<unsigned int>());
+        CCG_LAUNCH_CHECK();
+        enqueue_done(std::move(small), si, s);
+      } catch (...) {
+        for (Req *r : small) fail(r);
+      }
     }
     for (size_t i = nsmall; i < batch.size(); ++i) {
       Req *r = batch[i];
-      Csr G;
-      G.n = r->g.n;
-      G.m = r->g.m_dir;
-      G.rp = r->rp.as<uint64_t>();
-      G.col = r->col.p;
-      G.idb = (int)r->g.id_bytes;
-      G.err = reinterpret_cast<int *>(r->lab.as<uint32_t>() + r->g.n);
-      UfTuning tu;
-      tu.mode = r->tiled ? kUfTiled : kUfSampled;
-      tu.link_tiles = r->link_tiles ? 1 : 0;  // decided on the host: no device round trip
-      uf_components(G, r->lab.as<uint32_t>(), nullptr, tu, s, pool, c);
+      try {
+        CCG_CUDA(cudaStreamWaitEvent(s, r->copied, 0));
+        Csr G;
+        G.n = r->g.n;
+        G.m = r->g.m_dir;
+        G.rp = r->rp.as<uint64_t>();
+        G.col = r->col.p;
+        G.idb = (int)r->g.id_bytes;
+        G.err = reinterpret_cast<int *>(r->lab.as<uint32_t>() + r->g.n);
+        UfTuning tu;
+        tu.mode = r->tiled ? kUfTiled : kUfSampled;
+        tu.link_tiles = r->link_tiles ? 1 : 0;  // decided on the host: no device round trip
+        uf_components(G, r->lab.as<uint32_t>(), nullptr, tu, s, pool, c);
+      } catch (...) {
+        fail(r);
+        continue;
+      }
+      enqueue_done({r}, si, s);
     }
-    uint32_t bid;
-    {
-      std::lock_guard<std::mutex> lk(mu);
-      bid = (uint32_t)++batches;
-    }
-    for (Req *r : batch) {
-      r->batch_id = bid;
-      r->batch_size = (uint32_t)batch.size();
-      r->state = kLaunched;
-    }
-    Batch *b = new Batch{batch, this, si};
-    busy[si]++;
-    inflight++;
-    CCG_CUDA(cudaLaunchHostFunc(s, on_batch_done, b));
   }
 
   void loop() {
@@ -322,16 +364,10 @@ struct Server {
         try {
           launch(batch, (int)si);
         } catch (...) {
-          // leave the requests failed; their error word stays 0, so mark them
-          // done with a recorded error below
-          lk.lock();
-          for (Req *r : batch) {
-            r->t_done = now_s();
-            r->state = kDone;
-            r->batch_id = 0;
-          }
-          cv_done.notify_all();
-          continue;
+          // launch fails requests itself; this only catches a host allocation
+          // failure, after which no completion may be pending for the rest
+          for (Req *r : batch)
+            if (!r->enqueued && r->state.load() != kDone) fail(r);
         }
         lk.lock();
       }
@@ -489,7 +525,7 @@ static int collect(cc_server *h, uint64_t ticket, void *labels_out, int *done, d
   int rc = guard([&] {
     CCG_CUDA(cudaSetDevice(s.device));
     const uint64_t n = r->g.n;
-    if (!r->lab.p) throw Error(CC_ERR_CUDA, "request failed before launch");
+    if (!r->lab.p || r->failed) throw Error(CC_ERR_CUDA, "request failed before launch");
     std::vector<uint32_t> tmp;
     uint32_t *dst = static_cast<uint32_t *>(labels_out);
     if (r->g.id_bytes == 8) {
