@@ -522,23 +522,30 @@ __global__ void __launch_bounds__(1024, 2)
         bool uni = false, emit = false;
         uint32_t u = 0;
         if (valid) {
-          if (uu >= n) {
+          const uint32_t u32 = (uint32_t)uu;
+          // ids are checked in 32 bits when they are 32 bits wide (n < 2^32)
+          if (sizeof(T) == 8 ? uu >= n : u32 >= (uint32_t)n) {
             set_err(err, kErrBadId);
           } else if (LINK) {
-            if ((uint32_t)uu != vv && (!PART || same_part(pm, vv, (uint32_t)uu))) {
-              u = (uint32_t)uu;
-              if (u >= tt && u - tt < len) uni = true;
-              else emit = true;  // a cut edge in either direction
+            if (u32 != vv && (!PART || same_part(pm, vv, u32))) {
+              u = u32;
+              if (u - tt < len) uni = true;  // unsigned: also false for u < tt
+              else emit = true;              // a cut edge in either direction
             }
-          } else if ((uint32_t)uu < vv && (!PART || (uint32_t)uu >= lov)) {
-            u = (uint32_t)uu;  // each undirected edge once, from its larger end
-            if (u < tt) {
+          } else if (!PART || u32 >= lov) {
+            // each undirected edge once, from its larger end: u in [tt, vv)
+            // is u - tt < vi in unsigned arithmetic, u < tt is a cut edge
+            if (u32 - tt < vi) {
+              u = u32;
+              if (may_hook && !hooked) {
+                hooked = true;
+                uni = ts_cas(const_cast<PT *>(s + vi), vi, u - tt) != vi;  // hooked, or queue
+              } else {
+                uni = true;
+              }
+            } else if (u32 < tt) {
+              u = u32;
               emit = true;
-            } else if (may_hook && !hooked) {
-              hooked = true;
-              uni = ts_cas(const_cast<PT *>(s + vi), vi, u - tt) != vi;  // hooked, or queue
-            } else {
-              uni = true;
             }
           }
         }
