@@ -152,13 +152,17 @@ __global__ void k_hook_hubs(uint64_t n, const uint64_t *__restrict__ rp,
 // v's own entry is written: a halving store into p[x] could land after x's own
 // thread wrote its root (and leave x at an inner node), and writing the root
 // along the whole path was measured slower (store traffic on shared paths).
+// The walk reads through L1: roots do not change any more, and a stale inner
+// entry still names an ancestor, so a cached read is always a valid step; the
+// cache keeps a giant component's root entry from becoming one hot L2 line
+// that every vertex reads.
 __global__ void k_compress(uint64_t n, uint32_t *p, uint64_t v_begin = 0) {
   for (uint64_t v = v_begin + blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < n;
        v += (uint64_t)gridDim.x * blockDim.x) {
     const uint32_t r0 = p[v];
     if (r0 == (uint32_t)v) continue;
     uint32_t r = r0, nx;
-    while ((nx = ld_cg(p + r)) != r) r = nx;
+    while ((nx = p[r]) != r) r = nx;
     if (r != r0) p[v] = r;  // most vertices already point at their root
   }
 }
@@ -310,9 +314,11 @@ __global__ void k_aff_rest(uint64_t n, uint64_t m, const uint64_t *__restrict__ 
   uint32_t work = 0, rows = 0;  // neighbour ids and offset pairs this thread reads
   for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < n;
        v += (uint64_t)gridDim.x * blockDim.x) {
-    // the root first: rows inside the giant component never read their offsets
+    // the root first: rows inside the giant component never read their offsets.
+    // The parents were compressed before this pass, so p[v] == L settles most
+    // rows with one coalesced load (and no read of L's own, hot, entry).
     const uint32_t L = nparts > 1 ? Ls[pm.part((uint32_t)v)] : Ls[0];
-    if (uf_find(p, (uint32_t)v) == L) continue;
+    if (ld_cg(p + v) == L || uf_find(p, (uint32_t)v) == L) continue;
     ++rows;
     Row row;
     if (!load_row(rp, v, m, err, row) || row.e - row.b <= kAffRounds) continue;
@@ -522,30 +528,23 @@ __global__ void __launch_bounds__(1024, 2)
         bool uni = false, emit = false;
         uint32_t u = 0;
         if (valid) {
-          const uint32_t u32 = (uint32_t)uu;
-          // ids are checked in 32 bits when they are 32 bits wide (n < 2^32)
-          if (sizeof(T) == 8 ? uu >= n : u32 >= (uint32_t)n) {
+          if (uu >= n) {
             set_err(err, kErrBadId);
           } else if (LINK) {
-            if (u32 != vv && (!PART || same_part(pm, vv, u32))) {
-              u = u32;
-              if (u - tt < len) uni = true;  // unsigned: also false for u < tt
-              else emit = true;              // a cut edge in either direction
+            if ((uint32_t)uu != vv && (!PART || same_part(pm, vv, (uint32_t)uu))) {
+              u = (uint32_t)uu;
+              if (u >= tt && u - tt < len) uni = true;
+              else emit = true;  // a cut edge in either direction
             }
-          } else if (!PART || u32 >= lov) {
-            // each undirected edge once, from its larger end: u in [tt, vv)
-            // is u - tt < vi in unsigned arithmetic, u < tt is a cut edge
-            if (u32 - tt < vi) {
-              u = u32;
-              if (may_hook && !hooked) {
-                hooked = true;
-                uni = ts_cas(const_cast<PT *>(s + vi), vi, u - tt) != vi;  // hooked, or queue
-              } else {
-                uni = true;
-              }
-            } else if (u32 < tt) {
-              u = u32;
+          } else if ((uint32_t)uu < vv && (!PART || (uint32_t)uu >= lov)) {
+            u = (uint32_t)uu;  // each undirected edge once, from its larger end
+            if (u < tt) {
               emit = true;
+            } else if (may_hook && !hooked) {
+              hooked = true;
+              uni = ts_cas(const_cast<PT *>(s + vi), vi, u - tt) != vi;  // hooked, or queue
+            } else {
+              uni = true;
             }
           }
         }
