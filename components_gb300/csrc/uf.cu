@@ -39,6 +39,25 @@ __device__ __forceinline__ uint32_t uf_find(uint32_t *p, uint32_t v) {
   return cur;
 }
 
+// uf_find with the walk's loads through L1.  A cached entry may be stale, but
+// parents only ever move up the tree, so a stale entry still names an
+// ancestor: the walk ends at a node that was a root when cached.  Unions built
+// on it stay exact because the CAS that links checks the root on the L2 copy
+// and hands back the current parent when it fails.  Hot entries (the root of a
+// big component, a hub) are then served by L1 instead of one L2 line.
+__device__ __forceinline__ uint32_t uf_find_l1(uint32_t *p, uint32_t v) {
+  uint32_t cur = p[v];
+  if (cur == v) return v;
+  uint32_t prev = v;
+  uint32_t next;
+  while (cur > (next = p[cur])) {
+    st_cg(p + prev, next);
+    prev = cur;
+    cur = next;
+  }
+  return cur;
+}
+
 // Link the trees of a and b: the larger root is CAS'ed under the smaller one.
 __device__ __forceinline__ void uf_union(uint32_t *p, uint32_t a, uint32_t b) {
   uint32_t ra = uf_find(p, a), rb = uf_find(p, b);
@@ -650,7 +669,7 @@ __global__ void k_cut_union(const uint2 *__restrict__ cut, const unsigned long l
   for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < cnt;
        i += (uint64_t)gridDim.x * blockDim.x) {
     const uint2 e = cut[i];
-    uint32_t ra = uf_find(p, e.x), rb = uf_find(p, e.y);
+    uint32_t ra = uf_find_l1(p, e.x), rb = uf_find_l1(p, e.y);
     while (ra != rb) {
       if (ra < rb) {
         const uint32_t t = ra;
@@ -662,8 +681,8 @@ __global__ void k_cut_union(const uint2 *__restrict__ cut, const unsigned long l
         ra = rb;
         break;
       }
-      ra = uf_find(p, old);
-      rb = uf_find(p, rb);
+      ra = uf_find_l1(p, old);
+      rb = uf_find_l1(p, rb);
     }
     if (e.x != ra && ld_cg(p + e.x) != ra) st_cg(p + e.x, ra);
     if (e.y != ra && ld_cg(p + e.y) != ra) st_cg(p + e.y, ra);
