@@ -421,8 +421,8 @@ int ctx_run(cc_ctx *C, const cc_csr *g, cc_algo algo, const cc_config *cfg_in, u
         (algo == CC_ALLREDUCE || (algo == CC_EXP && g->num_parts == 1)) &&
         (C->uf.mode == ccg::kUfTiled ||
          (C->uf.mode == ccg::kUfAuto && n >= 4ull * C->uf.tile_vertices &&
-          ccg::host_tiles_suit(g->row_ptr, g->col, idb, n, m, C->uf.tile_vertices,
-                               C->uf.hub_degree))))
+          ccg::host_shares(g->row_ptr, g->col, idb, n, m, C->uf.tile_vertices,
+                           C->uf.hub_degree).tiles)))
       streamed = true;
     if (g->where == CC_HOST) {
       rp_d.alloc(8 * (n + 1), s, C->pool);

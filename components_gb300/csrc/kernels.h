@@ -27,7 +27,7 @@ struct Csr {
 // (exponential_contraction.h:391-411 FindLocalComponents).
 enum : int { kUfAuto = 0, kUfGlobal = 1, kUfTiled = 2, kUfSampled = 3 };
 struct UfTuning {
-  int mode = kUfAuto;  // auto: tiled when a row sample suits it (host_tiles_suit), else sampled
+  int mode = kUfAuto;  // auto: tiled, global (L2-resident, few hubs) or sampled from a row sample
   uint32_t hub_degree = 32;      // rows above: one warp per row
   uint32_t tile_vertices = 32768;  // vertices per CTA tile (2 bytes of shared memory each)
   uint32_t tile_threads = 1024;
@@ -46,15 +46,15 @@ struct HostSource {
 void uf_components(const Csr &g, uint32_t *parent, const PartMap *pm,
                    const UfTuning &tu, cudaStream_t s, cudaMemPool_t pool,
                    Counters &c, const HostSource *hs = nullptr);
-// Whether the tiled pass suits a host CSR: on a sample of 8192 rows, fewer than
-// half of the edges (u < v) leave their tile and fewer than a tenth lie in
-// rows above hub_degree.
-bool host_tiles_suit(const uint64_t *rp, const void *col, int idb, uint64_t n, uint64_t m,
-                     uint32_t tile, uint32_t hub_degree);
-// Whether the link rounds of sampled linking stay in their tile (at least three
-// quarters of the sampled rows' link-round entries), from a host CSR.
-bool host_link_tiles(const uint64_t *rp, const void *col, int idb, uint64_t n, uint64_t m,
-                     uint32_t tile);
+// The hook-schedule decisions on a stratified sample of 8192 rows of a host
+// CSR: the tiled pass suits it (< 50 % of the edges u < v leave their tile and
+// < 10 % lie in rows above hub_degree); the link rounds of sampled linking stay
+// in their tile (>= 75 % of the rows' link-round entries); few hub edges.
+struct HostShares {
+  bool tiles = false, link_tiles = false, few_hubs = true;
+};
+HostShares host_shares(const uint64_t *rp, const void *col, int idb, uint64_t n, uint64_t m,
+                       uint32_t tile, uint32_t hub_degree);
 
 // Write uint32 labels to an id_bytes-wide output array.
 void widen_labels(const uint32_t *in, void *out, int out_bytes, uint64_t n,

@@ -129,8 +129,7 @@ struct Req {
   uint32_t batch_id = 0, batch_size = 0;
   bool failed = false;    // could not be launched (collect reports CC_ERR_CUDA)
   bool enqueued = false;  // its completion callback is queued on a stream
-  bool tiled = false;       // large graph: tiled hook pass (estimated on the host)
-  bool link_tiles = false;  // large graph, sampled linking: tiled link rounds
+  UfTuning tu;  // large graph: hook schedule decided on the host
 };
 
 struct Batch {
@@ -188,12 +187,20 @@ struct Server {
   }
 
   // Hook schedule of a large graph, decided on the host CSR without a device
-  // round trip: the tiled pass when a row sample suits it, else sampled linking.
-  static bool prefers_tiles(const cc_csr &g) {
-    const UfTuning tu;
-    if (g.n < 4ull * tu.tile_vertices) return false;
-    return host_tiles_suit(g.row_ptr, g.col, (int)g.id_bytes, g.n, g.m_dir, tu.tile_vertices,
-                           tu.hub_degree);
+  // round trip, by the rule of the auto schedule: the tiled pass when a row
+  // sample suits it, the global hook when the graph is L2-resident with few
+  // hub rows, else sampled linking (with tiled link rounds when they stay in
+  // their tile).
+  static UfTuning schedule(const cc_csr &g) {
+    UfTuning tu;
+    const HostShares sh = host_shares(g.row_ptr, g.col, (int)g.id_bytes, g.n, g.m_dir,
+                                      tu.tile_vertices, tu.hub_degree);
+    const uint64_t ws = 8 * (g.n + 1) + g.m_dir * (uint64_t)g.id_bytes + 4 * g.n;
+    if (g.n >= 4ull * tu.tile_vertices && sh.tiles) tu.mode = kUfTiled;
+    else if (ws <= (96ull << 20) && sh.few_hubs) tu.mode = kUfGlobal;
+    else tu.mode = kUfSampled;
+    tu.link_tiles = g.n >= 4ull * tu.tile_vertices && sh.link_tiles ? 1 : 0;
+    return tu;
   }
 
   void stage(Req *r) {  // worker thread, no lock held
@@ -208,10 +215,7 @@ struct Server {
     CCG_CUDA(cudaMemsetAsync(r->lab.as<uint32_t>() + g.n, 0, 4, copy_stream));
     CCG_CUDA(cudaEventCreateWithFlags(&r->copied, cudaEventDisableTiming));
     CCG_CUDA(cudaEventRecord(r->copied, copy_stream));
-    r->tiled = g.n > cfg.smem_max_n && prefers_tiles(g);
-    r->link_tiles = g.n > cfg.smem_max_n && !r->tiled &&
-                    host_link_tiles(g.row_ptr, g.col, (int)g.id_bytes, g.n, g.m_dir,
-                                    UfTuning().tile_vertices);
+    if (g.n > cfg.smem_max_n) r->tu = schedule(g);
   }
 
   // A request that could not be launched: done, reported as failed by collect.
@@ -301,10 +305,8 @@ struct Server {
         G.col = r->col.p;
         G.idb = (int)r->g.id_bytes;
         G.err = reinterpret_cast<int *>(r->lab.as<uint32_t>() + r->g.n);
-        UfTuning tu;
-        tu.mode = r->tiled ? kUfTiled : kUfSampled;
-        tu.link_tiles = r->link_tiles ? 1 : 0;  // decided on the host: no device round trip
-        uf_components(G, r->lab.as<uint32_t>(), nullptr, tu, s, pool, c);
+        // schedule decided on the host: no device round trip in the loop
+        uf_components(G, r->lab.as<uint32_t>(), nullptr, r->tu, s, pool, c);
       } catch (...) {
         fail(r);
         continue;

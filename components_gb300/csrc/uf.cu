@@ -113,19 +113,29 @@ __global__ void k_init(uint64_t n, uint64_t m, const uint64_t *__restrict__ rp,
   }
 }
 
-template <class T, bool PART>
+// Where the hook kernel sends a row above hub_degree: a plain list of rows
+// (one warp per row later; the fixed-scratch solve) or warp-sized pieces.
+struct RowSink {
+  uint32_t *hubs;
+  uint64_t cap;
+  unsigned int *count;
+  __device__ __forceinline__ void put(uint32_t v, uint64_t, int *err) const {
+    const uint32_t slot = atomicAdd(count, 1u);
+    if (slot < cap) hubs[slot] = v;
+    else set_err(err, kErrOverflow);
+  }
+};
+
+template <class T, bool PART, class Sink>
 __global__ void k_hook(uint64_t n, uint64_t m, const uint64_t *__restrict__ rp,
                        const T *__restrict__ col, uint32_t *p, PartMap pm, uint32_t hub_degree,
-                       uint32_t *__restrict__ hubs, uint64_t hub_cap,
-                       unsigned int *__restrict__ nhubs, int *err) {
+                       Sink sink, int *err) {
   for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < n;
        v += (uint64_t)gridDim.x * blockDim.x) {
     Row r;
     if (!load_row(rp, v, m, err, r)) continue;
     if (r.e - r.b > hub_degree) {
-      uint32_t slot = atomicAdd(nhubs, 1u);
-      if (slot < hub_cap) hubs[slot] = (uint32_t)v;
-      else set_err(err, kErrOverflow);
+      sink.put((uint32_t)v, r.e - r.b, err);
       continue;
     }
     uint32_t lo = PART ? part_lo(pm, (uint32_t)v) : 0u;
@@ -208,6 +218,12 @@ __device__ __forceinline__ void queue_hub(const HubList &hl, uint32_t v, uint64_
   }
   for (uint32_t q = 0; q < np; ++q) hl.items[slot + q] = make_uint2(v, q);
 }
+struct PieceSink {
+  HubList hl;
+  __device__ __forceinline__ void put(uint32_t v, uint64_t len, int *err) const {
+    queue_hub(hl, v, len, err);
+  }
+};
 
 // ---- sampled linking (Afforest: Sutton, Ben-Nun, Barak, IPDPS 2018) ------------
 // Link every vertex to kAffRounds of its neighbours, compress, find
@@ -775,22 +791,21 @@ void run_uf(const Csr &g, uint32_t *parent, const PartMap &pm, uint32_t hub_degr
   k_init<T, PART><<<grid, kBlock, 0, s>>>(g.n, g.m, g.rp, col, parent, pm, g.err);
   CCG_LAUNCH_CHECK();
   c.toc(s, "uf_init", t0, 8 * (g.n + 1) + g.n * si + 4 * g.n);
-  const uint64_t hub_cap = g.m / (hub_degree + 1) + 1;
-  DevBuf hubs(sizeof(uint32_t) * hub_cap, s, pool);
-  DevBuf nh(sizeof(unsigned int), s, pool);
-  CCG_CUDA(cudaMemsetAsync(nh.p, 0, sizeof(unsigned int), s));
+  const uint64_t hub_cap = hub_list_cap(g.m, hub_degree);
+  DevBuf hubs(8 * hub_cap, s, pool), nh(4, s, pool);
+  CCG_CUDA(cudaMemsetAsync(nh.p, 0, 4, s));
+  const HubList hl{hubs.as<uint2>(), hub_cap, nh.as<unsigned int>()};
   // hook: offsets, every id once, one parent gather per edge, own parent r/w
   const uint64_t hook_bytes = 8 * (g.n + 1) + g.m * si + g.m * 4 + 2 * g.n * 4;
   cudaEvent_t t1 = c.tic(s);
-  k_hook<T, PART><<<grid, kBlock, 0, s>>>(g.n, g.m, g.rp, col, parent, pm, hub_degree,
-                                         hubs.as<uint32_t>(), hub_cap, nh.as<unsigned int>(),
-                                         g.err);
+  k_hook<T, PART, PieceSink><<<grid, kBlock, 0, s>>>(g.n, g.m, g.rp, col, parent, pm, hub_degree,
+                                                    PieceSink{hl}, g.err);
   CCG_LAUNCH_CHECK();
   c.toc(s, "uf_hook", t1, hook_bytes);
   cudaEvent_t t2 = c.tic(s);
-  k_hook_hubs<T, PART><<<kSMs * 8, kBlock, 0, s>>>(g.n, g.rp, col, parent, pm,
-                                                   hubs.as<uint32_t>(), hub_cap,
-                                                   nh.as<unsigned int>(), g.err);
+  // hub rows in pieces; every edge to a smaller id (the first one again too)
+  k_hub_pieces<T, PART, true><<<kSMs * 8, kBlock, 0, s>>>(g.n, g.m, g.rp, col, parent, pm, hl,
+                                                          g.err);
   CCG_LAUNCH_CHECK();
   c.toc(s, "uf_hook_hubs", t2, 0);
   cudaEvent_t t3 = c.tic(s);
@@ -954,7 +969,7 @@ inline bool tiles_fit(uint64_t tot, uint64_t cross, uint64_t hub) {
 // readback): the tiled pass, and whether the link rounds of sampled linking
 // run as a tiled pass (at least three quarters of their edges in the tile).
 struct Shares {
-  bool tiles = false, link_tiles = false;
+  bool tiles = false, link_tiles = false, few_hubs = true;
 };
 template <class T, bool PART>
 Shares sample_shares(const Csr &g, const PartMap &pm, uint32_t tile, uint32_t hub_degree,
@@ -973,6 +988,7 @@ Shares sample_shares(const Csr &g, const PartMap &pm, uint32_t tile, uint32_t hu
   Shares r;
   r.tiles = tiles_fit(h[0], h[1], h[2]);
   r.link_tiles = h[3] > 0 && 4 * h[4] < h[3];
+  r.few_hubs = 10 * h[2] < h[0] || h[0] == 0;
   return r;
 }
 
@@ -1073,6 +1089,10 @@ void run_uf_afforest(const Csr &g, uint32_t *parent, const PartMap &pm, const Uf
   c.add((link_tiles ? 2 : 1 + kAffRounds) + 6, link_bytes + rest_bytes + 6 * g.n * 4);
 }
 
+// Working set (offsets, ids, parents) that the 129 MB L2 keeps resident
+// during a hook pass, with room for the other streams' lines.
+constexpr uint64_t kL2Resident = 96ull << 20;
+
 template <class T, bool PART>
 void run_uf_mode(const Csr &g, uint32_t *parent, const PartMap &pm, const UfTuning &tu,
                  cudaStream_t s, cudaMemPool_t pool, Counters &c, const HostSource *hs) {
@@ -1087,8 +1107,15 @@ void run_uf_mode(const Csr &g, uint32_t *parent, const PartMap &pm, const UfTuni
     sh = sample_shares<T, PART>(g, pm, tu.tile_vertices, tu.hub_degree, s, pool, c);
   if (tu.link_tiles >= 0) sh.link_tiles = big && tu.link_tiles > 0;
   // the tiled pass wins when most edges stay inside their tile and few lie in
-  // hub rows (grids, geometric graphs); otherwise sampled linking
-  if (mode == kUfAuto) mode = (big && sh.tiles) ? kUfTiled : kUfSampled;
+  // hub rows (grids, geometric graphs); a graph that L2 holds and that has few
+  // hub rows is linked fastest by the plain global hook (every access an L2
+  // hit, no sampling rounds); otherwise sampled linking
+  if (mode == kUfAuto) {
+    const uint64_t ws = 8 * (g.n + 1) + g.m * (uint64_t)g.idb + 4 * g.n;
+    if (big && sh.tiles) mode = kUfTiled;
+    else if (ws <= kL2Resident && sh.few_hubs) mode = kUfGlobal;
+    else mode = kUfSampled;
+  }
   if (mode == kUfTiled) run_uf_tiled<T, PART>(g, parent, pm, tu, s, pool, c, nullptr);
   else if (mode == kUfSampled) run_uf_afforest<T, PART>(g, parent, pm, tu, sh.link_tiles, s, pool, c);
   else run_uf<T, PART>(g, parent, pm, tu.hub_degree, s, pool, c);
@@ -1114,48 +1141,40 @@ void uf_components(const Csr &g, uint32_t *parent, const PartMap *pm, const UfTu
   }
 }
 
-bool host_tiles_suit(const uint64_t *rp, const void *col, int idb, uint64_t n, uint64_t m,
-                     uint32_t tile, uint32_t hub_degree) {
+HostShares host_shares(const uint64_t *rp, const void *col, int idb, uint64_t n, uint64_t m,
+                       uint32_t tile, uint32_t hub_degree) {
   const uint64_t samples = std::min<uint64_t>(n, 8192);
-  uint64_t tot = 0, cross = 0, hub = 0;
+  uint64_t tot = 0, cross = 0, hub = 0, ltot = 0, lcross = 0;
+  auto id = [&](uint64_t k) -> uint64_t {
+    return idb == 8 ? static_cast<const uint64_t *>(col)[k] : static_cast<const uint32_t *>(col)[k];
+  };
   for (uint64_t i = 0; i < samples; ++i) {
     const uint64_t v = sample_row(i, samples, n), t0 = v / tile * tile;
     const uint64_t b = rp[v], e = rp[v + 1];
     if (e < b || e > m) continue;  // malformed rows are reported by the kernels
-    if (e - b > hub_degree) {
+    for (uint32_t r = 0; r < kAffRounds && r < e - b; ++r) {
+      const uint64_t u = id(b + link_pos(e - b, r));
+      if (u >= n || u == v) continue;
+      ++ltot;
+      lcross += u / tile != v / tile;
+    }
+    if (e - b > hub_degree) {  // hub rows are united globally
       tot += (e - b) / 2;
       hub += (e - b) / 2;
       continue;
     }
     for (uint64_t k = b; k < e; ++k) {
-      const uint64_t u = idb == 8 ? static_cast<const uint64_t *>(col)[k]
-                                  : static_cast<const uint32_t *>(col)[k];
+      const uint64_t u = id(k);
       if (u >= v) continue;
       ++tot;
       cross += u < t0;
     }
   }
-  return tiles_fit(tot, cross, hub);
-}
-
-bool host_link_tiles(const uint64_t *rp, const void *col, int idb, uint64_t n, uint64_t m,
-                     uint32_t tile) {
-  const uint64_t samples = std::min<uint64_t>(n, 8192);
-  uint64_t tot = 0, cross = 0;
-  for (uint64_t i = 0; i < samples; ++i) {
-    const uint64_t v = sample_row(i, samples, n);
-    const uint64_t b = rp[v], e = rp[v + 1];
-    if (e < b || e > m) continue;
-    for (uint32_t r = 0; r < kAffRounds && r < e - b; ++r) {
-      const uint64_t k = b + link_pos(e - b, r);
-      const uint64_t u = idb == 8 ? static_cast<const uint64_t *>(col)[k]
-                                  : static_cast<const uint32_t *>(col)[k];
-      if (u >= n || u == v) continue;
-      ++tot;
-      cross += u / tile != v / tile;
-    }
-  }
-  return tot > 0 && 4 * cross < tot;
+  HostShares r;
+  r.tiles = tiles_fit(tot, cross, hub);
+  r.link_tiles = ltot > 0 && 4 * lcross < ltot;
+  r.few_hubs = tot == 0 || 10 * hub < tot;
+  return r;
 }
 
 void widen_labels(const uint32_t *in, void *out, int out_bytes, uint64_t n, cudaStream_t s,
@@ -1267,9 +1286,9 @@ extern "C" int cc_gpu_run_noalloc(const uint64_t *row_ptr, const uint32_t *col, 
   const PartMap pm(n, 1);
   const unsigned grid = grid_for(n, kBlock, kSMs * 32);
   k_init<uint32_t, false><<<grid, kBlock, 0, s>>>(n, m_dir, row_ptr, col, labels_out, pm, err);
-  k_hook<uint32_t, false><<<grid, kBlock, 0, s>>>(n, m_dir, row_ptr, col, labels_out, pm,
-                                                  kNoAllocHubDegree, hubs, kNoAllocHubCap, nhubs,
-                                                  err);
+  k_hook<uint32_t, false, RowSink><<<grid, kBlock, 0, s>>>(
+      n, m_dir, row_ptr, col, labels_out, pm, kNoAllocHubDegree,
+      RowSink{hubs, kNoAllocHubCap, nhubs}, err);
   k_hook_hubs<uint32_t, false><<<kSMs * 8, kBlock, 0, s>>>(n, row_ptr, col, labels_out, pm, hubs,
                                                            kNoAllocHubCap, nhubs, err);
   k_compress<<<grid, kBlock, 0, s>>>(n, labels_out);

@@ -220,7 +220,9 @@ typedef struct cc_tuning {
                               vertex, then only rows outside the largest
                               component; AUTO picks TILED when a sample of rows
                               shows < 50 % tile-crossing edges and < 10 % of
-                              edges in hub rows, else SAMPLED */
+                              edges in hub rows, GLOBAL when the graph fits in
+                              96 MB (L2-resident) with < 10 % hub edges, else
+                              SAMPLED */
   uint32_t tile_vertices;  /* vertices per CTA tile, 2 bytes of shared memory
                               each (default 32768, 32 to 65536) */
   uint32_t tile_threads;   /* CTA size of the tiled pass (default 1024) */
