@@ -134,11 +134,14 @@ struct Chunk {
 };
 constexpr uint32_t kChunk = 1024;
 
+// Root of v with path halving; the loads go through L1 (a stale entry still
+// names an ancestor, and the CAS in g_union checks roots on the L2 copy), so a
+// large graph's hot root entry is not one L2 line that every thread reads.
 __device__ __forceinline__ uint32_t g_find(uint32_t *p, uint32_t v) {
-  uint32_t cur = ld_cg(p + v);
+  uint32_t cur = p[v];
   if (cur == v) return v;
   uint32_t prev = v, next;
-  while (cur > (next = ld_cg(p + cur))) {
+  while (cur > (next = p[cur])) {
     st_cg(p + prev, next);
     prev = cur;
     cur = next;
@@ -258,7 +261,7 @@ __global__ void k_large_finish(BatchArgs a, const Chunk *__restrict__ chunks, ui
     uint32_t v = c.first + (uint32_t)(t % kChunk);
     if (v >= n) continue;
     uint32_t r = (uint32_t)(v0 + v), nx;
-    while ((nx = ld_cg(par + r)) != r) r = nx;
+    while ((nx = par[r]) != r) r = nx;  // roots are final here: L1 reads are safe
     a.labels[v0 + v] = (uint32_t)(r - v0);
   }
 }

@@ -24,27 +24,13 @@
 namespace ccg {
 namespace {
 
-// Root of v with path halving.  parent[] only ever decreases along a path, so
-// a stale read still names an ancestor; writes only shorten paths.
-__device__ __forceinline__ uint32_t uf_find(uint32_t *p, uint32_t v) {
-  uint32_t cur = ld_cg(p + v);
-  if (cur == v) return v;
-  uint32_t prev = v;
-  uint32_t next;
-  while (cur > (next = ld_cg(p + cur))) {
-    st_cg(p + prev, next);
-    prev = cur;
-    cur = next;
-  }
-  return cur;
-}
-
-// uf_find with the walk's loads through L1.  A cached entry may be stale, but
-// parents only ever move up the tree, so a stale entry still names an
-// ancestor: the walk ends at a node that was a root when cached.  Unions built
-// on it stay exact because the CAS that links checks the root on the L2 copy
-// and hands back the current parent when it fails.  Hot entries (the root of a
-// big component, a hub) are then served by L1 instead of one L2 line.
+// Root of v with path halving.  parent[] only ever decreases along a path,
+// so a stale read still names an ancestor and writes only shorten paths.  The
+// walk's loads go through L1: a cached entry may be stale, but the walk then
+// ends at a node that was a root when cached; unions built on it stay exact
+// because the CAS that links checks the root on the L2 copy and hands back the
+// current parent when it fails.  Hot entries (the root of a big component, a
+// hub) are then served by L1 instead of all reading one L2 line.
 __device__ __forceinline__ uint32_t uf_find_l1(uint32_t *p, uint32_t v) {
   uint32_t cur = p[v];
   if (cur == v) return v;
@@ -59,8 +45,9 @@ __device__ __forceinline__ uint32_t uf_find_l1(uint32_t *p, uint32_t v) {
 }
 
 // Link the trees of a and b: the larger root is CAS'ed under the smaller one.
+// The finds read through L1 (uf_find_l1); the CAS decides.
 __device__ __forceinline__ void uf_union(uint32_t *p, uint32_t a, uint32_t b) {
-  uint32_t ra = uf_find(p, a), rb = uf_find(p, b);
+  uint32_t ra = uf_find_l1(p, a), rb = uf_find_l1(p, b);
   while (ra != rb) {
     if (ra < rb) {
       uint32_t t = ra;
@@ -69,8 +56,8 @@ __device__ __forceinline__ void uf_union(uint32_t *p, uint32_t a, uint32_t b) {
     }
     uint32_t old = atomicCAS(p + ra, ra, rb);
     if (old == ra) return;
-    ra = uf_find(p, old);
-    rb = uf_find(p, rb);
+    ra = uf_find_l1(p, old);
+    rb = uf_find_l1(p, rb);
   }
 }
 
@@ -353,7 +340,7 @@ __global__ void k_aff_rest(uint64_t n, uint64_t m, const uint64_t *__restrict__ 
     // The parents were compressed before this pass, so p[v] == L settles most
     // rows with one coalesced load (and no read of L's own, hot, entry).
     const uint32_t L = nparts > 1 ? Ls[pm.part((uint32_t)v)] : Ls[0];
-    if (ld_cg(p + v) == L || uf_find(p, (uint32_t)v) == L) continue;
+    if (ld_cg(p + v) == L || uf_find_l1(p, (uint32_t)v) == L) continue;
     ++rows;
     Row row;
     if (!load_row(rp, v, m, err, row) || row.e - row.b <= kAffRounds) continue;
