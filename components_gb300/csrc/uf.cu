@@ -555,8 +555,16 @@ __global__ void __launch_bounds__(1024, 2)
           } else if (LINK) {
             if ((uint32_t)uu != vv && (!PART || same_part(pm, vv, (uint32_t)uu))) {
               u = (uint32_t)uu;
-              if (u >= tt && u - tt < len) uni = true;
-              else emit = true;  // a cut edge in either direction
+              if (u >= tt && u - tt < len) {
+                if (may_hook && !hooked && u < vv) {  // the hook needs a smaller parent
+                  hooked = true;
+                  uni = ts_cas(const_cast<PT *>(s + vi), vi, u - tt) != vi;
+                } else {
+                  uni = true;
+                }
+              } else {
+                emit = true;  // a cut edge in either direction
+              }
             }
           } else if ((uint32_t)uu < vv && (!PART || (uint32_t)uu >= lov)) {
             u = (uint32_t)uu;  // each undirected edge once, from its larger end
@@ -609,7 +617,7 @@ __global__ void __launch_bounds__(1024, 2)
         for (uint32_t j = 0; j < maxdeg; ++j) {
           const bool valid = j < deg;
           const uint64_t k = rb + (LINK ? link_pos(rl, j) : j);
-          edge(valid, valid ? (uint64_t)__ldg(col + k) : 0ull, i, lo, !LINK);
+          edge(valid, valid ? (uint64_t)__ldg(col + k) : 0ull, i, lo, true);
         }
       } else {
         // skewed degrees: the 32 rows' edges as one flattened stream, lane k
