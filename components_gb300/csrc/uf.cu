@@ -655,13 +655,59 @@ __global__ void __launch_bounds__(1024, 2)
     // every vertex stores the global id of its tile-local root
     for (uint32_t i = threadIdx.x; i < len; i += blockDim.x) p[t0 + i] = tt + tw_find(s, i);
     const unsigned int nc = min(ccount, stage_cap);
-    if (threadIdx.x == 0) cbase = nc ? atomicAdd(ncut, (unsigned long long)nc) : 0ull;
-    __syncthreads();
-    for (uint32_t k = threadIdx.x; k < nc; k += blockDim.x) {
-      const uint2 c = cstage[k];
-      const unsigned long long g = cbase + k;
-      if (g < cut_cap) cut[g] = make_uint2(tt + tw_find(s, c.x), c.y);
-      else set_err(err, kErrOverflow);
+    if (LINK) {
+      // Link rounds: many rows of a tile link to the same far vertex (a hub),
+      // and after the near end becomes its tile-local root most staged edges
+      // repeat.  Duplicates are dropped through a hash set in the (now idle)
+      // union-queue memory; a key that finds no free slot in a few probes is
+      // kept, so the set only ever removes true repeats.
+      unsigned long long *set = reinterpret_cast<unsigned long long *>(queues);
+      const uint32_t slots = nw * kUnionQueue / 2;
+      for (uint32_t k = threadIdx.x; k < slots; k += blockDim.x) set[k] = ~0ull;
+      __syncthreads();  // every thread has read ccount into nc
+      if (threadIdx.x == 0) ccount = 0;  // reused: kept edges
+      __syncthreads();
+      for (uint32_t k = threadIdx.x; k < nc; k += blockDim.x) {
+        uint2 c = cstage[k];
+        c.x = tt + tw_find(s, c.x);
+        const unsigned long long key = ((unsigned long long)c.x << 32) | c.y;
+        uint32_t h = (uint32_t)(mix64(key) % slots);
+        bool keep = true;
+        for (int probe = 0; probe < 8; ++probe) {
+          const unsigned long long old = atomicCAS(set + h, ~0ull, key);
+          if (old == ~0ull) break;
+          if (old == key) {
+            keep = false;
+            break;
+          }
+          h = h + 1 == slots ? 0 : h + 1;
+        }
+        if (keep) atomicAdd(&ccount, 1u);
+        else c.y = kNone;  // ids are < n <= 2^32 - 2, so kNone marks a dropped edge
+        cstage[k] = c;
+      }
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        cbase = ccount ? atomicAdd(ncut, (unsigned long long)ccount) : 0ull;
+        ccount = 0;  // reused: fill position
+      }
+      __syncthreads();
+      for (uint32_t k = threadIdx.x; k < nc; k += blockDim.x) {
+        const uint2 c = cstage[k];
+        if (c.y == kNone) continue;
+        const unsigned long long g = cbase + atomicAdd(&ccount, 1u);
+        if (g < cut_cap) cut[g] = c;
+        else set_err(err, kErrOverflow);
+      }
+    } else {
+      if (threadIdx.x == 0) cbase = nc ? atomicAdd(ncut, (unsigned long long)nc) : 0ull;
+      __syncthreads();
+      for (uint32_t k = threadIdx.x; k < nc; k += blockDim.x) {
+        const uint2 c = cstage[k];
+        const unsigned long long g = cbase + k;
+        if (g < cut_cap) cut[g] = make_uint2(tt + tw_find(s, c.x), c.y);
+        else set_err(err, kErrOverflow);
+      }
     }
     __syncthreads();
   }
