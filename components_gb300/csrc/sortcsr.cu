@@ -221,50 +221,106 @@ __device__ __forceinline__ bool edge_crosses(const PartMap &pm, bool part, uint3
 // Emit key (cl[v] << b) | cl[w] for every kept edge; positions from one
 // warp-aggregated atomicAdd per warp step (the key order does not matter, the
 // sort follows).
+constexpr uint32_t kEmitStage = 4096;  // keys staged per CTA (32 KB) between flushes
+
+// Emit key (cl[v] << b) | cl[w] for every kept edge.  Each warp takes 32
+// consecutive rows and walks their edges as one flattened, coalesced stream
+// (lane k reads entry k of the rows' concatenated adjacency; its row is the
+// last lane whose degree prefix sum is <= k), so skewed degrees keep every
+// lane busy.  Kept keys are staged in shared memory and flushed with one
+// global atomic per flush, not one per warp step.  Rows longer than hub_limit
+// are left to k_emit_hubs.
 template <class T>
-__global__ void k_emit(uint64_t n, const uint64_t *__restrict__ rp, const T *__restrict__ col,
-                       const uint32_t *__restrict__ cl, PartMap pm, bool part, int b,
-                       uint64_t hub_limit, uint64_t *__restrict__ keys,
-                       unsigned long long *__restrict__ cnt) {
-  const unsigned lane = lane_id();
-  const uint64_t warp = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
-  const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
-  // one warp per 32 consecutive vertices; the warp walks their edges jointly.
-  // Rows longer than hub_limit are left to k_emit_hubs.
-  for (uint64_t v0 = warp * 32; v0 < n; v0 += nwarps * 32) {
-    uint64_t v = v0 + lane;
-    uint64_t eb = 0, ee = 0;
-    uint32_t cv = 0;
+__global__ void __launch_bounds__(kBlock) k_emit(uint64_t n, const uint64_t *__restrict__ rp,
+                                                 const T *__restrict__ col,
+                                                 const uint32_t *__restrict__ cl, PartMap pm,
+                                                 bool part, int b, uint64_t hub_limit,
+                                                 uint64_t *__restrict__ keys,
+                                                 unsigned long long *__restrict__ cnt) {
+  __shared__ uint64_t kst[kEmitStage];
+  __shared__ unsigned int sc;
+  __shared__ unsigned long long gbase;
+  const unsigned lane = lane_id(), wid = threadIdx.x >> 5;
+  const unsigned lt = (1u << lane) - 1u;
+  if (threadIdx.x == 0) sc = 0;
+  __syncthreads();
+  const uint64_t rows = blockDim.x;  // 32 rows per warp per step, the same steps for the whole CTA
+  for (uint64_t base = blockIdx.x * rows; base < n; base += (uint64_t)gridDim.x * rows) {
+    const uint64_t v0 = base + (uint64_t)wid * 32, v = v0 + lane;
+    uint64_t eb = 0;
+    uint32_t deg = 0, cv = 0;
     if (v < n) {
       eb = __ldg(rp + v);
-      ee = __ldg(rp + v + 1);
+      const uint64_t ee = __ldg(rp + v + 1);
+      if (ee - eb <= hub_limit) deg = (uint32_t)(ee - eb);
       cv = cl[v];
     }
-    uint64_t deg = ee - eb;
-    if (deg > hub_limit) deg = 0;
-    // maximum degree in this warp bounds the steps
-    uint64_t maxdeg = deg;
+    uint32_t inc = deg;
 #pragma unroll
-    for (int o = 16; o; o >>= 1) {
-      uint64_t y = __shfl_xor_sync(0xffffffffu, maxdeg, o);
-      maxdeg = y > maxdeg ? y : maxdeg;
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t t = __shfl_up_sync(0xffffffffu, inc, o);
+      if ((int)lane >= o) inc += t;
     }
-    for (uint64_t j = 0; j < maxdeg; ++j) {
+    const uint32_t total = __shfl_sync(0xffffffffu, inc, 31);
+    const uint32_t off = inc - deg;
+    for (uint32_t f0 = 0; f0 < total; f0 += 32) {
+      const uint32_t f = f0 + lane;
+      int r = 0;
+#pragma unroll
+      for (int step = 16; step; step >>= 1) {
+        const uint32_t o = __shfl_sync(0xffffffffu, off, r + step);
+        if (o <= f) r += step;
+      }
+      const uint32_t ro = __shfl_sync(0xffffffffu, off, r);
+      const uint32_t cvr = __shfl_sync(0xffffffffu, cv, r);
+      const uint64_t ebr = ((uint64_t)__shfl_sync(0xffffffffu, (uint32_t)(eb >> 32), r) << 32) |
+                           __shfl_sync(0xffffffffu, (uint32_t)eb, r);
       bool keep = false;
       uint64_t key = 0;
-      if (j < deg) {
-        uint32_t u = load_id(col, eb + j);
-        uint32_t cu = cl[u];
-        keep = cu != cv && edge_crosses(pm, part, (uint32_t)v, u);
-        key = ((uint64_t)cv << b) | cu;
+      if (f < total) {
+        const uint32_t u = load_id(col, ebr + (f - ro));
+        const uint32_t cu = cl[u];
+        keep = cu != cvr && edge_crosses(pm, part, (uint32_t)(v0 + r), u);
+        key = ((uint64_t)cvr << b) | cu;
       }
-      unsigned m = __ballot_sync(0xffffffffu, keep);
+      const unsigned m = __ballot_sync(0xffffffffu, keep);
       if (m) {
-        unsigned long long pos0 = 0;
-        if (lane == 0) pos0 = atomicAdd(cnt, (unsigned long long)__popc(m));
-        pos0 = __shfl_sync(0xffffffffu, pos0, 0);
-        if (keep) keys[pos0 + __popc(m & ((1u << lane) - 1u))] = key;
+        // reserve stage slots only while they fit, so sc always counts
+        // written keys; a step that does not fit goes straight out
+        unsigned int slot = kEmitStage;
+        if (lane == 0) {
+          unsigned int old = *static_cast<volatile unsigned int *>(&sc);
+          while (old + __popc(m) <= kEmitStage) {
+            const unsigned int prev = atomicCAS(&sc, old, old + __popc(m));
+            if (prev == old) {
+              slot = old;
+              break;
+            }
+            old = prev;
+          }
+        }
+        slot = __shfl_sync(0xffffffffu, slot, 0);
+        if (slot < kEmitStage) {
+          if (keep) kst[slot + __popc(m & lt)] = key;
+        } else {
+          unsigned long long pos0 = 0;
+          if (lane == 0) pos0 = atomicAdd(cnt, (unsigned long long)__popc(m));
+          pos0 = __shfl_sync(0xffffffffu, pos0, 0);
+          if (keep) keys[pos0 + __popc(m & lt)] = key;
+        }
       }
+    }
+    __syncthreads();
+    const unsigned int staged = sc;
+    __syncthreads();  // every thread has read sc before the next step changes it
+    const bool last = base + (uint64_t)gridDim.x * rows >= n;
+    if (staged > kEmitStage / 2 || (last && staged)) {
+      if (threadIdx.x == 0) gbase = atomicAdd(cnt, (unsigned long long)staged);
+      __syncthreads();
+      for (uint32_t k = threadIdx.x; k < staged; k += blockDim.x) keys[gbase + k] = kst[k];
+      __syncthreads();
+      if (threadIdx.x == 0) sc = 0;
+      __syncthreads();
     }
   }
 }
@@ -389,9 +445,9 @@ void emit_keys(const Csr &g, const uint32_t *cl, const PartMap &pm, bool part, i
                uint64_t *keys, unsigned long long *cnt, cudaStream_t s, cudaMemPool_t pool,
                Counters &c) {
   const T *col = static_cast<const T *>(g.col);
-  // k_emit walks up to max-degree steps per warp; rows above hub_limit go to
-  // the warp-per-row kernel so that one hub does not serialise 31 lanes.
-  const uint64_t hub_limit = 128;
+  // k_emit streams rows up to hub_limit entries; longer rows go to the
+  // piece-per-warp kernel so that one hub does not hold one warp for long.
+  const uint64_t hub_limit = 1024;
   const uint64_t cap = g.m / (hub_limit + 1) + g.m / kEmitPiece + 2;
   DevBuf hubs(8 * cap, s, pool), nh(4, s, pool);
   CCG_CUDA(cudaMemsetAsync(nh.p, 0, 4, s));
