@@ -279,9 +279,11 @@ __global__ void __launch_bounds__(kBlock) k_emit(uint64_t n, const uint64_t *__r
       uint64_t key = 0;
       if (f < total) {
         const uint32_t u = load_id(col, ebr + (f - ro));
-        const uint32_t cu = cl[u];
-        keep = cu != cvr && edge_crosses(pm, part, (uint32_t)(v0 + r), u);
-        key = ((uint64_t)cvr << b) | cu;
+        if (edge_crosses(pm, part, (uint32_t)(v0 + r), u)) {  // no gather for edges
+          const uint32_t cu = cl[u];                           // inside a rank
+          keep = cu != cvr;
+          key = ((uint64_t)cvr << b) | cu;
+        }
       }
       const unsigned m = __ballot_sync(0xffffffffu, keep);
       if (m) {
