@@ -113,6 +113,7 @@ GPU_SYMBOLS = {
     "cc_ctx_stats": (C.c_int, [_P, C.POINTER(cc_stats)]),
     "cc_ctx_arena_bytes": (_U64, [_P]),
     "cc_ctx_set_profiling": (C.c_int, [_P, C.c_int]),
+    "cc_ctx_profile_totals": (C.c_int, [_P, C.POINTER(cc_stats), C.POINTER(C.c_uint64)]),
     "cc_ctx_stream": (_P, [_P]),
     "cc_ctx_set_tuning": (C.c_int, [_P, C.POINTER(cc_tuning)]),
     "cc_ctx_get_tuning": (C.c_int, [_P, C.POINTER(cc_tuning)]),

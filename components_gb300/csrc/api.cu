@@ -376,6 +376,32 @@ void collect_kernel_stats(Counters &c, cc_stats &st) {
   c.clear_recs();
 }
 
+// Adds one profiled solve to the context's running totals.
+void accumulate_profile(cc_ctx *C, const cc_stats &st) {
+  cc_stats &t = C->prof_total;
+  for (uint32_t i = 0; i < st.nkernels; ++i) {
+    uint32_t k = 0;
+    for (; k < t.nkernels; ++k)
+      if (std::strncmp(t.kernels[k].name, st.kernels[i].name, sizeof(t.kernels[k].name)) == 0) break;
+    if (k == t.nkernels) {
+      if (t.nkernels >= CC_MAX_KSTATS) continue;
+      t.kernels[k] = st.kernels[i];
+      t.nkernels++;
+      continue;
+    }
+    t.kernels[k].launches += st.kernels[i].launches;
+    t.kernels[k].ms += st.kernels[i].ms;
+    t.kernels[k].bytes += st.kernels[i].bytes;
+  }
+  t.solve_ms += st.solve_ms;
+  t.total_ms += st.total_ms;
+  t.kernel_launches += st.kernel_launches;
+  t.bytes_algorithmic += st.bytes_algorithmic;
+  t.h2d_bytes += st.h2d_bytes;
+  t.d2h_bytes += st.d2h_bytes;
+  C->prof_solves++;
+}
+
 int ctx_run(cc_ctx *C, const cc_csr *g, cc_algo algo, const cc_config *cfg_in, uint64_t seed,
             void *labels_out, uint32_t labels_where) {
   return guard([&] {
@@ -418,12 +444,31 @@ int ctx_run(cc_ctx *C, const cc_csr *g, cc_algo algo, const cc_config *cfg_in, u
     ccg::HostSource hsrc{g->row_ptr, g->col, C->copy_stream};
     bool streamed = false;
     if (g->where == CC_HOST && n > 0 && m > 0 &&
-        (algo == CC_ALLREDUCE || (algo == CC_EXP && g->num_parts == 1)) &&
-        (C->uf.mode == ccg::kUfTiled ||
-         (C->uf.mode == ccg::kUfAuto && n >= 4ull * C->uf.tile_vertices &&
-          ccg::host_shares(g->row_ptr, g->col, idb, n, m, C->uf.tile_vertices,
-                           C->uf.hub_degree).tiles)))
-      streamed = true;
+        (algo == CC_ALLREDUCE || (algo == CC_EXP && g->num_parts == 1))) {
+      if (C->uf.mode == ccg::kUfTiled) {
+        streamed = true;
+      } else if (C->uf.mode == ccg::kUfAuto && n >= 4ull * C->uf.tile_vertices) {
+        // the host sample (8192 scattered rows) is remembered like the
+        // device one: a graph solved again from the same buffers skips it
+        ccg::UfDecisionCache &dc = C->host_cache;
+        if (!(dc.valid && dc.rp == g->row_ptr && dc.col == g->col && dc.n == n && dc.m == m &&
+              dc.tile == C->uf.tile_vertices && dc.hub == C->uf.hub_degree)) {
+          const ccg::HostShares hs = ccg::host_shares(g->row_ptr, g->col, idb, n, m,
+                                                      C->uf.tile_vertices, C->uf.hub_degree);
+          dc.rp = g->row_ptr;
+          dc.col = g->col;
+          dc.n = n;
+          dc.m = m;
+          dc.tile = C->uf.tile_vertices;
+          dc.hub = C->uf.hub_degree;
+          dc.tiles = hs.tiles;
+          dc.link_tiles = hs.link_tiles;
+          dc.few_hubs = hs.few_hubs;
+          dc.valid = true;
+        }
+        streamed = dc.tiles;
+      }
+    }
     if (g->where == CC_HOST) {
       rp_d.alloc(8 * (n + 1), s, C->pool);
       col_d.alloc((size_t)idb * (m ? m : 1), s, C->pool);
@@ -461,6 +506,7 @@ int ctx_run(cc_ctx *C, const cc_csr *g, cc_algo algo, const cc_config *cfg_in, u
     if (labels_streamed) hsrc.labels_out = labels_out;
     Solver S{C, s, C->pool, c, cfg, seed, st};
     S.uf = C->uf;
+    S.uf.cache = &C->uf_cache;
     if (streamed) S.hs = &hsrc;
     S.run(algo, G, g->num_parts, lab);
     CCG_CUDA(cudaEventRecord(ev[2], s));
@@ -498,6 +544,7 @@ int ctx_run(cc_ctx *C, const cc_csr *g, cc_algo algo, const cc_config *cfg_in, u
     st.num_components = ncomp;
     collect_kernel_stats(c, st);
     C->stats = st;
+    if (C->prof) accumulate_profile(C, st);
   });
 }
 
@@ -618,7 +665,18 @@ uint64_t cc_ctx_arena_bytes(cc_ctx *ctx) {
 
 int cc_ctx_set_profiling(cc_ctx *ctx, int on) {
   if (!ctx) return CC_ERR_INVALID;
+  if (on && !ctx->prof) {  // a new profiling window: the totals start from zero
+    ctx->prof_total = cc_stats{};
+    ctx->prof_solves = 0;
+  }
   ctx->prof = on != 0;
+  return CC_OK;
+}
+
+int cc_ctx_profile_totals(cc_ctx *ctx, cc_stats *out, uint64_t *solves) {
+  if (!ctx || !out) return CC_ERR_INVALID;
+  *out = ctx->prof_total;
+  if (solves) *solves = ctx->prof_solves;
   return CC_OK;
 }
 

@@ -26,7 +26,11 @@ struct cc_ctx {
   double geo_beta = -1.0;
   bool prof = false;
   ccg::UfTuning uf;  // hook-and-compress schedule (cc_ctx_set_tuning)
+  ccg::UfDecisionCache uf_cache;    // the last device graph's row-sample decisions
+  ccg::UfDecisionCache host_cache;  // the last host graph's (streamed input)
   cc_stats stats{};
+  cc_stats prof_total{};      // per-kernel sums over the solves since profiling was switched on
+  uint64_t prof_solves = 0;
   ccg::BatchCache *batch = nullptr;  // last recorded batch solve (CUDA graph)
 };
 

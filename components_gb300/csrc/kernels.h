@@ -26,12 +26,25 @@ struct Csr {
 // the minimum id of v's partition-local component
 // (exponential_contraction.h:391-411 FindLocalComponents).
 enum : int { kUfAuto = 0, kUfGlobal = 1, kUfTiled = 2, kUfSampled = 3 };
+// The row-sample decisions of one graph, remembered by a context so that a
+// graph solved again (same buffers, sizes and tuning) skips the sample and
+// its host round trip.  The decisions only pick a schedule: every schedule
+// gives the same labels, so a caller that rewrites a graph in place between
+// solves gets correct labels either way.
+struct UfDecisionCache {
+  const void *rp = nullptr, *col = nullptr;
+  uint64_t n = 0, m = 0, parts_key = 0;
+  uint32_t tile = 0, hub = 0;
+  bool valid = false;
+  bool tiles = false, link_tiles = false, few_hubs = true;
+};
 struct UfTuning {
   int mode = kUfAuto;  // auto: tiled, global (L2-resident, few hubs) or sampled from a row sample
-  uint32_t hub_degree = 32;      // rows above: one warp per row
+  uint32_t hub_degree = 32;      // rows above: split into pieces of 2048 edges
   uint32_t tile_vertices = 32768;  // vertices per CTA tile (2 bytes of shared memory each)
   uint32_t tile_threads = 1024;
   int link_tiles = -1;  // sampled linking: link rounds tiled (1) or global (0); -1 decide from a row sample
+  UfDecisionCache *cache = nullptr;  // the context's; nullptr: sample every time
 };
 // Host source of a caller graph whose device buffers are still empty: the
 // tiled pass copies tile-aligned chunks on `copy` and overlaps them with the

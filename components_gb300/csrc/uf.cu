@@ -1144,8 +1144,31 @@ void run_uf_mode(const Csr &g, uint32_t *parent, const PartMap &pm, const UfTuni
   int mode = tu.mode;
   const bool big = g.n >= 4ull * tu.tile_vertices;
   Shares sh;
-  if (big && (mode == kUfAuto || (mode == kUfSampled && tu.link_tiles < 0)))
-    sh = sample_shares<T, PART>(g, pm, tu.tile_vertices, tu.hub_degree, s, pool, c);
+  if (big && (mode == kUfAuto || (mode == kUfSampled && tu.link_tiles < 0))) {
+    UfDecisionCache *dc = tu.cache;
+    const uint64_t parts_key = ((uint64_t)pm.q << 32) ^ pm.rm ^ ((uint64_t)PART << 63);
+    if (dc && dc->valid && dc->rp == g.rp && dc->col == g.col && dc->n == g.n && dc->m == g.m &&
+        dc->parts_key == parts_key && dc->tile == tu.tile_vertices && dc->hub == tu.hub_degree) {
+      sh.tiles = dc->tiles;
+      sh.link_tiles = dc->link_tiles;
+      sh.few_hubs = dc->few_hubs;
+    } else {
+      sh = sample_shares<T, PART>(g, pm, tu.tile_vertices, tu.hub_degree, s, pool, c);
+      if (dc) {
+        dc->rp = g.rp;
+        dc->col = g.col;
+        dc->n = g.n;
+        dc->m = g.m;
+        dc->parts_key = parts_key;
+        dc->tile = tu.tile_vertices;
+        dc->hub = tu.hub_degree;
+        dc->tiles = sh.tiles;
+        dc->link_tiles = sh.link_tiles;
+        dc->few_hubs = sh.few_hubs;
+        dc->valid = true;
+      }
+    }
+  }
   if (tu.link_tiles >= 0) sh.link_tiles = big && tu.link_tiles > 0;
   // the tiled pass wins when most edges stay inside their tile and few lie in
   // hub rows (grids, geometric graphs); a graph that L2 holds and that has few

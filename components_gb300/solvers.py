@@ -70,6 +70,15 @@ class Context:
         _lib.check(_lib.gpu().cc_ctx_stats(self._h, C.byref(st)))
         return st.as_dict()
 
+    def profile_totals(self) -> dict:
+        """Sums over the solves since profiling was switched on, plus `solves`."""
+        st = _lib.cc_stats()
+        n = C.c_uint64()
+        _lib.check(_lib.gpu().cc_ctx_profile_totals(self._h, C.byref(st), C.byref(n)))
+        d = st.as_dict()
+        d["solves"] = int(n.value)
+        return d
+
     def arena_bytes(self) -> int:
         return int(_lib.gpu().cc_ctx_arena_bytes(self._h))
 

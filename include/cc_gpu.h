@@ -207,6 +207,11 @@ uint64_t cc_ctx_arena_bytes(cc_ctx *ctx);
 /* Per-kernel CUDA-event timing and a component count in cc_stats (off by
    default; it adds event records and one counting pass per solve). */
 int cc_ctx_set_profiling(cc_ctx *ctx, int on);
+/* Per-kernel sums (launches, ms, bytes), solve_ms, total_ms, launch and byte
+   counts over every solve since profiling was last switched on; *solves gets
+   their number.  (new, no counterpart in the reference: lets a caller time
+   many solves without reading statistics between them) */
+int cc_ctx_profile_totals(cc_ctx *ctx, cc_stats *out, uint64_t *solves);
 /* The cudaStream_t the context launches on. */
 void *cc_ctx_stream(cc_ctx *ctx);
 

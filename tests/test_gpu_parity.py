@@ -148,6 +148,10 @@ def test_context_reuse_and_stats(cuda):
     assert st["num_components"] == len(np.unique(want))
     assert st["kernel_launches"] > 0 and st["bytes_algorithmic"] > 0
     assert any(k.startswith("uf_") for k in st["kernels"])  # hook pass timed
+    tot = ctx.profile_totals()  # the three solves above, summed
+    assert tot["solves"] == 3 and tot["kernel_launches"] >= 3 * 2
+    for k, v in st["kernels"].items():
+        assert tot["kernels"][k]["launches"] >= v["launches"]
     arena = ctx.arena_bytes()
     gpu_labels(G, "exp", 1, "device", ctx=ctx)
     assert ctx.arena_bytes() == arena  # steady state: the pool is reused
