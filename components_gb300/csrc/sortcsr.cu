@@ -328,14 +328,31 @@ __global__ void __launch_bounds__(kBlock) k_emit(uint64_t n, const uint64_t *__r
 }
 
 // One warp per piece of a hub row (rows longer than the k_emit limit):
-// kEmitPiece edges each, so the longest row is spread over many warps.
+// kEmitPiece edges each, so the longest row is spread over many warps.  Each
+// warp collects its kept keys in its own shared-memory buffer and reserves
+// global room once per full buffer (a hub's edges mostly cross ranks, and one
+// global atomic per warp step on a single counter serialises).
+constexpr uint32_t kWarpKeys = 256;
 template <class T>
-__global__ void k_emit_hubs(const uint64_t *__restrict__ rp, const T *__restrict__ col,
-                            const uint32_t *__restrict__ cl, PartMap pm, bool part, int b,
-                            const uint2 *__restrict__ items, uint64_t cap,
-                            const unsigned int *__restrict__ d_nitems,
-                            uint64_t *__restrict__ keys, unsigned long long *__restrict__ cnt) {
-  const unsigned lane = lane_id();
+__global__ void __launch_bounds__(kBlock) k_emit_hubs(
+    const uint64_t *__restrict__ rp, const T *__restrict__ col, const uint32_t *__restrict__ cl,
+    PartMap pm, bool part, int b, const uint2 *__restrict__ items, uint64_t cap,
+    const unsigned int *__restrict__ d_nitems, uint64_t *__restrict__ keys,
+    unsigned long long *__restrict__ cnt) {
+  __shared__ uint64_t wbuf[kBlock / 32][kWarpKeys];
+  const unsigned lane = lane_id(), wid = threadIdx.x >> 5;
+  const unsigned lt = (1u << lane) - 1u;
+  uint64_t *buf = wbuf[wid];
+  uint32_t wn = 0;  // warp-uniform fill of buf
+  auto flush = [&]() {
+    __syncwarp();
+    unsigned long long pos0 = 0;
+    if (lane == 0) pos0 = atomicAdd(cnt, (unsigned long long)wn);
+    pos0 = __shfl_sync(0xffffffffu, pos0, 0);
+    for (uint32_t k = lane; k < wn; k += 32) keys[pos0 + k] = buf[k];
+    __syncwarp();
+    wn = 0;
+  };
   const uint64_t warp = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
   const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
   const uint64_t nitems = min((uint64_t)*d_nitems, cap);
@@ -356,15 +373,14 @@ __global__ void k_emit_hubs(const uint64_t *__restrict__ rp, const T *__restrict
         keep = cu != cv && edge_crosses(pm, part, v, u);
         key = ((uint64_t)cv << b) | cu;
       }
-      unsigned m = __ballot_sync(0xffffffffu, keep);
-      if (m) {
-        unsigned long long pos0 = 0;
-        if (lane == 0) pos0 = atomicAdd(cnt, (unsigned long long)__popc(m));
-        pos0 = __shfl_sync(0xffffffffu, pos0, 0);
-        if (keep) keys[pos0 + __popc(m & ((1u << lane) - 1u))] = key;
-      }
+      const unsigned m = __ballot_sync(0xffffffffu, keep);
+      if (!m) continue;
+      if (wn + __popc(m) > kWarpKeys) flush();
+      if (keep) buf[wn + __popc(m & lt)] = key;
+      wn += __popc(m);
     }
   }
+  if (wn) flush();
 }
 
 // Rows longer than `limit` (hubs) are listed for the warp-per-row kernel.
