@@ -161,11 +161,20 @@ __global__ void k_compose(uint64_t n, const uint32_t *__restrict__ cl,
   }
 }
 
-__global__ void k_canon_min(uint64_t n, const uint32_t *__restrict__ lab, uint32_t *__restrict__ mn) {
-  for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < n;
-       v += (uint64_t)gridDim.x * blockDim.x) {
-    uint32_t l = lab[v];
-    if ((uint32_t)v < ld_cg(mn + l)) atomicMin(mn + l, (uint32_t)v);
+// mn[l] <- minimum v with lab[v] == l.  The test before the atomic reads
+// through L1: mn only decreases, so a stale entry is never below the true one
+// and a skip it allows is right; it keeps a giant component's entry from being
+// one L2 line that every vertex reads.  Only a warp's smallest vertex of each
+// label tests at all.
+__global__ void k_canon_min(uint64_t n, uint32_t *mn, const uint32_t *__restrict__ lab) {
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  const uint64_t span = (n + 31) / 32 * 32;  // warp-uniform trip count
+  for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < span; v += stride) {
+    const bool in = v < n;
+    const uint32_t l = in ? lab[v] : 0xffffffffu;
+    const unsigned peers = __match_any_sync(0xffffffffu, l);
+    const bool first = (threadIdx.x & 31) == (unsigned)(__ffs(peers) - 1);
+    if (in && first && (uint32_t)v < mn[l]) atomicMin(mn + l, (uint32_t)v);
   }
 }
 __global__ void k_canon_apply(uint64_t n, uint32_t *__restrict__ lab, const uint32_t *__restrict__ mn) {
@@ -297,7 +306,7 @@ void canonicalize(uint32_t *lab, uint32_t *scratch, uint64_t n, cudaStream_t s, 
   if (n == 0) return;
   CCG_CUDA(cudaMemsetAsync(scratch, 0xff, 4 * n, s));
   unsigned grid = grid_for(n, kBlock, kSMs * 32);
-  k_canon_min<<<grid, kBlock, 0, s>>>(n, lab, scratch);
+  k_canon_min<<<grid, kBlock, 0, s>>>(n, scratch, lab);
   CCG_LAUNCH_CHECK();
   k_canon_apply<<<grid, kBlock, 0, s>>>(n, lab, scratch);
   CCG_LAUNCH_CHECK();
