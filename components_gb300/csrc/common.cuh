@@ -158,6 +158,13 @@ struct PartMap {
   __host__ __device__ __forceinline__ uint32_t part(uint32_t v) const {
     return v < big ? v / (q + 1) : rm + (q ? (v - big) / q : 0);
   }
+  // [lo, hi) of v's rank: one division per row, so that a kernel tests an
+  // edge's other end with two compares instead of a division per edge
+  __host__ __device__ __forceinline__ void bounds(uint32_t v, uint32_t &lo, uint32_t &hi) const {
+    const uint32_t r = part(v);
+    lo = r < rm ? r * (q + 1) : big + (r - rm) * q;
+    hi = lo + (r < rm ? q + 1 : q);
+  }
 };
 
 // SplitMix64 finaliser: the counter-based hash behind every random variate.

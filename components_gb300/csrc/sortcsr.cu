@@ -214,16 +214,11 @@ __global__ void k_radix_scatter(const uint64_t *__restrict__ keys, uint64_t *__r
 
 // ---- contraction -----------------------------------------------------------
 
-__device__ __forceinline__ bool edge_crosses(const PartMap &pm, bool part, uint32_t v, uint32_t w) {
-  return !part || pm.part(v) != pm.part(w);
-}
-
-// Emit key (cl[v] << b) | cl[w] for every kept edge; positions from one
-// warp-aggregated atomicAdd per warp step (the key order does not matter, the
-// sort follows).
 constexpr uint32_t kEmitStage = 4096;  // keys staged per CTA (32 KB) between flushes
 
-// Emit key (cl[v] << b) | cl[w] for every kept edge.  Each warp takes 32
+// Emit key (cl[v] << b) | cl[w] for every kept edge (kept: the clusters differ
+// and, with virtual ranks, the edge leaves v's rank; the key order does not
+// matter, the sort follows).  Each warp takes 32
 // consecutive rows and walks their edges as one flattened, coalesced stream
 // (lane k reads entry k of the rows' concatenated adjacency; its row is the
 // last lane whose degree prefix sum is <= k), so skewed degrees keep every
@@ -248,12 +243,13 @@ __global__ void __launch_bounds__(kBlock) k_emit(uint64_t n, const uint64_t *__r
   for (uint64_t base = blockIdx.x * rows; base < n; base += (uint64_t)gridDim.x * rows) {
     const uint64_t v0 = base + (uint64_t)wid * 32, v = v0 + lane;
     uint64_t eb = 0;
-    uint32_t deg = 0, cv = 0;
+    uint32_t deg = 0, cv = 0, lo = 0, hi = 0xffffffffu;  // lo, hi: v's rank when part
     if (v < n) {
       eb = __ldg(rp + v);
       const uint64_t ee = __ldg(rp + v + 1);
       if (ee - eb <= hub_limit) deg = (uint32_t)(ee - eb);
       cv = cl[v];
+      if (part) pm.bounds((uint32_t)v, lo, hi);
     }
     uint32_t inc = deg;
 #pragma unroll
@@ -273,14 +269,16 @@ __global__ void __launch_bounds__(kBlock) k_emit(uint64_t n, const uint64_t *__r
       }
       const uint32_t ro = __shfl_sync(0xffffffffu, off, r);
       const uint32_t cvr = __shfl_sync(0xffffffffu, cv, r);
+      const uint32_t lor = __shfl_sync(0xffffffffu, lo, r);
+      const uint32_t hir = __shfl_sync(0xffffffffu, hi, r);
       const uint64_t ebr = ((uint64_t)__shfl_sync(0xffffffffu, (uint32_t)(eb >> 32), r) << 32) |
                            __shfl_sync(0xffffffffu, (uint32_t)eb, r);
       bool keep = false;
       uint64_t key = 0;
       if (f < total) {
         const uint32_t u = load_id(col, ebr + (f - ro));
-        if (edge_crosses(pm, part, (uint32_t)(v0 + r), u)) {  // no gather for edges
-          const uint32_t cu = cl[u];                           // inside a rank
+        if (!part || u < lor || u >= hir) {  // no gather for edges inside a rank
+          const uint32_t cu = cl[u];
           keep = cu != cvr;
           key = ((uint64_t)cvr << b) | cu;
         }
@@ -363,6 +361,8 @@ __global__ void __launch_bounds__(kBlock) k_emit_hubs(
     const uint64_t eb = __ldg(rp + v) + (uint64_t)it.y * kEmitPiece;
     const uint64_t ee = min(re, eb + kEmitPiece);
     const uint32_t cv = cl[v];
+    uint32_t lo = 0, hi = 0xffffffffu;  // v's rank when part
+    if (part) pm.bounds(v, lo, hi);
     for (uint64_t e0 = eb; e0 < ee; e0 += 32) {
       const uint64_t e = e0 + lane;
       bool keep = false;
@@ -370,7 +370,7 @@ __global__ void __launch_bounds__(kBlock) k_emit_hubs(
       if (e < ee) {
         uint32_t u = load_id(col, e);
         uint32_t cu = cl[u];
-        keep = cu != cv && edge_crosses(pm, part, v, u);
+        keep = cu != cv && (!part || u < lo || u >= hi);
         key = ((uint64_t)cv << b) | cu;
       }
       const unsigned m = __ballot_sync(0xffffffffu, keep);

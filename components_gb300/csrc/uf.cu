@@ -237,9 +237,6 @@ __host__ __device__ __forceinline__ bool is_link_pos(uint64_t d, uint64_t j) {
   return false;
 }
 
-__device__ __forceinline__ bool same_part(const PartMap &pm, uint32_t v, uint32_t u) {
-  return pm.part(v) == pm.part(u);
-}
 
 template <class T, bool PART>
 __global__ void k_aff_link(uint64_t n, uint64_t m, const uint64_t *__restrict__ rp,
@@ -253,7 +250,9 @@ __global__ void k_aff_link(uint64_t n, uint64_t m, const uint64_t *__restrict__ 
       set_err(err, kErrBadId);
       continue;
     }
-    if (!PART || same_part(pm, (uint32_t)v, (uint32_t)u)) uf_union(p, (uint32_t)v, (uint32_t)u);
+    uint32_t lo = 0, hi = 0xffffffffu;
+    if (PART) pm.bounds((uint32_t)v, lo, hi);
+    if ((uint32_t)u >= lo && (uint32_t)u < hi) uf_union(p, (uint32_t)v, (uint32_t)u);
   }
 }
 
@@ -349,6 +348,8 @@ __global__ void k_aff_rest(uint64_t n, uint64_t m, const uint64_t *__restrict__ 
       continue;
     }
     work += (uint32_t)(row.e - row.b - kAffRounds);
+    uint32_t lo = 0, hi = 0xffffffffu;  // v's rank
+    if (PART) pm.bounds((uint32_t)v, lo, hi);
     for (uint64_t k = row.b; k < row.e; ++k) {
       if (is_link_pos(row.e - row.b, k - row.b)) continue;  // linked already
       uint64_t u = (uint64_t)__ldg(col + k);
@@ -356,7 +357,7 @@ __global__ void k_aff_rest(uint64_t n, uint64_t m, const uint64_t *__restrict__ 
         set_err(err, kErrBadId);
         continue;
       }
-      if (!PART || same_part(pm, (uint32_t)v, (uint32_t)u)) uf_union(p, (uint32_t)v, (uint32_t)u);
+      if ((uint32_t)u >= lo && (uint32_t)u < hi) uf_union(p, (uint32_t)v, (uint32_t)u);
     }
   }
   if (edges_read) {  // every thread of the warp reaches this point
@@ -390,7 +391,8 @@ __global__ void k_hub_pieces(uint64_t n, uint64_t m, const uint64_t *__restrict_
     if (re < rb || re > m) continue;  // recorded by the pass that queued the row
     const uint64_t b = rb + (uint64_t)it.y * kPiece;
     const uint64_t e = min(re, b + kPiece);
-    const uint32_t lo = PART ? part_lo(pm, v) : 0u;
+    uint32_t lo = 0, hi = 0xffffffffu;  // v's rank
+    if (PART) pm.bounds(v, lo, hi);
     for (uint64_t k = b + lane; k < e; k += 32) {
       const uint64_t u = (uint64_t)__ldg(col + k);
       if (u >= n) {
@@ -398,9 +400,9 @@ __global__ void k_hub_pieces(uint64_t n, uint64_t m, const uint64_t *__restrict_
         continue;
       }
       if (LESS) {
-        if (u < v && (!PART || (uint32_t)u >= lo)) uf_union(p, v, (uint32_t)u);
+        if (u < v && (uint32_t)u >= lo) uf_union(p, v, (uint32_t)u);
       } else if (!is_link_pos(re - rb, k - rb)) {  // the link rounds took those
-        if (!PART || same_part(pm, v, (uint32_t)u)) uf_union(p, v, (uint32_t)u);
+        if ((uint32_t)u >= lo && (uint32_t)u < hi) uf_union(p, v, (uint32_t)u);
       }
     }
   }
@@ -522,7 +524,7 @@ __global__ void __launch_bounds__(1024, 2)
     for (uint32_t g0 = wid * 32; g0 < len; g0 += nw * 32) {
       const uint32_t i = g0 + lane;
       uint64_t rb = 0, rl = 0;  // row start; row length (link mode)
-      uint32_t deg = 0, lo = 0;
+      uint32_t deg = 0, lo = 0, hi = 0xffffffffu;  // lo, hi: v's rank (PART)
       if (i < len) {
         const uint64_t v = t0 + i;
         rb = __ldg(rp + v);
@@ -534,7 +536,7 @@ __global__ void __launch_bounds__(1024, 2)
           queue_hub(hl, (uint32_t)v, re - rb, err);
         } else {
           deg = LINK ? (uint32_t)min(re - rb, (uint64_t)LINK) : (uint32_t)(re - rb);
-          if (PART) lo = part_lo(pm, (uint32_t)v);
+          if (PART) pm.bounds((uint32_t)v, lo, hi);
         }
       }
       // One edge (v, uu) per lane, all lanes together: an in-tile edge to a
@@ -545,7 +547,8 @@ __global__ void __launch_bounds__(1024, 2)
       // under a non-root keeps parents smaller than children, so the forest
       // stays acyclic.  Only the row-per-lane loop hooks.
       bool hooked = false;
-      auto edge = [&](bool valid, uint64_t uu, uint32_t vi, uint32_t lov, bool may_hook) {
+      auto edge = [&](bool valid, uint64_t uu, uint32_t vi, uint32_t lov, uint32_t hiv,
+                      bool may_hook) {
         const uint32_t vv = tt + vi;
         bool uni = false, emit = false;
         uint32_t u = 0;
@@ -553,7 +556,7 @@ __global__ void __launch_bounds__(1024, 2)
           if (uu >= n) {
             set_err(err, kErrBadId);
           } else if (LINK) {
-            if ((uint32_t)uu != vv && (!PART || same_part(pm, vv, (uint32_t)uu))) {
+            if ((uint32_t)uu != vv && (!PART || ((uint32_t)uu >= lov && (uint32_t)uu < hiv))) {
               u = (uint32_t)uu;
               if (u >= tt && u - tt < len) {
                 if (may_hook && !hooked && u < vv) {  // the hook needs a smaller parent
@@ -617,7 +620,7 @@ __global__ void __launch_bounds__(1024, 2)
         for (uint32_t j = 0; j < maxdeg; ++j) {
           const bool valid = j < deg;
           const uint64_t k = rb + (LINK ? link_pos(rl, j) : j);
-          edge(valid, valid ? (uint64_t)__ldg(col + k) : 0ull, i, lo, true);
+          edge(valid, valid ? (uint64_t)__ldg(col + k) : 0ull, i, lo, hi, true);
         }
       } else {
         // skewed degrees: the 32 rows' edges as one flattened stream, lane k
@@ -640,9 +643,10 @@ __global__ void __launch_bounds__(1024, 2)
           const uint32_t ro = __shfl_sync(0xffffffffu, off, r);
           const uint64_t rbr = shfl64(rb, r);
           const uint32_t lor = PART ? __shfl_sync(0xffffffffu, lo, r) : 0u;
+          const uint32_t hir = PART && LINK ? __shfl_sync(0xffffffffu, hi, r) : 0xffffffffu;
           const bool valid = f < total;
           edge(valid, valid ? (uint64_t)__ldg(col + rbr + (f - ro)) : 0ull, g0 + (uint32_t)r, lor,
-               false);
+               hir, false);
         }
       }
     }
