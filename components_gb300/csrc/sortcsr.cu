@@ -259,54 +259,67 @@ __global__ void __launch_bounds__(kBlock) k_emit(uint64_t n, const uint64_t *__r
     }
     const uint32_t total = __shfl_sync(0xffffffffu, inc, 31);
     const uint32_t off = inc - deg;
-    for (uint32_t f0 = 0; f0 < total; f0 += 32) {
-      const uint32_t f = f0 + lane;
-      int r = 0;
+    // four steps of 32 entries at a time: their loads are issued together
+    // (one load in flight per warp left the pass latency-bound)
+    constexpr int kSteps = 4;
+    for (uint32_t f0 = 0; f0 < total; f0 += 32 * kSteps) {
+      uint32_t us[kSteps];
+      int rs[kSteps];
 #pragma unroll
-      for (int step = 16; step; step >>= 1) {
-        const uint32_t o = __shfl_sync(0xffffffffu, off, r + step);
-        if (o <= f) r += step;
+      for (int q = 0; q < kSteps; ++q) {
+        const uint32_t f = f0 + 32 * q + lane;
+        int r = 0;
+#pragma unroll
+        for (int step = 16; step; step >>= 1) {
+          const uint32_t o = __shfl_sync(0xffffffffu, off, r + step);
+          if (o <= f) r += step;
+        }
+        rs[q] = r;
+        const uint32_t ro = __shfl_sync(0xffffffffu, off, r);
+        const uint64_t ebr = ((uint64_t)__shfl_sync(0xffffffffu, (uint32_t)(eb >> 32), r) << 32) |
+                             __shfl_sync(0xffffffffu, (uint32_t)eb, r);
+        us[q] = f < total ? load_id(col, ebr + (f - ro)) : 0u;
       }
-      const uint32_t ro = __shfl_sync(0xffffffffu, off, r);
-      const uint32_t cvr = __shfl_sync(0xffffffffu, cv, r);
-      const uint32_t lor = __shfl_sync(0xffffffffu, lo, r);
-      const uint32_t hir = __shfl_sync(0xffffffffu, hi, r);
-      const uint64_t ebr = ((uint64_t)__shfl_sync(0xffffffffu, (uint32_t)(eb >> 32), r) << 32) |
-                           __shfl_sync(0xffffffffu, (uint32_t)eb, r);
-      bool keep = false;
-      uint64_t key = 0;
-      if (f < total) {
-        const uint32_t u = load_id(col, ebr + (f - ro));
-        if (!part || u < lor || u >= hir) {  // no gather for edges inside a rank
-          const uint32_t cu = cl[u];
+#pragma unroll
+      for (int q = 0; q < kSteps; ++q) {
+        if (f0 + 32 * q >= total) break;  // warp-uniform
+        const int r = rs[q];
+        const uint32_t u = us[q];
+        const uint32_t cvr = __shfl_sync(0xffffffffu, cv, r);
+        const uint32_t lor = __shfl_sync(0xffffffffu, lo, r);
+        const uint32_t hir = __shfl_sync(0xffffffffu, hi, r);
+        bool keep = false;
+        uint64_t key = 0;
+        if (f0 + 32 * q + lane < total && (!part || u < lor || u >= hir)) {
+          const uint32_t cu = cl[u];  // no gather for edges inside a rank
           keep = cu != cvr;
           key = ((uint64_t)cvr << b) | cu;
         }
-      }
-      const unsigned m = __ballot_sync(0xffffffffu, keep);
-      if (m) {
-        // reserve stage slots only while they fit, so sc always counts
-        // written keys; a step that does not fit goes straight out
-        unsigned int slot = kEmitStage;
-        if (lane == 0) {
-          unsigned int old = *static_cast<volatile unsigned int *>(&sc);
-          while (old + __popc(m) <= kEmitStage) {
-            const unsigned int prev = atomicCAS(&sc, old, old + __popc(m));
-            if (prev == old) {
-              slot = old;
-              break;
+        const unsigned m = __ballot_sync(0xffffffffu, keep);
+        if (m) {
+          // reserve stage slots only while they fit, so sc always counts
+          // written keys; a step that does not fit goes straight out
+          unsigned int slot = kEmitStage;
+          if (lane == 0) {
+            unsigned int old = *static_cast<volatile unsigned int *>(&sc);
+            while (old + __popc(m) <= kEmitStage) {
+              const unsigned int prev = atomicCAS(&sc, old, old + __popc(m));
+              if (prev == old) {
+                slot = old;
+                break;
+              }
+              old = prev;
             }
-            old = prev;
           }
-        }
-        slot = __shfl_sync(0xffffffffu, slot, 0);
-        if (slot < kEmitStage) {
-          if (keep) kst[slot + __popc(m & lt)] = key;
-        } else {
-          unsigned long long pos0 = 0;
-          if (lane == 0) pos0 = atomicAdd(cnt, (unsigned long long)__popc(m));
-          pos0 = __shfl_sync(0xffffffffu, pos0, 0);
-          if (keep) keys[pos0 + __popc(m & lt)] = key;
+          slot = __shfl_sync(0xffffffffu, slot, 0);
+          if (slot < kEmitStage) {
+            if (keep) kst[slot + __popc(m & lt)] = key;
+          } else {
+            unsigned long long pos0 = 0;
+            if (lane == 0) pos0 = atomicAdd(cnt, (unsigned long long)__popc(m));
+            pos0 = __shfl_sync(0xffffffffu, pos0, 0);
+            if (keep) keys[pos0 + __popc(m & lt)] = key;
+          }
         }
       }
     }
