@@ -80,6 +80,7 @@ void ctx_init(cc_ctx *c, int device, void *stream) {
   CCG_CUDA(cudaMalloc(&c->d_geo, sizeof(uint64_t) * ccg::kGeoMax));
   CCG_CUDA(cudaHostAlloc(&c->h_flag, sizeof(int), cudaHostAllocDefault));
   CCG_CUDA(cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking));
+  for (auto &e : c->ev) CCG_CUDA(cudaEventCreate(&e));
 }
 
 void ctx_free(cc_ctx *c) {
@@ -98,6 +99,10 @@ void ctx_free(cc_ctx *c) {
     cudaStreamDestroy(c->copy_stream);
   }
   if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
+  for (auto &e : c->ev)
+    if (e) cudaEventDestroy(e);
+  for (auto e : c->ev_pool) cudaEventDestroy(e);
+  c->ev_pool.clear();
 }
 
 void check_csr_args(const cc_csr *g) {
@@ -421,16 +426,10 @@ int ctx_run(cc_ctx *C, const cc_csr *g, cc_algo algo, const cc_config *cfg_in, u
     std::memset(&st, 0, sizeof(st));
     Counters c;
     c.prof = C->prof;
+    c.pool = &C->ev_pool;
     const uint64_t n = g->n, m = g->m_dir;
     const int idb = (int)g->id_bytes;
-    cudaEvent_t ev[4];
-    for (auto &e : ev) CCG_CUDA(cudaEventCreate(&e));
-    struct EvGuard {
-      cudaEvent_t *e;
-      ~EvGuard() {
-        for (int i = 0; i < 4; ++i) cudaEventDestroy(e[i]);
-      }
-    } evg{ev};
+    cudaEvent_t *ev = C->ev;  // the context's: no event creation per solve
     CCG_CUDA(cudaEventRecord(ev[0], s));
     DevBuf rp_d, col_d;
     Csr G;

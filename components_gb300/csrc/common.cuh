@@ -50,30 +50,49 @@ struct Counters {
     uint64_t bytes;
   };
   std::vector<Rec> recs;
+  // Events for tic/toc: taken from `pool` (owned by a context and kept across
+  // solves, so profiling adds no event creation per solve) or, without one,
+  // created and destroyed per use.
+  std::vector<cudaEvent_t> *pool = nullptr;
+  size_t used = 0;
   void add(uint64_t nl, uint64_t b) {
     launches += nl;
     bytes += b;
   }
+  cudaEvent_t event() {
+    if (pool) {
+      if (used == pool->size()) {
+        cudaEvent_t e;
+        if (cudaEventCreate(&e) != cudaSuccess) return nullptr;
+        pool->push_back(e);
+      }
+      return (*pool)[used++];
+    }
+    cudaEvent_t e;
+    return cudaEventCreate(&e) == cudaSuccess ? e : nullptr;
+  }
   cudaEvent_t tic(cudaStream_t s) {
     if (!prof) return nullptr;
-    cudaEvent_t e;
-    if (cudaEventCreate(&e) != cudaSuccess) return nullptr;
-    cudaEventRecord(e, s);
+    cudaEvent_t e = event();
+    if (e) cudaEventRecord(e, s);
     return e;
   }
   void toc(cudaStream_t s, const char *name, cudaEvent_t a, uint64_t b) {
     if (!prof || !a) return;
-    cudaEvent_t e;
-    if (cudaEventCreate(&e) != cudaSuccess) return;
+    cudaEvent_t e = event();
+    if (!e) return;
     cudaEventRecord(e, s);
     recs.push_back({name, a, e, b});
   }
   void clear_recs() {
-    for (auto &r : recs) {
-      cudaEventDestroy(r.a);
-      cudaEventDestroy(r.b);
+    if (!pool) {
+      for (auto &r : recs) {
+        cudaEventDestroy(r.a);
+        cudaEventDestroy(r.b);
+      }
     }
     recs.clear();
+    used = 0;
   }
 };
 

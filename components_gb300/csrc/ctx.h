@@ -4,6 +4,7 @@
 
 #include <memory>
 #include <string>
+#include <vector>
 
 #include "kernels.h"
 
@@ -25,6 +26,8 @@ struct cc_ctx {
   int geo_len = 0;
   double geo_beta = -1.0;
   bool prof = false;
+  cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};  // solve bracketing events, reused
+  std::vector<cudaEvent_t> ev_pool;  // per-kernel profiling events, reused across solves
   ccg::UfTuning uf;  // hook-and-compress schedule (cc_ctx_set_tuning)
   ccg::UfDecisionCache uf_cache;    // the last device graph's row-sample decisions
   ccg::UfDecisionCache host_cache;  // the last host graph's (streamed input)

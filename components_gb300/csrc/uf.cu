@@ -19,6 +19,10 @@
 #include <algorithm>
 #include <vector>
 
+#include <map>
+#include <mutex>
+#include <tuple>
+
 #include "kernels.h"
 
 namespace ccg {
@@ -870,7 +874,37 @@ struct TileShape {
   unsigned grid = 0;
 };
 template <class T, bool PART, int LINK>
+TileShape tile_shape_uncached(uint64_t n, const UfTuning &tu);
+
+// The launch shape depends on the device, the tile and the CTA size only (the
+// grid is clamped to the graph below); it is computed once per combination,
+// because the attribute and occupancy queries cost more host time than a
+// small solve.
+template <class T, bool PART, int LINK>
 TileShape tile_shape(uint64_t n, const UfTuning &tu) {
+  static std::mutex mu;
+  static std::map<std::tuple<int, uint32_t, uint32_t>, TileShape> cache;
+  int dev = 0;
+  CCG_CUDA(cudaGetDevice(&dev));
+  const auto key = std::make_tuple(dev, tu.tile_vertices, tu.tile_threads);
+  TileShape t;
+  {
+    std::lock_guard<std::mutex> lk(mu);
+    auto it = cache.find(key);
+    if (it != cache.end()) t = it->second;
+  }
+  if (t.threads == 0) {
+    t = tile_shape_uncached<T, PART, LINK>(~0ull >> 1, tu);  // the widest grid for this shape
+    std::lock_guard<std::mutex> lk(mu);
+    cache[key] = t;
+  }
+  const uint64_t tiles = (n + t.tile - 1) / t.tile;
+  t.grid = (unsigned)std::min<uint64_t>(tiles, (uint64_t)t.grid);
+  return t;
+}
+
+template <class T, bool PART, int LINK>
+TileShape tile_shape_uncached(uint64_t n, const UfTuning &tu) {
   TileShape t;
   t.tile = tu.tile_vertices;
   t.threads = (int)tu.tile_threads;
@@ -889,7 +923,11 @@ TileShape tile_shape(uint64_t n, const UfTuning &tu) {
   if (t.stage < 64) throw Error(CC_ERR_INVALID, "tile does not fit in shared memory");
   t.smem = tile_smem_bytes<uint16_t>(t.tile, (uint32_t)t.threads, t.stage);
   const void *fn = (const void *)k_tile3<T, PART, uint16_t, LINK>;
-  CCG_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)t.smem));
+  // the attribute only ever grows: launch shapes cached for other tiles keep working
+  cudaFuncAttributes fa;
+  CCG_CUDA(cudaFuncGetAttributes(&fa, fn));
+  if ((size_t)fa.maxDynamicSharedSizeBytes < t.smem)
+    CCG_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)t.smem));
   int per_sm = 0;
   CCG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, t.threads, t.smem));
   if (per_sm < 1) throw Error(CC_ERR_INVALID, "tile does not fit in shared memory");
