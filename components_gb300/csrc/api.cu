@@ -39,6 +39,10 @@ void throw_on_kernel_error(cc_ctx *C, cudaStream_t s) {
   int e = 0;
   CCG_CUDA(cudaMemcpyAsync(&e, C->d_err, sizeof(int), cudaMemcpyDeviceToHost, s));
   CCG_CUDA(cudaStreamSynchronize(s));
+  throw_on_error_word(e);
+}
+
+void throw_on_error_word(int e) {
   if (e == kErrBadOffsets) throw Error(CC_ERR_INVALID, "CSR offsets are not monotone or exceed m_dir");
   if (e == kErrBadId) throw Error(CC_ERR_INVALID, "CSR holds a vertex id >= n");
   if (e == kErrOverflow) throw Error(CC_ERR_INVALID, "CSR offsets disagree with m_dir");
@@ -78,7 +82,7 @@ void ctx_init(cc_ctx *c, int device, void *stream) {
   CCG_CUDA(cudaMalloc(&c->d_flag, sizeof(int)));
   CCG_CUDA(cudaMalloc(&c->d_err, sizeof(int)));
   CCG_CUDA(cudaMalloc(&c->d_geo, sizeof(uint64_t) * ccg::kGeoMax));
-  CCG_CUDA(cudaHostAlloc(&c->h_flag, sizeof(int), cudaHostAllocDefault));
+  CCG_CUDA(cudaHostAlloc(&c->h_flag, 2 * sizeof(int), cudaHostAllocDefault));  // flag, error word
   CCG_CUDA(cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking));
   for (auto &e : c->ev) CCG_CUDA(cudaEventCreate(&e));
 }
@@ -531,8 +535,10 @@ int ctx_run(cc_ctx *C, const cc_csr *g, cc_algo algo, const cc_config *cfg_in, u
     CCG_CUDA(cudaEventRecord(ev[3], s));
     unsigned long long ncomp = 0;
     if (C->prof) CCG_CUDA(cudaMemcpyAsync(&ncomp, cnt.p, 8, cudaMemcpyDeviceToHost, s));
+    // the error word rides along into pinned memory: one synchronisation ends the solve
+    CCG_CUDA(cudaMemcpyAsync(C->h_flag + 1, C->d_err, sizeof(int), cudaMemcpyDeviceToHost, s));
     CCG_CUDA(cudaStreamSynchronize(s));
-    S.check_err();
+    ccg::throw_on_error_word(C->h_flag[1]);
     float t_solve = 0.f, t_total = 0.f;
     CCG_CUDA(cudaEventElapsedTime(&t_solve, ev[1], ev[2]));
     CCG_CUDA(cudaEventElapsedTime(&t_total, ev[0], ev[3]));

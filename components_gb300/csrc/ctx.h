@@ -21,7 +21,7 @@ struct cc_ctx {
   cudaMemPool_t pool = nullptr;
   int *d_flag = nullptr;
   int *d_err = nullptr;
-  int *h_flag = nullptr;  // pinned
+  int *h_flag = nullptr;  // pinned: [0] round flag, [1] error word at the end of a solve
   uint64_t *d_geo = nullptr;
   int geo_len = 0;
   double geo_beta = -1.0;
@@ -62,5 +62,7 @@ int guard(F &&f) {
 // Read the context's error word after the stream drains; throw CC_ERR_INVALID
 // when a kernel recorded a bad offset or id.
 void throw_on_kernel_error(cc_ctx *C, cudaStream_t s);
+// The same check on an error word already copied to the host.
+void throw_on_error_word(int e);
 
 }  // namespace ccg
