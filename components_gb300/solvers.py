@@ -135,14 +135,19 @@ class _Solver:
         self.rank_ = rank
         self.size_ = size
         self.ctx = context
-        self.last_stats: dict = {}
+        self._ran_on: Context | None = None
+
+    @property
+    def last_stats(self) -> dict:
+        """Statistics of the last solve on this solver's context (read on demand)."""
+        return self._ran_on.stats() if self._ran_on is not None else {}
 
     def FindComponents(self, G: StaticGraph, labels) -> None:
         _check_labels(G, labels)
         ctx = self.ctx or default_context()
         g = G.with_parts(self.size_) if G.num_parts != self.size_ else G
         ctx.run(g, self.ALGO, self.config_.to_c(), int(self.config_.seed), labels)
-        self.last_stats = ctx.stats()
+        self._ran_on = ctx
 
     # driver statistics (exponential_contraction.h:325-335): no exchange on
     # one device
