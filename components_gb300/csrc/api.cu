@@ -514,7 +514,7 @@ int ctx_run(cc_ctx *C, const cc_csr *g, cc_algo algo, const cc_config *cfg_in, u
     S.run(algo, G, g->num_parts, lab);
     CCG_CUDA(cudaEventRecord(ev[2], s));
     DevBuf cnt(8, s, C->pool);
-    if (C->prof) ccg::count_roots(lab, n, cnt.as<unsigned long long>(), s, c);
+    if (C->prof_count) ccg::count_roots(lab, n, cnt.as<unsigned long long>(), s, c);
     if (labels_streamed) {
       st.d2h_bytes = 4 * n;  // copied by the final pass
     } else if (n) {
@@ -534,7 +534,7 @@ int ctx_run(cc_ctx *C, const cc_csr *g, cc_algo algo, const cc_config *cfg_in, u
     }
     CCG_CUDA(cudaEventRecord(ev[3], s));
     unsigned long long ncomp = 0;
-    if (C->prof) CCG_CUDA(cudaMemcpyAsync(&ncomp, cnt.p, 8, cudaMemcpyDeviceToHost, s));
+    if (C->prof_count) CCG_CUDA(cudaMemcpyAsync(&ncomp, cnt.p, 8, cudaMemcpyDeviceToHost, s));
     // the error word rides along into pinned memory: one synchronisation ends the solve
     CCG_CUDA(cudaMemcpyAsync(C->h_flag + 1, C->d_err, sizeof(int), cudaMemcpyDeviceToHost, s));
     CCG_CUDA(cudaStreamSynchronize(s));
@@ -670,11 +670,13 @@ uint64_t cc_ctx_arena_bytes(cc_ctx *ctx) {
 
 int cc_ctx_set_profiling(cc_ctx *ctx, int on) {
   if (!ctx) return CC_ERR_INVALID;
-  if (on && !ctx->prof) {  // a new profiling window: the totals start from zero
+  const bool kernels = (on & CC_PROF_KERNELS) != 0;
+  if (kernels && !ctx->prof) {  // a new profiling window: the totals start from zero
     ctx->prof_total = cc_stats{};
     ctx->prof_solves = 0;
   }
-  ctx->prof = on != 0;
+  ctx->prof = kernels;
+  ctx->prof_count = (on & CC_PROF_COMPONENTS) != 0;
   return CC_OK;
 }
 

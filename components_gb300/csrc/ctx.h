@@ -25,7 +25,8 @@ struct cc_ctx {
   uint64_t *d_geo = nullptr;
   int geo_len = 0;
   double geo_beta = -1.0;
-  bool prof = false;
+  bool prof = false;        // per-kernel CUDA-event timing (CC_PROF_KERNELS)
+  bool prof_count = false;  // component count after each solve (CC_PROF_COMPONENTS)
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};  // solve bracketing events, reused
   std::vector<cudaEvent_t> ev_pool;  // per-kernel profiling events, reused across solves
   ccg::UfTuning uf;  // hook-and-compress schedule (cc_ctx_set_tuning)

@@ -34,7 +34,7 @@ class Context:
             s = stream.cuda_stream if hasattr(stream, "cuda_stream") else int(stream)
         _lib.check(_lib.gpu().cc_ctx_create(C.byref(self._h), device, s))
         if profiling:
-            _lib.check(_lib.gpu().cc_ctx_set_profiling(self._h, 1))
+            self.set_profiling(True, components=True)
 
     @property
     def handle(self):
@@ -56,8 +56,11 @@ class Context:
         return {"hook_mode": t.hook_mode, "tile_vertices": t.tile_vertices,
                 "tile_threads": t.tile_threads, "hub_degree": t.hub_degree}
 
-    def set_profiling(self, on: bool) -> None:
-        _lib.check(_lib.gpu().cc_ctx_set_profiling(self._h, int(on)))
+    def set_profiling(self, on: bool, components: bool = False) -> None:
+        """Per-kernel CUDA-event timing; with `components` also the component
+        count of each solve (one extra pass over the labels)."""
+        flags = (_lib.CC_PROF_KERNELS if on else 0) | (_lib.CC_PROF_COMPONENTS if components else 0)
+        _lib.check(_lib.gpu().cc_ctx_set_profiling(self._h, flags))
 
     def run(self, g: StaticGraph, algo: int, cfg: _lib.cc_config, seed: int, labels) -> None:
         csr = g.to_c()

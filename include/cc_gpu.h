@@ -204,9 +204,12 @@ int cc_ctx_run(cc_ctx *ctx, const cc_csr *g, cc_algo algo,
 int cc_ctx_stats(cc_ctx *ctx, cc_stats *out);
 /* Device bytes the context holds in its arena (grows on demand, reused). */
 uint64_t cc_ctx_arena_bytes(cc_ctx *ctx);
-/* Per-kernel CUDA-event timing and a component count in cc_stats (off by
-   default; it adds event records and one counting pass per solve). */
-int cc_ctx_set_profiling(cc_ctx *ctx, int on);
+/* Profiling, off by default.  `flags`: CC_PROF_KERNELS = per-kernel
+   CUDA-event timing in cc_stats.kernels (adds event records between the
+   kernels), CC_PROF_COMPONENTS = cc_stats.num_components (adds one counting
+   pass over the labels and a readback per solve); 0 switches both off. */
+enum { CC_PROF_KERNELS = 1, CC_PROF_COMPONENTS = 2 };
+int cc_ctx_set_profiling(cc_ctx *ctx, int flags);
 /* Per-kernel sums (launches, ms, bytes), solve_ms, total_ms, launch and byte
    counts over every solve since profiling was last switched on; *solves gets
    their number.  (new, no counterpart in the reference: lets a caller time
