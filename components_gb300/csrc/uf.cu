@@ -176,14 +176,31 @@ __global__ void k_hook_hubs(uint64_t n, const uint64_t *__restrict__ rp,
 // entry still names an ancestor, so a cached read is always a valid step; the
 // cache keeps a giant component's root entry from becoming one hot L2 line
 // that every vertex reads.
+// Each thread walks two vertices' chains side by side (v and v + stride, both
+// coalesced across the warp), so two dependent loads are in flight at a time.
 __global__ void k_compress(uint64_t n, uint32_t *p, uint64_t v_begin = 0) {
-  for (uint64_t v = v_begin + blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < n;
-       v += (uint64_t)gridDim.x * blockDim.x) {
-    const uint32_t r0 = p[v];
-    if (r0 == (uint32_t)v) continue;
-    uint32_t r = r0, nx;
-    while ((nx = p[r]) != r) r = nx;
-    if (r != r0) p[v] = r;  // most vertices already point at their root
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t a = v_begin + blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; a < n;
+       a += 2 * stride) {
+    const uint64_t b = a + stride;
+    const bool hb = b < n;
+    const uint32_t ra = p[a], rb = hb ? p[b] : 0u;
+    uint32_t x = ra, y = rb;
+    bool da = ra == (uint32_t)a, db = !hb || rb == (uint32_t)b;
+    while (!(da && db)) {
+      const uint32_t nx = da ? x : p[x];
+      const uint32_t ny = db ? y : p[y];
+      if (!da) {
+        if (nx == x) da = true;
+        else x = nx;
+      }
+      if (!db) {
+        if (ny == y) db = true;
+        else y = ny;
+      }
+    }
+    if (x != ra) p[a] = x;  // most vertices already point at their root
+    if (hb && y != rb) p[b] = y;
   }
 }
 
