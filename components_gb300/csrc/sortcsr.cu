@@ -214,17 +214,43 @@ __global__ void k_radix_scatter(const uint64_t *__restrict__ keys, uint64_t *__r
 
 // ---- contraction -----------------------------------------------------------
 
-constexpr uint32_t kEmitStage = 4096;  // keys staged per CTA (32 KB) between flushes
+// Kept keys of one warp, staged in the warp's own shared-memory buffer and
+// written out with one global reservation per full buffer (kept keys are rare
+// on most graphs, and one atomic per warp step on the single counter would
+// serialise where they are not).  Warps never wait for one another.
+constexpr uint32_t kWarpKeys = 256;
+struct WarpKeys {
+  uint64_t *buf;
+  uint32_t fill;  // warp-uniform
+  __device__ __forceinline__ void flush(unsigned lane, uint64_t *__restrict__ keys,
+                                        unsigned long long *__restrict__ cnt) {
+    __syncwarp();
+    unsigned long long pos0 = 0;
+    if (lane == 0) pos0 = atomicAdd(cnt, (unsigned long long)fill);
+    pos0 = __shfl_sync(0xffffffffu, pos0, 0);
+    for (uint32_t k = lane; k < fill; k += 32) keys[pos0 + k] = buf[k];
+    __syncwarp();
+    fill = 0;
+  }
+  // one step of the warp: lanes with keep set add their key
+  __device__ __forceinline__ void put(bool keep, uint64_t key, unsigned lane,
+                                      uint64_t *__restrict__ keys,
+                                      unsigned long long *__restrict__ cnt) {
+    const unsigned m = __ballot_sync(0xffffffffu, keep);
+    if (!m) return;
+    if (fill + __popc(m) > kWarpKeys) flush(lane, keys, cnt);
+    if (keep) buf[fill + __popc(m & ((1u << lane) - 1u))] = key;
+    fill += __popc(m);
+  }
+};
 
 // Emit key (cl[v] << b) | cl[w] for every kept edge (kept: the clusters differ
 // and, with virtual ranks, the edge leaves v's rank; the key order does not
-// matter, the sort follows).  Each warp takes 32
-// consecutive rows and walks their edges as one flattened, coalesced stream
-// (lane k reads entry k of the rows' concatenated adjacency; its row is the
-// last lane whose degree prefix sum is <= k), so skewed degrees keep every
-// lane busy.  Kept keys are staged in shared memory and flushed with one
-// global atomic per flush, not one per warp step.  Rows longer than hub_limit
-// are left to k_emit_hubs.
+// matter, the sort follows).  Each warp takes 32 consecutive rows at a time
+// and walks their edges as one flattened, coalesced stream (lane k reads
+// entry k of the rows' concatenated adjacency; its row is the last lane whose
+// degree prefix sum is <= k), so skewed degrees keep every lane busy.  Rows
+// longer than hub_limit are left to k_emit_hubs.
 template <class T>
 __global__ void __launch_bounds__(kBlock) k_emit(uint64_t n, const uint64_t *__restrict__ rp,
                                                  const T *__restrict__ col,
@@ -232,16 +258,13 @@ __global__ void __launch_bounds__(kBlock) k_emit(uint64_t n, const uint64_t *__r
                                                  bool part, int b, uint64_t hub_limit,
                                                  uint64_t *__restrict__ keys,
                                                  unsigned long long *__restrict__ cnt) {
-  __shared__ uint64_t kst[kEmitStage];
-  __shared__ unsigned int sc;
-  __shared__ unsigned long long gbase;
+  __shared__ uint64_t wbuf[kBlock / 32][kWarpKeys];
   const unsigned lane = lane_id(), wid = threadIdx.x >> 5;
-  const unsigned lt = (1u << lane) - 1u;
-  if (threadIdx.x == 0) sc = 0;
-  __syncthreads();
-  const uint64_t rows = blockDim.x;  // 32 rows per warp per step, the same steps for the whole CTA
-  for (uint64_t base = blockIdx.x * rows; base < n; base += (uint64_t)gridDim.x * rows) {
-    const uint64_t v0 = base + (uint64_t)wid * 32, v = v0 + lane;
+  WarpKeys st{wbuf[wid], 0};
+  const uint64_t warp = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
+  const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+  for (uint64_t v0 = warp * 32; v0 < n; v0 += nwarps * 32) {
+    const uint64_t v = v0 + lane;
     uint64_t eb = 0;
     uint32_t deg = 0, cv = 0, lo = 0, hi = 0xffffffffu;  // lo, hi: v's rank when part
     if (v < n) {
@@ -295,55 +318,15 @@ __global__ void __launch_bounds__(kBlock) k_emit(uint64_t n, const uint64_t *__r
           keep = cu != cvr;
           key = ((uint64_t)cvr << b) | cu;
         }
-        const unsigned m = __ballot_sync(0xffffffffu, keep);
-        if (m) {
-          // reserve stage slots only while they fit, so sc always counts
-          // written keys; a step that does not fit goes straight out
-          unsigned int slot = kEmitStage;
-          if (lane == 0) {
-            unsigned int old = *static_cast<volatile unsigned int *>(&sc);
-            while (old + __popc(m) <= kEmitStage) {
-              const unsigned int prev = atomicCAS(&sc, old, old + __popc(m));
-              if (prev == old) {
-                slot = old;
-                break;
-              }
-              old = prev;
-            }
-          }
-          slot = __shfl_sync(0xffffffffu, slot, 0);
-          if (slot < kEmitStage) {
-            if (keep) kst[slot + __popc(m & lt)] = key;
-          } else {
-            unsigned long long pos0 = 0;
-            if (lane == 0) pos0 = atomicAdd(cnt, (unsigned long long)__popc(m));
-            pos0 = __shfl_sync(0xffffffffu, pos0, 0);
-            if (keep) keys[pos0 + __popc(m & lt)] = key;
-          }
-        }
+        st.put(keep, key, lane, keys, cnt);
       }
     }
-    __syncthreads();
-    const unsigned int staged = sc;
-    __syncthreads();  // every thread has read sc before the next step changes it
-    const bool last = base + (uint64_t)gridDim.x * rows >= n;
-    if (staged > kEmitStage / 2 || (last && staged)) {
-      if (threadIdx.x == 0) gbase = atomicAdd(cnt, (unsigned long long)staged);
-      __syncthreads();
-      for (uint32_t k = threadIdx.x; k < staged; k += blockDim.x) keys[gbase + k] = kst[k];
-      __syncthreads();
-      if (threadIdx.x == 0) sc = 0;
-      __syncthreads();
-    }
   }
+  if (st.fill) st.flush(lane, keys, cnt);
 }
 
 // One warp per piece of a hub row (rows longer than the k_emit limit):
-// kEmitPiece edges each, so the longest row is spread over many warps.  Each
-// warp collects its kept keys in its own shared-memory buffer and reserves
-// global room once per full buffer (a hub's edges mostly cross ranks, and one
-// global atomic per warp step on a single counter serialises).
-constexpr uint32_t kWarpKeys = 256;
+// kEmitPiece edges each, so the longest row is spread over many warps.
 template <class T>
 __global__ void __launch_bounds__(kBlock) k_emit_hubs(
     const uint64_t *__restrict__ rp, const T *__restrict__ col, const uint32_t *__restrict__ cl,
@@ -352,18 +335,7 @@ __global__ void __launch_bounds__(kBlock) k_emit_hubs(
     unsigned long long *__restrict__ cnt) {
   __shared__ uint64_t wbuf[kBlock / 32][kWarpKeys];
   const unsigned lane = lane_id(), wid = threadIdx.x >> 5;
-  const unsigned lt = (1u << lane) - 1u;
-  uint64_t *buf = wbuf[wid];
-  uint32_t wn = 0;  // warp-uniform fill of buf
-  auto flush = [&]() {
-    __syncwarp();
-    unsigned long long pos0 = 0;
-    if (lane == 0) pos0 = atomicAdd(cnt, (unsigned long long)wn);
-    pos0 = __shfl_sync(0xffffffffu, pos0, 0);
-    for (uint32_t k = lane; k < wn; k += 32) keys[pos0 + k] = buf[k];
-    __syncwarp();
-    wn = 0;
-  };
+  WarpKeys st{wbuf[wid], 0};
   const uint64_t warp = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
   const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
   const uint64_t nitems = min((uint64_t)*d_nitems, cap);
@@ -386,14 +358,10 @@ __global__ void __launch_bounds__(kBlock) k_emit_hubs(
         keep = cu != cv && (!part || u < lo || u >= hi);
         key = ((uint64_t)cv << b) | cu;
       }
-      const unsigned m = __ballot_sync(0xffffffffu, keep);
-      if (!m) continue;
-      if (wn + __popc(m) > kWarpKeys) flush();
-      if (keep) buf[wn + __popc(m & lt)] = key;
-      wn += __popc(m);
+      st.put(keep, key, lane, keys, cnt);
     }
   }
-  if (wn) flush();
+  if (st.fill) st.flush(lane, keys, cnt);
 }
 
 // Rows longer than `limit` (hubs) are listed for the warp-per-row kernel.

@@ -519,6 +519,7 @@ __device__ __forceinline__ uint64_t shfl64(uint64_t x, int src) {
 // id of its tile-local root.
 constexpr uint32_t kUnionQueue = 64;  // per warp: < 32 pending + up to 32 new
 constexpr uint32_t kTileMax = 65536;  // queue entries pack two 16-bit tile indices
+constexpr uint32_t kLinkGroups = 1;   // link mode: 32-row blocks per warp step (1 measured best of 1, 2, 4)
 
 template <class PT>
 size_t tile_smem_bytes(uint32_t tile, uint32_t threads, uint32_t stage) {
@@ -555,132 +556,175 @@ __global__ void __launch_bounds__(1024, 2)
     if (threadIdx.x == 0) ccount = 0;
     __syncthreads();
     uint32_t qn = 0;  // warp-uniform queue fill
-    for (uint32_t g0 = wid * 32; g0 < len; g0 += nw * 32) {
-      const uint32_t i = g0 + lane;
-      uint64_t rb = 0, rl = 0;  // row start; row length (link mode)
-      uint32_t deg = 0, lo = 0, hi = 0xffffffffu;  // lo, hi: v's rank (PART)
-      if (i < len) {
-        const uint64_t v = t0 + i;
-        rb = __ldg(rp + v);
-        const uint64_t re = __ldg(rp + v + 1);
-        if (LINK) rl = re - rb;
-        if (re < rb || re > m) {
-          set_err(err, kErrBadOffsets);
-        } else if (!LINK && re - rb > hub_degree) {
-          queue_hub(hl, (uint32_t)v, re - rb, err);
-        } else {
-          deg = LINK ? (uint32_t)min(re - rb, (uint64_t)LINK) : (uint32_t)(re - rb);
-          if (PART) pm.bounds((uint32_t)v, lo, hi);
+    // One edge (v, uu) per lane, all lanes together: an in-tile edge to a
+    // smaller id goes to the warp's union queue (32 queued entries make a
+    // union step), an edge to an earlier tile to the cut stage.
+    // hook: the lane's row may link itself under its first in-tile smaller
+    // neighbour with one CAS (no finds) while it is still a root; a link
+    // under a non-root keeps parents smaller than children, so the forest
+    // stays acyclic.  Only the row-per-lane loops hook.
+    bool hooked = false;
+    auto edge = [&](bool valid, uint64_t uu, uint32_t vi, uint32_t lov, uint32_t hiv,
+                    bool may_hook) {
+      const uint32_t vv = tt + vi;
+      bool uni = false, emit = false;
+      uint32_t u = 0;
+      if (valid) {
+        if (uu >= n) {
+          set_err(err, kErrBadId);
+        } else if (LINK) {
+          if ((uint32_t)uu != vv && (!PART || ((uint32_t)uu >= lov && (uint32_t)uu < hiv))) {
+            u = (uint32_t)uu;
+            if (u >= tt && u - tt < len) {
+              if (may_hook && !hooked && u < vv) {  // the hook needs a smaller parent
+                hooked = true;
+                uni = ts_cas(const_cast<PT *>(s + vi), vi, u - tt) != vi;
+              } else {
+                uni = true;
+              }
+            } else {
+              emit = true;  // a cut edge in either direction
+            }
+          }
+        } else if ((uint32_t)uu < vv && (!PART || (uint32_t)uu >= lov)) {
+          u = (uint32_t)uu;  // each undirected edge once, from its larger end
+          if (u < tt) {
+            emit = true;
+          } else if (may_hook && !hooked) {
+            hooked = true;
+            uni = ts_cas(const_cast<PT *>(s + vi), vi, u - tt) != vi;  // hooked, or queue
+          } else {
+            uni = true;
+          }
         }
       }
-      // One edge (v, uu) per lane, all lanes together: an in-tile edge to a
-      // smaller id goes to the warp's union queue (32 queued entries make a
-      // union step), an edge to an earlier tile to the cut stage.
-      // hook: the lane's row may link itself under its first in-tile smaller
-      // neighbour with one CAS (no finds) while it is still a root; a link
-      // under a non-root keeps parents smaller than children, so the forest
-      // stays acyclic.  Only the row-per-lane loop hooks.
-      bool hooked = false;
-      auto edge = [&](bool valid, uint64_t uu, uint32_t vi, uint32_t lov, uint32_t hiv,
-                      bool may_hook) {
-        const uint32_t vv = tt + vi;
-        bool uni = false, emit = false;
-        uint32_t u = 0;
-        if (valid) {
-          if (uu >= n) {
-            set_err(err, kErrBadId);
-          } else if (LINK) {
-            if ((uint32_t)uu != vv && (!PART || ((uint32_t)uu >= lov && (uint32_t)uu < hiv))) {
-              u = (uint32_t)uu;
-              if (u >= tt && u - tt < len) {
-                if (may_hook && !hooked && u < vv) {  // the hook needs a smaller parent
-                  hooked = true;
-                  uni = ts_cas(const_cast<PT *>(s + vi), vi, u - tt) != vi;
-                } else {
-                  uni = true;
-                }
-              } else {
-                emit = true;  // a cut edge in either direction
-              }
-            }
-          } else if ((uint32_t)uu < vv && (!PART || (uint32_t)uu >= lov)) {
-            u = (uint32_t)uu;  // each undirected edge once, from its larger end
-            if (u < tt) {
-              emit = true;
-            } else if (may_hook && !hooked) {
-              hooked = true;
-              uni = ts_cas(const_cast<PT *>(s + vi), vi, u - tt) != vi;  // hooked, or queue
-            } else {
-              uni = true;
-            }
+      const unsigned um = __ballot_sync(0xffffffffu, uni);
+      if (uni) q[qn + __popc(um & lt)] = vi | ((u - tt) << 16);
+      qn += __popc(um);
+      if (qn >= 32) {  // a full union step: the newest 32 entries
+        __syncwarp();
+        const uint32_t w = q[qn - 32 + lane];
+        tw_union(s, w & 0xffffu, w >> 16);
+        qn -= 32;
+        __syncwarp();
+      }
+      const unsigned em = __ballot_sync(0xffffffffu, emit);
+      if (em) {
+        unsigned int base = 0;
+        if (lane == (unsigned)(__ffs(em) - 1)) base = atomicAdd(&ccount, (unsigned)__popc(em));
+        base = __shfl_sync(0xffffffffu, base, __ffs(em) - 1);
+        const unsigned int slot = base + __popc(em & lt);
+        const bool over = emit && slot >= stage_cap;
+        if (emit && !over) cstage[slot] = make_uint2(vi, u);  // near end as a tile index for now
+        const unsigned om = __ballot_sync(0xffffffffu, over);
+        if (om) {
+          unsigned long long gb = 0;
+          if (lane == (unsigned)(__ffs(om) - 1)) gb = atomicAdd(ncut, (unsigned long long)__popc(om));
+          gb = __shfl_sync(0xffffffffu, gb, __ffs(om) - 1);
+          if (over) {
+            const unsigned long long gs = gb + __popc(om & lt);
+            if (gs < cut_cap) cut[gs] = make_uint2(vv, u);
+            else set_err(err, kErrOverflow);
           }
         }
-        const unsigned um = __ballot_sync(0xffffffffu, uni);
-        if (uni) q[qn + __popc(um & lt)] = vi | ((u - tt) << 16);
-        qn += __popc(um);
-        if (qn >= 32) {  // a full union step: the newest 32 entries
-          __syncwarp();
-          const uint32_t w = q[qn - 32 + lane];
-          tw_union(s, w & 0xffffu, w >> 16);
-          qn -= 32;
-          __syncwarp();
-        }
-        const unsigned em = __ballot_sync(0xffffffffu, emit);
-        if (em) {
-          unsigned int base = 0;
-          if (lane == (unsigned)(__ffs(em) - 1)) base = atomicAdd(&ccount, (unsigned)__popc(em));
-          base = __shfl_sync(0xffffffffu, base, __ffs(em) - 1);
-          const unsigned int slot = base + __popc(em & lt);
-          const bool over = emit && slot >= stage_cap;
-          if (emit && !over) cstage[slot] = make_uint2(vi, u);  // near end as a tile index for now
-          const unsigned om = __ballot_sync(0xffffffffu, over);
-          if (om) {
-            unsigned long long gb = 0;
-            if (lane == (unsigned)(__ffs(om) - 1)) gb = atomicAdd(ncut, (unsigned long long)__popc(om));
-            gb = __shfl_sync(0xffffffffu, gb, __ffs(om) - 1);
-            if (over) {
-              const unsigned long long gs = gb + __popc(om & lt);
-              if (gs < cut_cap) cut[gs] = make_uint2(vv, u);
-              else set_err(err, kErrOverflow);
-            }
-          }
-        }
-      };
-      const uint32_t maxdeg = __reduce_max_sync(0xffffffffu, deg);
-      const uint32_t total = __reduce_add_sync(0xffffffffu, deg);
-      if (maxdeg <= 2 * ((total + 31) / 32) + 1) {
-        // even degrees: lane = row, maxdeg steps, the ids of 32 neighbouring
-        // rows are adjacent in memory
-        for (uint32_t j = 0; j < maxdeg; ++j) {
-          const bool valid = j < deg;
-          const uint64_t k = rb + (LINK ? link_pos(rl, j) : j);
-          edge(valid, valid ? (uint64_t)__ldg(col + k) : 0ull, i, lo, hi, true);
-        }
-      } else {
-        // skewed degrees: the 32 rows' edges as one flattened stream, lane k
-        // reads entry k; its row is the last lane whose prefix sum is <= k
-        uint32_t inc = deg;
+      }
+    };
+    if constexpr (LINK > 0) {
+      // Link mode reads at most LINK entries per row, so every warp takes
+      // kLinkGroups blocks of 32 rows at once (lane = row) and issues all of
+      // their offset loads, then all of their id loads, before any
+      // shared-memory work: the pass is bound by the latency of these two
+      // dependent loads, not by issue.
+      constexpr uint32_t R = kLinkGroups;
+      for (uint32_t g0 = wid * 32 * R; g0 < len; g0 += nw * 32 * R) {
+        uint64_t rb[R], re[R];
 #pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-          const uint32_t t = __shfl_up_sync(0xffffffffu, inc, o);
-          if ((int)lane >= o) inc += t;
-        }
-        const uint32_t off = inc - deg;
-        for (uint32_t f0 = 0; f0 < total; f0 += 32) {
-          const uint32_t f = f0 + lane;
-          int r = 0;
-#pragma unroll
-          for (int step = 16; step; step >>= 1) {
-            const uint32_t o = __shfl_sync(0xffffffffu, off, r + step);
-            if (o <= f) r += step;
+        for (uint32_t r = 0; r < R; ++r) {
+          const uint32_t i = g0 + 32 * r + lane;
+          rb[r] = re[r] = 0;
+          if (i < len) {
+            rb[r] = __ldg(rp + t0 + i);
+            re[r] = __ldg(rp + t0 + i + 1);
           }
-          const uint32_t ro = __shfl_sync(0xffffffffu, off, r);
-          const uint64_t rbr = shfl64(rb, r);
-          const uint32_t lor = PART ? __shfl_sync(0xffffffffu, lo, r) : 0u;
-          const uint32_t hir = PART && LINK ? __shfl_sync(0xffffffffu, hi, r) : 0xffffffffu;
-          const bool valid = f < total;
-          edge(valid, valid ? (uint64_t)__ldg(col + rbr + (f - ro)) : 0ull, g0 + (uint32_t)r, lor,
-               hir, false);
+        }
+        uint32_t deg[R];
+#pragma unroll
+        for (uint32_t r = 0; r < R; ++r) {
+          deg[r] = 0;
+          if (re[r] < rb[r] || re[r] > m) set_err(err, kErrBadOffsets);
+          else deg[r] = (uint32_t)min(re[r] - rb[r], (uint64_t)LINK);
+        }
+        T id[R][LINK];
+#pragma unroll
+        for (uint32_t r = 0; r < R; ++r)
+#pragma unroll
+          for (uint32_t j = 0; j < (uint32_t)LINK; ++j)
+            id[r][j] = j < deg[r] ? __ldg(col + rb[r] + link_pos(re[r] - rb[r], j)) : (T)0;
+#pragma unroll
+        for (uint32_t r = 0; r < R; ++r) {
+          const uint32_t i = g0 + 32 * r + lane;
+          uint32_t lo = 0, hi = 0xffffffffu;  // v's rank (PART)
+          if (PART && i < len) pm.bounds(tt + i, lo, hi);
+          const uint32_t maxdeg = __reduce_max_sync(0xffffffffu, deg[r]);
+          hooked = false;
+#pragma unroll
+          for (uint32_t j = 0; j < (uint32_t)LINK; ++j)
+            if (j < maxdeg) edge(j < deg[r], (uint64_t)id[r][j], i, lo, hi, true);
+        }
+      }
+    } else {
+      for (uint32_t g0 = wid * 32; g0 < len; g0 += nw * 32) {
+        const uint32_t i = g0 + lane;
+        uint64_t rb = 0;  // row start
+        uint32_t deg = 0, lo = 0, hi = 0xffffffffu;  // lo, hi: v's rank (PART)
+        if (i < len) {
+          const uint64_t v = t0 + i;
+          rb = __ldg(rp + v);
+          const uint64_t re = __ldg(rp + v + 1);
+          if (re < rb || re > m) {
+            set_err(err, kErrBadOffsets);
+          } else if (re - rb > hub_degree) {
+            queue_hub(hl, (uint32_t)v, re - rb, err);
+          } else {
+            deg = (uint32_t)(re - rb);
+            if (PART) pm.bounds((uint32_t)v, lo, hi);
+          }
+        }
+        hooked = false;
+        const uint32_t maxdeg = __reduce_max_sync(0xffffffffu, deg);
+        const uint32_t total = __reduce_add_sync(0xffffffffu, deg);
+        if (maxdeg <= 2 * ((total + 31) / 32) + 1) {
+          // even degrees: lane = row, maxdeg steps, the ids of 32 neighbouring
+          // rows are adjacent in memory
+          for (uint32_t j = 0; j < maxdeg; ++j) {
+            const bool valid = j < deg;
+            edge(valid, valid ? (uint64_t)__ldg(col + rb + j) : 0ull, i, lo, hi, true);
+          }
+        } else {
+          // skewed degrees: the 32 rows' edges as one flattened stream, lane k
+          // reads entry k; its row is the last lane whose prefix sum is <= k
+          uint32_t inc = deg;
+#pragma unroll
+          for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t t = __shfl_up_sync(0xffffffffu, inc, o);
+            if ((int)lane >= o) inc += t;
+          }
+          const uint32_t off = inc - deg;
+          for (uint32_t f0 = 0; f0 < total; f0 += 32) {
+            const uint32_t f = f0 + lane;
+            int r = 0;
+#pragma unroll
+            for (int step = 16; step; step >>= 1) {
+              const uint32_t o = __shfl_sync(0xffffffffu, off, r + step);
+              if (o <= f) r += step;
+            }
+            const uint32_t ro = __shfl_sync(0xffffffffu, off, r);
+            const uint64_t rbr = shfl64(rb, r);
+            const uint32_t lor = PART ? __shfl_sync(0xffffffffu, lo, r) : 0u;
+            const bool valid = f < total;
+            edge(valid, valid ? (uint64_t)__ldg(col + rbr + (f - ro)) : 0ull, g0 + (uint32_t)r, lor,
+                 0xffffffffu, false);
+          }
         }
       }
     }
