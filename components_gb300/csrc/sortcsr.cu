@@ -214,31 +214,97 @@ __global__ void k_radix_scatter(const uint64_t *__restrict__ keys, uint64_t *__r
 
 // ---- contraction -----------------------------------------------------------
 
+// Keys a CTA has written already: an open-addressing set in shared memory.
+// Cut edges between two clusters repeat many times on graphs with large
+// components (every edge between two of them gives the same key), so dropping
+// repeats before they are written shrinks the sort that follows.  A key that
+// finds no free slot in a few probes is written anyway, so the set only ever
+// drops true repeats.  ~0 marks a free slot and is never a key (cluster ids
+// are below n < 2^32, so both halves cannot be all ones).
+constexpr uint32_t kEmitSet = 2048;  // slots (16 KB)
+__device__ __forceinline__ void emit_set_clear(unsigned long long *set) {
+  for (uint32_t i = threadIdx.x; i < kEmitSet; i += blockDim.x) set[i] = ~0ull;
+  __syncthreads();
+}
+__device__ __forceinline__ bool emit_set_seen(unsigned long long *set, uint64_t key) {
+  uint32_t h = (uint32_t)mix64(key) & (kEmitSet - 1);
+#pragma unroll 1
+  for (int probe = 0; probe < 8; ++probe) {
+    const unsigned long long cur = atomicCAS(set + h, ~0ull, (unsigned long long)key);
+    if (cur == ~0ull) return false;  // inserted: the first time this CTA sees the key
+    if (cur == key) return true;
+    h = (h + 1) & (kEmitSet - 1);
+  }
+  return false;
+}
+
 // Kept keys of one warp, staged in the warp's own shared-memory buffer and
-// written out with one global reservation per full buffer (kept keys are rare
-// on most graphs, and one atomic per warp step on the single counter would
-// serialise where they are not).  Warps never wait for one another.
+// written out with one global reservation per full buffer (one atomic per
+// warp step on the single counter would serialise where keys are many).
+// Repeats are dropped through the CTA's set when a buffer is written out, not
+// in the edge loop.  A warp's first buffer is written out early, at
+// kEmitTrial keys: unless a quarter of them equal the key staged before them,
+// the warp never consults the set (its keys come from small clusters, and the
+// set's 64-bit compare-and-swaps would only cost time); a warp that stops
+// finding repeats in the set stops too.  Warps never wait for one another.
 constexpr uint32_t kWarpKeys = 256;
+constexpr unsigned kEmitCtasPerSM = 32;
+constexpr uint32_t kEmitTrial = 64;
+constexpr uint32_t kEmitSteps = 4;  // 32-entry steps of k_emit between flush checks
 struct WarpKeys {
   uint64_t *buf;
-  uint32_t fill;  // warp-uniform
+  unsigned long long *set;
+  uint32_t steady;           // flush threshold after the trial
+  uint32_t fill = 0;         // warp-uniform
+  uint32_t trigger = kEmitTrial;  // flush once fill reaches this
+  bool dedup = true;         // warp-uniform
   __device__ __forceinline__ void flush(unsigned lane, uint64_t *__restrict__ keys,
                                         unsigned long long *__restrict__ cnt) {
     __syncwarp();
+    uint32_t out = fill;
+    if (dedup && trigger == kEmitTrial) {
+      // the trial: keys equal to the one staged just before them predict
+      // repeats in the set; without them the keys come from small clusters
+      // and the set would only cost time
+      uint32_t reps = 0;
+      for (uint32_t k0 = 0; k0 < fill; k0 += 32) {
+        const uint32_t k = k0 + lane;
+        reps += __popc(__ballot_sync(0xffffffffu, k < fill && k > 0 && buf[k] == buf[k - 1]));
+      }
+      if (4 * reps < fill) dedup = false;
+    }
+    if (dedup) {
+      // survivors are packed in place: chunk k0's writes land below k0 + 32,
+      // in entries every lane has read already
+      out = 0;
+      for (uint32_t k0 = 0; k0 < fill; k0 += 32) {
+        const uint32_t k = k0 + lane;
+        uint64_t key = 0;
+        bool keep = false;
+        if (k < fill) {
+          key = buf[k];
+          keep = !emit_set_seen(set, key);
+        }
+        const unsigned m = __ballot_sync(0xffffffffu, keep);
+        if (keep) buf[out + __popc(m & ((1u << lane) - 1u))] = key;
+        out += __popc(m);
+      }
+      __syncwarp();
+      if (4 * out > 3 * fill) dedup = false;
+    }
     unsigned long long pos0 = 0;
-    if (lane == 0) pos0 = atomicAdd(cnt, (unsigned long long)fill);
+    if (lane == 0 && out) pos0 = atomicAdd(cnt, (unsigned long long)out);
     pos0 = __shfl_sync(0xffffffffu, pos0, 0);
-    for (uint32_t k = lane; k < fill; k += 32) keys[pos0 + k] = buf[k];
+    for (uint32_t k = lane; k < out; k += 32) keys[pos0 + k] = buf[k];
     __syncwarp();
     fill = 0;
+    trigger = steady;
   }
-  // one step of the warp: lanes with keep set add their key
-  __device__ __forceinline__ void put(bool keep, uint64_t key, unsigned lane,
-                                      uint64_t *__restrict__ keys,
-                                      unsigned long long *__restrict__ cnt) {
+  // one step of the warp: lanes with keep set add their key (the caller
+  // flushes at trigger, which leaves room for the steps that come before the
+  // next check)
+  __device__ __forceinline__ void put(bool keep, uint64_t key, unsigned lane) {
     const unsigned m = __ballot_sync(0xffffffffu, keep);
-    if (!m) return;
-    if (fill + __popc(m) > kWarpKeys) flush(lane, keys, cnt);
     if (keep) buf[fill + __popc(m & ((1u << lane) - 1u))] = key;
     fill += __popc(m);
   }
@@ -259,8 +325,10 @@ __global__ void __launch_bounds__(kBlock) k_emit(uint64_t n, const uint64_t *__r
                                                  uint64_t *__restrict__ keys,
                                                  unsigned long long *__restrict__ cnt) {
   __shared__ uint64_t wbuf[kBlock / 32][kWarpKeys];
+  __shared__ unsigned long long set[kEmitSet];
   const unsigned lane = lane_id(), wid = threadIdx.x >> 5;
-  WarpKeys st{wbuf[wid], 0};
+  emit_set_clear(set);
+  WarpKeys st{wbuf[wid], set, kWarpKeys - 32 * kEmitSteps};
   const uint64_t warp = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
   const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
   for (uint64_t v0 = warp * 32; v0 < n; v0 += nwarps * 32) {
@@ -284,7 +352,7 @@ __global__ void __launch_bounds__(kBlock) k_emit(uint64_t n, const uint64_t *__r
     const uint32_t off = inc - deg;
     // four steps of 32 entries at a time: their loads are issued together
     // (one load in flight per warp left the pass latency-bound)
-    constexpr int kSteps = 4;
+    constexpr int kSteps = (int)kEmitSteps;
     for (uint32_t f0 = 0; f0 < total; f0 += 32 * kSteps) {
       uint32_t us[kSteps];
       int rs[kSteps];
@@ -315,11 +383,12 @@ __global__ void __launch_bounds__(kBlock) k_emit(uint64_t n, const uint64_t *__r
         uint64_t key = 0;
         if (f0 + 32 * q + lane < total && (!part || u < lor || u >= hir)) {
           const uint32_t cu = cl[u];  // no gather for edges inside a rank
-          keep = cu != cvr;
           key = ((uint64_t)cvr << b) | cu;
+          keep = cu != cvr;
         }
-        st.put(keep, key, lane, keys, cnt);
+        st.put(keep, key, lane);
       }
+      if (st.fill >= st.trigger) st.flush(lane, keys, cnt);
     }
   }
   if (st.fill) st.flush(lane, keys, cnt);
@@ -334,8 +403,10 @@ __global__ void __launch_bounds__(kBlock) k_emit_hubs(
     const unsigned int *__restrict__ d_nitems, uint64_t *__restrict__ keys,
     unsigned long long *__restrict__ cnt) {
   __shared__ uint64_t wbuf[kBlock / 32][kWarpKeys];
+  __shared__ unsigned long long set[kEmitSet];
   const unsigned lane = lane_id(), wid = threadIdx.x >> 5;
-  WarpKeys st{wbuf[wid], 0};
+  emit_set_clear(set);
+  WarpKeys st{wbuf[wid], set, kWarpKeys - 32};
   const uint64_t warp = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
   const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
   const uint64_t nitems = min((uint64_t)*d_nitems, cap);
@@ -355,10 +426,11 @@ __global__ void __launch_bounds__(kBlock) k_emit_hubs(
       if (e < ee) {
         uint32_t u = load_id(col, e);
         uint32_t cu = cl[u];
-        keep = cu != cv && (!part || u < lo || u >= hi);
         key = ((uint64_t)cv << b) | cu;
+        keep = cu != cv && (!part || u < lo || u >= hi);
       }
-      st.put(keep, key, lane, keys, cnt);
+      st.put(keep, key, lane);
+      if (st.fill >= st.trigger) st.flush(lane, keys, cnt);
     }
   }
   if (st.fill) st.flush(lane, keys, cnt);
@@ -451,13 +523,14 @@ void emit_keys(const Csr &g, const uint32_t *cl, const PartMap &pm, bool part, i
   DevBuf hubs(8 * cap, s, pool), nh(4, s, pool);
   CCG_CUDA(cudaMemsetAsync(nh.p, 0, 4, s));
   unsigned grid = grid_for(g.n, kBlock, kSMs * 32);
+  const unsigned egrid = grid_for(g.n, kBlock, kSMs * kEmitCtasPerSM);
   cudaEvent_t t0 = c.tic(s);
   k_list_hubs<<<grid, kBlock, 0, s>>>(g.n, g.rp, hub_limit, hubs.as<uint2>(), cap,
                                       nh.as<unsigned int>());
   CCG_LAUNCH_CHECK();
-  k_emit<T><<<grid, kBlock, 0, s>>>(g.n, g.rp, col, cl, pm, part, b, hub_limit, keys, cnt);
+  k_emit<T><<<egrid, kBlock, 0, s>>>(g.n, g.rp, col, cl, pm, part, b, hub_limit, keys, cnt);
   CCG_LAUNCH_CHECK();
-  k_emit_hubs<T><<<kSMs * 8, kBlock, 0, s>>>(g.rp, col, cl, pm, part, b, hubs.as<uint2>(), cap,
+  k_emit_hubs<T><<<kSMs * kEmitCtasPerSM, kBlock, 0, s>>>(g.rp, col, cl, pm, part, b, hubs.as<uint2>(), cap,
                                              nh.as<unsigned int>(), keys, cnt);
   CCG_LAUNCH_CHECK();
   c.toc(s, "contract_emit", t0, 8 * (g.n + 1) + g.m * ((uint64_t)g.idb + 4) + 4 * g.n);
