@@ -212,8 +212,6 @@ def workload_single(args, name):
     peak, _ = peaks()
     for algo, P, seq in [("exp", 1, 1), ("exp", 16, 1), ("exp", 16, 0), ("allreduce", 1, 1),
                          ("shortcuts", 1, 1), ("local", 1, 1)]:
-        if name == "rhg" and algo in ("shortcuts", "local") and args.rhg_log2n > 24:
-            continue
         ctx = cc.Context(0)
         solver = cc.SOLVERS[algo](cc.Config(seed=ALGO_SEED, sequential_limit=seq), 0, P, ctx)
         ms, kern, st = _timed_solves(solver, D, lab, args.steps, args.warmup, ctx)

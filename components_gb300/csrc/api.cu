@@ -213,7 +213,7 @@ struct Solver {
     {
       DevBuf k0(8 * G.n, s, pool), k1(8 * G.n, s, pool);
       ccg::local_sweeps(G, vid, seed, level, cl.as<uint32_t>(), k0.as<uint64_t>(),
-                        k1.as<uint64_t>(), s, c);
+                        k1.as<uint64_t>(), s, pool, c);
       note_level(level, G, 2);
     }
     ccg::Contracted H;
@@ -242,13 +242,14 @@ struct Solver {
     note_level(0, g, 0);
   }
 
-  // Caller graph as a trusted uint32 graph (ids copied and checked).
+  // Caller graph as a trusted uint32 graph: checked, and 64-bit ids narrowed
+  // into a copy (32-bit ids are used in place once the check has passed).
   Csr as_u32(const Csr &g, DevBuf &col32) {
-    col32.alloc(4 * (g.m ? g.m : 1), s, pool);
-    ccg::sanitize_ids(g, col32.as<uint32_t>(), s, c);
+    if (g.idb != 4) col32.alloc(4 * (g.m ? g.m : 1), s, pool);
+    ccg::sanitize_ids(g, g.idb != 4 ? col32.as<uint32_t>() : nullptr, s, c);
     check_err();
     Csr h = g;
-    h.col = col32.p;
+    if (g.idb != 4) h.col = col32.p;
     h.idb = 4;
     h.err = nullptr;
     return h;
@@ -815,7 +816,8 @@ int cc_debug_local_sweeps(const cc_csr *g, const uint32_t *vid, uint64_t seed, u
     cudaStream_t s = C->stream;
     Counters c;
     DevBuf k0(8 * (G.n ? G.n : 1), s, C->pool), k1(8 * (G.n ? G.n : 1), s, C->pool);
-    ccg::local_sweeps(G, vid, seed, level, cluster_out, k0.as<uint64_t>(), k1.as<uint64_t>(), s, c);
+    ccg::local_sweeps(G, vid, seed, level, cluster_out, k0.as<uint64_t>(), k1.as<uint64_t>(), s,
+                      C->pool, c);
     CCG_CUDA(cudaStreamSynchronize(s));
   });
 }

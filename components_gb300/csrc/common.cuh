@@ -203,4 +203,40 @@ __device__ __forceinline__ void warp_flag(int pred, int *flag) {
   if (b && (threadIdx.x & 31) == (unsigned)(__ffs(b) - 1)) atomicOr(flag, 1);
 }
 
+// Rows longer than a limit, as (row, piece) work items of kRowPiece entries:
+// the sweeps hand each item to one warp, so a hub row of a hundred thousand
+// entries is spread over many warps instead of holding one.
+constexpr uint64_t kRowPiece = 2048;
+inline uint64_t row_pieces_cap(uint64_t m, uint64_t limit) {
+  return m / (limit + 1) + m / kRowPiece + 2;
+}
+struct RowPieces {
+  uint2 *items;  // (row, piece index)
+  uint64_t cap;
+  unsigned int *count;
+};
+namespace {
+__global__ void k_row_pieces(uint64_t n, const uint64_t *__restrict__ rp, uint64_t limit,
+                             RowPieces rpc) {
+  for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < n;
+       v += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t d = rp[v + 1] - rp[v];
+    if (d <= limit) continue;
+    const uint32_t np = (uint32_t)((d + kRowPiece - 1) / kRowPiece);
+    const unsigned int slot = atomicAdd(rpc.count, np);
+    for (uint32_t q = 0; q < np && (uint64_t)slot + q < rpc.cap; ++q)
+      rpc.items[slot + q] = make_uint2((uint32_t)v, q);
+  }
+}
+}  // namespace
+// Entries [b, e) of work item h.
+__device__ __forceinline__ void row_piece(const RowPieces &rpc, const uint64_t *__restrict__ rp,
+                                          uint64_t h, uint32_t &v, uint64_t &b, uint64_t &e) {
+  const uint2 it = rpc.items[h];
+  v = it.x;
+  const uint64_t re = __ldg(rp + v + 1);
+  b = __ldg(rp + v) + (uint64_t)it.y * kRowPiece;
+  e = min(re, b + kRowPiece);
+}
+
 }  // namespace ccg

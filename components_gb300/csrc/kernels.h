@@ -110,9 +110,9 @@ constexpr int kGeoMax = 4096;
 int geo_table_build(double beta, std::vector<uint64_t> &t);
 void geo_table_upload(double beta, uint64_t *d_table, int *len_out, cudaStream_t s);
 
-// Copy of a caller CSR's ids as uint32 with bounds checks (ids < n, offsets
-// monotone and <= m); failures go to g.err.  Used before kernels that assume
-// a trusted uint32 graph.
+// Bounds checks of a caller CSR (ids < n, offsets monotone and <= m; failures
+// go to g.err) and, when col32 is given, a uint32 copy of its ids.  Used
+// before kernels that assume a trusted uint32 graph.
 void sanitize_ids(const Csr &g, uint32_t *col32, cudaStream_t s, Counters &c);
 
 // Exponential-shift decomposition on g (exponential_contraction.h:439-628).
@@ -128,7 +128,7 @@ int ldd_decompose(const Csr &g, const uint32_t *vid, uint64_t seed, uint32_t lev
 // [0,99], then two Jacobi sweeps of the lexicographic minimum over N[v].
 void local_sweeps(const Csr &g, const uint32_t *vid, uint64_t seed, uint32_t level,
                   uint32_t *cluster, uint64_t *k0, uint64_t *k1, cudaStream_t s,
-                  Counters &c);
+                  cudaMemPool_t pool, Counters &c);
 
 // ---- propagation kernels (prop.cu) -----------------------------------------
 // Min-label propagation rounds (propagation.h:72-149) on lab (in place).

@@ -94,7 +94,7 @@ __global__ void k_ldd_init(uint64_t n, const uint32_t *__restrict__ vid, uint64_
 }
 
 constexpr uint64_t kOne = 1ull << 32;
-constexpr uint64_t kRowLimit = 64;  // rows above this are relaxed warp-per-row
+constexpr uint64_t kRowLimit = 64;  // rows above this are relaxed a warp per piece
 
 // One Gauss-Seidel style sweep: key[v] <- min(key[v], min_w key[w] + 2^32).
 // Stale neighbour reads are upper bounds of the fixpoint, so in-place updates
@@ -119,17 +119,18 @@ __global__ void k_ldd_round(uint64_t n, const uint64_t *__restrict__ rp,
   warp_flag(changed, flag);
 }
 
-__global__ void k_ldd_round_hubs(const uint64_t *__restrict__ rp, const uint32_t *__restrict__ col,
-                                 const uint32_t *__restrict__ hubs,
-                                 const unsigned int *__restrict__ nh, uint64_t *key, int *flag) {
+// Rows above kRowLimit entries, one warp per piece of the row.
+__global__ void k_ldd_round_pieces(const uint64_t *__restrict__ rp, const uint32_t *__restrict__ col,
+                                   RowPieces rpc, uint64_t *key, int *flag) {
   const unsigned lane = threadIdx.x & 31;
   const uint64_t warp = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
   const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
-  const uint32_t nhubs = *nh;
+  const uint64_t ni = min((uint64_t)*rpc.count, rpc.cap);
   int changed = 0;
-  for (uint64_t h = warp; h < nhubs; h += nwarps) {
-    uint32_t v = hubs[h];
-    uint64_t b = __ldg(rp + v), e = __ldg(rp + v + 1);
+  for (uint64_t h = warp; h < ni; h += nwarps) {
+    uint32_t v;
+    uint64_t b, e;
+    row_piece(rpc, rp, h, v, b, e);
     uint64_t best = ~0ull;
     for (uint64_t j = b + lane; j < e; j += 32) {
       uint64_t kw = ld_cg(key + __ldg(col + j)) + kOne;
@@ -149,13 +150,6 @@ __global__ void k_ldd_round_hubs(const uint64_t *__restrict__ rp, const uint32_t
     }
   }
   warp_flag(changed, flag);
-}
-
-__global__ void k_list_rows(uint64_t n, const uint64_t *__restrict__ rp, uint64_t limit,
-                            uint32_t *__restrict__ hubs, unsigned int *__restrict__ nh) {
-  for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < n;
-       v += (uint64_t)gridDim.x * blockDim.x)
-    if (rp[v + 1] - rp[v] > limit) hubs[atomicAdd(nh, 1u)] = (uint32_t)v;
 }
 
 // Start-time gated round t (RunContractionBFS, exponential_contraction.h:
@@ -195,7 +189,9 @@ __global__ void k_local_init(uint64_t n, const uint32_t *__restrict__ vid, uint6
   }
 }
 
-// Jacobi sweep: out[v] = min over N[v] (closed neighbourhood) of in[].
+// Jacobi sweep: out[v] = min over N[v] (closed neighbourhood) of in[].  Rows
+// above kRowLimit entries only store in[v] here; k_min_sweep_pieces folds
+// their neighbours in afterwards, one warp per piece of the row.
 __global__ void k_min_sweep(uint64_t n, const uint64_t *__restrict__ rp,
                             const uint32_t *__restrict__ col, const uint64_t *__restrict__ in,
                             uint64_t *__restrict__ out) {
@@ -203,11 +199,37 @@ __global__ void k_min_sweep(uint64_t n, const uint64_t *__restrict__ rp,
        v += (uint64_t)gridDim.x * blockDim.x) {
     uint64_t b = __ldg(rp + v), e = __ldg(rp + v + 1);
     uint64_t best = in[v];
-    for (uint64_t j = b; j < e; ++j) {
-      uint64_t kw = __ldg(in + __ldg(col + j));
-      best = kw < best ? kw : best;
+    if (e - b <= kRowLimit) {
+      for (uint64_t j = b; j < e; ++j) {
+        uint64_t kw = __ldg(in + __ldg(col + j));
+        best = kw < best ? kw : best;
+      }
     }
     out[v] = best;
+  }
+}
+
+__global__ void k_min_sweep_pieces(const uint64_t *__restrict__ rp, const uint32_t *__restrict__ col,
+                                   RowPieces rpc, const uint64_t *__restrict__ in, uint64_t *out) {
+  const unsigned lane = threadIdx.x & 31;
+  const uint64_t warp = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
+  const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+  const uint64_t ni = min((uint64_t)*rpc.count, rpc.cap);
+  for (uint64_t h = warp; h < ni; h += nwarps) {
+    uint32_t v;
+    uint64_t b, e;
+    row_piece(rpc, rp, h, v, b, e);
+    uint64_t best = ~0ull;
+    for (uint64_t j = b + lane; j < e; j += 32) {
+      const uint64_t kw = __ldg(in + __ldg(col + j));
+      best = kw < best ? kw : best;
+    }
+#pragma unroll
+    for (int o = 16; o; o >>= 1) {
+      const uint64_t y = __shfl_xor_sync(0xffffffffu, best, o);
+      best = y < best ? y : best;
+    }
+    if (lane == 0) atomicMin(reinterpret_cast<unsigned long long *>(out + v), (unsigned long long)best);
   }
 }
 
@@ -251,10 +273,11 @@ int ldd_decompose(const Csr &g, const uint32_t *vid, uint64_t seed, uint32_t lev
     // every vertex is final once; every edge pushed once
     c.add(rounds, 8 * (g.n + 1) + g.m * 4 + g.m * 8 + (uint64_t)rounds * g.n * 8);
   } else {
-    DevBuf hubs(4 * (g.m / (kRowLimit + 1) + 1), s, pool), nh(4, s, pool);
-    CCG_CUDA(cudaMemsetAsync(nh.p, 0, 4, s));
-    k_list_rows<<<grid, kBlock, 0, s>>>(g.n, g.rp, kRowLimit, hubs.as<uint32_t>(),
-                                        nh.as<unsigned int>());
+    const uint64_t cap = row_pieces_cap(g.m, kRowLimit);
+    DevBuf items(8 * cap, s, pool), cnt(4, s, pool);
+    CCG_CUDA(cudaMemsetAsync(cnt.p, 0, 4, s));
+    const RowPieces rpc{items.as<uint2>(), cap, cnt.as<unsigned int>()};
+    k_row_pieces<<<grid, kBlock, 0, s>>>(g.n, g.rp, kRowLimit, rpc);
     CCG_LAUNCH_CHECK();
     for (;;) {
       if (rounds >= max_rounds) return -1;
@@ -263,8 +286,7 @@ int ldd_decompose(const Csr &g, const uint32_t *vid, uint64_t seed, uint32_t lev
       cudaEvent_t t0 = c.tic(s);
       k_ldd_round<<<grid, kBlock, 0, s>>>(g.n, g.rp, col, key, dev_flag);
       CCG_LAUNCH_CHECK();
-      k_ldd_round_hubs<<<kSMs * 4, kBlock, 0, s>>>(g.rp, col, hubs.as<uint32_t>(),
-                                                   nh.as<unsigned int>(), key, dev_flag);
+      k_ldd_round_pieces<<<kSMs * 8, kBlock, 0, s>>>(g.rp, col, rpc, key, dev_flag);
       CCG_LAUNCH_CHECK();
       c.toc(s, "ldd_round", t0, round_bytes);
       CCG_CUDA(cudaMemcpyAsync((void *)host_flag, dev_flag, sizeof(int), cudaMemcpyDeviceToHost, s));
@@ -281,20 +303,33 @@ int ldd_decompose(const Csr &g, const uint32_t *vid, uint64_t seed, uint32_t lev
 }
 
 void local_sweeps(const Csr &g, const uint32_t *vid, uint64_t seed, uint32_t level,
-                  uint32_t *cluster, uint64_t *k0, uint64_t *k1, cudaStream_t s, Counters &c) {
+                  uint32_t *cluster, uint64_t *k0, uint64_t *k1, cudaStream_t s, cudaMemPool_t pool,
+                  Counters &c) {
   if (g.n == 0) return;
   const uint32_t *col = static_cast<const uint32_t *>(g.col);
   unsigned grid = grid_for(g.n, kBlock, kSMs * 32);
+  const uint64_t cap = row_pieces_cap(g.m, kRowLimit);
+  DevBuf items(8 * cap, s, pool), cnt(4, s, pool);
+  CCG_CUDA(cudaMemsetAsync(cnt.p, 0, 4, s));
+  const RowPieces rpc{items.as<uint2>(), cap, cnt.as<unsigned int>()};
   k_local_init<<<grid, kBlock, 0, s>>>(g.n, vid, seed, level, k0);
   CCG_LAUNCH_CHECK();
-  k_min_sweep<<<grid, kBlock, 0, s>>>(g.n, g.rp, col, k0, k1);  // N(v)
+  cudaEvent_t t0 = c.tic(s);
+  k_row_pieces<<<grid, kBlock, 0, s>>>(g.n, g.rp, kRowLimit, rpc);
   CCG_LAUNCH_CHECK();
-  k_min_sweep<<<grid, kBlock, 0, s>>>(g.n, g.rp, col, k1, k0);  // N(N(v))
-  CCG_LAUNCH_CHECK();
+  for (int r = 0; r < 2; ++r) {  // N(v), then N(N(v))
+    const uint64_t *in = r ? k1 : k0;
+    uint64_t *out = r ? k0 : k1;
+    k_min_sweep<<<grid, kBlock, 0, s>>>(g.n, g.rp, col, in, out);
+    CCG_LAUNCH_CHECK();
+    k_min_sweep_pieces<<<kSMs * 8, kBlock, 0, s>>>(g.rp, col, rpc, in, out);
+    CCG_LAUNCH_CHECK();
+  }
+  const uint64_t sweep = 8 * (g.n + 1) + g.m * 4 + g.m * 8 + 2 * g.n * 8;
+  c.toc(s, "local_sweeps", t0, 2 * sweep);
   k_low_word<<<grid, kBlock, 0, s>>>(g.n, k0, cluster);
   CCG_LAUNCH_CHECK();
-  const uint64_t sweep = 8 * (g.n + 1) + g.m * 4 + g.m * 8 + 2 * g.n * 8;
-  c.add(4, 12 * g.n + 2 * sweep + 12 * g.n);
+  c.add(6, 12 * g.n + 2 * sweep + 12 * g.n);
 }
 
 }  // namespace ccg

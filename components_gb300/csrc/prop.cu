@@ -7,13 +7,6 @@ namespace {
 
 constexpr uint64_t kRowLimit = 64;
 
-__global__ void k_rows_over(uint64_t n, const uint64_t *__restrict__ rp, uint64_t limit,
-                            uint32_t *__restrict__ rows, unsigned int *__restrict__ nr) {
-  for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < n;
-       v += (uint64_t)gridDim.x * blockDim.x)
-    if (rp[v + 1] - rp[v] > limit) rows[atomicAdd(nr, 1u)] = (uint32_t)v;
-}
-
 // ---- Propagation (propagation.h:72-149) ------------------------------------
 // lab[v] <- min(lab[v], min_u lab[u]) in place.  The reference updates local
 // vertices in place during a sweep (SetVertexPayload) and sees ghosts from
@@ -38,17 +31,19 @@ __global__ void k_labels_round(uint64_t n, const uint64_t *__restrict__ rp,
   warp_flag(changed, flag);
 }
 
-__global__ void k_labels_round_rows(const uint64_t *__restrict__ rp, const uint32_t *__restrict__ col,
-                                    const uint32_t *__restrict__ rows,
-                                    const unsigned int *__restrict__ nr, uint32_t *lab, int *flag) {
+// Rows above kRowLimit entries, one warp per piece of the row.
+__global__ void k_labels_round_pieces(const uint64_t *__restrict__ rp,
+                                      const uint32_t *__restrict__ col, RowPieces rpc, uint32_t *lab,
+                                      int *flag) {
   const unsigned lane = threadIdx.x & 31;
   const uint64_t warp = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
   const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
-  const uint32_t cnt = *nr;
+  const uint64_t ni = min((uint64_t)*rpc.count, rpc.cap);
   int changed = 0;
-  for (uint64_t h = warp; h < cnt; h += nwarps) {
-    uint32_t v = rows[h];
-    uint64_t b = __ldg(rp + v), e = __ldg(rp + v + 1);
+  for (uint64_t h = warp; h < ni; h += nwarps) {
+    uint32_t v;
+    uint64_t b, e;
+    row_piece(rpc, rp, h, v, b, e);
     uint32_t best = kNone;
     for (uint64_t j = b + lane; j < e; j += 32) {
       uint32_t x = ld_cg(lab + __ldg(col + j));
@@ -77,28 +72,33 @@ __global__ void k_sc_min(uint64_t n, const uint64_t *__restrict__ rp,
   for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < n;
        v += (uint64_t)gridDim.x * blockDim.x) {
     uint64_t b = __ldg(rp + v), e = __ldg(rp + v + 1);
-    if (e - b > kRowLimit) continue;
     uint32_t l = f[v], best = l;
-    for (uint64_t j = b; j < e; ++j) {
-      uint32_t x = __ldg(f + __ldg(col + j));
-      best = x < best ? x : best;
+    if (e - b <= kRowLimit) {  // longer rows: k_sc_min_pieces folds their neighbours in
+      for (uint64_t j = b; j < e; ++j) {
+        uint32_t x = __ldg(f + __ldg(col + j));
+        best = x < best ? x : best;
+      }
     }
     nf[v] = best;
     if (best < l) atomicMin(upd + l, best);
   }
 }
 
-__global__ void k_sc_min_rows(const uint64_t *__restrict__ rp, const uint32_t *__restrict__ col,
-                              const uint32_t *__restrict__ rows, const unsigned int *__restrict__ nr,
-                              const uint32_t *__restrict__ f, uint32_t *__restrict__ nf,
-                              uint32_t *__restrict__ upd) {
+// Rows above kRowLimit entries, one warp per piece of the row: each piece's
+// minimum is folded into nf[v] (which k_sc_min set to f[v]) and, when it is
+// below v's label, into the update addressed to that label; the minima over
+// pieces are the row's minimum, so nf and upd end as with one pass per row.
+__global__ void k_sc_min_pieces(const uint64_t *__restrict__ rp, const uint32_t *__restrict__ col,
+                                RowPieces rpc, const uint32_t *__restrict__ f, uint32_t *nf,
+                                uint32_t *upd) {
   const unsigned lane = threadIdx.x & 31;
   const uint64_t warp = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
   const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
-  const uint32_t cnt = *nr;
-  for (uint64_t h = warp; h < cnt; h += nwarps) {
-    uint32_t v = rows[h];
-    uint64_t b = __ldg(rp + v), e = __ldg(rp + v + 1);
+  const uint64_t ni = min((uint64_t)*rpc.count, rpc.cap);
+  for (uint64_t h = warp; h < ni; h += nwarps) {
+    uint32_t v;
+    uint64_t b, e;
+    row_piece(rpc, rp, h, v, b, e);
     uint32_t best = kNone;
     for (uint64_t j = b + lane; j < e; j += 32) {
       uint32_t x = __ldg(f + __ldg(col + j));
@@ -106,10 +106,11 @@ __global__ void k_sc_min_rows(const uint64_t *__restrict__ rp, const uint32_t *_
     }
     best = __reduce_min_sync(0xffffffffu, best);
     if (lane == 0) {
-      uint32_t l = f[v];
-      best = best < l ? best : l;
-      nf[v] = best;
-      if (best < l) atomicMin(upd + l, best);
+      const uint32_t l = f[v];
+      if (best < l) {
+        atomicMin(nf + v, best);
+        atomicMin(upd + l, best);
+      }
     }
   }
 }
@@ -210,10 +211,11 @@ int labels_propagate(const Csr &g, uint32_t *lab, int max_rounds, cudaStream_t s
   if (g.n == 0) return 0;
   const uint32_t *col = static_cast<const uint32_t *>(g.col);
   unsigned grid = grid_for(g.n, kBlock, kSMs * 32);
-  DevBuf rows(4 * (g.m / (kRowLimit + 1) + 1), s, pool), nr(4, s, pool);
-  CCG_CUDA(cudaMemsetAsync(nr.p, 0, 4, s));
-  k_rows_over<<<grid, kBlock, 0, s>>>(g.n, g.rp, kRowLimit, rows.as<uint32_t>(),
-                                      nr.as<unsigned int>());
+  const uint64_t cap = row_pieces_cap(g.m, kRowLimit);
+  DevBuf items(8 * cap, s, pool), cnt(4, s, pool);
+  CCG_CUDA(cudaMemsetAsync(cnt.p, 0, 4, s));
+  const RowPieces rpc{items.as<uint2>(), cap, cnt.as<unsigned int>()};
+  k_row_pieces<<<grid, kBlock, 0, s>>>(g.n, g.rp, kRowLimit, rpc);
   CCG_LAUNCH_CHECK();
   int rounds = 0;
   const uint64_t round_bytes = 8 * (g.n + 1) + g.m * 4 + g.m * 4 + 2 * g.n * 4;
@@ -223,8 +225,7 @@ int labels_propagate(const Csr &g, uint32_t *lab, int max_rounds, cudaStream_t s
     cudaEvent_t t0 = c.tic(s);
     k_labels_round<<<grid, kBlock, 0, s>>>(g.n, g.rp, col, lab, dev_flag);
     CCG_LAUNCH_CHECK();
-    k_labels_round_rows<<<kSMs * 4, kBlock, 0, s>>>(g.rp, col, rows.as<uint32_t>(),
-                                                    nr.as<unsigned int>(), lab, dev_flag);
+    k_labels_round_pieces<<<kSMs * 8, kBlock, 0, s>>>(g.rp, col, rpc, lab, dev_flag);
     CCG_LAUNCH_CHECK();
     c.toc(s, "labels_round", t0, round_bytes);
     CCG_CUDA(cudaMemcpyAsync((void *)host_flag, dev_flag, sizeof(int), cudaMemcpyDeviceToHost, s));
@@ -243,16 +244,17 @@ int shortcut_propagate(const Csr &g, uint32_t *lab, uint32_t hitters, int max_ro
   const uint32_t *col = static_cast<const uint32_t *>(g.col);
   unsigned grid = grid_for(g.n, kBlock, kSMs * 32);
   DevBuf nfb(4 * g.n, s, pool), updb(4 * g.n, s, pool);
-  DevBuf rows(4 * (g.m / (kRowLimit + 1) + 1), s, pool), nr(4, s, pool);
+  const uint64_t cap = row_pieces_cap(g.m, kRowLimit);
+  DevBuf items(8 * cap, s, pool), npieces(4, s, pool);
+  const RowPieces rpc{items.as<uint2>(), cap, npieces.as<unsigned int>()};
   DevBuf cnt, heavy;
   if (hitters) {
     cnt.alloc(4 * g.n, s, pool);
     heavy.alloc(g.n, s, pool);
     CCG_CUDA(cudaMemsetAsync(heavy.p, 0, g.n, s));
   }
-  CCG_CUDA(cudaMemsetAsync(nr.p, 0, 4, s));
-  k_rows_over<<<grid, kBlock, 0, s>>>(g.n, g.rp, kRowLimit, rows.as<uint32_t>(),
-                                      nr.as<unsigned int>());
+  CCG_CUDA(cudaMemsetAsync(npieces.p, 0, 4, s));
+  k_row_pieces<<<grid, kBlock, 0, s>>>(g.n, g.rp, kRowLimit, rpc);
   CCG_LAUNCH_CHECK();
   uint32_t *f = lab, *nf = nfb.as<uint32_t>();
   int rounds = 0;
@@ -262,8 +264,7 @@ int shortcut_propagate(const Csr &g, uint32_t *lab, uint32_t hitters, int max_ro
     cudaEvent_t t0 = c.tic(s);
     k_sc_min<<<grid, kBlock, 0, s>>>(g.n, g.rp, col, f, nf, updb.as<uint32_t>());
     CCG_LAUNCH_CHECK();
-    k_sc_min_rows<<<kSMs * 4, kBlock, 0, s>>>(g.rp, col, rows.as<uint32_t>(), nr.as<unsigned int>(),
-                                              f, nf, updb.as<uint32_t>());
+    k_sc_min_pieces<<<kSMs * 8, kBlock, 0, s>>>(g.rp, col, rpc, f, nf, updb.as<uint32_t>());
     CCG_LAUNCH_CHECK();
     if (hitters) {
       CCG_CUDA(cudaMemsetAsync(cnt.p, 0, 4 * g.n, s));

@@ -884,23 +884,24 @@ __global__ void k_widen(const uint32_t *__restrict__ in, OUT *__restrict__ out, 
     out[v] = (OUT)in[v];
 }
 
-// uint32 copy of the ids with the same checks as the hook kernels; a bad id
-// becomes the row's own vertex (a self-loop, ignored by every kernel).
+// The caller's offsets and ids checked (a bad one is recorded in the error
+// word, and the solve stops before anything reads the graph again); 64-bit
+// ids are also narrowed into a uint32 copy (out, else null).  Offsets and ids
+// are two flat grid-stride loops: a hub row costs no more than any other
+// stretch of entries.
 template <class T>
 __global__ void k_sanitize(uint64_t n, uint64_t m, const uint64_t *__restrict__ rp,
                            const T *__restrict__ col, uint32_t *__restrict__ out, int *err) {
-  for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < n;
-       v += (uint64_t)gridDim.x * blockDim.x) {
-    Row r;
-    if (!load_row(rp, v, m, err, r)) continue;
-    for (uint64_t k = r.b; k < r.e; ++k) {
-      uint64_t u = (uint64_t)__ldg(col + k);
-      if (u >= n) {
-        set_err(err, kErrBadId);
-        u = v;
-      }
-      out[k] = (uint32_t)u;
-    }
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  const uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+  for (uint64_t v = t; v < n; v += stride) {
+    const uint64_t b = __ldg(rp + v), e = __ldg(rp + v + 1);
+    if (e < b || e > m) set_err(err, kErrBadOffsets);
+  }
+  for (uint64_t k = t; k < m; k += stride) {
+    const uint64_t u = (uint64_t)__ldg(col + k);
+    if (u >= n) set_err(err, kErrBadId);
+    if (out) out[k] = (uint32_t)u;
   }
 }
 
@@ -1371,7 +1372,7 @@ void widen_labels(const uint32_t *in, void *out, int out_bytes, uint64_t n, cuda
 
 void sanitize_ids(const Csr &g, uint32_t *col32, cudaStream_t s, Counters &c) {
   if (g.n == 0) return;
-  unsigned grid = grid_for(g.n, kBlock, kSMs * 32);
+  unsigned grid = grid_for(std::max(g.n, g.m), kBlock, kSMs * 32);
   if (g.idb == 8)
     k_sanitize<uint64_t><<<grid, kBlock, 0, s>>>(g.n, g.m, g.rp,
                                                  static_cast<const uint64_t *>(g.col), col32, g.err);
@@ -1379,7 +1380,7 @@ void sanitize_ids(const Csr &g, uint32_t *col32, cudaStream_t s, Counters &c) {
     k_sanitize<uint32_t><<<grid, kBlock, 0, s>>>(g.n, g.m, g.rp,
                                                  static_cast<const uint32_t *>(g.col), col32, g.err);
   CCG_LAUNCH_CHECK();
-  c.add(1, 8 * (g.n + 1) + g.m * ((uint64_t)g.idb + 4));
+  c.add(1, 8 * (g.n + 1) + g.m * ((uint64_t)g.idb + (col32 ? 4 : 0)));
 }
 
 }  // namespace ccg
