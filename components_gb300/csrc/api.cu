@@ -119,6 +119,14 @@ void check_csr_args(const cc_csr *g) {
     throw Error(CC_ERR_UNSUPPORTED, "n >= 2^32-1 vertices is not supported (uint32 labels inside)");
   if (g->n > 0 && !g->row_ptr) throw Error(CC_ERR_INVALID, "row_ptr is NULL");
   if (g->m_dir > 0 && !g->col) throw Error(CC_ERR_INVALID, "col is NULL");
+  // the kernels load device offsets and ids as whole words (and ids in
+  // 16-byte vectors from the first 16-byte boundary on); host arrays are
+  // copied into fresh device buffers first
+  if (g->where == CC_DEVICE) {
+    if ((uintptr_t)g->row_ptr % 8 != 0) throw Error(CC_ERR_INVALID, "row_ptr is not 8-byte aligned");
+    if ((uintptr_t)g->col % g->id_bytes != 0)
+      throw Error(CC_ERR_INVALID, "col is not aligned to id_bytes");
+  }
 }
 
 // Round cap of the iterative loops.  After r rounds every key (label) is at

@@ -890,6 +890,12 @@ __global__ void k_widen(const uint32_t *__restrict__ in, OUT *__restrict__ out, 
 // are two flat grid-stride loops: a hub row costs no more than any other
 // stretch of entries.
 template <class T>
+__device__ __forceinline__ void sanitize_one(uint64_t k, uint64_t u, uint64_t n,
+                                             uint32_t *__restrict__ out, int *err) {
+  if (u >= n) set_err(err, kErrBadId);
+  if (out) out[k] = (uint32_t)u;
+}
+template <class T>
 __global__ void k_sanitize(uint64_t n, uint64_t m, const uint64_t *__restrict__ rp,
                            const T *__restrict__ col, uint32_t *__restrict__ out, int *err) {
   const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
@@ -898,11 +904,23 @@ __global__ void k_sanitize(uint64_t n, uint64_t m, const uint64_t *__restrict__ 
     const uint64_t b = __ldg(rp + v), e = __ldg(rp + v + 1);
     if (e < b || e > m) set_err(err, kErrBadOffsets);
   }
-  for (uint64_t k = t; k < m; k += stride) {
-    const uint64_t u = (uint64_t)__ldg(col + k);
-    if (u >= n) set_err(err, kErrBadId);
-    if (out) out[k] = (uint32_t)u;
+  // ids in 16-byte loads from the first 16-byte boundary on; the entries
+  // before it and after the last whole vector one at a time
+  constexpr uint64_t kVec = 16 / sizeof(T);
+  const uint64_t mis = ((uintptr_t)col & 15) / sizeof(T);
+  const uint64_t head = min(m, mis ? kVec - mis : 0);
+  const uint64_t nvec = (m - head) / kVec;
+  const uint4 *vcol = reinterpret_cast<const uint4 *>(col + head);
+  for (uint64_t q = t; q < nvec; q += stride) {
+    const uint4 w = __ldg(vcol + q);
+    const T *x = reinterpret_cast<const T *>(&w);
+    const uint64_t k0 = head + q * kVec;
+#pragma unroll
+    for (uint64_t j = 0; j < kVec; ++j) sanitize_one<T>(k0 + j, (uint64_t)x[j], n, out, err);
   }
+  for (uint64_t k = t; k < head; k += stride) sanitize_one<T>(k, (uint64_t)__ldg(col + k), n, out, err);
+  for (uint64_t k = head + nvec * kVec + t; k < m; k += stride)
+    sanitize_one<T>(k, (uint64_t)__ldg(col + k), n, out, err);
 }
 
 template <class T, bool PART>
@@ -1372,7 +1390,7 @@ void widen_labels(const uint32_t *in, void *out, int out_bytes, uint64_t n, cuda
 
 void sanitize_ids(const Csr &g, uint32_t *col32, cudaStream_t s, Counters &c) {
   if (g.n == 0) return;
-  unsigned grid = grid_for(std::max(g.n, g.m), kBlock, kSMs * 32);
+  unsigned grid = grid_for(std::max(g.n, g.m / 4), kBlock, kSMs * 32);
   if (g.idb == 8)
     k_sanitize<uint64_t><<<grid, kBlock, 0, s>>>(g.n, g.m, g.rp,
                                                  static_cast<const uint64_t *>(g.col), col32, g.err);

@@ -95,6 +95,16 @@ def test_strerror_and_invalid_args_need_no_gpu():
     assert lib.cc_csr_validate(C.byref(g), 0) == _lib.CC_ERR_INVALID
 
 
+def test_misaligned_device_arrays_are_rejected_before_any_device_call():
+    lib = _lib.gpu()
+    g = _lib.cc_csr(2, 2, 0x1000, 0x2002, 4, 1, _lib.CC_DEVICE, 0)  # col 2 bytes past a word
+    assert lib.cc_csr_validate(C.byref(g), 0) == _lib.CC_ERR_INVALID
+    g = _lib.cc_csr(2, 2, 0x1004, 0x2000, 4, 1, _lib.CC_DEVICE, 0)  # offsets not 8-byte aligned
+    assert lib.cc_csr_validate(C.byref(g), 0) == _lib.CC_ERR_INVALID
+    g = _lib.cc_csr(2, 2, 0x1000, 0x2004, 8, 1, _lib.CC_DEVICE, 0)  # 64-bit ids 4 bytes off
+    assert lib.cc_csr_validate(C.byref(g), 0) == _lib.CC_ERR_INVALID
+
+
 def test_host_validation():
     lib = _lib.gpu()
     rp = np.array([0, 1, 2], np.uint64)

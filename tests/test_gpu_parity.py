@@ -138,6 +138,38 @@ def test_invalid_ids_are_reported_not_faulted(cuda):
     assert np.array_equal(gpu_labels(good, "exp", 1), [0, 0, 2, 2])
 
 
+@pytest.mark.parametrize("idb", [4, 8])
+def test_id_check_at_every_offset_of_col(cuda, idb):
+    """The propagation options check ids in 16-byte vectors from the first
+    16-byte boundary of col on: labels are right and a bad id is reported
+    wherever it sits (before that boundary, inside a vector, after the last
+    whole vector), for col starting at every id offset from a boundary."""
+    import torch
+    G = cc.gen_gnm(300, 700, seed=5, id_bytes=idb)
+    want = oracle.uf_labels(G)
+    dt = torch.int32 if idb == 4 else torch.int64
+    rp = torch.from_numpy(G.row_ptr.view(np.int64)).to("cuda:0")
+    ids = torch.from_numpy(np.ascontiguousarray(G.col).view(np.int32 if idb == 4 else np.int64))
+    for shift in range(16 // idb):
+        buf = torch.zeros(G.m + 16, dtype=dt, device="cuda:0")
+        col = buf[shift:shift + G.m]
+        col.copy_(ids.to("cuda:0"))
+        D = StaticGraph(rp, col)
+        for algo in ("shortcuts", "labels", "local"):
+            lab = torch.full((G.n,), -1, dtype=dt, device="cuda:0")
+            cc.SOLVERS[algo](cc.Config(seed=1001), 0, 1).FindComponents(D, lab)
+            got = lab.cpu().numpy().view(np.uint32 if idb == 4 else np.uint64).astype(np.uint64)
+            assert np.array_equal(got, want), (shift, algo)
+        for pos in (0, 1, 2, G.m // 2, G.m - 2, G.m - 1):
+            old = int(col[pos].item())
+            col[pos] = G.n + 7
+            lab = torch.full((G.n,), -1, dtype=dt, device="cuda:0")
+            with pytest.raises(_lib.CCError) as ei:
+                cc.SOLVERS["shortcuts"](cc.Config(seed=1001), 0, 1).FindComponents(D, lab)
+            assert ei.value.status == _lib.CC_ERR_INVALID, (shift, pos)
+            col[pos] = old
+
+
 def test_context_reuse_and_stats(cuda):
     ctx = cc.Context(0, profiling=True)
     G = cc.gen_grid(300, 200, 0.5, seed=3)
