@@ -73,8 +73,11 @@ def test_ldd_on_grid_and_hub(cuda):
 
 def test_local_sweeps_match_oracle(cuda):
     import torch
-    for seed, (n, m) in enumerate([(500, 900), (5000, 20000)]):
-        G = cc.gen_gnm(n, m, seed=seed + 3, id_bytes=4)
+    hubs = cc.from_edges(9000, [(h, i) for h in (4, 700, 8000) for i in range(0, 9000, 1 + h % 3)
+                                if i != h] + [(1, 2), (2, 3)])  # rows of 3000-9000 entries: pieces
+    for seed, G in enumerate([cc.gen_gnm(500, 900, seed=3, id_bytes=4),
+                              cc.gen_gnm(5000, 20000, seed=4, id_bytes=4), hubs]):
+        n = G.n
         vid = np.arange(n, dtype=np.uint64) * 2 + 5
         D, g = _dev(G)
         v = _t(vid.astype(np.uint32), np.int32)
@@ -121,6 +124,25 @@ def test_contraction_matches_oracle(cuda):
         assert np.array_equal(vid_g.astype(np.uint64), vid_w)
         nw = np.where(newid_w == np.uint64(2**64 - 1), np.uint64(0xFFFFFFFF), newid_w)
         assert np.array_equal(newid_g.astype(np.uint64), nw)
+
+
+def test_contraction_with_repeated_keys_matches_oracle(cuda):
+    """Few clusters: almost every cut key repeats, so the emit kernels' set of
+    written keys drops most of them before the sort (a hub row of 6000
+    entries takes the piece-per-warp kernel); the quotient graph is the
+    oracle's."""
+    rng = np.random.default_rng(11)
+    n = 20000
+    e = rng.integers(0, n, size=(200000, 2))
+    hub = np.stack([np.zeros(6000, np.int64), np.arange(1, 6001)], axis=1)
+    G = cc.from_edges(n, np.concatenate([e, hub]))
+    for ncl in (2, 3, 40):
+        cl = rng.integers(0, ncl, n).astype(np.uint64)
+        rp_w, col_w, vid_w, newid_w = oracle.contract(G, cl, ncl)
+        rp_g, col_g, vid_g, newid_g = gpu_contract(G, cl, ncl)
+        assert np.array_equal(rp_g, rp_w), ncl
+        assert np.array_equal(col_g.astype(np.uint64), col_w), ncl
+        assert np.array_equal(vid_g.astype(np.uint64), vid_w), ncl
 
 
 def test_cut_graph_matches_oracle(cuda):
