@@ -71,7 +71,9 @@ typedef struct cc_csr {
   const void *col;          /* m_dir neighbour ids, id_bytes each */
   uint32_t id_bytes;        /* 4 (uint32 ids) or 8 (uint64 ids) */
   uint32_t num_parts;       /* virtual ranks P >= 1 */
-  uint32_t where;           /* CC_HOST or CC_DEVICE for row_ptr and col */
+  uint32_t where;           /* CC_HOST or CC_DEVICE for row_ptr and col; device row_ptr
+                               8-byte aligned and col aligned to id_bytes, else
+                               CC_ERR_INVALID before any launch */
   uint32_t reserved;        /* must be 0 */
 } cc_csr;
 
