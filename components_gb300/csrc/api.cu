@@ -102,6 +102,7 @@ void ctx_free(cc_ctx *c) {
     cudaStreamSynchronize(c->copy_stream);
     cudaStreamDestroy(c->copy_stream);
   }
+  c->stager.reset();  // joins the host threads, frees the page-locked staging
   if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
   for (auto &e : c->ev)
     if (e) cudaEventDestroy(e);
@@ -481,6 +482,10 @@ int ctx_run(cc_ctx *C, const cc_csr *g, cc_algo algo, const cc_config *cfg_in, u
         streamed = dc.tiles;
       }
     }
+    if (streamed) {
+      if (!C->stager) C->stager.reset(new ccg::HostStager());
+      hsrc.stager = C->stager.get();
+    }
     if (g->where == CC_HOST) {
       rp_d.alloc(8 * (n + 1), s, C->pool);
       col_d.alloc((size_t)idb * (m ? m : 1), s, C->pool);
@@ -521,6 +526,7 @@ int ctx_run(cc_ctx *C, const cc_csr *g, cc_algo algo, const cc_config *cfg_in, u
     S.uf.cache = &C->uf_cache;
     if (streamed) S.hs = &hsrc;
     S.run(algo, G, g->num_parts, lab);
+    if (streamed) st.h2d_bytes = hsrc.h2d_bytes;  // offsets partly sent as degree bytes
     CCG_CUDA(cudaEventRecord(ev[2], s));
     DevBuf cnt(8, s, C->pool);
     if (C->prof_count) ccg::count_roots(lab, n, cnt.as<unsigned long long>(), s, c);

@@ -6,6 +6,7 @@
 #include <string>
 #include <vector>
 
+#include "hostpool.h"
 #include "kernels.h"
 
 namespace ccg {
@@ -36,6 +37,8 @@ struct cc_ctx {
   cc_stats prof_total{};      // per-kernel sums over the solves since profiling was switched on
   uint64_t prof_solves = 0;
   ccg::BatchCache *batch = nullptr;  // last recorded batch solve (CUDA graph)
+  // host threads and page-locked staging of the streamed input (made on first use)
+  std::unique_ptr<ccg::HostStager> stager;
 };
 
 namespace ccg {

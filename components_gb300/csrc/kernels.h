@@ -49,12 +49,15 @@ struct UfTuning {
 // Host source of a caller graph whose device buffers are still empty: the
 // tiled pass copies tile-aligned chunks on `copy` and overlaps them with the
 // tile kernel (rp/col of the Csr are the destination device buffers).
+struct HostStager;
 struct HostSource {
   const uint64_t *rp;
   const void *col;
   cudaStream_t copy;
   void *labels_out = nullptr;  // host uint32 labels: each chunk is copied out on `copy`
                                // as soon as the final compression has finished it
+  HostStager *stager = nullptr;  // when set: rows below 255 entries go as degree bytes
+  mutable uint64_t h2d_bytes = 0;  // bytes the streamed pass copied to the device
 };
 void uf_components(const Csr &g, uint32_t *parent, const PartMap *pm,
                    const UfTuning &tu, cudaStream_t s, cudaMemPool_t pool,
@@ -76,6 +79,11 @@ void widen_labels(const uint32_t *in, void *out, int out_bytes, uint64_t n,
 // ---- scan / radix sort / component graph (sortcsr.cu) ----------------------
 // Stable LSD radix sort of uint64 keys on bits [0, bits); returns the buffer
 // (keys or tmp) that holds the result.
+// Row offsets rp[0 .. count] of `count` rows from their degree bytes:
+// rp[0] = base, rp[i + 1] = base + deg[0] + ... + deg[i] (the sum of one call
+// must stay below 2^32).
+void offsets_from_degrees(const uint8_t *deg, uint64_t count, uint64_t base, uint64_t *rp,
+                          cudaStream_t s, cudaMemPool_t pool, Counters &c);
 uint64_t *radix_sort_u64(uint64_t *keys, uint64_t *tmp, uint64_t n, int bits,
                          cudaStream_t s, cudaMemPool_t pool, Counters &c);
 

@@ -541,6 +541,27 @@ void emit_keys(const Csr &g, const uint32_t *cl, const PartMap &pm, bool part, i
 
 }  // namespace
 
+namespace {
+struct GetDeg {
+  const uint8_t *d;
+  __device__ uint32_t operator()(uint64_t i) const { return d[i]; }
+};
+struct PutOffset {
+  uint64_t *rp;
+  uint64_t base;
+  __device__ void operator()(uint64_t i, uint32_t excl, uint32_t f) const {
+    rp[i + 1] = base + excl + f;
+    if (i == 0) rp[0] = base;
+  }
+};
+}  // namespace
+
+void offsets_from_degrees(const uint8_t *deg, uint64_t count, uint64_t base, uint64_t *rp,
+                          cudaStream_t s, cudaMemPool_t pool, Counters &c) {
+  if (count == 0) return;
+  scan_generic(count, GetDeg{deg}, PutOffset{rp, base}, nullptr, s, pool, c);
+}
+
 uint64_t *radix_sort_u64(uint64_t *keys, uint64_t *tmp, uint64_t n, int bits, cudaStream_t s,
                          cudaMemPool_t pool, Counters &c) {
   if (n <= 1) return keys;

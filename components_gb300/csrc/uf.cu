@@ -23,6 +23,7 @@
 #include <mutex>
 #include <tuple>
 
+#include "hostpool.h"
 #include "kernels.h"
 
 namespace ccg {
@@ -801,11 +802,14 @@ __global__ void __launch_bounds__(1024, 2)
 // has a parent, so no CAS can target it).  The store is skipped when the entry
 // already holds the root: many cut edges share a few endpoints (a tile root, a
 // hub), and repeated stores into those hot entries serialise in L2.
+// Entries [*from, *ncut) of the list (from null: all of it).
 __global__ void k_cut_union(const uint2 *__restrict__ cut, const unsigned long long *__restrict__ ncut,
-                            uint64_t cut_cap, uint32_t *p) {
+                            uint64_t cut_cap, uint32_t *p,
+                            const unsigned long long *__restrict__ from = nullptr) {
   uint64_t cnt = *ncut;
   if (cnt > cut_cap) cnt = cut_cap;
-  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < cnt;
+  const uint64_t first = from ? *from : 0;
+  for (uint64_t i = first + blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < cnt;
        i += (uint64_t)gridDim.x * blockDim.x) {
     const uint2 e = cut[i];
     uint32_t ra = uf_find_l1(p, e.x), rb = uf_find_l1(p, e.y);
@@ -1041,11 +1045,12 @@ void run_uf_tiled(const Csr &g, uint32_t *parent, const PartMap &pm, const UfTun
   const unsigned grid = ts.grid;
   const uint64_t hub_cap = hub_list_cap(g.m, tu.hub_degree);
   const uint64_t cut_cap = g.m + 1;
-  DevBuf hubs(8 * hub_cap, s, pool), nh(4, s, pool), cut(8 * cut_cap, s, pool), cnt(8, s, pool);
+  DevBuf hubs(8 * hub_cap, s, pool), nh(4, s, pool), cut(8 * cut_cap, s, pool), cnt(16, s, pool);
   const HubList hl{hubs.as<uint2>(), hub_cap, nh.as<unsigned int>()};
   CCG_CUDA(cudaMemsetAsync(nh.p, 0, 4, s));
-  CCG_CUDA(cudaMemsetAsync(cnt.p, 0, 8, s));
+  CCG_CUDA(cudaMemsetAsync(cnt.p, 0, 16, s));
   unsigned long long *ncut = cnt.as<unsigned long long>();
+  unsigned long long *united = ncut + 1;  // streamed input: cut edges united so far
   // tile pass: offsets, every id once, own parent written once (the parent
   // chains stay in shared memory); cut edges are counted where read
   const uint64_t tile_bytes = 8 * (g.n + 1) + g.m * si + 4 * g.n;
@@ -1058,14 +1063,50 @@ void run_uf_tiled(const Csr &g, uint32_t *parent, const PartMap &pm, const UfTun
   } else {
     // Copy tile-aligned chunks of the caller's host CSR on the copy stream and
     // run each chunk's tiles as soon as its slice is on the device: the tile
-    // pass overlaps the host-to-device transfer.
+    // pass overlaps the host-to-device transfer.  A chunk's cut edges lead to
+    // earlier tiles only, so they are united right after its tiles (later
+    // tiles never touch those entries), and only the last chunk's remain once
+    // the transfer ends.
+    // Rows are sent as one degree byte each when every row of the chunk has
+    // fewer than 255 entries (the host threads encode the next chunk while
+    // the copy engine moves this one; the device rebuilds the offsets with a
+    // prefix sum), else as their 8-byte offsets.  The first chunk always goes
+    // as offsets: the copy engine starts at once, and the encoding of the
+    // later chunks (host threads) and the copies (host link) then run side by
+    // side.
     const uint64_t chunk = (uint64_t)grid * tile;  // one full wave of CTAs
+    uint8_t *hdeg = hs->stager ? hs->stager->staging(g.n) : nullptr;
+    DevBuf ddeg;
+    if (hdeg) ddeg.alloc(g.n, s, pool);
+    uint64_t *drp = const_cast<uint64_t *>(g.rp);
     for (uint64_t v0 = 0; v0 < g.n; v0 += chunk) {
       const uint64_t v1 = std::min<uint64_t>(g.n, v0 + chunk);
       const uint64_t e0 = hs->rp[v0], e1 = hs->rp[v1];
       if (e1 < e0 || e1 > g.m) throw Error(CC_ERR_INVALID, "CSR offsets are not monotone or exceed m_dir");
-      CCG_CUDA(cudaMemcpyAsync(const_cast<uint64_t *>(g.rp) + v0, hs->rp + v0, 8 * (v1 - v0 + 1),
-                               cudaMemcpyHostToDevice, hs->copy));
+      bool coded = false;
+      if (hdeg && v0 > 0 && e1 - e0 < (1ull << 32)) {
+        constexpr uint64_t kPart = 1 << 16;
+        std::atomic<int> wide{0};
+        hs->stager->pool.run((unsigned)((v1 - v0 + kPart - 1) / kPart), [&](unsigned i) {
+          const uint64_t a = v0 + (uint64_t)i * kPart, b = std::min<uint64_t>(v1, a + kPart);
+          uint64_t prev = hs->rp[a], mx = 0;
+          for (uint64_t v = a; v < b; ++v) {
+            const uint64_t nx = hs->rp[v + 1], d = nx - prev;  // wraps to huge when not monotone
+            mx = d > mx ? d : mx;
+            hdeg[v] = (uint8_t)d;
+            prev = nx;
+          }
+          if (mx >= 255) wide.store(1);
+        });
+        coded = wide.load() == 0;
+      }
+      if (coded)
+        CCG_CUDA(cudaMemcpyAsync(ddeg.as<uint8_t>() + v0, hdeg + v0, v1 - v0, cudaMemcpyHostToDevice,
+                                 hs->copy));
+      else
+        CCG_CUDA(cudaMemcpyAsync(drp + v0, hs->rp + v0, 8 * (v1 - v0 + 1), cudaMemcpyHostToDevice,
+                                 hs->copy));
+      hs->h2d_bytes += (coded ? v1 - v0 : 8 * (v1 - v0 + 1)) + si * (e1 - e0);
       if (e1 > e0)
         CCG_CUDA(cudaMemcpyAsync(static_cast<char *>(const_cast<void *>(g.col)) + si * e0,
                                  static_cast<const char *>(hs->col) + si * e0, si * (e1 - e0),
@@ -1075,19 +1116,25 @@ void run_uf_tiled(const Csr &g, uint32_t *parent, const PartMap &pm, const UfTun
       CCG_CUDA(cudaEventRecord(ev, hs->copy));
       CCG_CUDA(cudaStreamWaitEvent(s, ev, 0));
       cudaEventDestroy(ev);
+      if (coded) offsets_from_degrees(ddeg.as<uint8_t>() + v0, v1 - v0, e0, drp + v0, s, pool, c);
       const unsigned cgrid = (unsigned)std::min<uint64_t>((v1 - v0 + tile - 1) / tile, grid);
       k_tile3<T, PART, uint16_t, 0><<<cgrid, threads, smem, s>>>(g.n, g.m, v0, v1, g.rp, col,
                                                               parent, pm, tile, stage,
                                                               tu.hub_degree, hl, cut.as<uint2>(),
                                                               cut_cap, ncut, g.err);
       CCG_LAUNCH_CHECK();
+      k_cut_union<<<kSMs * 16, kBlock, 0, s>>>(cut.as<uint2>(), ncut, cut_cap, parent, united);
+      CCG_LAUNCH_CHECK();
+      CCG_CUDA(cudaMemcpyAsync(united, ncut, 8, cudaMemcpyDeviceToDevice, s));
     }
   }
   c.toc(s, hs ? "uf_tile_streamed" : "uf_tile", t0, tile_bytes);
-  cudaEvent_t t1 = c.tic(s);
-  k_cut_union<<<kSMs * 16, kBlock, 0, s>>>(cut.as<uint2>(), ncut, cut_cap, parent);
-  CCG_LAUNCH_CHECK();
-  c.toc(s, "uf_cut_union", t1, 0);
+  if (!hs) {
+    cudaEvent_t t1 = c.tic(s);
+    k_cut_union<<<kSMs * 16, kBlock, 0, s>>>(cut.as<uint2>(), ncut, cut_cap, parent);
+    CCG_LAUNCH_CHECK();
+    c.toc(s, "uf_cut_union", t1, 0);
+  }
   cudaEvent_t t2 = c.tic(s);
   k_hub_pieces<T, PART, true><<<kSMs * 8, kBlock, 0, s>>>(g.n, g.m, g.rp, col, parent, pm,
                                                           hl, g.err);
