@@ -344,8 +344,12 @@ def workload_serve(args):
             t_next = time.perf_counter()
             for i, G in enumerate(reqs):
                 t_next += gaps[i]
-                while time.perf_counter() < t_next:
-                    pass
+                while True:  # sleep (releasing the GIL) until just before the arrival, then spin
+                    dt = t_next - time.perf_counter()
+                    if dt <= 0:
+                        break
+                    if dt > 5e-4:
+                        time.sleep(dt - 3e-4)
                 tickets[i] = srv.submit(G)
             submitted.set()
 
