@@ -7,14 +7,16 @@
 //   batching   whenever one of the compute streams has finished its previous
 //              batch, every staged request (up to max_batch_graphs) is
 //              coalesced into one launch on it: graphs up to smem_max_n
-//              vertices are solved one CTA each (union-find in shared memory,
-//              CTAs pull graphs from a queue), larger ones by the grid-wide
-//              hook-and-compress; the stream first waits on the copy events
+//              vertices and 32768 entries are solved one CTA each (union-find
+//              in shared memory, CTAs pull graphs from a queue), larger ones by
+//              the grid-wide hook-and-compress; the stream first waits on the
+//              copy events
 //   completion a host callback after the batch marks its requests done
 //   collect    the client copies the labels back, which frees the request's
 //              device memory and budget
-// Copies of new requests overlap the batches already running, and two
-// compute streams let consecutive batches overlap on the device.
+// Copies of new requests overlap the batches already running, and several
+// compute streams (four by default) let batches overlap on the device, so a
+// small request does not wait for a stream that is busy with large graphs.
 #include <algorithm>
 #include <atomic>
 #include <chrono>
@@ -117,6 +119,8 @@ __global__ void k_serve_smem(const GraphDesc *__restrict__ descs, uint32_t count
 }
 
 enum ReqState { kWaiting = 0, kStaged = 1, kLaunched = 2, kDone = 3 };
+constexpr uint64_t kSmemMaxEntries = 32768;
+constexpr double kAdmitSlice = 300e-6;  // seconds of staging before a free stream gets work
 
 struct Req {
   uint64_t id = 0;
@@ -179,9 +183,15 @@ struct Server {
     s->cv_worker.notify_all();
   }
 
+  // Solved by one CTA in shared memory: at most smem_max_n vertices and
+  // kSmemMaxEntries entries.  One CTA walks a graph's entries at the latency of
+  // its own loads (a lone graph of 200,000 entries took 2 ms that way); the
+  // grid-wide path solves it in a fraction of that.
+  bool small(const cc_csr &g) const { return g.n <= cfg.smem_max_n && g.m_dir <= kSmemMaxEntries; }
+
   uint64_t bytes_needed(const cc_csr &g) const {
     uint64_t b = 8 * (g.n + 1) + (uint64_t)g.id_bytes * g.m_dir + 4 * (g.n + 1) + 3 * 256;
-    if (g.n > cfg.smem_max_n)  // hook scratch: cut list and hub pieces
+    if (!small(g))  // hook scratch: cut list and hub pieces
       b += 8 * (g.m_dir + 1) + 8 * (g.m_dir / 33 + g.m_dir / 2048 + 2) + 8192;
     return b;
   }
@@ -215,7 +225,7 @@ struct Server {
     CCG_CUDA(cudaMemsetAsync(r->lab.as<uint32_t>() + g.n, 0, 4, copy_stream));
     CCG_CUDA(cudaEventCreateWithFlags(&r->copied, cudaEventDisableTiming));
     CCG_CUDA(cudaEventRecord(r->copied, copy_stream));
-    if (g.n > cfg.smem_max_n) r->tu = schedule(g);
+    if (!small(g)) r->tu = schedule(g);
   }
 
   // A request that could not be launched: done, reported as failed by collect.
@@ -252,7 +262,7 @@ struct Server {
   void launch(std::vector<Req *> &batch, int si) {  // worker thread, no lock held
     cudaStream_t s = streams[si];
     std::stable_partition(batch.begin(), batch.end(),
-                          [&](Req *r) { return r->g.n <= cfg.smem_max_n; });
+                          [&](Req *r) { return small(r->g); });
     {
       std::lock_guard<std::mutex> lk(mu);
       const uint32_t bid = (uint32_t)++batches;
@@ -265,10 +275,10 @@ struct Server {
     GraphDesc *hd = desc_host[si];
     uint32_t nsmall = 0;
     for (Req *r : batch)
-      if (r->g.n <= cfg.smem_max_n) ++nsmall;
+      if (small(r->g)) ++nsmall;
     Counters c;
     if (nsmall) {
-      std::vector<Req *> small(batch.begin(), batch.begin() + nsmall);
+      std::vector<Req *> smalls(batch.begin(), batch.begin() + nsmall);
       try {
         for (uint32_t i = 0; i < nsmall; ++i) {
           Req *r = batch[i];
@@ -289,9 +299,9 @@ struct Server {
         k_serve_smem<<<grid, 256, smem, s>>>(desc_dev[si].as<GraphDesc>(), nsmall,
                                              queue_dev[si].as<unsigned int>());
         CCG_LAUNCH_CHECK();
-        enqueue_done(std::move(small), si, s);
+        enqueue_done(std::move(smalls), si, s);
       } catch (...) {
-        for (Req *r : small) fail(r);
+        for (Req *r : smalls) fail(r);
       }
     }
     for (size_t i = nsmall; i < batch.size(); ++i) {
@@ -326,8 +336,18 @@ struct Server {
         return stop || admit || (!staged.empty() && free_stream);
       });
       if (stop && waiting.empty() && staged.empty()) break;
-      // admission, in arrival order, while the budget allows
+      // admission, in arrival order, while the budget allows.  Staging is host
+      // work (a large request's copy and schedule take up to 1.6 ms), so during
+      // a burst the worker stops admitting after kAdmitSlice seconds whenever a
+      // compute stream is free, launches what is staged, and comes back: the
+      // first requests of a burst do not wait for the last ones to be staged.
+      const double t_admit0 = now_s();
       while (!waiting.empty() && used + waiting.front()->need <= cfg.hbm_budget_bytes) {
+        if (!staged.empty() && now_s() - t_admit0 > kAdmitSlice) {
+          bool free_stream = false;
+          for (auto &b : busy) free_stream |= b.load() == 0;
+          if (free_stream) break;
+        }
         Req *r = waiting.front();
         waiting.pop_front();
         used += r->need;
@@ -390,7 +410,7 @@ void cc_serve_config_default(cc_serve_config *c) {
   std::memset(c, 0, sizeof(*c));
   c->hbm_budget_bytes = 120ull << 30;
   c->max_batch_graphs = 1024;
-  c->compute_streams = 2;
+  c->compute_streams = 4;  // measured: p99 10 ms at 80 % load against 16-20 ms with 2
   c->smem_max_n = 16384;
 }
 

@@ -30,7 +30,7 @@ typedef struct cc_server cc_server;
 typedef struct cc_serve_config {
   uint64_t hbm_budget_bytes;   /* device bytes requests may hold (default 120 GB) */
   uint32_t max_batch_graphs;   /* graphs coalesced into one launch (default 1024) */
-  uint32_t compute_streams;    /* batches in flight at once (default 2) */
+  uint32_t compute_streams;    /* batches in flight at once (default 4) */
   uint32_t smem_max_n;         /* graphs up to this many vertices go one CTA each (default 16384) */
   uint32_t batch_window_us;    /* a free stream waits up to this long after the oldest staged
                                   request for more to coalesce, unless the batch is full
