@@ -62,7 +62,7 @@ struct HostSource {
 void uf_components(const Csr &g, uint32_t *parent, const PartMap *pm,
                    const UfTuning &tu, cudaStream_t s, cudaMemPool_t pool,
                    Counters &c, const HostSource *hs = nullptr);
-// The hook-schedule decisions on a stratified sample of 8192 rows of a host
+// The hook-schedule decisions on a stratified sample of (up to 8192) rows of a host
 // CSR: the tiled pass suits it (< 50 % of the edges u < v leave their tile and
 // < 10 % lie in rows above hub_degree); the link rounds of sampled linking stay
 // in their tile (>= 75 % of the rows' link-round entries); few hub edges.
@@ -70,7 +70,7 @@ struct HostShares {
   bool tiles = false, link_tiles = false, few_hubs = true;
 };
 HostShares host_shares(const uint64_t *rp, const void *col, int idb, uint64_t n, uint64_t m,
-                       uint32_t tile, uint32_t hub_degree);
+                       uint32_t tile, uint32_t hub_degree, uint64_t max_samples = 8192);
 
 // Write uint32 labels to an id_bytes-wide output array.
 void widen_labels(const uint32_t *in, void *out, int out_bytes, uint64_t n,

@@ -1388,8 +1388,8 @@ void uf_components(const Csr &g, uint32_t *parent, const PartMap *pm, const UfTu
 }
 
 HostShares host_shares(const uint64_t *rp, const void *col, int idb, uint64_t n, uint64_t m,
-                       uint32_t tile, uint32_t hub_degree) {
-  const uint64_t samples = std::min<uint64_t>(n, 8192);
+                       uint32_t tile, uint32_t hub_degree, uint64_t max_samples) {
+  const uint64_t samples = std::min<uint64_t>(n, max_samples);
   uint64_t tot = 0, cross = 0, hub = 0, ltot = 0, lcross = 0;
   auto id = [&](uint64_t k) -> uint64_t {
     return idb == 8 ? static_cast<const uint64_t *>(col)[k] : static_cast<const uint32_t *>(col)[k];
