@@ -31,7 +31,8 @@ typedef struct cc_serve_config {
   uint64_t hbm_budget_bytes;   /* device bytes requests may hold (default 120 GB) */
   uint32_t max_batch_graphs;   /* graphs coalesced into one launch (default 1024) */
   uint32_t compute_streams;    /* batches in flight at once (default 4) */
-  uint32_t smem_max_n;         /* graphs up to this many vertices go one CTA each (default 16384) */
+  uint32_t smem_max_n;         /* graphs up to this many vertices (and 32768 entries) go one
+                                  CTA each (default 16384) */
   uint32_t batch_window_us;    /* a free stream waits up to this long after the oldest staged
                                   request for more to coalesce, unless the batch is full
                                   (default 0: launch at once) */
