@@ -222,8 +222,9 @@ def test_hook_modes_agree(cuda, mode):
 
 
 def test_streamed_host_input(cuda):
-    """Host CSR copied in tile-aligned chunks under the tile pass: same labels
-    for pageable and pinned buffers, both id widths, many chunks."""
+    """Host CSR copied in tile-aligned chunks under the tile pass (each chunk's
+    cut edges united before the next chunk's tiles): same labels for pageable
+    and pinned buffers, both id widths, many chunks, with virtual ranks."""
     import torch
     for idb in (4, 8):
         G = cc.gen_grid(1100, 900, 0.55, seed=12, id_bytes=idb)
@@ -232,7 +233,8 @@ def test_streamed_host_input(cuda):
             ctx = cc.Context(0)
             ctx.set_tuning(hook_mode=_lib.CC_HOOK_TILED, tile_vertices=tile, tile_threads=256)
             for algo in ("exp", "allreduce"):
-                assert np.array_equal(gpu_labels(G, algo, 1, "host", ctx=ctx), want), (idb, tile, algo)
+                for P in (1, 3):
+                    assert np.array_equal(gpu_labels(G, algo, P, "host", ctx=ctx), want), (idb, tile, algo, P)
             Pn = G.pinned()
             dt = torch.int32 if idb == 4 else torch.int64
             lab = torch.empty(G.n, dtype=dt).pin_memory()
