@@ -8,8 +8,9 @@ Native parts (built in-tree by components_gb300.build):
 from .config import Config, parse_parameters
 from .graph import StaticGraph, from_edges, gen_gnm, gen_grid, gen_rhg, read_metis
 from .solvers import (AllReduce, Context, ExponentialContraction, LocalContraction, Propagation,
-                      ShortcutPropagation, SOLVERS, find_components)
+                      ShortcutPropagation, SOLVERS, component_sizes, find_components)
 
 __all__ = ["Config", "parse_parameters", "StaticGraph", "from_edges", "gen_gnm", "gen_grid",
            "gen_rhg", "read_metis", "AllReduce", "Context", "ExponentialContraction",
-           "LocalContraction", "Propagation", "ShortcutPropagation", "SOLVERS", "find_components"]
+           "LocalContraction", "Propagation", "ShortcutPropagation", "SOLVERS", "component_sizes",
+           "find_components"]

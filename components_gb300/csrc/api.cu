@@ -670,6 +670,54 @@ int cc_ctx_run(cc_ctx *ctx, const cc_csr *g, cc_algo algo, const cc_config *cfg,
   return ctx_run(ctx, g, algo, cfg, seed, labels_out, labels_where);
 }
 
+int cc_component_sizes(cc_ctx *ctx, const void *labels, uint32_t id_bytes, uint32_t where, uint64_t n,
+                       uint64_t *pairs, uint64_t cap, uint64_t *npairs, uint64_t *num_components) {
+  return guard([&] {
+    if (id_bytes != 4 && id_bytes != 8) throw Error(CC_ERR_INVALID, "id_bytes must be 4 or 8");
+    if (where != CC_HOST && where != CC_DEVICE) throw Error(CC_ERR_INVALID, "bad where");
+    if (n > 0 && !labels) throw Error(CC_ERR_INVALID, "labels is NULL");
+    if (cap > 0 && !pairs) throw Error(CC_ERR_INVALID, "pairs is NULL");
+    if (!npairs) throw Error(CC_ERR_INVALID, "npairs is NULL");
+    if (n >= 0xffffffffull) throw Error(CC_ERR_UNSUPPORTED, "n >= 2^32-1 labels is not supported");
+    if (where == CC_DEVICE && (uintptr_t)labels % id_bytes != 0)
+      throw Error(CC_ERR_INVALID, "labels are not aligned to id_bytes");
+    cc_ctx *C = ctx ? ctx : default_ctx();
+    CCG_CUDA(cudaSetDevice(C->device));
+    cudaStream_t s = C->stream;
+    Counters c;
+    DevBuf lab_d;
+    const void *lab = labels;
+    if (where == CC_HOST && n) {
+      lab_d.alloc((size_t)id_bytes * n, s, C->pool);
+      CCG_CUDA(cudaMemcpyAsync(lab_d.p, labels, (size_t)id_bytes * n, cudaMemcpyHostToDevice, s));
+      lab = lab_d.p;
+    }
+    // distinct sizes k_1 < ... < k_D of components that cover n vertices:
+    // D (D + 1) / 2 <= n
+    const uint64_t dmax = (uint64_t)std::sqrt(2.0 * (double)n) + 2;
+    DevBuf cnt(4 * (n ? n : 1), s, C->pool), hist(4 * (n + 1), s, C->pool),
+        out(16 * dmax, s, C->pool), dcount(4, s, C->pool);
+    CCG_CUDA(cudaMemsetAsync(C->d_err, 0, sizeof(int), s));
+    ccg::component_size_hist(lab, (int)id_bytes, n, cnt.as<uint32_t>(), hist.as<uint32_t>(),
+                             C->d_err, s, c);
+    ccg::compact_histogram(hist.as<uint32_t>(), n + 1, out.as<uint64_t>(), dmax,
+                           dcount.as<uint32_t>(), s, C->pool, c);
+    uint32_t d = 0;
+    CCG_CUDA(cudaMemcpyAsync(&d, dcount.p, 4, cudaMemcpyDeviceToHost, s));
+    ccg::throw_on_kernel_error(C, s);  // synchronises
+    if (d > dmax) throw Error(CC_ERR_INVALID, "more distinct component sizes than n allows");
+    std::vector<uint64_t> h(2 * (size_t)d);
+    if (d) CCG_CUDA(cudaMemcpyAsync(h.data(), out.p, 16 * (size_t)d, cudaMemcpyDeviceToHost, s));
+    CCG_CUDA(cudaStreamSynchronize(s));
+    uint64_t nontrivial = 0;  // the reference's NUM COMPONENTS leaves out isolated vertices
+    for (uint32_t i = 0; i < d; ++i)
+      if (h[2 * i] != 1) nontrivial += h[2 * i + 1];
+    std::memcpy(pairs, h.data(), 16 * (size_t)std::min<uint64_t>(d, cap));
+    *npairs = d;
+    if (num_components) *num_components = nontrivial;
+  });
+}
+
 int cc_ctx_stats(cc_ctx *ctx, cc_stats *out) {
   if (!ctx || !out) return CC_ERR_INVALID;
   *out = ctx->stats;

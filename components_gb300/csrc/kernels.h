@@ -79,6 +79,14 @@ void widen_labels(const uint32_t *in, void *out, int out_bytes, uint64_t n,
 // ---- scan / radix sort / component graph (sortcsr.cu) ----------------------
 // Stable LSD radix sort of uint64 keys on bits [0, bits); returns the buffer
 // (keys or tmp) that holds the result.
+// (i, hist[i]) for every nonzero hist[i], i ascending, into pairs (2 words
+// each, at most cap pairs); *d_count receives the number of nonzero entries.
+void compact_histogram(const uint32_t *hist, uint64_t len, uint64_t *pairs, uint64_t cap,
+                       uint32_t *d_count, cudaStream_t s, cudaMemPool_t pool, Counters &c);
+// cnt[l] = vertices labelled l (n words), hist[k] = labels held by k vertices
+// (n + 1 words); a label >= n is reported in *err.
+void component_size_hist(const void *lab, int id_bytes, uint64_t n, uint32_t *cnt, uint32_t *hist,
+                         int *err, cudaStream_t s, Counters &c);
 // Row offsets rp[0 .. count] of `count` rows from their degree bytes:
 // rp[0] = base, rp[i + 1] = base + deg[0] + ... + deg[i] (the sum of one call
 // must stay below 2^32).

@@ -192,6 +192,41 @@ __global__ void k_count_roots(uint64_t n, const uint32_t *__restrict__ lab,
   for (int o = 16; o; o >>= 1) c += __shfl_xor_sync(__activemask(), c, o);
   if ((threadIdx.x & 31) == 0 && c) atomicAdd(cnt, c);
 }
+// ---- component sizes (OutputComponents, static_graph.h:504-591) ------------
+// cnt[l] = number of vertices labelled l.  A warp's lanes with the same label
+// add once (labels come in runs: most vertices of a large component sit next
+// to each other), so a giant component does not turn into one hot counter.
+template <class T>
+__global__ void k_comp_count(uint64_t n, const T *__restrict__ lab, uint32_t *__restrict__ cnt,
+                             int *err) {
+  const unsigned lane = threadIdx.x & 31;
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t base = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) & ~31ull; base < n;
+       base += stride) {
+    const uint64_t v = base + lane;
+    uint64_t l = v < n ? (uint64_t)lab[v] : ~0ull - lane;  // lanes past n match nothing
+    if (v < n && l >= n) {
+      set_err(err, kErrBadId);
+      l = ~0ull - lane;
+    }
+    const unsigned peers = __match_any_sync(0xffffffffu, l);
+    if (l < n && lane == (unsigned)(__ffs(peers) - 1)) atomicAdd(cnt + l, (unsigned)__popc(peers));
+  }
+}
+// hist[s] = number of labels held by s vertices (s >= 1), aggregated per warp
+// the same way (most components are small, so a few sizes are hot).
+__global__ void k_comp_hist(uint64_t n, const uint32_t *__restrict__ cnt, uint32_t *__restrict__ hist) {
+  const unsigned lane = threadIdx.x & 31;
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t base = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) & ~31ull; base < n;
+       base += stride) {
+    const uint64_t v = base + lane;
+    const uint32_t c = v < n ? cnt[v] : 0u;
+    const unsigned peers = __match_any_sync(0xffffffffu, c);
+    if (c && lane == (unsigned)(__ffs(peers) - 1)) atomicAdd(hist + c, (unsigned)__popc(peers));
+  }
+}
+
 __global__ void k_gather(uint64_t n, const uint32_t *__restrict__ src, const uint32_t *__restrict__ idx,
                          uint32_t *__restrict__ out) {
   for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n;
@@ -321,6 +356,22 @@ void count_roots(const uint32_t *lab, uint64_t n, unsigned long long *d_count, c
   k_count_roots<<<grid_for(n, kBlock, kSMs * 8), kBlock, 0, s>>>(n, lab, d_count);
   CCG_LAUNCH_CHECK();
   c.add(1, 4 * n);
+}
+
+void component_size_hist(const void *lab, int id_bytes, uint64_t n, uint32_t *cnt, uint32_t *hist,
+                         int *err, cudaStream_t s, Counters &c) {
+  CCG_CUDA(cudaMemsetAsync(cnt, 0, 4 * n, s));
+  CCG_CUDA(cudaMemsetAsync(hist, 0, 4 * (n + 1), s));
+  if (n == 0) return;
+  const unsigned grid = grid_for(n, kBlock, kSMs * 16);
+  if (id_bytes == 8)
+    k_comp_count<uint64_t><<<grid, kBlock, 0, s>>>(n, static_cast<const uint64_t *>(lab), cnt, err);
+  else
+    k_comp_count<uint32_t><<<grid, kBlock, 0, s>>>(n, static_cast<const uint32_t *>(lab), cnt, err);
+  CCG_LAUNCH_CHECK();
+  k_comp_hist<<<grid, kBlock, 0, s>>>(n, cnt, hist);
+  CCG_LAUNCH_CHECK();
+  c.add(2, (uint64_t)id_bytes * n + 4 * n + 4 * n + 4 * n);
 }
 
 void gather_u32(const uint32_t *src, const uint32_t *idx, uint32_t *out, uint64_t n,

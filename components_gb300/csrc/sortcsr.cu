@@ -556,6 +556,29 @@ struct PutOffset {
 };
 }  // namespace
 
+namespace {
+struct GetNonzero {
+  const uint32_t *h;
+  __device__ uint32_t operator()(uint64_t i) const { return h[i] ? 1u : 0u; }
+};
+struct PutPair {
+  const uint32_t *h;
+  uint64_t *pairs;
+  uint64_t cap;
+  __device__ void operator()(uint64_t i, uint32_t excl, uint32_t f) const {
+    if (f && excl < cap) {
+      pairs[2 * (uint64_t)excl] = i;
+      pairs[2 * (uint64_t)excl + 1] = h[i];
+    }
+  }
+};
+}  // namespace
+
+void compact_histogram(const uint32_t *hist, uint64_t len, uint64_t *pairs, uint64_t cap,
+                       uint32_t *d_count, cudaStream_t s, cudaMemPool_t pool, Counters &c) {
+  scan_generic(len, GetNonzero{hist}, PutPair{hist, pairs, cap}, d_count, s, pool, c);
+}
+
 void offsets_from_degrees(const uint8_t *deg, uint64_t count, uint64_t base, uint64_t *rp,
                           cudaStream_t s, cudaMemPool_t pool, Counters &c) {
   if (count == 0) return;

@@ -205,3 +205,31 @@ def find_components(G: StaticGraph, algo: str = "exp", conf: Config | None = Non
         labels = np.empty(G.n, np.uint32 if G.id_bytes == 4 else np.uint64)
     SOLVERS[algo](conf, 0, G.num_parts, context).FindComponents(G, labels)
     return labels
+
+
+def component_sizes(labels, context: Context | None = None):
+    """Component-size summary of a label array, computed on the device
+    (OutputComponents, static_graph.h:504-591): an (k, 2) uint64 array of
+    (size, number of components of that size) rows in ascending size, and the
+    number of components with more than one vertex (the reference's
+    "NUM COMPONENTS").  `labels`: numpy or torch CUDA array of uint32/uint64
+    labels below len(labels), e.g. the output of FindComponents."""
+    if _is_torch(labels):
+        import torch
+        if labels.dtype not in (torch.int32, torch.int64) or not labels.is_contiguous():
+            raise ValueError("labels: a contiguous int32/int64 tensor")
+        where = _lib.CC_DEVICE if labels.is_cuda else _lib.CC_HOST
+        idb, n, ptr = labels.element_size(), labels.numel(), labels.data_ptr()
+    else:
+        labels = np.ascontiguousarray(labels)
+        if labels.dtype.itemsize not in (4, 8) or labels.dtype.kind not in "iu":
+            raise ValueError("labels: a 32- or 64-bit integer array")
+        where, idb, n, ptr = _lib.CC_HOST, labels.dtype.itemsize, labels.size, labels.ctypes.data
+    cap = int(np.sqrt(2.0 * n)) + 2
+    pairs = np.zeros((cap, 2), np.uint64)
+    k, nc = C.c_uint64(), C.c_uint64()
+    h = context.handle if context is not None else None
+    _lib.check(_lib.gpu().cc_component_sizes(h, ptr, idb, where, n, pairs.ctypes.data, cap,
+                                             C.byref(k), C.byref(nc)))
+    return pairs[: min(k.value, cap)].copy(), int(nc.value)
+

@@ -203,6 +203,18 @@ int cc_ctx_destroy(cc_ctx *ctx);
 int cc_ctx_run(cc_ctx *ctx, const cc_csr *g, cc_algo algo,
                const cc_config *cfg, uint64_t seed, void *labels_out,
                uint32_t labels_where);
+/*
+ * Component-size summary of a label array (OutputComponents,
+ * static_graph.h:504-591), on the device: the (size, number of components of
+ * that size) pairs in ascending size, as 2 * min(*npairs, cap) words of
+ * `pairs`, and in *num_components the number of components with more than one
+ * vertex (the reference's "NUM COMPONENTS").  labels: n values below n (the
+ * solvers' canonical labels), id_bytes 4 or 8, where CC_HOST or CC_DEVICE.
+ * *npairs receives the number of distinct sizes (at most sqrt(2n) + 1; pairs
+ * beyond cap are not written).  ctx NULL: the default context.
+ */
+int cc_component_sizes(cc_ctx *ctx, const void *labels, uint32_t id_bytes, uint32_t where, uint64_t n,
+                       uint64_t *pairs, uint64_t cap, uint64_t *npairs, uint64_t *num_components);
 int cc_ctx_stats(cc_ctx *ctx, cc_stats *out);
 /* Device bytes the context holds in its arena (grows on demand, reused). */
 uint64_t cc_ctx_arena_bytes(cc_ctx *ctx);

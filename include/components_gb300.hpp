@@ -22,6 +22,7 @@
 #pragma once
 
 #include <cstdint>
+#include <iostream>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -138,5 +139,26 @@ class AllReduce : public Solver<CC_ALLREDUCE> {
  public:
   using Solver<CC_ALLREDUCE>::Solver;
 };
+
+// The reference's StaticGraph::OutputComponents (static_graph.h:504-591) for
+// the labels of a FindComponents call: the component-size distribution, in
+// ascending size, and the number of components with more than one vertex,
+// printed in the reference's format.  The counting runs on the device.
+inline uint64_t OutputComponents(const std::vector<unsigned long long> &labels,
+                                 std::ostream &os = std::cout) {
+  const uint64_t n = labels.size();
+  uint64_t cap = 2;
+  while (cap * cap < 2 * n) cap *= 2;
+  cap += 2;
+  std::vector<uint64_t> pairs(2 * cap);
+  uint64_t k = 0, num = 0;
+  check(cc_component_sizes(nullptr, labels.data(), 8, CC_HOST, n, pairs.data(), cap, &k, &num));
+  os << "COMPONENTS [ ";
+  for (uint64_t i = 0; i < k && i < cap; ++i)
+    os << "size=" << pairs[2 * i] << " (num=" << pairs[2 * i + 1] << ") ";
+  os << "]" << std::endl;
+  os << "NUM COMPONENTS " << num << std::endl;
+  return num;
+}
 
 }  // namespace ccgpu

@@ -2,7 +2,8 @@
 // app/exp_contraction.cpp:95-129 against a graph type that offers the
 // StaticGraph accessors the header reads.  Prints one line per solver:
 // "<name> <label_0> <label_1> ..." for the graph given on stdin
-// ("n m" then m undirected edges "u w").
+// ("n m" then m undirected edges "u w"), then the component summary lines
+// "COMPONENTS [ size=.. (num=..) ... ]" and "NUM COMPONENTS k".
 #include <cstdio>
 #include <functional>
 #include <vector>
@@ -69,6 +70,11 @@ int main() {
     run<ccgpu::ShortcutPropagation>("shortcuts", conf, 3, G);
     run<ccgpu::Propagation>("labels", conf, 3, G);
     run<ccgpu::AllReduce<TinyStaticGraph>>("allreduce", conf, 3, G);
+    // the drivers' closing summary (StaticGraph::OutputComponents)
+    std::vector<unsigned long long> labels(G.GetVertexVectorSize(), 0);
+    ccgpu::ExponentialContraction comp(conf, 0, 1);
+    comp.FindComponents(G, labels);
+    ccgpu::OutputComponents(labels);
   } catch (const ccgpu::Error &e) {
     std::fprintf(stderr, "%s\n", e.what());
     return 1;

@@ -33,7 +33,12 @@ def test_cpp_dropin_solvers(cuda, tmp_path):
     out = subprocess.run([str(exe)], input=text, capture_output=True, text=True, check=True).stdout
     want = oracle.uf_labels(cc.from_edges(n, edges))
     lines = out.strip().splitlines()
+    summary, lines = lines[5:], lines[:5]
     assert [ln.split()[0] for ln in lines] == ["exp", "local", "shortcuts", "labels", "allreduce"]
+    # OutputComponents: size distribution in ascending size, components of more than one vertex
+    sizes, counts = np.unique(np.unique(want, return_counts=True)[1], return_counts=True)
+    assert summary[0] == "COMPONENTS [ " + "".join(f"size={s} (num={c}) " for s, c in zip(sizes, counts)) + "]"
+    assert summary[1] == f"NUM COMPONENTS {int(counts[sizes != 1].sum())}"
     for ln in lines:
         toks = ln.split()
         labels = np.array([int(t) for t in toks[1:1 + n]], np.uint64)

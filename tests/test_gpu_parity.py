@@ -170,6 +170,29 @@ def test_id_check_at_every_offset_of_col(cuda, idb):
             col[pos] = old
 
 
+@pytest.mark.parametrize("idb", [4, 8])
+def test_component_sizes_match_numpy(cuda, idb):
+    """OutputComponents on the device: (size, count) pairs in ascending size
+    and the number of components with more than one vertex, for host and
+    device labels; a label >= n is reported, not counted."""
+    import torch
+    graphs = [cc.gen_grid(300, 200, 0.5, seed=3, id_bytes=idb), cc.gen_gnm(20000, 9000, seed=4, id_bytes=idb),
+              cc.from_edges(7, [], id_bytes=idb), cc.gen_rhg(1 << 14, 8.0, 2.6, seed=2, id_bytes=idb)]
+    for G in graphs:
+        lab = cc.find_components(G, "exp")
+        sizes, counts = np.unique(np.unique(lab, return_counts=True)[1], return_counts=True)
+        want = np.stack([sizes, counts], axis=1).astype(np.uint64)
+        for labels in (lab, torch.from_numpy(lab.view(np.int32 if idb == 4 else np.int64)).to("cuda:0")):
+            got, num = cc.component_sizes(labels)
+            assert np.array_equal(got, want), G.n
+            assert num == int(counts[sizes != 1].sum())
+    bad = np.array([0, 1, 9], np.uint32 if idb == 4 else np.uint64)  # 9 >= n = 3
+    with pytest.raises(_lib.CCError) as ei:
+        cc.component_sizes(bad)
+    assert ei.value.status == _lib.CC_ERR_INVALID
+    assert cc.component_sizes(np.zeros(0, np.uint32))[0].shape == (0, 2)
+
+
 def test_context_reuse_and_stats(cuda):
     ctx = cc.Context(0, profiling=True)
     G = cc.gen_grid(300, 200, 0.5, seed=3)
