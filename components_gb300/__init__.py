@@ -6,11 +6,13 @@ Native parts (built in-tree by components_gb300.build):
   _build/libccgen.so  seeded synthetic graph generators (include/cc_gen.h)
 """
 from .config import Config, parse_parameters
-from .graph import StaticGraph, from_edges, gen_gnm, gen_grid, gen_rhg, read_metis
+from .graph import (StaticGraph, from_edges, gen_gnm, gen_gnm_device, gen_grid, gen_grid_device,
+                    gen_rhg, read_metis)
 from .solvers import (AllReduce, Context, ExponentialContraction, LocalContraction, Propagation,
                       ShortcutPropagation, SOLVERS, component_sizes, find_components)
 
-__all__ = ["Config", "parse_parameters", "StaticGraph", "from_edges", "gen_gnm", "gen_grid",
+__all__ = ["Config", "parse_parameters", "StaticGraph", "from_edges", "gen_gnm", "gen_gnm_device",
+           "gen_grid", "gen_grid_device",
            "gen_rhg", "read_metis", "AllReduce", "Context", "ExponentialContraction",
            "LocalContraction", "Propagation", "ShortcutPropagation", "SOLVERS", "component_sizes",
            "find_components"]

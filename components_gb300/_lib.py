@@ -112,6 +112,10 @@ GPU_SYMBOLS = {
     "cc_ctx_destroy": (C.c_int, [_P]),
     "cc_ctx_run": (C.c_int, [_P, C.POINTER(cc_csr), C.c_int, C.POINTER(cc_config), _U64, _P, _U32]),
     "cc_ctx_stats": (C.c_int, [_P, C.POINTER(cc_stats)]),
+    "cc_gen_grid_device": (C.c_int, [_P, C.c_uint64, C.c_uint64, C.c_double, C.c_uint64, C.c_uint32,
+                                     _P, _P, C.c_uint64, C.POINTER(C.c_uint64)]),
+    "cc_gen_gnm_device": (C.c_int, [_P, C.c_uint64, C.c_uint64, C.c_uint64, C.c_uint32, _P, _P,
+                                    C.c_uint64, C.POINTER(C.c_uint64)]),
     "cc_component_sizes": (C.c_int, [_P, _P, C.c_uint32, C.c_uint32, C.c_uint64, _P, C.c_uint64,
                                      C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]),
     "cc_ctx_arena_bytes": (_U64, [_P]),

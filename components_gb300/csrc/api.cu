@@ -630,6 +630,10 @@ int validate_host(const cc_csr *g, int check_sym) {
 
 }  // namespace
 
+namespace ccg {
+cc_ctx *default_context() { return default_ctx(); }
+}  // namespace ccg
+
 // ============================== C ABI ========================================
 extern "C" {
 

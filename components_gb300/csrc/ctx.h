@@ -46,6 +46,9 @@ namespace ccg {
 // Last error text of this thread (cc_gpu_strerror).
 std::string &last_error();
 
+// The calling thread's context on the current device (made on first use).
+cc_ctx *default_context();
+
 template <class F>
 int guard(F &&f) {
   try {

@@ -87,6 +87,9 @@ void compact_histogram(const uint32_t *hist, uint64_t len, uint64_t *pairs, uint
 // (n + 1 words); a label >= n is reported in *err.
 void component_size_hist(const void *lab, int id_bytes, uint64_t n, uint32_t *cnt, uint32_t *hist,
                          int *err, cudaStream_t s, Counters &c);
+// Adjacent-unique copy of n sorted keys into out; *d_count = number kept.
+void unique_sorted_keys(const uint64_t *sorted, uint64_t n, uint64_t *out, uint32_t *d_count,
+                        cudaStream_t s, cudaMemPool_t pool, Counters &c);
 // Row offsets rp[0 .. count] of `count` rows from their degree bytes:
 // rp[0] = base, rp[i + 1] = base + deg[0] + ... + deg[i] (the sum of one call
 // must stay below 2^32).

@@ -579,6 +579,11 @@ void compact_histogram(const uint32_t *hist, uint64_t len, uint64_t *pairs, uint
   scan_generic(len, GetNonzero{hist}, PutPair{hist, pairs, cap}, d_count, s, pool, c);
 }
 
+void unique_sorted_keys(const uint64_t *sorted, uint64_t n, uint64_t *out, uint32_t *d_count,
+                        cudaStream_t s, cudaMemPool_t pool, Counters &c) {
+  scan_generic(n, GetUniq{sorted}, PutUniq{sorted, out}, d_count, s, pool, c);
+}
+
 void offsets_from_degrees(const uint8_t *deg, uint64_t count, uint64_t base, uint64_t *rp,
                           cudaStream_t s, cudaMemPool_t pool, Counters &c) {
   if (count == 0) return;

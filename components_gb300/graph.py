@@ -165,6 +165,31 @@ def gen_grid(X: int, Y: int, p: float = 0.5, seed: int = 1, id_bytes: int = 4,
     return _HostGraph(hg).to_static(num_parts)
 
 
+def _device_graph(fill, n: int, cap: int, id_bytes: int, device, num_parts: int) -> StaticGraph:
+    import torch
+    rp = torch.empty(n + 1, dtype=torch.int64, device=device)
+    col = torch.empty(max(cap, 1), dtype=torch.int32 if id_bytes == 4 else torch.int64, device=device)
+    m = C.c_uint64()
+    with torch.cuda.device(rp.device):
+        _lib.check(fill(rp.data_ptr(), col.data_ptr(), cap, C.byref(m)))
+    return StaticGraph(rp, col[: m.value].clone(), num_parts)  # exact-size storage
+
+
+def gen_grid_device(X: int, Y: int, p: float = 0.5, seed: int = 1, id_bytes: int = 4,
+                    num_parts: int = 1, device="cuda") -> StaticGraph:
+    """gen_grid built on the device (the same graph, torch CUDA tensors)."""
+    return _device_graph(lambda rp, col, cap, m: _lib.gpu().cc_gen_grid_device(
+        None, X, Y, p, seed, id_bytes, rp, col, cap, m), X * Y, 2 * ((X - 1) * Y + X * (Y - 1)),
+        id_bytes, device, num_parts)
+
+
+def gen_gnm_device(n: int, m: int, seed: int = 1, id_bytes: int = 8, num_parts: int = 1,
+                   device="cuda") -> StaticGraph:
+    """gen_gnm built on the device (the same graph, torch CUDA tensors)."""
+    return _device_graph(lambda rp, col, cap, mm: _lib.gpu().cc_gen_gnm_device(
+        None, n, m, seed, id_bytes, rp, col, cap, mm), n, 2 * m, id_bytes, device, num_parts)
+
+
 def gen_rhg(n: int, avg_deg: float = 16.0, gamma: float = 2.6, seed: int = 1, id_bytes: int = 4,
             num_parts: int = 1) -> StaticGraph:
     """Random hyperbolic graph, threshold model (-gen rhg -n log2 n -d d -gamma g)."""

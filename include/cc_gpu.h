@@ -215,6 +215,19 @@ int cc_ctx_run(cc_ctx *ctx, const cc_csr *g, cc_algo algo,
  */
 int cc_component_sizes(cc_ctx *ctx, const void *labels, uint32_t id_bytes, uint32_t where, uint64_t n,
                        uint64_t *pairs, uint64_t cap, uint64_t *npairs, uint64_t *num_components);
+/*
+ * The seeded G(n, m) and 2D bond-percolation generators of cc_gen.h, run on
+ * the device: the same graph as cc_gen_gnm / cc_gen_grid for the same
+ * arguments (the same hash of (seed, index), the same sorted rows), written
+ * into the caller's device buffers row_ptr (n + 1 offsets) and col (cap ids
+ * of id_bytes); *m_dir receives the number of entries (CC_ERR_INVALID when it
+ * exceeds cap; 4 X Y and 2 m always suffice).  ctx NULL: the default context.
+ */
+int cc_gen_grid_device(cc_ctx *ctx, uint64_t X, uint64_t Y, double p, uint64_t seed, uint32_t id_bytes,
+                       uint64_t *row_ptr, void *col, uint64_t cap, uint64_t *m_dir);
+int cc_gen_gnm_device(cc_ctx *ctx, uint64_t n, uint64_t m, uint64_t seed, uint32_t id_bytes,
+                      uint64_t *row_ptr, void *col, uint64_t cap, uint64_t *m_dir);
+
 int cc_ctx_stats(cc_ctx *ctx, cc_stats *out);
 /* Device bytes the context holds in its arena (grows on demand, reused). */
 uint64_t cc_ctx_arena_bytes(cc_ctx *ctx);

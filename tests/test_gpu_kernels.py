@@ -187,3 +187,25 @@ def test_shortcut_rounds_match_oracle(cuda):
             _lib.check(_lib.gpu().cc_debug_shortcut(C.byref(g), lab.data_ptr(), hitters, C.byref(r)))
             assert np.array_equal(lab.cpu().numpy().view(np.uint32).astype(np.uint64), want)
             assert r.value == rounds_w
+
+
+def test_device_generators_equal_host_generators(cuda):
+    """cc_gen_grid_device / cc_gen_gnm_device build the very graphs of the host
+    generators (same hash, same sorted rows), for both id widths."""
+    for idb in (4, 8):
+        for X, Y, p, seed in [(300, 200, 0.5, 1), (1, 50, 0.7, 2), (64, 1, 1.0, 3), (40, 30, 0.0, 4),
+                              (513, 129, 0.35, 9)]:
+            H = cc.gen_grid(X, Y, p, seed=seed, id_bytes=idb)
+            D = cc.gen_grid_device(X, Y, p, seed=seed, id_bytes=idb)
+            rp, col = D.numpy()
+            assert np.array_equal(rp, np.asarray(H.row_ptr, np.uint64)), (X, Y, p, idb)
+            assert np.array_equal(col, np.asarray(H.col).astype(np.uint64)), (X, Y, p, idb)
+        for n, m, seed in [(1 << 12, 3 << 12, 5), (1000, 4000, 6), (1, 3, 7), (17, 400, 8), (5000, 0, 9)]:
+            H = cc.gen_gnm(n, m, seed=seed, id_bytes=idb)
+            D = cc.gen_gnm_device(n, m, seed=seed, id_bytes=idb)
+            rp, col = D.numpy()
+            assert np.array_equal(rp, np.asarray(H.row_ptr, np.uint64)), (n, m, idb)
+            assert np.array_equal(col, np.asarray(H.col).astype(np.uint64)), (n, m, idb)
+    G = cc.gen_grid_device(700, 500, 0.5, seed=6)
+    lab = cc.find_components(G, "exp")
+    assert np.array_equal(lab.cpu().numpy().view(np.uint32).astype(np.uint64), oracle.uf_labels(G))
