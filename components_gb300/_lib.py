@@ -141,6 +141,9 @@ GEN_SYMBOLS = {
     "cc_gen_rhg": (C.c_int, [_U64, C.c_double, C.c_double, _U64, _U32, C.POINTER(cc_host_graph)]),
     "cc_host_graph_free": (None, [C.POINTER(cc_host_graph)]),
     "cc_gen_rhg_radius": (C.c_double, [_U64, C.c_double, C.c_double]),
+    "cc_read_metis": (C.c_int, [C.c_char_p, _U32, C.POINTER(cc_host_graph)]),
+    "cc_read_edge_list": (C.c_int, [C.c_char_p, _U32, C.POINTER(cc_host_graph)]),
+    "cc_read_binary_edges": (C.c_int, [C.c_char_p, _U32, C.POINTER(cc_host_graph)]),
 }
 
 _gpu = None

@@ -6,6 +6,7 @@
 // same graph on every host and for every thread count.
 #include <algorithm>
 #include <cmath>
+#include <cstdio>
 #include <cstdlib>
 #include <cstring>
 #include <vector>
@@ -447,6 +448,158 @@ void cc_host_batch_free(cc_host_batch *b) {
   std::free(b->col);
   b->voff = b->row_ptr = nullptr;
   b->col = nullptr;
+}
+
+}  // extern "C"
+
+// ---- input files (the reference's GraphIO readers, lib/io/graph_io.h) --------
+// Every reader collects the undirected edges, drops self-loops and repeats,
+// and builds the symmetric CSR with sorted rows, as the generators do.
+namespace {
+
+bool slurp(const char *path, std::vector<char> &buf) {
+  FILE *f = path ? std::fopen(path, "rb") : nullptr;
+  if (!f) return false;
+  std::fseek(f, 0, SEEK_END);
+  const long len = std::ftell(f);
+  std::fseek(f, 0, SEEK_SET);
+  if (len < 0) {
+    std::fclose(f);
+    return false;
+  }
+  buf.resize((size_t)len + 1);
+  const size_t got = len ? std::fread(buf.data(), 1, (size_t)len, f) : 0;
+  std::fclose(f);
+  buf.resize(got);
+  buf.push_back('\n');  // every line ends with a newline
+  return got == (size_t)len;
+}
+
+// Unsigned decimal at p (spaces and tabs skipped first); false at the end of
+// the line.
+bool next_uint(const char *&p, const char *eol, uint64_t &v) {
+  while (p < eol && (*p == ' ' || *p == '\t' || *p == '\r')) ++p;
+  if (p >= eol || *p < '0' || *p > '9') return false;
+  v = 0;
+  while (p < eol && *p >= '0' && *p <= '9') v = 10 * v + (uint64_t)(*p++ - '0');
+  return true;
+}
+
+// CSR of the undirected edges (u, w) (0-based, below n) collected as keys.
+int csr_from_edges(std::vector<uint64_t> &keys, uint64_t n, uint32_t idb, cc_host_graph *out) {
+  const int b = bits_for(n);
+  radix_u64(keys, 2 * b);
+  keys.erase(std::unique(keys.begin(), keys.end()), keys.end());
+  return csr_from_keys(keys, b, n, idb, out);
+}
+void add_edge(std::vector<uint64_t> &keys, int b, uint64_t u, uint64_t w) {
+  if (u == w) return;
+  keys.push_back((u << b) | w);
+  keys.push_back((w << b) | u);
+}
+
+}  // namespace
+
+extern "C" {
+
+// METIS text (ReadMETISFile, graph_io.h:281-382): '%' comment lines, a header
+// "n m ..." (m is not trusted), then one line per vertex with its 1-based
+// neighbours.
+int cc_read_metis(const char *path, uint32_t id_bytes, cc_host_graph *out) {
+  if (!out || (id_bytes != 4 && id_bytes != 8)) return CC_ERR_INVALID;
+  std::memset(out, 0, sizeof(*out));
+  std::vector<char> buf;
+  if (!slurp(path, buf)) return CC_ERR_INVALID;
+  const char *p = buf.data(), *end = buf.data() + buf.size();
+  auto line = [&](const char *&a, const char *&e) {  // next line that is not a comment
+    while (p < end) {
+      a = p;
+      e = static_cast<const char *>(std::memchr(p, '\n', (size_t)(end - p)));
+      p = e + 1;
+      if (*a != '%') return true;
+    }
+    return false;
+  };
+  const char *a, *e;
+  uint64_t n = 0, m_hdr = 0;
+  if (!line(a, e) || !next_uint(a, e, n) || !next_uint(a, e, m_hdr)) return CC_ERR_INVALID;
+  if (n == 0 || n >= (1ull << 32) || (id_bytes == 4 && n >= 0xffffffffull)) return CC_ERR_INVALID;
+  const int b = bits_for(n);
+  std::vector<uint64_t> keys;
+  keys.reserve(2 * m_hdr + 16);
+  for (uint64_t v = 0; v < n; ++v) {
+    if (!line(a, e)) break;  // missing trailing lines: isolated vertices
+    uint64_t t;
+    while (next_uint(a, e, t)) {
+      if (t == 0 || t > n) return CC_ERR_INVALID;
+      add_edge(keys, b, v, t - 1);
+    }
+  }
+  return csr_from_edges(keys, n, id_bytes, out);
+}
+
+// Sorted edge file (ReadSortedEdgeFile, graph_io.h:385-670, records parsed as
+// in connect_io.h:216-260): '%' comment lines, a header "<type> n m", then
+// records "e u w" of 1-based endpoints, one per undirected edge; other
+// records are skipped.
+int cc_read_edge_list(const char *path, uint32_t id_bytes, cc_host_graph *out) {
+  if (!out || (id_bytes != 4 && id_bytes != 8)) return CC_ERR_INVALID;
+  std::memset(out, 0, sizeof(*out));
+  std::vector<char> buf;
+  if (!slurp(path, buf)) return CC_ERR_INVALID;
+  const char *p = buf.data(), *end = buf.data() + buf.size();
+  uint64_t n = 0, m_hdr = 0;
+  bool header = false;
+  std::vector<uint64_t> keys;
+  int b = 1;
+  while (p < end) {
+    const char *a = p, *e = static_cast<const char *>(std::memchr(p, '\n', (size_t)(end - p)));
+    p = e + 1;
+    while (a < e && (*a == ' ' || *a == '\t')) ++a;
+    if (a >= e || *a == '%') continue;
+    if (!header) {  // "<type> n m"
+      while (a < e && *a != ' ' && *a != '\t') ++a;
+      if (!next_uint(a, e, n) || !next_uint(a, e, m_hdr)) return CC_ERR_INVALID;
+      if (n == 0 || n >= (1ull << 32)) return CC_ERR_INVALID;
+      b = bits_for(n);
+      keys.reserve(2 * m_hdr);
+      header = true;
+      continue;
+    }
+    if (*a != 'e') continue;
+    ++a;
+    uint64_t u, w;
+    if (!next_uint(a, e, u) || !next_uint(a, e, w)) return CC_ERR_INVALID;
+    if (u == 0 || w == 0 || u > n || w > n) return CC_ERR_INVALID;
+    add_edge(keys, b, u - 1, w - 1);
+  }
+  if (!header) return CC_ERR_INVALID;
+  return csr_from_edges(keys, n, id_bytes, out);
+}
+
+// Sorted binary edges (ReadSortedBinaryFile, graph_io.h:910-1175): uint64 n,
+// uint64 m, then m pairs of uint64 1-based endpoints (host byte order).
+int cc_read_binary_edges(const char *path, uint32_t id_bytes, cc_host_graph *out) {
+  if (!out || (id_bytes != 4 && id_bytes != 8)) return CC_ERR_INVALID;
+  std::memset(out, 0, sizeof(*out));
+  std::vector<char> buf;
+  if (!slurp(path, buf)) return CC_ERR_INVALID;
+  const size_t len = buf.size() - 1;  // the appended newline
+  if (len < 16) return CC_ERR_INVALID;
+  uint64_t n = 0, m = 0;
+  std::memcpy(&n, buf.data(), 8);
+  std::memcpy(&m, buf.data() + 8, 8);
+  if (n == 0 || n >= (1ull << 32) || m > (len - 16) / 16) return CC_ERR_INVALID;
+  const int b = bits_for(n);
+  std::vector<uint64_t> keys;
+  keys.reserve(2 * m);
+  for (uint64_t i = 0; i < m; ++i) {
+    uint64_t uw[2];
+    std::memcpy(uw, buf.data() + 16 + 16 * i, 16);
+    if (uw[0] == 0 || uw[1] == 0 || uw[0] > n || uw[1] > n) return CC_ERR_INVALID;
+    add_edge(keys, b, uw[0] - 1, uw[1] - 1);
+  }
+  return csr_from_edges(keys, n, id_bytes, out);
 }
 
 }  // extern "C"

@@ -116,20 +116,30 @@ def from_edges(n: int, edges, id_bytes: int = 4, num_parts: int = 1) -> StaticGr
     return StaticGraph(rp, col, num_parts)
 
 
+def _read(fn: str, path: str, id_bytes: int, num_parts: int) -> StaticGraph:
+    hg = _lib.cc_host_graph()
+    _lib.check(getattr(_lib.gen(), fn)(str(path).encode(), id_bytes, C.byref(hg)))
+    return _HostGraph(hg).to_static(num_parts)
+
+
 def read_metis(path: str, id_bytes: int = 4, num_parts: int = 1) -> StaticGraph:
     """METIS text format (GraphIO::ReadMETISFile, graph_io.h:280-382): a header
     `n m`, then one line of 1-based neighbour ids per vertex; `%` lines are
     comments.  The header's m is not trusted (example/simple.graph states 5
-    for 4 edges); the adjacency is symmetrised."""
-    with open(path) as f:
-        lines = [ln for ln in f.read().splitlines() if not ln.startswith("%")]
-    n = int(lines[0].split()[0])
-    edges = []
-    for v in range(n):
-        toks = lines[1 + v].split() if 1 + v < len(lines) else []
-        for t in toks:
-            edges.append((v, int(t) - 1))
-    return from_edges(n, edges, id_bytes, num_parts)
+    for 4 edges); the adjacency is symmetrised.  Parsed by libccgen."""
+    return _read("cc_read_metis", path, id_bytes, num_parts)
+
+
+def read_edge_list(path: str, id_bytes: int = 4, num_parts: int = 1) -> StaticGraph:
+    """Sorted edge file (GraphIO::ReadSortedEdgeFile, graph_io.h:385-670): a
+    header `<type> n m`, then `e u w` records with 1-based endpoints."""
+    return _read("cc_read_edge_list", path, id_bytes, num_parts)
+
+
+def read_binary_edges(path: str, id_bytes: int = 4, num_parts: int = 1) -> StaticGraph:
+    """Sorted binary file (GraphIO::ReadSortedBinaryFile, graph_io.h:910-1175):
+    uint64 n, uint64 m, then m pairs of uint64 1-based endpoints."""
+    return _read("cc_read_binary_edges", path, id_bytes, num_parts)
 
 
 class _HostGraph:

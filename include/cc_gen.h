@@ -64,6 +64,18 @@ int cc_gen_batch(uint32_t k, double log2_nmin, double log2_nmax, double dmin, do
                  uint64_t seed, cc_host_batch *out);
 void cc_host_batch_free(cc_host_batch *b);
 
+/* Input files, as the reference drivers read them with -input (GraphIO,
+   lib/io/graph_io.h): METIS text ("n m" header, one line of 1-based
+   neighbours per vertex, '%' comments), the sorted edge file ("<type> n m"
+   header, "e u w" records of 1-based endpoints) and the sorted binary file
+   (uint64 n, uint64 m, m pairs of uint64 1-based endpoints).  The result is
+   the symmetric CSR with sorted rows, self-loops and repeated edges dropped;
+   a malformed file or an endpoint outside [1, n] gives CC_ERR_INVALID.  Free
+   with cc_host_graph_free. */
+int cc_read_metis(const char *path, uint32_t id_bytes, cc_host_graph *out);
+int cc_read_edge_list(const char *path, uint32_t id_bytes, cc_host_graph *out);
+int cc_read_binary_edges(const char *path, uint32_t id_bytes, cc_host_graph *out);
+
 #ifdef __cplusplus
 }
 #endif

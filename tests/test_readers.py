@@ -1,0 +1,75 @@
+"""The input-file readers of libccgen (METIS text, sorted edge file, sorted
+binary file; the reference's GraphIO formats) against from_edges on the same
+edges, and their error reports.  Host code: no GPU."""
+from __future__ import annotations
+
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+import components_gb300 as cc
+from components_gb300 import _lib
+
+GOLD = np.load(Path(__file__).with_name("golden") / "golden.npz")
+
+
+def same_csr(a, b):
+    ra, ca = a.numpy()
+    rb, cb = b.numpy()
+    return np.array_equal(ra, rb) and np.array_equal(ca, cb)
+
+
+def write_metis(path, n, edges, header_m=None, comment=True):
+    adj = [[] for _ in range(n)]
+    for u, w in edges:
+        adj[u].append(w)
+        adj[w].append(u)
+    lines = (["% restated test input"] if comment else []) + [f"{n} {header_m if header_m is not None else len(edges)}"]
+    lines += [" ".join(str(w + 1) for w in row) for row in adj]
+    Path(path).write_text("\n".join(lines) + "\n")
+
+
+def test_metis_fixture(tmp_path):
+    n, edges = int(GOLD["simple_n"][0]), [tuple(map(int, e)) for e in GOLD["simple_edges"]]
+    p = tmp_path / "simple.graph"
+    write_metis(p, n, edges, header_m=len(edges) + 1)  # the fixture's header overstates m
+    G = cc.read_metis(str(p))
+    assert same_csr(G, cc.from_edges(n, edges))
+
+
+@pytest.mark.parametrize("idb", [4, 8])
+def test_readers_match_from_edges(tmp_path, idb):
+    rng = np.random.default_rng(3)
+    n = 700
+    e = rng.integers(0, n, size=(2000, 2))
+    edges = [(int(u), int(w)) for u, w in e]  # self-loops and repeats included: dropped by all
+    want = cc.from_edges(n, edges, id_bytes=idb)
+    pm = tmp_path / "g.metis"
+    write_metis(pm, n, [(u, w) for u, w in edges if u != w])
+    assert same_csr(cc.read_metis(str(pm), id_bytes=idb), want)
+    pe = tmp_path / "g.edges"
+    pe.write_text(f"% comment\np {n} {len(edges)}\n" + "".join(f"e {u + 1} {w + 1}\n" for u, w in edges)
+                  + "c ignored record\n")
+    assert same_csr(cc.read_edge_list(str(pe), id_bytes=idb), want)
+    pb = tmp_path / "g.bin"
+    pb.write_bytes(np.array([n, len(edges)], np.uint64).tobytes()
+                   + (np.array(edges, np.uint64) + 1).tobytes())
+    assert same_csr(cc.read_binary_edges(str(pb), id_bytes=idb), want)
+
+
+def test_reader_errors(tmp_path):
+    bad = [("m0", "3 1\n0\n\n\n", cc.read_metis), ("mbig", "3 1\n4\n\n\n", cc.read_metis),
+           ("e0", "p 3 1\ne 0 1\n", cc.read_edge_list), ("nohdr", "% only\n", cc.read_edge_list)]
+    for name, text, fn in bad:
+        p = tmp_path / name
+        p.write_text(text)
+        with pytest.raises(_lib.CCError) as ei:
+            fn(str(p))
+        assert ei.value.status == _lib.CC_ERR_INVALID, name
+    p = tmp_path / "short.bin"
+    p.write_bytes(np.array([3, 5], np.uint64).tobytes() + np.array([1, 2], np.uint64).tobytes())
+    with pytest.raises(_lib.CCError):
+        cc.read_binary_edges(str(p))
+    with pytest.raises(_lib.CCError):
+        cc.read_metis(str(tmp_path / "missing.graph"))
