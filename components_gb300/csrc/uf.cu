@@ -696,10 +696,15 @@ __global__ void __launch_bounds__(1024, 2)
         const uint32_t total = __reduce_add_sync(0xffffffffu, deg);
         if (maxdeg <= 2 * ((total + 31) / 32) + 1) {
           // even degrees: lane = row, maxdeg steps, the ids of 32 neighbouring
-          // rows are adjacent in memory
+          // rows are adjacent in memory.  A step where no lane holds an edge to
+          // a smaller id (or a bad id) has nothing to unite or emit and skips
+          // the edge logic: on sorted rows the later entries are the larger
+          // neighbours.
           for (uint32_t j = 0; j < maxdeg; ++j) {
             const bool valid = j < deg;
-            edge(valid, valid ? (uint64_t)__ldg(col + rb + j) : 0ull, i, lo, hi, true);
+            const uint64_t uu = valid ? (uint64_t)__ldg(col + rb + j) : 0ull;
+            if (__any_sync(0xffffffffu, valid && (uu >= n || (uint32_t)uu < tt + i)))
+              edge(valid, uu, i, lo, hi, true);
           }
         } else {
           // skewed degrees: the 32 rows' edges as one flattened stream, lane k
