@@ -73,3 +73,16 @@ def test_reader_errors(tmp_path):
         cc.read_binary_edges(str(p))
     with pytest.raises(_lib.CCError):
         cc.read_metis(str(tmp_path / "missing.graph"))
+
+
+def test_metis_line_endings_and_whitespace(tmp_path):
+    """CRLF line ends, tabs, trailing spaces, comment lines between vertex
+    lines and a missing last line (an isolated vertex) read as the same graph."""
+    n, edges = 5, [(0, 1), (1, 2), (3, 4)]
+    text = "% c\r\n5 3\r\n2 \r\n1\t3\r\n% between\r\n2\r\n5\r\n4\r\n"
+    p = tmp_path / "crlf.graph"
+    p.write_bytes(text.encode())
+    assert same_csr(cc.read_metis(str(p)), cc.from_edges(n, edges))
+    q = tmp_path / "short.graph"
+    q.write_text("4 1\n2\n1\n")  # vertices 2 and 3 have no line: isolated
+    assert same_csr(cc.read_metis(str(q)), cc.from_edges(4, [(0, 1)]))
