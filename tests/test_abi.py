@@ -105,6 +105,20 @@ def test_misaligned_device_arrays_are_rejected_before_any_device_call():
     assert lib.cc_csr_validate(C.byref(g), 0) == _lib.CC_ERR_INVALID
 
 
+def test_size_limits_are_reported_before_any_device_call():
+    """Labels are 32-bit inside: n >= 2^32 - 1 is refused up front, as is a
+    G(n, m) draw of 2^32 or more directed entries and a grid of 2^30 vertices
+    on the device generators (their offsets use a 32-bit scan)."""
+    lib = _lib.gpu()
+    g = _lib.cc_csr(1 << 32, 0, 0x1000, 0, 4, 1, _lib.CC_DEVICE, 0)
+    assert lib.cc_csr_validate(C.byref(g), 0) == _lib.CC_ERR_UNSUPPORTED
+    m = C.c_uint64()
+    assert lib.cc_gen_gnm_device(None, 1 << 20, 1 << 31, 1, 4, 0x1000, 0x2000, 1, C.byref(m)) == \
+        _lib.CC_ERR_UNSUPPORTED
+    assert lib.cc_gen_grid_device(None, 1 << 15, 1 << 15, 0.5, 1, 4, 0x1000, 0x2000, 1, C.byref(m)) == \
+        _lib.CC_ERR_UNSUPPORTED
+
+
 def test_host_validation():
     lib = _lib.gpu()
     rp = np.array([0, 1, 2], np.uint64)
