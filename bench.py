@@ -60,6 +60,22 @@ def dist_env():
     return rank, world, local
 
 
+def max_over_ranks(x: float, world: int, device=None) -> float:
+    """The slowest rank's value of x (every rank calls it; one rank: x)."""
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_gedges(world: int, m: int, ms_per_step: float) -> float:
+    """Gedges/s of the whole job: every rank solves its own m-entry replica."""
+    return world * m / (ms_per_step * 1e-3) / 1e9
+
+
 def peaks():
     p = ROOT / "MEASURED_PEAKS.json"
     if p.exists():
@@ -483,13 +499,9 @@ def main():
     launches = tot["kernel_launches"]
     kstats = tot["kernels"]
     solve_ms_mean = tot["solve_ms"] / max(tot["solves"], 1)
-    elapsed_ms = ev0.elapsed_time(ev1)
-    if world > 1:
-        t = torch.tensor([elapsed_ms], device=f"cuda:{local}")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        elapsed_ms = float(t.item())
+    elapsed_ms = max_over_ranks(ev0.elapsed_time(ev1), world, f"cuda:{local}")
     ms_per_step = elapsed_ms / args.steps
-    value = world * m / (ms_per_step * 1e-3) / 1e9
+    value = whole_job_gedges(world, m, ms_per_step)
     clock = clocks.summary()
 
     # labels checked against the oracle once (outside the timed region)
@@ -513,11 +525,8 @@ def main():
     barrier()
     e2e_s = (time.perf_counter() - t0) / args.steps
     e2e_st = solver.last_stats  # bytes the library moved over the host link in the last step
-    if world > 1:
-        t = torch.tensor([e2e_s], device=f"cuda:{local}")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e_s = float(t.item())
-    e2e_value = world * m / e2e_s / 1e9
+    e2e_s = max_over_ranks(e2e_s, world, f"cuda:{local}")
+    e2e_value = whole_job_gedges(world, m, e2e_s * 1e3)
     if checked is not None:
         checked = checked and bool(np.array_equal(hlab.numpy().view(np.uint32).astype(np.uint64),
                                                   lab.cpu().numpy().view(np.uint32).astype(np.uint64)))
