@@ -3,7 +3,8 @@
 A plain-C restatement (cc_oracle.c) of the reference's connected-components
 algorithms plus an independent union-find.  Only tests/, the smoke check of
 __graft_entry__ and the CPU-baseline legs of bench.py use it, and only as the
-checker or the timed CPU baseline; the product (components_gb300) never does.
+answer the GPU labels are compared with or as the timed CPU baseline; the
+product (components_gb300) never does.
 
 Parity is pinned to the reference's only fixture (example/simple.graph,
 canonical labels [0,0,0,3,3,3]) and to the union-find: connected components
