@@ -142,6 +142,37 @@ def read_binary_edges(path: str, id_bytes: int = 4, num_parts: int = 1) -> Stati
     return _read("cc_read_binary_edges", path, id_bytes, num_parts)
 
 
+def load_graph(conf, id_bytes: int = 4, num_parts: int = 1) -> StaticGraph:
+    """The input of the reference drivers (IOUtility::LoadGraph,
+    io_utils.h:33-56) from a parsed Config: `-input file|edgefile|binary -in
+    <path>` reads the file (METIS text, sorted edge file, sorted binary file);
+    otherwise `-gen gnm_undirected|grid_2d|rhg` with `-n -m -p -d -gamma
+    -seed` builds the graph with the seeded generators.  Partitioned edge
+    files (one per rank) and the other KaGen models are refused."""
+    t = conf.input_type
+    if t == "file":
+        return read_metis(conf.input_file, id_bytes, num_parts)
+    if t == "edgefile":
+        return read_edge_list(conf.input_file, id_bytes, num_parts)
+    if t == "binary":
+        return read_binary_edges(conf.input_file, id_bytes, num_parts)
+    if t == "partition":
+        raise ValueError("-input partition (one edge file per rank) is not read on one device")
+    if conf.gen == "gnm_undirected":
+        return gen_gnm(conf.gen_n, conf.gen_m, seed=conf.seed, id_bytes=id_bytes, num_parts=num_parts)
+    if conf.gen == "grid_2d":
+        if conf.gen_periodic:
+            raise ValueError("-periodic grids are not generated")
+        return gen_grid(conf.gen_n, conf.gen_m, conf.gen_p, seed=conf.seed, id_bytes=id_bytes,
+                        num_parts=num_parts)
+    if conf.gen == "rhg":
+        return gen_rhg(conf.gen_n, conf.gen_d, conf.gen_gamma, seed=conf.seed, id_bytes=id_bytes,
+                       num_parts=num_parts)
+    if conf.gen != "null":
+        raise ValueError(f"generator {conf.gen} is not supported")
+    raise ValueError("I/O type not supported: give -input file|edgefile|binary -in <path>, or -gen")
+
+
 class _HostGraph:
     """Owns a graph allocated by libccgen; frees it on close."""
 

@@ -86,3 +86,28 @@ def test_metis_line_endings_and_whitespace(tmp_path):
     q = tmp_path / "short.graph"
     q.write_text("4 1\n2\n1\n")  # vertices 2 and 3 have no line: isolated
     assert same_csr(cc.read_metis(str(q)), cc.from_edges(4, [(0, 1)]))
+
+
+def test_load_graph_dispatches_like_the_drivers(tmp_path):
+    """-input file|edgefile|binary -in <path> and -gen gnm_undirected|grid_2d|rhg
+    through the parsed Config, as IOUtility::LoadGraph dispatches."""
+    n, edges = 6, [(0, 1), (1, 2), (3, 4), (4, 5)]
+    want = cc.from_edges(n, edges)
+    pm = tmp_path / "g.graph"
+    write_metis(pm, n, edges)
+    pe = tmp_path / "g.edges"
+    pe.write_text(f"p {n} {len(edges)}\n" + "".join(f"e {u + 1} {w + 1}\n" for u, w in edges))
+    pb = tmp_path / "g.bin"
+    pb.write_bytes(np.array([n, len(edges)], np.uint64).tobytes() + (np.array(edges, np.uint64) + 1).tobytes())
+    for kind, path in (("file", pm), ("edgefile", pe), ("binary", pb)):
+        conf = cc.parse_parameters(["-input", kind, "-in", str(path)])
+        assert same_csr(cc.load_graph(conf), want), kind
+    conf = cc.parse_parameters(["-gen", "gnm_undirected", "-n", "10", "-m", "12", "-seed", "3"])
+    assert same_csr(cc.load_graph(conf), cc.gen_gnm(1 << 10, 1 << 12, seed=3, id_bytes=4))
+    conf = cc.parse_parameters(["-gen", "grid_2d", "-n", "40", "-m", "30", "-p", "0.5", "-seed", "2"])
+    assert same_csr(cc.load_graph(conf), cc.gen_grid(40, 30, 0.5, seed=2))
+    conf = cc.parse_parameters(["-gen", "rhg", "-n", "12", "-d", "8", "-gamma", "2.6", "-seed", "4"])
+    assert same_csr(cc.load_graph(conf), cc.gen_rhg(1 << 12, 8.0, 2.6, seed=4))
+    for bad in (["-input", "partition", "-in", str(pe)], ["-gen", "ba"], ["-gen", "grid_2d", "-periodic"], []):
+        with pytest.raises(ValueError):
+            cc.load_graph(cc.parse_parameters(bad))
