@@ -111,3 +111,43 @@ def test_load_graph_dispatches_like_the_drivers(tmp_path):
     for bad in (["-input", "partition", "-in", str(pe)], ["-gen", "ba"], ["-gen", "grid_2d", "-periodic"], []):
         with pytest.raises(ValueError):
             cc.load_graph(cc.parse_parameters(bad))
+
+
+def test_cpp_load_graph(tmp_path):
+    """ccgpu::LoadGraph (include/components_gb300_io.hpp), compiled with g++
+    and linked with libccgen: the same CSR as the Python readers and
+    generators."""
+    import shutil
+    import subprocess
+    cxx = shutil.which("g++")
+    if not cxx:
+        pytest.skip("g++ missing")
+    root = Path(__file__).resolve().parent.parent
+    exe = tmp_path / "io_main"
+    gen_lib, gpu_lib = _lib.BUILD / "libccgen.so", _lib.gpu_lib_path()
+    subprocess.run([cxx, "-O2", "-std=c++17", "-I", str(root / "include"), str(root / "tests" / "cpp" / "io_main.cpp"),
+                    "-o", str(exe), str(gen_lib), str(gpu_lib), f"-Wl,-rpath,{gen_lib.parent}"], check=True)
+
+    def run(*args):
+        out = subprocess.run([str(exe), *map(str, args)], capture_output=True, text=True, timeout=120)
+        assert out.returncode == 0, out.stderr
+        lines = out.stdout.splitlines()
+        rp = np.array(lines[1].split(), np.uint64)
+        col = np.array(lines[2].split(), np.uint64)
+        return rp, col
+
+    def same(rpcol, G):
+        rp, col = G.numpy()
+        return np.array_equal(rpcol[0], rp) and np.array_equal(rpcol[1], col)
+
+    n, edges = 6, [(0, 1), (1, 2), (3, 4), (4, 5)]
+    pm = tmp_path / "g.graph"
+    write_metis(pm, n, edges)
+    assert same(run("file", pm), cc.from_edges(n, edges))
+    pb = tmp_path / "g.bin"
+    pb.write_bytes(np.array([n, len(edges)], np.uint64).tobytes() + (np.array(edges, np.uint64) + 1).tobytes())
+    assert same(run("binary", pb), cc.from_edges(n, edges))
+    assert same(run("gen", "gnm_undirected", 500, 900, 1.0, 16.0, 2.2, 3), cc.gen_gnm(500, 900, seed=3))
+    assert same(run("gen", "grid_2d", 30, 20, 0.5, 16.0, 2.2, 2), cc.gen_grid(30, 20, 0.5, seed=2))
+    bad = subprocess.run([str(exe), "gen", "ba", "10", "10", "1", "1", "1", "1"], capture_output=True, text=True)
+    assert bad.returncode == 1 and "not supported" in bad.stderr
