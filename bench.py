@@ -1,26 +1,36 @@
 #!/usr/bin/env python3
 """Benchmark of the connected-components solve on GB300.
 
-Workload (one step = one CC solve): the 8192 x 8192 2D bond-percolation grid
-(each lattice edge kept with p = 0.5, seed 1; 67,108,864 vertices,
-134,191,308 directed CSR entries, uint32 ids), solved by the exp_contraction
-option (ExponentialContraction::FindComponents) with the reference's default
-Config (beta 0.1, seq 1, algorithm seed 1001 = seed + 0 + 1000), one rank.
+Headline workload (one step = one CC solve): the random hyperbolic graph of
+n = 2^26 vertices, expected average degree 16, degree exponent gamma = 2.6
+(threshold model, input seed 1; about 1.095e9 directed CSR entries, uint32
+ids), solved by the exp_contraction option
+(ExponentialContraction::FindComponents, app/exp_contraction.cpp:104-105)
+with the reference's default Config (beta 0.1, seq 1, algorithm seed
+1001 = seed + 0 + 1000), one rank.  It is the largest configuration that fits
+one GPU (-gen rhg -n 26 -d 16 -gamma 2.6).
 
-  value   Gedges/s = directed CSR entries / device time of the solve, input
-          resident in HBM (CUDA events on the library's stream)
-  e2e     the same metric through the C ABI with pinned HOST buffers: the
-          host->device copy of the CSR and the device->host copy of the
-          labels are inside the timed region
+  value     Gedges/s = directed CSR entries / device time of the solve, input
+            resident in HBM (CUDA events on the library's stream)
+  e2e       the same metric through the C ABI with pinned HOST buffers: the
+            host->device copy of the CSR and the device->host copy of the
+            labels are inside the timed region
   roofline  the dominant kernel's algorithmic bytes per launch / its average
-          CUDA-event duration, against the measured HBM copy bandwidth
+            CUDA-event duration, against the measured HBM copy bandwidth
+  cpu_baseline  the CPU restatement of ExponentialContraction (oracle/) with
+            one rank per host core on the same graph, a bounded sample
 
-Inputs (1.07 GB CSR + 0.27 GB labels) are larger than the 129 MB L2, so no
+Inputs (4.9 GB CSR + 0.27 GB labels) are larger than the 129 MB L2, so no
 flush is needed between steps.
 
+--workload grid prints the same line for the 8192 x 8192 bond-percolation
+grid (p = 0.5, uint32 ids); --workload gnm | rhg-options | batch | serve
+print the other configurations' lines.
+
 --impl reference times the CPU restatement of the reference algorithm
-(oracle/, all host threads as ranks) on the same workload and prints the same
-JSON line with "impl": "reference".
+(oracle/, one rank per host core) on the same graph, built by the oracle's
+own input path (no GPU library is loaded), and prints the same JSON line with
+"impl": "reference".
 
 Multi-GPU (torchrun, N ranks): every rank solves its own replica (a single
 graph does not shard on this path: replicas only); value = N x E / max-over-
@@ -43,14 +53,66 @@ import numpy as np
 ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
-GRID_X = GRID_Y = 8192
-GRID_P = 0.5
 INPUT_SEED = 1
 ALGO_SEED = 1001
-METRIC = "Gedges/s per CC solve (exp_contraction, 2D bond percolation 8192x8192, p=0.5)"
+BETA, SEQ = 0.1, 1
+RHG_LOG2N, RHG_DEG, RHG_GAMMA = 26, 16.0, 2.6
+GRID_SIDE, GRID_P = 8192, 0.5
 UNIT = "Gedges/s"
 FALLBACK_HBM = 6800.0
 L2_BYTES = 129 * 1024 * 1024
+
+
+# ---- the two single-graph workloads -------------------------------------------
+class Workload:
+    """One graph family at one size: how each arm builds it and how the JSON
+    line names it.  Both arms build the same graph bit for bit (the same
+    generator code; the reference arm's copy is linked into the oracle)."""
+
+    def __init__(self, name: str, args):
+        self.name = name
+        if name == "rhg":
+            k = args.rhg_log2n
+            self.n = 1 << k
+            self.desc = (f"random hyperbolic graph n=2^{k}, avg degree {RHG_DEG:g}, gamma {RHG_GAMMA} "
+                         f"(threshold model, seed {INPUT_SEED}), exp_contraction")
+            self.metric = (f"Gedges/s per CC solve (exp_contraction, random hyperbolic graph n=2^{k}, "
+                           f"d=16, gamma=2.6)")
+            self.flags = f"-gen rhg -n {k} -d 16 -gamma 2.6"
+        else:
+            side = args.grid
+            self.n = side * side
+            self.desc = f"grid2d {side}x{side} p={GRID_P} (seed {INPUT_SEED}), exp_contraction"
+            self.metric = f"Gedges/s per CC solve (exp_contraction, 2D bond percolation {side}x{side}, p=0.5)"
+            self.flags = f"-gen grid_2d -n {side} -m {side} -p 0.5"
+        self.args = args
+
+    def ours(self):
+        """The graph for the GPU arm (components_gb300 host generators)."""
+        import components_gb300 as cc
+        if self.name == "rhg":
+            return cc.gen_rhg(self.n, RHG_DEG, RHG_GAMMA, seed=INPUT_SEED, id_bytes=4)
+        return cc.gen_grid(self.args.grid, self.args.grid, GRID_P, seed=INPUT_SEED, id_bytes=4)
+
+    def oracle(self):
+        """The same graph through the oracle's own input path."""
+        import oracle
+        if self.name == "rhg":
+            return oracle.gen_rhg(self.n, RHG_DEG, RHG_GAMMA, seed=INPUT_SEED, id_bytes=4)
+        return oracle.gen_grid(self.args.grid, self.args.grid, GRID_P, seed=INPUT_SEED, id_bytes=4)
+
+    def config(self, n: int, m: int, world: int) -> dict:
+        """The config dict of the JSON line, identical in both arms."""
+        return {"workload": self.desc, "reference_flags": self.flags, "n": n, "m_dir": m,
+                "id_bytes": 4, "algo": "exp_contraction", "beta": BETA, "seq": SEQ,
+                "algo_seed": ALGO_SEED, "parallelism": f"replicas x{world}",
+                "l2": l2_note(8 * (n + 1) + 4 * m + 4 * n)}
+
+
+def l2_note(nbytes: int) -> str:
+    if nbytes > L2_BYTES:
+        return f"inputs larger than L2 ({nbytes / 1e9:.2f} GB CSR+labels > 129 MB), no flush"
+    return f"inputs of {nbytes / 1e6:.1f} MB fit L2 (a reduced size for profiling, not the config)"
 
 
 def dist_env():
@@ -84,13 +146,14 @@ def peaks():
     return FALLBACK_HBM, "fallback 6.8 TB/s (MEASURED_PEAKS.json absent)"
 
 
-def traffic_from_profile(kernel: str):
-    """dram bytes per launch of `kernel` from the committed ncu summary."""
+def traffic_from_profile(kernel: str, workload: str):
+    """dram bytes per launch of `kernel` on `workload` from the committed ncu
+    summaries (profiles/traffic.json)."""
     p = ROOT / "profiles" / "traffic.json"
     if not p.exists():
         return None, None
     d = json.loads(p.read_text())
-    e = d.get(kernel)
+    e = d.get(workload, {}).get(kernel)
     if not e:
         return None, None
     return e.get("dram_bytes_per_launch"), e.get("source")
@@ -155,41 +218,187 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-def make_graph(side: int = GRID_X):
-    import components_gb300 as cc
-    return cc.gen_grid(side, side, GRID_P, seed=INPUT_SEED, id_bytes=4)
-
-
-def cpu_reference_run(G, steps, warmup, sample_rows=None):
-    """Time the oracle's restatement of ExponentialContraction with one
-    thread per rank, P = host cores.  Returns (Gedges/s, per-step s, sample)."""
+def cpu_reference_run(G, steps: int, warmup: int):
+    """Time the oracle's restatement of ExponentialContraction with one rank
+    per host core (OpenMP threads) on G (any graph with numpy() and n).
+    Returns (Gedges/s, mean seconds per solve, ranks)."""
+    import ctypes as C
     import oracle
     threads = os.cpu_count() or 1
     os.environ.setdefault("OMP_NUM_THREADS", str(threads))
-    if sample_rows:
-        import components_gb300 as cc
-        Gs = cc.gen_grid(GRID_X, sample_rows, GRID_P, seed=INPUT_SEED, id_bytes=4)
-        sample = f"{GRID_X}x{sample_rows} rows of the same grid family (p={GRID_P}, seed {INPUT_SEED})"
-    else:
-        Gs = G
-        sample = f"full {GRID_X}x{GRID_Y} grid"
-    n, rp, col = oracle.csr_u64(Gs)
-    out = np.empty(n, np.uint64)
-    import ctypes as C
+    n, rp, col = oracle.csr_u64(G)
+    out = np.empty(max(n, 1), np.uint64)
     rounds = C.c_uint64()
     times = []
     for i in range(warmup + steps):
         t0 = time.perf_counter()
-        oracle.lib().or_exp_contraction(n, rp, col, threads, 0.1, 1, 0, ALGO_SEED + i, out,
+        oracle.lib().or_exp_contraction(n, rp, col, threads, BETA, SEQ, 0, ALGO_SEED + i, out,
                                         C.byref(rounds))
         t = time.perf_counter() - t0
         if i >= warmup:
             times.append(t)
-    m = int(rp[-1])
-    mean = sum(times) / len(times)
-    return m / mean / 1e9, mean, threads, sample
+    m = int(rp[-1]) if n else 0
+    mean = sum(times) / max(len(times), 1)
+    return m / mean / 1e9, mean, threads
 
 
+def reference_arm(args, wl: Workload, world: int) -> dict:
+    """The reference arm: the oracle's restatement on the host cores, on the
+    graph built by the oracle's own input path.  Imports nothing of
+    components_gb300 and loads no GPU library."""
+    import oracle
+    oracle.build()
+    H = wl.oracle()
+    gps, mean_s, threads = cpu_reference_run(H, max(args.steps, 1), args.warmup)
+    sample = (f"the full graph ({wl.flags}), {max(args.steps, 1)} solves after {args.warmup} warm-up, "
+              f"{mean_s:.2f} s each; oracle/cc_oracle.c restatement of ExponentialContraction "
+              f"(exponential_contraction.h:59-319) with {threads} ranks as threads")
+    return {
+        "impl": "reference", "metric": wl.metric, "value": gps, "unit": UNIT,
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": mean_s * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "u64", "data": "synthetic (seeded stand-in for KaGen)",
+        "config": wl.config(H.n, H.m, world),
+        "cpu_baseline": {"value": gps, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": gps, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+
+
+def gpu_arm(args, wl: Workload, rank: int, world: int, local: int) -> dict | None:
+    """The headline line of our arm (every rank solves its own replica)."""
+    import torch
+    import components_gb300 as cc
+
+    G = wl.ours()
+    n, m = G.n, G.m
+    conf = cc.Config(seed=ALGO_SEED, beta=BETA, sequential_limit=SEQ)
+    ctx = cc.Context(local)
+    ctx.set_tuning(hook_mode=args.hook_mode, tile_vertices=args.tile, tile_threads=args.tile_threads)
+    stream = torch.cuda.ExternalStream(ctx.stream_handle)
+    D = G.to_device(f"cuda:{local}")
+    lab = torch.empty(n, dtype=torch.int32, device=f"cuda:{local}")
+    solver = cc.ExponentialContraction(conf, 0, 1, ctx)
+
+    def barrier():
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+
+    # ---- device-resident solve ---------------------------------------------
+    for _ in range(args.warmup):
+        solver.FindComponents(D, lab)
+    ctx.set_profiling(True)
+    barrier()
+    with ClockSampler(local) as clocks:
+        ev0 = torch.cuda.Event(enable_timing=True)
+        ev1 = torch.cuda.Event(enable_timing=True)
+        ev0.record(stream)
+        for _ in range(args.steps):
+            solver.FindComponents(D, lab)
+        ev1.record(stream)
+        barrier()
+    # per-kernel CUDA-event times of the timed solves, summed by the library
+    tot = ctx.profile_totals()
+    ctx.set_profiling(False)
+    launches = tot["kernel_launches"]
+    kstats = tot["kernels"]
+    solve_ms_mean = tot["solve_ms"] / max(tot["solves"], 1)
+    elapsed_ms = max_over_ranks(ev0.elapsed_time(ev1), world, f"cuda:{local}")
+    ms_per_step = elapsed_ms / args.steps
+    value = whole_job_gedges(world, m, ms_per_step)
+    clock = clocks.summary()
+    got_dev = lab.cpu().numpy().view(np.uint32).copy()
+
+    # ---- end to end through the C ABI with pinned host buffers ---------------
+    Hp = G.pinned()
+    hlab = torch.empty(n, dtype=torch.int32).pin_memory()
+    for _ in range(max(1, args.warmup)):
+        solver.FindComponents(Hp, hlab)
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        solver.FindComponents(Hp, hlab)
+    barrier()
+    e2e_s = (time.perf_counter() - t0) / args.steps
+    e2e_st = solver.last_stats  # bytes the library moved over the host link in the last step
+    e2e_s = max_over_ranks(e2e_s, world, f"cuda:{local}")
+    e2e_value = whole_job_gedges(world, m, e2e_s * 1e3)
+    got_host = hlab.numpy().view(np.uint32).copy()
+    del Hp
+
+    # ---- roofline of the dominant kernel -------------------------------------
+    top = max(kstats.items(), key=lambda kv: kv[1]["ms"]) if kstats else (None, None)
+    peak, peak_src = peaks()
+    roof = None
+    if top[0]:
+        name, k = top
+        per_launch_bytes = k["bytes"] / max(k["launches"], 1)
+        per_launch_ms = k["ms"] / max(k["launches"], 1)
+        achieved = per_launch_bytes / (per_launch_ms * 1e-3) / 1e9
+        traffic, traffic_src = traffic_from_profile(name, wl.name)
+        roof = {"bound": "hbm", "kernel": name, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "traffic": traffic,
+                "algorithmic_bytes_per_launch": per_launch_bytes, "ms_per_launch": per_launch_ms,
+                "peak_source": peak_src, "traffic_source": traffic_src}
+    ksum = max(sum(x["ms"] for x in kstats.values()), 1e-12)
+    share = {k: v["ms"] / ksum for k, v in kstats.items()}
+    per_kernel = {k: {"launches_per_solve": v["launches"] / max(tot["solves"], 1),
+                      "ms_per_launch": v["ms"] / max(v["launches"], 1),
+                      "frac": (v["bytes"] / max(v["launches"], 1) / (v["ms"] / max(v["launches"], 1) * 1e-3)
+                               / 1e9 / peak) if v["bytes"] and v["ms"] > 0 else None}
+                  for k, v in kstats.items()}
+
+    if world > 1:
+        torch.distributed.barrier()
+    if rank != 0:
+        return None
+
+    # labels checked against the oracle's union-find once (outside the timed regions)
+    checked = None
+    if not args.no_check:
+        import oracle
+        oracle.build()
+        want = oracle.uf_labels(G)
+        checked = bool(np.array_equal(got_dev.astype(np.uint64), want)
+                       and np.array_equal(got_host, got_dev))
+
+    # ---- CPU baseline: the oracle restatement on a bounded sample -------------
+    cpu = None
+    if world == 1 and args.cpu_steps > 0:
+        gps, mean_s, threads = cpu_reference_run(G, args.cpu_steps, 1)
+        cpu = {"value": gps, "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": f"the full graph, {args.cpu_steps} timed solves after 1 warm-up "
+                         f"({mean_s:.2f} s each); oracle/cc_oracle.c restatement of "
+                         f"ExponentialContraction with {threads} ranks as threads"}
+
+    return {
+        "metric": wl.metric, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "u32",
+        "data": "synthetic (seeded stand-in for KaGen)",
+        "config": wl.config(n, m, world),
+        "virtual_ranks": 1,
+        "e2e": {"value": e2e_value, "unit": UNIT,
+                "h2d_bytes_per_step": int(e2e_st["h2d_bytes"]), "d2h_bytes_per_step": int(e2e_st["d2h_bytes"]),
+                "input_bytes_per_step": 8 * (n + 1) + 4 * m,
+                "h2d_note": "CSR copied from pinned host memory inside the timed call (row offsets of "
+                            "rows under 255 entries may cross as one degree byte each when the "
+                            "graph is streamed under the tiled pass)",
+                "ms_per_step": e2e_s * 1e3},
+        "gpu_launches": launches,
+        "roofline": roof,
+        "kernel_share": share,
+        "per_kernel": per_kernel,
+        "solve_ms_mean": solve_ms_mean,
+        "labels_match_oracle": checked,
+        "clocks": clock,
+        "cpu_baseline": cpu,
+    }
+
+
+# ---- the other configurations' lines -------------------------------------------
 def _timed_solves(solver, D, lab, steps, warmup, ctx):
     for _ in range(warmup):
         solver.FindComponents(D, lab)
@@ -207,7 +416,7 @@ def _timed_solves(solver, D, lab, steps, warmup, ctx):
     return ms, kern, st
 
 
-def workload_single(args, name):
+def workload_options(args, name):
     """G(2^20, 2^22) with 64-bit ids, or the 2^k-vertex RHG (d = 16, gamma = 2.6):
     one JSON line per (algo option, virtual ranks)."""
     import torch
@@ -218,7 +427,7 @@ def workload_single(args, name):
         G = cc.gen_gnm(1 << 20, 1 << 22, seed=INPUT_SEED, id_bytes=8)
         desc = "G(n=2^20, m=2^22) uniform endpoints, u64 ids"
     else:
-        G = cc.gen_rhg(1 << args.rhg_log2n, 16.0, 2.6, seed=INPUT_SEED, id_bytes=4)
+        G = cc.gen_rhg(1 << args.rhg_log2n, RHG_DEG, RHG_GAMMA, seed=INPUT_SEED, id_bytes=4)
         desc = f"RHG n=2^{args.rhg_log2n}, d=16, gamma=2.6 (threshold model), u32 ids"
     gen_s = time.time() - t0
     want = oracle.uf_labels(G) if not args.no_check else None
@@ -282,7 +491,17 @@ def workload_batch(args):
     torch.cuda.synchronize()
     batched_s = (time.perf_counter() - t0) / args.steps
     batched = lab.cpu().numpy().view(np.uint32).copy()
-    # plain path: one cc_ctx_run per graph, inputs already on the device
+    # plain path, looped in C++: one cc_ctx_run per graph, inputs already on the device
+    conf = cc.Config(seed=ALGO_SEED)
+    plain_c = torch.empty(bt.total_n, dtype=torch.int32, device="cuda:0")
+    B.plain_run(D, ctx, plain_c, "exp", conf)  # warm-up (and the per-graph offsets)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    B.plain_run(D, ctx, plain_c, "exp", conf)
+    torch.cuda.synchronize()
+    plain_c_s = time.perf_counter() - t0
+    same_c = bool(np.array_equal(plain_c.cpu().numpy().view(np.uint32), batched))
+    # the same loop from Python (ctypes and tensor slicing per graph)
     v, r, c = bt.numpy()
     graphs = []
     for i in range(bt.k):
@@ -304,8 +523,11 @@ def workload_batch(args):
     print(json.dumps({
         "workload": "batch", "graphs": bt.k, "total_n": bt.total_n, "total_m": bt.total_m,
         "metric": "graphs/s", "batched_graphs_per_s": bt.k / batched_s,
-        "plain_graphs_per_s": bt.k / plain_s, "speedup": plain_s / batched_s,
-        "batched_ms": batched_s * 1e3, "plain_ms": plain_s * 1e3,
+        "plain_graphs_per_s": bt.k / plain_c_s, "speedup": plain_c_s / batched_s,
+        "plain_loop": "C++ (cc_batch_run_plain: one cc_ctx_run per graph)",
+        "plain_python_graphs_per_s": bt.k / plain_s, "speedup_vs_python_loop": plain_s / batched_s,
+        "batched_ms": batched_s * 1e3, "plain_ms": plain_c_s * 1e3, "plain_python_ms": plain_s * 1e3,
+        "labels_bit_identical_c_loop": same_c,
         "batched_gedges_per_s": bt.total_m / batched_s / 1e9,
         "labels_bit_identical": same, "tuning": tune.as_dict(), "gen_s": gen_s}), flush=True)
     ctx.close()
@@ -352,7 +574,6 @@ def workload_serve(args):
         gaps = rng.exponential(1.0 / rate, len(reqs))
         results = [None] * len(reqs)
         infos = [None] * len(reqs)
-        import threading
         tickets = [None] * len(reqs)
 
         def producer():
@@ -391,7 +612,7 @@ def workload_serve(args):
                   f"n log-uniform in [2^10, 2^{args.serve_log2n_max}]"}), flush=True)
 
 
-def main():
+def parse_args(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=10)
@@ -399,60 +620,52 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-steps", type=int, default=2)
     ap.add_argument("--no-check", action="store_true")
-    ap.add_argument("--grid", type=int, default=GRID_X,
+    ap.add_argument("--workload", default="rhg",
+                    choices=["rhg", "grid", "gnm", "rhg-options", "batch", "serve"],
+                    help="rhg (the headline line) or grid print the contract line; the others "
+                         "print their own lines")
+    ap.add_argument("--rhg-log2n", type=int, default=RHG_LOG2N,
+                    help="RHG size (default 2^26; smaller sizes are for ncu captures)")
+    ap.add_argument("--grid", type=int, default=GRID_SIDE,
                     help="grid side (default 8192; smaller sides are for ncu captures)")
     ap.add_argument("--hook-mode", type=int, default=0,
-                    help="hook schedule (cc_tuning.hook_mode: 0 auto, 1 global, 2 tiled)")
+                    help="hook schedule (cc_tuning.hook_mode: 0 auto, 1 global, 2 tiled, 3 sampled)")
     ap.add_argument("--tile", type=int, default=0, help="cc_tuning.tile_vertices (0 = default)")
     ap.add_argument("--tile-threads", type=int, default=0, help="cc_tuning.tile_threads")
-    ap.add_argument("--workload", default="grid", choices=["grid", "gnm", "rhg", "batch", "serve"],
-                    help="grid (the headline line); the others print their own lines")
-    ap.add_argument("--rhg-log2n", type=int, default=26)
     ap.add_argument("--batch-k", type=int, default=4096)
     ap.add_argument("--serve-requests", type=int, default=600)
     ap.add_argument("--serve-pool", type=int, default=24)
     ap.add_argument("--serve-log2n-max", type=float, default=22)
-    args = ap.parse_args()
+    return ap.parse_args(argv)
+
+
+def main(argv=None):
+    args = parse_args(argv)
     rank, world, local = dist_env()
-    if args.workload != "grid" and args.impl == "ours":
-        import __graft_entry__ as ge
+
+    if args.impl == "reference":
+        # rank 0 alone runs the CPU reference; the other ranks exit without work
+        if rank != 0:
+            return 0
+        wl = Workload(args.workload if args.workload in ("rhg", "grid") else "rhg", args)
+        print(json.dumps(reference_arm(args, wl, world)), flush=True)
+        return 0
+
+    import torch
+    import __graft_entry__ as ge
+    if args.workload not in ("rhg", "grid"):
         ge.build()
-        import torch
         torch.cuda.set_device(0)
-        if args.workload in ("gnm", "rhg"):
-            workload_single(args, args.workload)
+        if args.workload == "gnm":
+            workload_options(args, "gnm")
+        elif args.workload == "rhg-options":
+            workload_options(args, "rhg")
         elif args.workload == "batch":
             workload_batch(args)
         else:
             workload_serve(args)
         return 0
 
-    if args.impl == "reference":
-        if rank != 0:
-            return 0
-        import __graft_entry__ as ge
-        import oracle
-        oracle.build()
-        ge.build()
-        G = make_graph(args.grid)
-        gps, mean_s, threads, sample = cpu_reference_run(G, max(args.steps, 1), args.warmup)
-        line = {
-            "impl": "reference", "metric": METRIC, "value": gps, "unit": UNIT,
-            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": mean_s * 1e3, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "u64", "data": "synthetic",
-            "config": {"workload": f"grid2d {args.grid}x{args.grid} p=0.5, exp_contraction", "n": G.n,
-                       "m_dir": G.m, "ranks": threads, "beta": 0.1, "seq": 1},
-            "cpu_baseline": {"value": gps, "unit": UNIT, "cores": threads, "kind": "port",
-                             "sample": sample + "; oracle/cc_oracle.c restatement of "
-                             "ExponentialContraction, one thread per rank"},
-            "e2e": {"value": gps, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-        }
-        print(json.dumps(line))
-        return 0
-
-    import torch
-    import __graft_entry__ as ge
     if rank == 0 or world == 1:
         ge.build()
     if world > 1:
@@ -461,129 +674,9 @@ def main():
         dist.barrier()
         ge.build()
     torch.cuda.set_device(local)
-    import components_gb300 as cc
-    from components_gb300 import _lib
-
-    G = make_graph(args.grid)
-    n, m = G.n, G.m
-    conf = cc.Config(seed=ALGO_SEED)
-    ctx = cc.Context(local)
-    ctx.set_tuning(hook_mode=args.hook_mode, tile_vertices=args.tile, tile_threads=args.tile_threads)
-    stream = torch.cuda.ExternalStream(ctx.stream_handle)
-    D = G.to_device(f"cuda:{local}")
-    lab = torch.empty(n, dtype=torch.int32, device=f"cuda:{local}")
-    solver = cc.ExponentialContraction(conf, 0, 1, ctx)
-
-    def barrier():
-        torch.cuda.synchronize()
-        if world > 1:
-            torch.distributed.barrier()
-        torch.cuda.synchronize()
-
-    # ---- device-resident solve -------------------------------------------
-    for _ in range(args.warmup):
-        solver.FindComponents(D, lab)
-    ctx.set_profiling(True)
-    barrier()
-    with ClockSampler(local) as clocks:
-        ev0 = torch.cuda.Event(enable_timing=True)
-        ev1 = torch.cuda.Event(enable_timing=True)
-        ev0.record(stream)
-        for _ in range(args.steps):
-            solver.FindComponents(D, lab)
-        ev1.record(stream)
-        barrier()
-    # per-kernel CUDA-event times of the timed solves, summed by the library
-    tot = ctx.profile_totals()
-    ctx.set_profiling(False)
-    launches = tot["kernel_launches"]
-    kstats = tot["kernels"]
-    solve_ms_mean = tot["solve_ms"] / max(tot["solves"], 1)
-    elapsed_ms = max_over_ranks(ev0.elapsed_time(ev1), world, f"cuda:{local}")
-    ms_per_step = elapsed_ms / args.steps
-    value = whole_job_gedges(world, m, ms_per_step)
-    clock = clocks.summary()
-
-    # labels checked against the oracle once (outside the timed region)
-    checked = None
-    if rank == 0 and not args.no_check:
-        import oracle
-        oracle.build()
-        want = oracle.uf_labels(G)
-        got = lab.cpu().numpy().view(np.uint32).astype(np.uint64)
-        checked = bool(np.array_equal(got, want))
-
-    # ---- end to end through the C ABI with pinned host buffers ---------------
-    Hp = G.pinned()
-    hlab = torch.empty(n, dtype=torch.int32).pin_memory()
-    for _ in range(max(1, args.warmup)):
-        solver.FindComponents(Hp, hlab)
-    barrier()
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        solver.FindComponents(Hp, hlab)
-    barrier()
-    e2e_s = (time.perf_counter() - t0) / args.steps
-    e2e_st = solver.last_stats  # bytes the library moved over the host link in the last step
-    e2e_s = max_over_ranks(e2e_s, world, f"cuda:{local}")
-    e2e_value = whole_job_gedges(world, m, e2e_s * 1e3)
-    if checked is not None:
-        checked = checked and bool(np.array_equal(hlab.numpy().view(np.uint32).astype(np.uint64),
-                                                  lab.cpu().numpy().view(np.uint32).astype(np.uint64)))
-
-    # ---- roofline of the dominant kernel -------------------------------------
-    top = max(kstats.items(), key=lambda kv: kv[1]["ms"]) if kstats else (None, None)
-    peak, peak_src = peaks()
-    roof = None
-    if top[0]:
-        name, k = top
-        per_launch_bytes = k["bytes"] / max(k["launches"], 1)
-        per_launch_ms = k["ms"] / max(k["launches"], 1)
-        achieved = per_launch_bytes / (per_launch_ms * 1e-3) / 1e9
-        traffic, traffic_src = traffic_from_profile(name)
-        roof = {"bound": "hbm", "kernel": name, "achieved": achieved, "peak": peak, "unit": "GB/s",
-                "frac": achieved / peak, "traffic": traffic,
-                "algorithmic_bytes_per_launch": per_launch_bytes, "ms_per_launch": per_launch_ms,
-                "peak_source": peak_src, "traffic_source": traffic_src}
-    share = {k: v["ms"] / max(sum(x["ms"] for x in kstats.values()), 1e-12) for k, v in kstats.items()}
-
-    if world > 1:
-        torch.distributed.barrier()
-    if rank != 0:
-        return 0
-
-    # ---- CPU baseline: the oracle restatement on a bounded sample -------------
-    cpu = None
-    if world == 1 and args.cpu_steps > 0:
-        gps, mean_s, threads, sample = cpu_reference_run(G, args.cpu_steps, 1)
-        cpu = {"value": gps, "unit": UNIT, "cores": threads, "kind": "port",
-               "sample": f"{sample}, {args.cpu_steps} timed solves after 1 warm-up "
-                         f"({mean_s:.2f} s each); oracle/cc_oracle.c restatement of "
-                         "ExponentialContraction with one thread per rank"}
-
-    line = {
-        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
-        "config": {"workload": f"grid2d {args.grid}x{args.grid} p=0.5 (seed 1), exp_contraction, 1 rank",
-                   "n": n, "m_dir": m, "id_bytes": 4, "beta": 0.1, "seq": 1,
-                   "algo_seed": ALGO_SEED, "parallelism": f"replicas x{world}",
-                   "l2": "inputs larger than L2 (1.34 GB CSR+labels > 129 MB), no flush"},
-        "e2e": {"value": e2e_value, "unit": UNIT,
-                "h2d_bytes_per_step": int(e2e_st["h2d_bytes"]), "d2h_bytes_per_step": int(e2e_st["d2h_bytes"]),
-                "input_bytes_per_step": 8 * (n + 1) + 4 * m,
-                "h2d_note": "row offsets of rows under 255 entries cross the host link as one degree byte each "
-                            "(encoded by host threads inside the timed call), ids as they are",
-                "ms_per_step": e2e_s * 1e3},
-        "gpu_launches": launches,
-        "roofline": roof,
-        "kernel_share": share,
-        "solve_ms_mean": solve_ms_mean,
-        "labels_match_oracle": checked,
-        "clocks": clock,
-        "cpu_baseline": cpu,
-    }
-    print(json.dumps(line))
+    line = gpu_arm(args, Workload(args.workload, args), rank, world, local)
+    if line is not None:
+        print(json.dumps(line), flush=True)
     return 0
 
 

@@ -133,6 +133,8 @@ GPU_SYMBOLS = {
     "cc_debug_local_components": (C.c_int, [C.POINTER(cc_csr), _P]),
     "cc_debug_radix_sort": (C.c_int, [_P, _U64, C.c_int]),
     "cc_debug_shortcut": (C.c_int, [C.POINTER(cc_csr), _P, _U32, _P]),
+    "cc_debug_set_round_cap": (C.c_int, [_P, _U32]),
+    "cc_serve_debug_fail_next": (C.c_int, [_P, C.c_int]),
 }
 
 GEN_SYMBOLS = {
@@ -141,6 +143,7 @@ GEN_SYMBOLS = {
     "cc_gen_rhg": (C.c_int, [_U64, C.c_double, C.c_double, _U64, _U32, C.POINTER(cc_host_graph)]),
     "cc_host_graph_free": (None, [C.POINTER(cc_host_graph)]),
     "cc_gen_rhg_radius": (C.c_double, [_U64, C.c_double, C.c_double]),
+    "cc_gen_rhg_verify": (_U64, [_U64, C.c_double, C.c_double, _U64, C.POINTER(cc_host_graph)]),
     "cc_read_metis": (C.c_int, [C.c_char_p, _U32, C.POINTER(cc_host_graph)]),
     "cc_read_edge_list": (C.c_int, [C.c_char_p, _U32, C.POINTER(cc_host_graph)]),
     "cc_read_binary_edges": (C.c_int, [C.c_char_p, _U32, C.POINTER(cc_host_graph)]),

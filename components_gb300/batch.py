@@ -56,6 +56,8 @@ def _bind():
         ("cc_batch_tuning_default", None, [C.POINTER(cc_batch_tuning)]),
         ("cc_batch_run", C.c_int, [P, C.POINTER(cc_batch), C.POINTER(cc_batch_tuning), P, C.c_uint32]),
         ("cc_batch_autotune", C.c_int, [P, C.POINTER(cc_batch), C.c_int, C.POINTER(cc_batch_tuning)]),
+        ("cc_batch_run_plain", C.c_int, [P, C.POINTER(cc_batch), C.c_int, C.POINTER(_lib.cc_config),
+                                         C.c_uint64, P]),
     ]:
         fn = getattr(g, name)
         fn.restype, fn.argtypes = res, args
@@ -192,3 +194,16 @@ def autotune(batch: Batch, ctx=None, reps: int = 3) -> cc_batch_tuning:
     t = cc_batch_tuning()
     _lib.check(_lib.gpu().cc_batch_autotune(ctx.handle, C.byref(b), reps, C.byref(t)))
     return t
+
+
+def plain_run(batch: Batch, ctx, labels, algo: str = "exp", conf=None) -> None:
+    """The plain path: one cc_ctx_run per graph, looped in C++
+    (cc_batch_run_plain); device batch and device labels (total_n int32)."""
+    from .config import Config
+    _bind()
+    if not batch.on_device:
+        raise ValueError("plain_run takes a device batch")
+    conf = conf or Config()
+    b = batch.to_c()
+    _lib.check(_lib.gpu().cc_batch_run_plain(ctx.handle, C.byref(b), _lib.ALGOS[algo],
+                                             C.byref(conf.to_c()), int(conf.seed), labels.data_ptr()))

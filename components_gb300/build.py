@@ -81,7 +81,7 @@ def build_gpu(force: bool = False, jobs: int | None = None) -> Path:
 def build_gen(force: bool = False) -> Path:
     BUILD.mkdir(exist_ok=True)
     out = BUILD / "libccgen.so"
-    srcs = [CSRC / "gen.cpp", ROOT / "include" / "cc_gen.h"]
+    srcs = [CSRC / "gen.cpp", CSRC / "rhg.h", ROOT / "include" / "cc_gen.h"]
     if not force and not _stale(out, srcs):
         return out
     cxx = shutil.which("g++") or "g++"

@@ -93,6 +93,8 @@ void ctx_free(cc_ctx *c) {
   if (c->stream) cudaStreamSynchronize(c->stream);
   ccg::batch_cache_free(c->batch);
   c->batch = nullptr;
+  c->plain_rp.release();
+  if (c->stream) cudaStreamSynchronize(c->stream);
   if (c->d_flag) cudaFree(c->d_flag);
   if (c->d_err) cudaFree(c->d_err);
   if (c->d_geo) cudaFree(c->d_geo);
@@ -134,7 +136,12 @@ void check_csr_args(const cc_csr *g) {
 // most the minimum over the r-hop neighbourhood, so each fixpoint is reached
 // within n+1 rounds; hitting the cap means a fault, reported as
 // CC_ERR_NO_CONVERGENCE.
-int round_cap(uint64_t n) { return (int)std::min<uint64_t>(n + 2, 1u << 20); }
+// A context may lower it (cc_debug_set_round_cap) so that tests can reach the
+// error path without a faulty kernel.
+int round_cap(const cc_ctx *C, uint64_t n) {
+  const uint64_t cap = std::min<uint64_t>(n + 2, 1u << 20);
+  return (int)(C && C->round_cap ? std::min<uint64_t>(cap, C->round_cap) : cap);
+}
 
 // ---- the solvers -----------------------------------------------------------
 
@@ -190,7 +197,7 @@ struct Solver {
     {
       DevBuf key(8 * G.n, s, pool);
       int rounds = ccg::ldd_decompose(G, vid, seed, level, C->d_geo, C->geo_len, cfg.bfs != 0,
-                                      cl.as<uint32_t>(), key.as<uint64_t>(), round_cap(G.n), s, pool, c,
+                                      cl.as<uint32_t>(), key.as<uint64_t>(), round_cap(C, G.n), s, pool, c,
                                       C->h_flag, C->d_flag);
       if (rounds < 0) throw Error(CC_ERR_NO_CONVERGENCE, "decomposition did not converge");
       note_level(level, G, rounds);
@@ -338,7 +345,7 @@ struct Solver {
             G.rp = G0.rp.as<uint64_t>();
             G.col = G0.col.p;
             ccg::iota_u32(f.as<uint32_t>(), G0.n, s, c);
-            int r = ccg::shortcut_propagate(G, f.as<uint32_t>(), cfg.number_of_hitters, round_cap(G.n),
+            int r = ccg::shortcut_propagate(G, f.as<uint32_t>(), cfg.number_of_hitters, round_cap(C, G.n),
                                             s, pool, c, C->h_flag, C->d_flag);
             if (r < 0) throw Error(CC_ERR_NO_CONVERGENCE, "shortcut propagation did not converge");
             note_level(1, G, r);
@@ -350,7 +357,7 @@ struct Solver {
           DevBuf col32;
           Csr G = as_u32(g, col32);
           ccg::iota_u32(lab, n, s, c);
-          int r = ccg::shortcut_propagate(G, lab, cfg.number_of_hitters, round_cap(G.n), s, pool, c,
+          int r = ccg::shortcut_propagate(G, lab, cfg.number_of_hitters, round_cap(C, G.n), s, pool, c,
                                           C->h_flag, C->d_flag);
           if (r < 0) throw Error(CC_ERR_NO_CONVERGENCE, "shortcut propagation did not converge");
           note_level(0, G, r);
@@ -361,7 +368,7 @@ struct Solver {
         DevBuf col32;
         Csr G = as_u32(g, col32);
         ccg::iota_u32(lab, n, s, c);
-        uint64_t cap = n + 2;
+        uint64_t cap = C->round_cap ? std::min<uint64_t>(n + 2, C->round_cap) : n + 2;
         int r = ccg::labels_propagate(G, lab, (int)std::min<uint64_t>(cap, 0x7fffffff), s, pool, c,
                                       C->h_flag, C->d_flag);
         if (r < 0) throw Error(CC_ERR_NO_CONVERGENCE, "label propagation did not converge");
@@ -867,7 +874,7 @@ int cc_debug_ldd(const cc_csr *g, const uint32_t *vid, uint64_t seed, uint32_t l
     Counters c;
     DevBuf key(8 * (G.n ? G.n : 1), s, C->pool);
     int r = ccg::ldd_decompose(G, vid, seed, level, C->d_geo, C->geo_len, gated != 0, cluster_out,
-                               key.as<uint64_t>(), round_cap(G.n), s, C->pool, c, C->h_flag, C->d_flag);
+                               key.as<uint64_t>(), round_cap(C, G.n), s, C->pool, c, C->h_flag, C->d_flag);
     CCG_CUDA(cudaStreamSynchronize(s));
     if (r < 0) throw Error(CC_ERR_NO_CONVERGENCE, "decomposition did not converge");
     if (rounds_out) *rounds_out = (uint32_t)r;
@@ -954,6 +961,12 @@ int cc_debug_radix_sort(uint64_t *keys, uint64_t n, int bits) {
   });
 }
 
+int cc_debug_set_round_cap(cc_ctx *ctx, uint32_t cap) {
+  if (!ctx) return CC_ERR_INVALID;
+  ctx->round_cap = cap;
+  return CC_OK;
+}
+
 int cc_debug_shortcut(const cc_csr *g, uint32_t *labels_inout, uint32_t hitters,
                       uint32_t *rounds_out) {
   return guard([&] {
@@ -961,7 +974,7 @@ int cc_debug_shortcut(const cc_csr *g, uint32_t *labels_inout, uint32_t hitters,
     cc_ctx *C = default_ctx();
     cudaStream_t s = C->stream;
     Counters c;
-    int r = ccg::shortcut_propagate(G, labels_inout, hitters, round_cap(G.n), s, C->pool, c, C->h_flag,
+    int r = ccg::shortcut_propagate(G, labels_inout, hitters, round_cap(C, G.n), s, C->pool, c, C->h_flag,
                                     C->d_flag);
     CCG_CUDA(cudaStreamSynchronize(s));
     if (r < 0) throw Error(CC_ERR_NO_CONVERGENCE, "shortcut propagation did not converge");

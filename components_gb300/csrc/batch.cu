@@ -343,7 +343,7 @@ void launch_batch(const BatchArgs &a, const BatchPlan &P, BatchDev &D, const cc_
     if (smem > 48 * 1024)
       CCG_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int per_sm = smem_blocks_per_sm(fn, threads, smem);
-    unsigned grid = (unsigned)std::min<uint64_t>((uint64_t)per_sm * kSMs, cnt);
+    unsigned grid = (unsigned)std::min<uint64_t>((uint64_t)per_sm * num_sms(), cnt);
     unsigned int *q = D.queues.as<unsigned int>() + b;
     if (t.edge_parallel[b])
       k_batch_smem<true><<<grid, threads, smem, s>>>(a, D.lists[b].as<uint32_t>(), cnt, q);
@@ -354,7 +354,7 @@ void launch_batch(const BatchArgs &a, const BatchPlan &P, BatchDev &D, const cc_
   }
   if (!P.chunks.empty()) {
     uint32_t nch = (uint32_t)P.chunks.size();
-    unsigned grid = grid_for((uint64_t)nch * kChunk, kBlock, kSMs * 32);
+    unsigned grid = grid_for((uint64_t)nch * kChunk, kBlock, num_sms() * 32);
     uint32_t *par = D.par.as<uint32_t>();
     const Chunk *ch = D.chunks.as<Chunk>();
     k_large_init<<<grid, kBlock, 0, s>>>(a, ch, nch, par);
@@ -362,7 +362,7 @@ void launch_batch(const BatchArgs &a, const BatchPlan &P, BatchDev &D, const cc_
     k_large_hook<<<grid, kBlock, 0, s>>>(a, ch, nch, par, t.hub_degree ? t.hub_degree : 32,
                                          D.hubs.as<uint32_t>(), D.hub_cap, D.nh.as<unsigned int>());
     CCG_LAUNCH_CHECK();
-    k_large_hubs<<<kSMs * 8, kBlock, 0, s>>>(a, D.big.as<uint32_t>(), (uint32_t)P.big.size(), par,
+    k_large_hubs<<<num_sms() * 8, kBlock, 0, s>>>(a, D.big.as<uint32_t>(), (uint32_t)P.big.size(), par,
                                              D.hubs.as<uint32_t>(), D.hub_cap,
                                              D.nh.as<unsigned int>());
     CCG_LAUNCH_CHECK();
@@ -444,6 +444,16 @@ double time_plan(const BatchArgs &a, const BatchPlan &P, const cc_batch_tuning &
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   return ms / reps;
+}
+
+// Per-graph row offsets starting at 0 for the plain per-graph loop: graph i's
+// n_i + 1 offsets land at local[voff[i] + i ...] (one CTA per graph).
+__global__ void k_rebase_offsets(const uint64_t *__restrict__ voff, const uint64_t *__restrict__ rp,
+                                 uint32_t k, uint64_t *__restrict__ local) {
+  for (uint32_t i = blockIdx.x; i < k; i += gridDim.x) {
+    const uint64_t a = voff[i], b = voff[i + 1], base = rp[a];
+    for (uint64_t j = threadIdx.x; j <= b - a; j += blockDim.x) local[a + i + j] = rp[a + j] - base;
+  }
 }
 
 }  // namespace
@@ -653,6 +663,44 @@ int cc_batch_autotune(cc_ctx *ctx, const cc_batch *b, int reps, cc_batch_tuning 
     best.use_graph = 1;
     *out = best;
   });
+}
+
+int cc_batch_run_plain(cc_ctx *ctx, const cc_batch *b, cc_algo algo, const cc_config *cfg,
+                       uint64_t seed, uint32_t *labels_out) {
+  using namespace ccg;
+  if (!ctx) return CC_ERR_INVALID;
+  int rc = guard([&] {
+    check_batch(b);
+    if (b->where != CC_DEVICE) throw Error(CC_ERR_INVALID, "the plain loop takes device arrays");
+    if (b->total_n > 0 && !labels_out) throw Error(CC_ERR_INVALID, "labels_out is NULL");
+    CCG_CUDA(cudaSetDevice(ctx->device));
+    cudaStream_t s = ctx->stream;
+    const std::vector<uint64_t> voff = host_voff(b, s);
+    std::vector<uint64_t> bounds(b->k + 1);  // global row offset at each graph's first row
+    for (uint32_t i = 0; i <= b->k; ++i)
+      CCG_CUDA(cudaMemcpyAsync(&bounds[i], b->row_ptr + voff[i], 8, cudaMemcpyDeviceToHost, s));
+    ctx->plain_rp.alloc(8 * (b->total_n + b->k + 1), s, ctx->pool);
+    if (b->k)
+      k_rebase_offsets<<<std::min<uint32_t>(b->k, 65535), 256, 0, s>>>(b->voff, b->row_ptr, b->k,
+                                                                      ctx->plain_rp.as<uint64_t>());
+    CCG_LAUNCH_CHECK();
+    CCG_CUDA(cudaStreamSynchronize(s));
+    for (uint32_t i = 0; i < b->k; ++i) {
+      cc_csr g;
+      std::memset(&g, 0, sizeof(g));
+      g.n = voff[i + 1] - voff[i];
+      g.m_dir = bounds[i + 1] - bounds[i];
+      g.row_ptr = ctx->plain_rp.as<uint64_t>() + voff[i] + i;
+      g.col = b->col + bounds[i];
+      g.id_bytes = 4;
+      g.num_parts = 1;
+      g.where = CC_DEVICE;
+      if (g.n == 0) continue;
+      const int st = cc_ctx_run(ctx, &g, algo, cfg, seed, labels_out + voff[i], CC_DEVICE);
+      if (st != CC_OK) throw Error(st, "plain solve of one graph failed");
+    }
+  });
+  return rc;
 }
 
 }  // extern "C"

@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <atomic>
 #include <cstdio>
 #include <stdexcept>
 #include <string>
@@ -35,7 +36,20 @@ struct Error : std::runtime_error {
 
 constexpr uint32_t kNone = 0xffffffffu;
 constexpr int kBlock = 256;
-constexpr int kSMs = 152;  // GB300: 2 dies x 76 SMs
+// SMs of the current device (152 on a GB300: two dies of 76), queried once per
+// device; grid caps are multiples of it.
+inline int num_sms() {
+  static std::atomic<int> cache[64];
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 152;
+  int v = cache[dev].load(std::memory_order_relaxed);
+  if (v == 0) {
+    if (cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || v <= 0)
+      v = 152;
+    cache[dev].store(v, std::memory_order_relaxed);
+  }
+  return v;
+}
 
 // Per-solve launch bookkeeping, reported through cc_stats.  With prof on,
 // tic()/toc() bracket single kernels with CUDA events on their stream; the
@@ -139,7 +153,7 @@ struct DevBuf {
   template <class T> T *as() const { return static_cast<T *>(p); }
 };
 
-inline unsigned grid_for(uint64_t work, int block = kBlock, unsigned cap = kSMs * 16) {
+inline unsigned grid_for(uint64_t work, int block = kBlock, unsigned cap = num_sms() * 16) {
   uint64_t g = (work + block - 1) / block;
   if (g == 0) g = 1;
   if (g > cap) g = cap;

@@ -31,12 +31,14 @@ struct cc_ctx {
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};  // solve bracketing events, reused
   std::vector<cudaEvent_t> ev_pool;  // per-kernel profiling events, reused across solves
   ccg::UfTuning uf;  // hook-and-compress schedule (cc_ctx_set_tuning)
+  uint32_t round_cap = 0;  // test hook: lower cap on the iterative rounds (0: n + 2)
   ccg::UfDecisionCache uf_cache;    // the last device graph's row-sample decisions
   ccg::UfDecisionCache host_cache;  // the last host graph's (streamed input)
   cc_stats stats{};
   cc_stats prof_total{};      // per-kernel sums over the solves since profiling was switched on
   uint64_t prof_solves = 0;
   ccg::BatchCache *batch = nullptr;  // last recorded batch solve (CUDA graph)
+  DevBuf plain_rp;  // per-graph offsets of cc_batch_run_plain (kept for the next call)
   // host threads and page-locked staging of the streamed input (made on first use)
   std::unique_ptr<ccg::HostStager> stager;
 };

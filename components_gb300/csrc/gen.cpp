@@ -13,6 +13,7 @@
 
 #include "../../include/cc_gen.h"
 #include "../../include/cc_gpu.h"
+#include "rhg.h"
 
 #ifdef _OPENMP
 #include <omp.h>
@@ -177,72 +178,77 @@ int cc_gen_grid(uint64_t X, uint64_t Y, double p, uint64_t seed, uint32_t id_byt
 }  // extern "C"
 
 // ---- random hyperbolic graphs (threshold model) ------------------------------
-// Krioukov et al., "Hyperbolic geometry of complex networks" (Phys. Rev. E 82,
-// 2010), threshold (T = 0) model: n points in a disk of radius R, angle uniform,
-// radius with density alpha sinh(alpha r) / (cosh(alpha R) - 1), alpha =
-// (gamma - 1) / 2; u ~ w iff their hyperbolic distance is at most R.  With
-//   cosh d = cosh(r1 - r2) + 2 sin^2(dtheta / 2) sinh r1 sinh r2
-// the rule is  sin^2(dtheta / 2) <= q(r1, r2) = (cosh R - cosh(r1 - r2)) /
-// (2 sinh r1 sinh r2), and the largest connecting angle is 2 asin(sqrt(q)).
+// The model, the exact edge test and the candidate search are in rhg.h, shared
+// with the device generator; here the disk radius for a target average degree
+// and the host's neighbour search.
 namespace {
 
-inline double rhg_q(double R_cosh, double r1, double r2, double s1, double s2) {
-  return (R_cosh - std::cosh(r1 - r2)) / (2.0 * s1 * s2);
-}
-inline double rhg_theta_max(double R, double r1, double r2) {
-  if (r1 + r2 <= R) return M_PI;
-  double q = rhg_q(std::cosh(R), r1, r2, std::sinh(r1), std::sinh(r2));
-  if (q >= 1.0) return M_PI;
-  if (q <= 0.0) return 0.0;
-  return 2.0 * std::asin(std::sqrt(q));
-}
-inline double rhg_radius(double u, double alpha, double R) {  // inverse CDF
-  return std::acosh(1.0 + u * (std::cosh(alpha * R) - 1.0)) / alpha;
+// Sorted keys, points and per-band cell tables of one graph.
+struct RhgLayout {
+  std::vector<rhg::Point> pt;                 // by vertex id (angular order)
+  std::vector<std::vector<uint32_t>> band;    // vertex ids per band, ascending
+  std::vector<std::vector<uint64_t>> cell;    // per band: 2^L + 1 cell starts into band[b]
+  std::vector<int> L;
+};
+
+void rhg_layout(const rhg::Params &P, RhgLayout &lay) {
+  const uint64_t n = P.n;
+  std::vector<uint64_t> key(n);
+  long long i;
+#pragma omp parallel for schedule(static)
+  for (i = 0; i < (long long)n; ++i) key[i] = rhg::angle_key(P, (uint64_t)i);
+  radix_u64(key, 64);
+  lay.pt.resize(n);
+#pragma omp parallel for schedule(static)
+  for (i = 0; i < (long long)n; ++i) lay.pt[i] = rhg::point(P, key[i]);
+  std::vector<uint64_t>().swap(key);
+  lay.band.assign(P.nb, {});
+  for (uint64_t v = 0; v < n; ++v) lay.band[lay.pt[v].band].push_back((uint32_t)v);
+  lay.cell.assign(P.nb, {});
+  lay.L.assign(P.nb, 0);
+  for (int b = 0; b < P.nb; ++b) {
+    const int L = rhg::cell_bits(lay.band[b].size());
+    lay.L[b] = L;
+    std::vector<uint64_t> &c = lay.cell[b];
+    c.assign((1ull << L) + 1, 0);
+    for (uint32_t v : lay.band[b]) c[rhg::cell_of(lay.pt[v].phi, L) + 1]++;
+    for (uint64_t k = 0; k < (1ull << L); ++k) c[k + 1] += c[k];
+  }
 }
 
-// Expected average degree for radius R: (n - 1) * E[theta_max / pi], the
-// expectation over two independent radii.  Midpoint rule on a uniform grid in
-// r with density weights: the few vertices near the centre have degrees close
-// to n, so the grid must resolve small radii too (a grid in CDF space does
-// not, and underestimates the degree).
-double rhg_avg_degree(uint64_t n, double alpha, double R) {
-  const int N = 1200;
-  std::vector<double> r(N), w(N), ch(N), sh(N);
-  double wsum = 0.0;
-  for (int i = 0; i < N; ++i) {
-    r[i] = (i + 0.5) * R / N;
-    w[i] = std::sinh(alpha * r[i]);
-    wsum += w[i];
-    ch[i] = std::cosh(r[i]);
-    sh[i] = std::sinh(r[i]);
-  }
-  const double coshR = std::cosh(R);
-  double acc = 0.0;
-  for (int i = 0; i < N; ++i) {
-    double row = 0.0;
-    for (int j = 0; j < N; ++j) {
-      double th;
-      if (r[i] + r[j] <= R) {
-        th = M_PI;
-      } else {
-        double q = rhg_q(coshR, r[i], r[j], sh[i], sh[j]);
-        th = q >= 1.0 ? M_PI : (q <= 0.0 ? 0.0 : 2.0 * std::asin(std::sqrt(q)));
+// Every neighbour of v, appended to out (unsorted: band by band).
+void rhg_neighbours(const rhg::Params &P, const RhgLayout &lay, uint64_t v,
+                    std::vector<uint32_t> &out) {
+  const rhg::Point &pv = lay.pt[v];
+  for (int b = 0; b < P.nb; ++b) {
+    const std::vector<uint32_t> &bp = lay.band[b];
+    if (bp.empty()) continue;
+    uint64_t half = 0;
+    const int L = lay.L[b];
+    const bool win = L > 0 && rhg::window(P, pv, b, &half);
+    auto scan = [&](uint64_t k0, uint64_t k1) {
+      for (uint64_t k = k0; k < k1; ++k) {
+        const uint32_t w = bp[k];
+        if (w == v) continue;
+        const rhg::Point &pw = lay.pt[w];
+        if (win && pw.phi - (pv.phi - half) > 2 * half) continue;
+        if (rhg::adjacent(P, pv, pw)) out.push_back(w);
       }
-      row += w[j] * th;
+    };
+    if (!win) {
+      scan(0, bp.size());
+      continue;
     }
-    acc += w[i] * row;
+    const uint64_t lo = pv.phi - half, hi = pv.phi + half;
+    const uint64_t c0 = rhg::cell_of(lo, L), c1 = rhg::cell_of(hi, L);
+    const std::vector<uint64_t> &c = lay.cell[b];
+    if (lo > pv.phi || hi < pv.phi) {  // the window crosses angle 0
+      scan(c[c0], bp.size());
+      scan(0, c[c1 + 1]);
+    } else {
+      scan(c[c0], c[c1 + 1]);
+    }
   }
-  return (double)(n - 1) * acc / (wsum * wsum * M_PI);
-}
-
-double rhg_target_radius(uint64_t n, double alpha, double deg) {
-  double lo = 1e-3, hi = 2.0 * std::log((double)n) + 40.0;
-  for (int it = 0; it < 40; ++it) {  // average degree decreases with R
-    double mid = 0.5 * (lo + hi);
-    if (rhg_avg_degree(n, alpha, mid) > deg) lo = mid;
-    else hi = mid;
-  }
-  return 0.5 * (lo + hi);
 }
 
 }  // namespace
@@ -251,49 +257,13 @@ extern "C" {
 
 int cc_gen_rhg(uint64_t n, double avg_deg, double gamma, uint64_t seed, uint32_t id_bytes,
                cc_host_graph *out) {
-  if (!out || (id_bytes != 4 && id_bytes != 8) || n < 2 || n >= (1ull << 32) || gamma <= 2.0 ||
-      avg_deg <= 0.0)
-    return CC_ERR_INVALID;
+  if (!out || (id_bytes != 4 && id_bytes != 8)) return CC_ERR_INVALID;
+  rhg::Params P;
+  int st = rhg::make_params(n, avg_deg, gamma, seed, &P);
+  if (st != CC_OK) return st;
   std::memset(out, 0, sizeof(*out));
-  const double alpha = (gamma - 1.0) / 2.0;
-  const double R = rhg_target_radius(n, alpha, avg_deg);
-  const double coshR = std::cosh(R);
-  // points, numbered in angular order
-  const int idbits = bits_for(n);
-  std::vector<uint64_t> key(n);
-  long long i;
-#pragma omp parallel for schedule(static)
-  for (i = 0; i < (long long)n; ++i)
-    key[i] = ((hash3(seed, (uint64_t)i, 21) >> idbits) << idbits) | (uint64_t)i;
-  radix_u64(key, 64);
-  std::vector<double> th(n), rad(n), sh(n);
-#pragma omp parallel for schedule(static)
-  for (i = 0; i < (long long)n; ++i) {
-    uint64_t src = key[i] & ((1ull << idbits) - 1);
-    th[i] = 2.0 * M_PI * (double)(key[i] >> idbits) / std::ldexp(1.0, 64 - idbits);
-    rad[i] = rhg_radius(unit(hash3(seed, src, 22)), alpha, R);
-    sh[i] = std::sinh(rad[i]);
-  }
-  std::vector<uint64_t>().swap(key);
-  // radial bands: [0, R/2) and unit-width bands above; per band the points in
-  // angular order and uniform angular cells of about two points each
-  std::vector<double> edges{0.0};
-  for (double b = R / 2; b < R; b += 1.0) edges.push_back(b);
-  edges.push_back(R + 1e-9);
-  const int nb = (int)edges.size() - 1;
-  std::vector<std::vector<uint32_t>> band(nb);
-  for (uint64_t v = 0; v < n; ++v) {
-    int b = (int)(std::upper_bound(edges.begin(), edges.end(), rad[v]) - edges.begin()) - 1;
-    band[std::min(std::max(b, 0), nb - 1)].push_back((uint32_t)v);
-  }
-  std::vector<std::vector<uint64_t>> cell(nb);
-  std::vector<uint64_t> ncell(nb);
-  for (int b = 0; b < nb; ++b) {
-    ncell[b] = std::max<uint64_t>(1, band[b].size() / 2);
-    cell[b].assign(ncell[b] + 1, 0);
-    for (uint32_t v : band[b]) cell[b][std::min<uint64_t>(ncell[b] - 1, (uint64_t)(th[v] / (2 * M_PI) * ncell[b])) + 1]++;
-    for (uint64_t c = 0; c < ncell[b]; ++c) cell[b][c + 1] += cell[b][c];
-  }
+  RhgLayout lay;
+  rhg_layout(P, lay);
   // neighbours of every point, threads over contiguous point ranges
   int T = 1;
 #ifdef _OPENMP
@@ -312,40 +282,8 @@ int cc_gen_rhg(uint64_t n, double avg_deg, double gamma, uint64_t seed, uint32_t
     out_t.reserve((size_t)((hi - lo) * avg_deg * 1.1));
     for (uint64_t v = lo; v < hi; ++v) {
       const uint64_t before = out_t.size();
-      for (int b = 0; b < nb; ++b) {
-        if (band[b].empty()) continue;
-        const double dmax = rhg_theta_max(R, rad[v], edges[b]);
-        if (dmax <= 0.0) continue;
-        const double C = (double)ncell[b];
-        auto scan = [&](double a0, double a1) {  // angles within [a0, a1], 0 <= a0 <= a1 <= 2pi
-          uint64_t c0 = (uint64_t)std::max(0.0, std::floor(a0 / (2 * M_PI) * C));
-          uint64_t c1 = std::min<uint64_t>(ncell[b] - 1, (uint64_t)(a1 / (2 * M_PI) * C));
-          for (uint64_t k = cell[b][c0]; k < cell[b][c1 + 1]; ++k) {
-            const uint32_t w = band[b][k];
-            if (w == v || th[w] < a0 || th[w] > a1) continue;
-            double dth = std::fabs(th[v] - th[w]);
-            if (dth > M_PI) dth = 2 * M_PI - dth;
-            const double s = std::sin(0.5 * dth);
-            if (s * s <= rhg_q(coshR, rad[v], rad[w], sh[v], sh[w])) out_t.push_back(w);
-          }
-        };
-        if (dmax >= M_PI) {
-          scan(0.0, 2 * M_PI);
-        } else {
-          double a0 = th[v] - dmax, a1 = th[v] + dmax;
-          if (a0 < 0) {
-            scan(0.0, a1);
-            scan(a0 + 2 * M_PI, 2 * M_PI);
-          } else if (a1 > 2 * M_PI) {
-            scan(a0, 2 * M_PI);
-            scan(0.0, a1 - 2 * M_PI);
-          } else {
-            scan(a0, a1);
-          }
-        }
-      }
+      rhg_neighbours(P, lay, v, out_t);
       std::sort(out_t.begin() + before, out_t.end());
-      out_t.erase(std::unique(out_t.begin() + before, out_t.end()), out_t.end());
       deg[v + 1] = out_t.size() - before;
     }
   }
@@ -366,7 +304,38 @@ int cc_gen_rhg(uint64_t n, double avg_deg, double gamma, uint64_t seed, uint32_t
 }
 
 double cc_gen_rhg_radius(uint64_t n, double avg_deg, double gamma) {
-  return rhg_target_radius(n, (gamma - 1.0) / 2.0, avg_deg);
+  rhg::Params P;
+  return rhg::make_params(n, avg_deg, gamma, 1, &P) == CC_OK ? P.R : -1.0;
+}
+
+uint64_t cc_gen_rhg_verify(uint64_t n, double avg_deg, double gamma, uint64_t seed,
+                           const cc_host_graph *g) {
+  rhg::Params P;
+  if (!g || g->n != n || rhg::make_params(n, avg_deg, gamma, seed, &P) != CC_OK) return ~0ull;
+  std::vector<uint64_t> key(n);
+  for (uint64_t i = 0; i < n; ++i) key[i] = rhg::angle_key(P, i);
+  std::sort(key.begin(), key.end());
+  std::vector<rhg::Point> pt(n);
+  for (uint64_t i = 0; i < n; ++i) pt[i] = rhg::point(P, key[i]);
+  auto id = [&](uint64_t e) -> uint64_t {
+    return g->id_bytes == 8 ? static_cast<const uint64_t *>(g->col)[e]
+                            : static_cast<const uint32_t *>(g->col)[e];
+  };
+  uint64_t bad = 0;
+  long long v;
+#pragma omp parallel for schedule(dynamic, 64) reduction(+ : bad)
+  for (v = 0; v < (long long)n; ++v) {
+    uint64_t e = g->row_ptr[v];
+    const uint64_t end = g->row_ptr[v + 1];
+    for (uint64_t w = 0; w < n; ++w) {
+      const bool want = w != (uint64_t)v && rhg::adjacent(P, pt[v], pt[w]);
+      const bool have = e < end && id(e) == w;
+      if (have) ++e;
+      if (want != have) ++bad;
+    }
+    if (e != end) bad += end - e;
+  }
+  return bad;
 }
 
 void cc_host_graph_free(cc_host_graph *g) {

@@ -111,7 +111,7 @@ int cc_gen_grid_device(cc_ctx *ctx, uint64_t X, uint64_t Y, double p, uint64_t s
     const bool all = p >= 1.0, none = p <= 0.0;
     const ccg::GridEdges ge{X, Y, seed, (all || none) ? 0ull : (uint64_t)std::ldexp(p, 64), all, none};
     DevBuf deg(n, s, C->pool);
-    const unsigned grid = ccg::grid_for(n, ccg::kBlock, ccg::kSMs * 16);
+    const unsigned grid = ccg::grid_for(n, ccg::kBlock, ccg::num_sms() * 16);
     ccg::k_grid_degrees<<<grid, ccg::kBlock, 0, s>>>(ge, deg.as<uint8_t>());
     CCG_LAUNCH_CHECK();
     ccg::offsets_from_degrees(deg.as<uint8_t>(), n, 0, row_ptr, s, C->pool, c);
@@ -147,7 +147,7 @@ int cc_gen_gnm_device(cc_ctx *ctx, uint64_t n, uint64_t m, uint64_t seed, uint32
     uint64_t u = 0;
     const uint64_t *sorted = keys.as<uint64_t>();
     if (nk) {
-      ccg::k_gnm_keys<<<ccg::grid_for(m, ccg::kBlock, ccg::kSMs * 16), ccg::kBlock, 0, s>>>(
+      ccg::k_gnm_keys<<<ccg::grid_for(m, ccg::kBlock, ccg::num_sms() * 16), ccg::kBlock, 0, s>>>(
           n, m, seed, b, keys.as<uint64_t>());
       CCG_LAUNCH_CHECK();
       sorted = ccg::radix_sort_u64(keys.as<uint64_t>(), tmp.as<uint64_t>(), nk, 2 * b, s, C->pool, c);
@@ -164,7 +164,7 @@ int cc_gen_gnm_device(cc_ctx *ctx, uint64_t n, uint64_t m, uint64_t seed, uint32
     }
     *m_dir = u;
     if (u > cap) throw Error(CC_ERR_INVALID, "col capacity below the generated entries");
-    const unsigned grid = ccg::grid_for(std::max<uint64_t>(n + 1, u), ccg::kBlock, ccg::kSMs * 16);
+    const unsigned grid = ccg::grid_for(std::max<uint64_t>(n + 1, u), ccg::kBlock, ccg::num_sms() * 16);
     if (id_bytes == 8)
       ccg::k_keys_to_csr<uint64_t><<<grid, ccg::kBlock, 0, s>>>(uniq.as<uint64_t>(), u, n, b, row_ptr,
                                                                 static_cast<uint64_t *>(col));

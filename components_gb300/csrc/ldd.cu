@@ -249,7 +249,7 @@ int ldd_decompose(const Csr &g, const uint32_t *vid, uint64_t seed, uint32_t lev
                   Counters &c, volatile int *host_flag, int *dev_flag) {
   if (g.n == 0) return 0;
   const uint32_t *col = static_cast<const uint32_t *>(g.col);
-  unsigned grid = grid_for(g.n, kBlock, kSMs * 32);
+  unsigned grid = grid_for(g.n, kBlock, num_sms() * 32);
   DevBuf mx(4, s, pool);
   CCG_CUDA(cudaMemsetAsync(mx.p, 0, 4, s));
   k_ldd_init<<<grid, kBlock, 0, s>>>(g.n, vid, seed, level, d_geo, geo_len, key,
@@ -286,7 +286,7 @@ int ldd_decompose(const Csr &g, const uint32_t *vid, uint64_t seed, uint32_t lev
       cudaEvent_t t0 = c.tic(s);
       k_ldd_round<<<grid, kBlock, 0, s>>>(g.n, g.rp, col, key, dev_flag);
       CCG_LAUNCH_CHECK();
-      k_ldd_round_pieces<<<kSMs * 8, kBlock, 0, s>>>(g.rp, col, rpc, key, dev_flag);
+      k_ldd_round_pieces<<<num_sms() * 8, kBlock, 0, s>>>(g.rp, col, rpc, key, dev_flag);
       CCG_LAUNCH_CHECK();
       c.toc(s, "ldd_round", t0, round_bytes);
       CCG_CUDA(cudaMemcpyAsync((void *)host_flag, dev_flag, sizeof(int), cudaMemcpyDeviceToHost, s));
@@ -307,7 +307,7 @@ void local_sweeps(const Csr &g, const uint32_t *vid, uint64_t seed, uint32_t lev
                   Counters &c) {
   if (g.n == 0) return;
   const uint32_t *col = static_cast<const uint32_t *>(g.col);
-  unsigned grid = grid_for(g.n, kBlock, kSMs * 32);
+  unsigned grid = grid_for(g.n, kBlock, num_sms() * 32);
   const uint64_t cap = row_pieces_cap(g.m, kRowLimit);
   DevBuf items(8 * cap, s, pool), cnt(4, s, pool);
   CCG_CUDA(cudaMemsetAsync(cnt.p, 0, 4, s));
@@ -322,7 +322,7 @@ void local_sweeps(const Csr &g, const uint32_t *vid, uint64_t seed, uint32_t lev
     uint64_t *out = r ? k0 : k1;
     k_min_sweep<<<grid, kBlock, 0, s>>>(g.n, g.rp, col, in, out);
     CCG_LAUNCH_CHECK();
-    k_min_sweep_pieces<<<kSMs * 8, kBlock, 0, s>>>(g.rp, col, rpc, in, out);
+    k_min_sweep_pieces<<<num_sms() * 8, kBlock, 0, s>>>(g.rp, col, rpc, in, out);
     CCG_LAUNCH_CHECK();
   }
   const uint64_t sweep = 8 * (g.n + 1) + g.m * 4 + g.m * 8 + 2 * g.n * 8;

@@ -245,7 +245,7 @@ int labels_propagate(const Csr &g, uint32_t *lab, int max_rounds, cudaStream_t s
                      cudaMemPool_t pool, Counters &c, volatile int *host_flag, int *dev_flag) {
   if (g.n == 0) return 0;
   const uint32_t *col = static_cast<const uint32_t *>(g.col);
-  unsigned grid = grid_for(g.n, kBlock, kSMs * 32);
+  unsigned grid = grid_for(g.n, kBlock, num_sms() * 32);
   const uint64_t cap = row_pieces_cap(g.m, kRowLimit);
   DevBuf items(8 * cap, s, pool), cnt(4, s, pool);
   CCG_CUDA(cudaMemsetAsync(cnt.p, 0, 4, s));
@@ -260,7 +260,7 @@ int labels_propagate(const Csr &g, uint32_t *lab, int max_rounds, cudaStream_t s
     cudaEvent_t t0 = c.tic(s);
     k_labels_round<<<grid, kBlock, 0, s>>>(g.n, g.rp, col, lab, dev_flag);
     CCG_LAUNCH_CHECK();
-    k_labels_round_pieces<<<kSMs * 8, kBlock, 0, s>>>(g.rp, col, rpc, lab, dev_flag);
+    k_labels_round_pieces<<<num_sms() * 8, kBlock, 0, s>>>(g.rp, col, rpc, lab, dev_flag);
     CCG_LAUNCH_CHECK();
     c.toc(s, "labels_round", t0, round_bytes);
     CCG_CUDA(cudaMemcpyAsync((void *)host_flag, dev_flag, sizeof(int), cudaMemcpyDeviceToHost, s));
@@ -277,7 +277,7 @@ int shortcut_propagate(const Csr &g, uint32_t *lab, uint32_t hitters, int max_ro
                        int *dev_flag) {
   if (g.n == 0) return 0;
   const uint32_t *col = static_cast<const uint32_t *>(g.col);
-  unsigned grid = grid_for(g.n, kBlock, kSMs * 32);
+  unsigned grid = grid_for(g.n, kBlock, num_sms() * 32);
   DevBuf nfb(4 * g.n, s, pool), updb(4 * g.n, s, pool);
   const uint64_t cap = row_pieces_cap(g.m, kRowLimit);
   DevBuf items(8 * cap, s, pool), npieces(4, s, pool);
@@ -299,7 +299,7 @@ int shortcut_propagate(const Csr &g, uint32_t *lab, uint32_t hitters, int max_ro
     cudaEvent_t t0 = c.tic(s);
     k_sc_min<<<grid, kBlock, 0, s>>>(g.n, g.rp, col, f, nf, updb.as<uint32_t>());
     CCG_LAUNCH_CHECK();
-    k_sc_min_pieces<<<kSMs * 8, kBlock, 0, s>>>(g.rp, col, rpc, f, nf, updb.as<uint32_t>());
+    k_sc_min_pieces<<<num_sms() * 8, kBlock, 0, s>>>(g.rp, col, rpc, f, nf, updb.as<uint32_t>());
     CCG_LAUNCH_CHECK();
     if (hitters) {
       CCG_CUDA(cudaMemsetAsync(cnt.p, 0, 4 * g.n, s));
@@ -333,7 +333,7 @@ int shortcut_propagate(const Csr &g, uint32_t *lab, uint32_t hitters, int max_ro
 void compose_labels(const uint32_t *cl, const uint32_t *newid, const uint32_t *next,
                     const uint32_t *rep, uint32_t *out, uint64_t n, cudaStream_t s, Counters &c) {
   if (n == 0) return;
-  k_compose<<<grid_for(n, kBlock, kSMs * 32), kBlock, 0, s>>>(n, cl, newid, next, rep, out);
+  k_compose<<<grid_for(n, kBlock, num_sms() * 32), kBlock, 0, s>>>(n, cl, newid, next, rep, out);
   CCG_LAUNCH_CHECK();
   c.add(1, 16 * n);
 }
@@ -341,7 +341,7 @@ void compose_labels(const uint32_t *cl, const uint32_t *newid, const uint32_t *n
 void canonicalize(uint32_t *lab, uint32_t *scratch, uint64_t n, cudaStream_t s, Counters &c) {
   if (n == 0) return;
   CCG_CUDA(cudaMemsetAsync(scratch, 0xff, 4 * n, s));
-  unsigned grid = grid_for(n, kBlock, kSMs * 32);
+  unsigned grid = grid_for(n, kBlock, num_sms() * 32);
   k_canon_min<<<grid, kBlock, 0, s>>>(n, scratch, lab);
   CCG_LAUNCH_CHECK();
   k_canon_apply<<<grid, kBlock, 0, s>>>(n, lab, scratch);
@@ -353,7 +353,7 @@ void count_roots(const uint32_t *lab, uint64_t n, unsigned long long *d_count, c
                  Counters &c) {
   CCG_CUDA(cudaMemsetAsync(d_count, 0, 8, s));
   if (n == 0) return;
-  k_count_roots<<<grid_for(n, kBlock, kSMs * 8), kBlock, 0, s>>>(n, lab, d_count);
+  k_count_roots<<<grid_for(n, kBlock, num_sms() * 8), kBlock, 0, s>>>(n, lab, d_count);
   CCG_LAUNCH_CHECK();
   c.add(1, 4 * n);
 }
@@ -363,7 +363,7 @@ void component_size_hist(const void *lab, int id_bytes, uint64_t n, uint32_t *cn
   CCG_CUDA(cudaMemsetAsync(cnt, 0, 4 * n, s));
   CCG_CUDA(cudaMemsetAsync(hist, 0, 4 * (n + 1), s));
   if (n == 0) return;
-  const unsigned grid = grid_for(n, kBlock, kSMs * 16);
+  const unsigned grid = grid_for(n, kBlock, num_sms() * 16);
   if (id_bytes == 8)
     k_comp_count<uint64_t><<<grid, kBlock, 0, s>>>(n, static_cast<const uint64_t *>(lab), cnt, err);
   else
@@ -377,14 +377,14 @@ void component_size_hist(const void *lab, int id_bytes, uint64_t n, uint32_t *cn
 void gather_u32(const uint32_t *src, const uint32_t *idx, uint32_t *out, uint64_t n,
                 cudaStream_t s, Counters &c) {
   if (n == 0) return;
-  k_gather<<<grid_for(n, kBlock, kSMs * 32), kBlock, 0, s>>>(n, src, idx, out);
+  k_gather<<<grid_for(n, kBlock, num_sms() * 32), kBlock, 0, s>>>(n, src, idx, out);
   CCG_LAUNCH_CHECK();
   c.add(1, 12 * n);
 }
 
 void iota_u32(uint32_t *out, uint64_t n, cudaStream_t s, Counters &c) {
   if (n == 0) return;
-  k_iota<<<grid_for(n, kBlock, kSMs * 32), kBlock, 0, s>>>(n, out);
+  k_iota<<<grid_for(n, kBlock, num_sms() * 32), kBlock, 0, s>>>(n, out);
   CCG_LAUNCH_CHECK();
   c.add(1, 4 * n);
 }

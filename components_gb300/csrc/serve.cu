@@ -131,7 +131,9 @@ struct Req {
   cudaEvent_t copied = nullptr;
   std::atomic<int> state{kWaiting};
   uint32_t batch_id = 0, batch_size = 0;
-  bool failed = false;    // could not be launched (collect reports CC_ERR_CUDA)
+  bool failed = false;    // could not be staged or launched (collect reports fail_status)
+  int fail_status = CC_ERR_CUDA;
+  int inject = 0;         // test hook: fail on purpose at staging (1) or launch (2)
   bool enqueued = false;  // its completion callback is queued on a stream
   UfTuning tu;  // large graph: hook schedule decided on the host
 };
@@ -160,6 +162,7 @@ struct Server {
   uint64_t next_id = 1, used = 0, peak = 0, batches = 0, submitted = 0, completed = 0,
            collected = 0;
   bool stop = false;
+  std::atomic<int> inject_next{0};  // test hook (cc_serve_debug_fail_next)
   std::thread worker;
   std::atomic<int> inflight{0};
 
@@ -217,6 +220,7 @@ struct Server {
 
   void stage(Req *r) {  // worker thread, no lock held
     const cc_csr &g = r->g;
+    if (r->inject == 1) throw Error(CC_ERR_OOM, "injected staging failure (test hook)");
     r->rp.alloc(8 * (g.n + 1), copy_stream, pool);
     r->col.alloc((size_t)g.id_bytes * (g.m_dir ? g.m_dir : 1), copy_stream, pool);
     r->lab.alloc(4 * (g.n + 1), copy_stream, pool);
@@ -297,7 +301,7 @@ struct Server {
                                         (int)smem));
         int per_sm = 1;
         CCG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_serve_smem, 256, smem));
-        unsigned grid = (unsigned)std::min<uint64_t>((uint64_t)std::max(per_sm, 1) * kSMs, nsmall);
+        unsigned grid = (unsigned)std::min<uint64_t>((uint64_t)std::max(per_sm, 1) * num_sms(), nsmall);
         k_serve_smem<<<grid, 256, smem, s>>>(desc_dev[si].as<GraphDesc>(), nsmall,
                                              queue_dev[si].as<unsigned int>());
         CCG_LAUNCH_CHECK();
@@ -309,6 +313,7 @@ struct Server {
     for (size_t i = nsmall; i < batch.size(); ++i) {
       Req *r = batch[i];
       try {
+        if (r->inject == 2) throw Error(CC_ERR_CUDA, "injected launch failure (test hook)");
         CCG_CUDA(cudaStreamWaitEvent(s, r->copied, 0));
         Csr G;
         G.n = r->g.n;
@@ -356,13 +361,23 @@ struct Server {
         peak = std::max(peak, used);
         r->t_admit = now_s();
         lk.unlock();
+        int st = CC_OK;
         try {
           stage(r);
+        } catch (const Error &e) {
+          st = e.status;
         } catch (...) {
+          st = CC_ERR_CUDA;
+        }
+        if (st != CC_OK) {
+          // the copy stream is left to finish what was enqueued; collect
+          // reports the status and retires the request (its buffers and its
+          // share of the budget)
           lk.lock();
-          used -= r->need;
+          r->failed = true;
+          r->fail_status = st;
           r->t_done = now_s();
-          r->state = kDone;  // collect reports the failure through the error word
+          r->state = kDone;
           cv_done.notify_all();
           continue;
         }
@@ -508,6 +523,7 @@ int cc_serve_submit(cc_server *h, const cc_csr *g, uint64_t *ticket) {
   r->need = s.bytes_needed(*g);
   if (r->need > s.cfg.hbm_budget_bytes) return CC_ERR_BUSY;
   r->t_submit = now_s();
+  r->inject = s.inject_next.exchange(0);
   {
     std::lock_guard<std::mutex> lk(s.mu);
     r->id = s.next_id++;
@@ -549,7 +565,8 @@ static int collect(cc_server *h, uint64_t ticket, void *labels_out, int *done, d
   int rc = guard([&] {
     CCG_CUDA(cudaSetDevice(s.device));
     const uint64_t n = r->g.n;
-    if (!r->lab.p || r->failed) throw Error(CC_ERR_CUDA, "request failed before launch");
+    if (r->failed) throw Error(r->fail_status, "request failed before launch");
+    if (!r->lab.p) throw Error(CC_ERR_CUDA, "request has no label buffer");
     std::vector<uint32_t> tmp;
     uint32_t *dst = static_cast<uint32_t *>(labels_out);
     if (r->g.id_bytes == 8) {
@@ -612,6 +629,12 @@ int cc_serve_get_stats(cc_server *h, cc_serve_stats *out) {
   out->bytes_in_use = s.used;
   out->peak_bytes_in_use = s.peak;
   out->waiting = s.waiting.size();
+  return CC_OK;
+}
+
+int cc_serve_debug_fail_next(cc_server *h, int where) {
+  if (!h || where < 0 || where > 2) return CC_ERR_INVALID;
+  h->s->inject_next = where;
   return CC_OK;
 }
 

@@ -522,15 +522,15 @@ void emit_keys(const Csr &g, const uint32_t *cl, const PartMap &pm, bool part, i
   const uint64_t cap = g.m / (hub_limit + 1) + g.m / kEmitPiece + 2;
   DevBuf hubs(8 * cap, s, pool), nh(4, s, pool);
   CCG_CUDA(cudaMemsetAsync(nh.p, 0, 4, s));
-  unsigned grid = grid_for(g.n, kBlock, kSMs * 32);
-  const unsigned egrid = grid_for(g.n, kBlock, kSMs * kEmitCtasPerSM);
+  unsigned grid = grid_for(g.n, kBlock, num_sms() * 32);
+  const unsigned egrid = grid_for(g.n, kBlock, num_sms() * kEmitCtasPerSM);
   cudaEvent_t t0 = c.tic(s);
   k_list_hubs<<<grid, kBlock, 0, s>>>(g.n, g.rp, hub_limit, hubs.as<uint2>(), cap,
                                       nh.as<unsigned int>());
   CCG_LAUNCH_CHECK();
   k_emit<T><<<egrid, kBlock, 0, s>>>(g.n, g.rp, col, cl, pm, part, b, hub_limit, keys, cnt);
   CCG_LAUNCH_CHECK();
-  k_emit_hubs<T><<<kSMs * kEmitCtasPerSM, kBlock, 0, s>>>(g.rp, col, cl, pm, part, b, hubs.as<uint2>(), cap,
+  k_emit_hubs<T><<<num_sms() * kEmitCtasPerSM, kBlock, 0, s>>>(g.rp, col, cl, pm, part, b, hubs.as<uint2>(), cap,
                                              nh.as<unsigned int>(), keys, cnt);
   CCG_LAUNCH_CHECK();
   c.toc(s, "contract_emit", t0, 8 * (g.n + 1) + g.m * ((uint64_t)g.idb + 4) + 4 * g.n);
@@ -657,7 +657,7 @@ void contract_graph(const Csr &g, const uint32_t *cl, uint64_t ncl,
   c.add(0, 8 * ne + 8 * ne);  // dedup: read keys, write uniques (upper bound)
   // source flags -> new ids (order preserving)
   CCG_CUDA(cudaMemsetAsync(out.newid.p, 0, 4 * ncl, s));
-  k_mark_src<<<grid_for(ne, kBlock, kSMs * 16), kBlock, 0, s>>>(uk, d_u.as<uint32_t>(), b,
+  k_mark_src<<<grid_for(ne, kBlock, num_sms() * 16), kBlock, 0, s>>>(uk, d_u.as<uint32_t>(), b,
                                                                out.newid.as<uint32_t>());
   CCG_LAUNCH_CHECK();
   scan_generic(ncl, GetFlag{out.newid.as<uint32_t>()}, PutNewId{out.newid.as<uint32_t>()},
@@ -673,11 +673,11 @@ void contract_graph(const Csr &g, const uint32_t *cl, uint64_t ncl,
   out.col.alloc(4 * out.m, s, pool);
   out.vid.alloc(4 * (out.n ? out.n : 1), s, pool);
   cudaEvent_t tb = c.tic(s);
-  k_build_csr<<<grid_for(out.m, kBlock, kSMs * 16), kBlock, 0, s>>>(
+  k_build_csr<<<grid_for(out.m, kBlock, num_sms() * 16), kBlock, 0, s>>>(
       uk, d_u.as<uint32_t>(), b, out.newid.as<uint32_t>(), out.rp.as<uint64_t>(),
       out.col.as<uint32_t>(), d_nv.as<uint32_t>());
   CCG_LAUNCH_CHECK();
-  k_vid<<<grid_for(ncl, kBlock, kSMs * 16), kBlock, 0, s>>>(ncl, out.newid.as<uint32_t>(),
+  k_vid<<<grid_for(ncl, kBlock, num_sms() * 16), kBlock, 0, s>>>(ncl, out.newid.as<uint32_t>(),
                                                            vid_of_cluster, out.vid.as<uint32_t>());
   CCG_LAUNCH_CHECK();
   // CSR rebuild: unique keys read, offsets + ids written, id map

@@ -97,6 +97,7 @@ __global__ void k_init(uint64_t n, uint64_t m, const uint64_t *__restrict__ rp,
     uint32_t par = (uint32_t)v;
     if (load_row(rp, v, m, err, r) && r.b < r.e) {
       uint64_t u = (uint64_t)__ldg(col + r.b);
+      if (u >= n) set_err(err, kErrBadId);  // k_hook checks the other entries
       bool ok = u < v;
       if (PART && ok) ok = (uint32_t)u >= part_lo(pm, (uint32_t)v);
       if (ok) par = (uint32_t)u;
@@ -936,7 +937,7 @@ template <class T, bool PART>
 void run_uf(const Csr &g, uint32_t *parent, const PartMap &pm, uint32_t hub_degree,
             cudaStream_t s, cudaMemPool_t pool, Counters &c) {
   const T *col = static_cast<const T *>(g.col);
-  unsigned grid = grid_for(g.n, kBlock, kSMs * 32);
+  unsigned grid = grid_for(g.n, kBlock, num_sms() * 32);
   const uint64_t si = (uint64_t)g.idb;
   cudaEvent_t t0 = c.tic(s);
   k_init<T, PART><<<grid, kBlock, 0, s>>>(g.n, g.m, g.rp, col, parent, pm, g.err);
@@ -955,12 +956,12 @@ void run_uf(const Csr &g, uint32_t *parent, const PartMap &pm, uint32_t hub_degr
   c.toc(s, "uf_hook", t1, hook_bytes);
   cudaEvent_t t2 = c.tic(s);
   // hub rows in pieces; every edge to a smaller id (the first one again too)
-  k_hub_pieces<T, PART, true><<<kSMs * 8, kBlock, 0, s>>>(g.n, g.m, g.rp, col, parent, pm, hl,
+  k_hub_pieces<T, PART, true><<<num_sms() * 8, kBlock, 0, s>>>(g.n, g.m, g.rp, col, parent, pm, hl,
                                                           g.err);
   CCG_LAUNCH_CHECK();
   c.toc(s, "uf_hook_hubs", t2, 0);
   cudaEvent_t t3 = c.tic(s);
-  k_compress<<<grid_for(g.n, kBlock, kSMs * 32), kBlock, 0, s>>>(g.n, parent);
+  k_compress<<<grid_for(g.n, kBlock, num_sms() * 32), kBlock, 0, s>>>(g.n, parent);
   CCG_LAUNCH_CHECK();
   c.toc(s, "uf_compress", t3, 3 * g.n * 4);
   c.add(4, (8 * (g.n + 1) + g.n * si + 4 * g.n) + hook_bytes + 3 * g.n * 4);
@@ -1034,7 +1035,7 @@ TileShape tile_shape_uncached(uint64_t n, const UfTuning &tu) {
   CCG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, t.threads, t.smem));
   if (per_sm < 1) throw Error(CC_ERR_INVALID, "tile does not fit in shared memory");
   const uint64_t tiles = (n + t.tile - 1) / t.tile;
-  t.grid = (unsigned)std::min<uint64_t>(tiles, (uint64_t)per_sm * kSMs);
+  t.grid = (unsigned)std::min<uint64_t>(tiles, (uint64_t)per_sm * num_sms());
   return t;
 }
 
@@ -1128,7 +1129,7 @@ void run_uf_tiled(const Csr &g, uint32_t *parent, const PartMap &pm, const UfTun
                                                               tu.hub_degree, hl, cut.as<uint2>(),
                                                               cut_cap, ncut, g.err);
       CCG_LAUNCH_CHECK();
-      k_cut_union<<<kSMs * 16, kBlock, 0, s>>>(cut.as<uint2>(), ncut, cut_cap, parent, united);
+      k_cut_union<<<num_sms() * 16, kBlock, 0, s>>>(cut.as<uint2>(), ncut, cut_cap, parent, united);
       CCG_LAUNCH_CHECK();
       CCG_CUDA(cudaMemcpyAsync(united, ncut, 8, cudaMemcpyDeviceToDevice, s));
     }
@@ -1136,12 +1137,12 @@ void run_uf_tiled(const Csr &g, uint32_t *parent, const PartMap &pm, const UfTun
   c.toc(s, hs ? "uf_tile_streamed" : "uf_tile", t0, tile_bytes);
   if (!hs) {
     cudaEvent_t t1 = c.tic(s);
-    k_cut_union<<<kSMs * 16, kBlock, 0, s>>>(cut.as<uint2>(), ncut, cut_cap, parent);
+    k_cut_union<<<num_sms() * 16, kBlock, 0, s>>>(cut.as<uint2>(), ncut, cut_cap, parent);
     CCG_LAUNCH_CHECK();
     c.toc(s, "uf_cut_union", t1, 0);
   }
   cudaEvent_t t2 = c.tic(s);
-  k_hub_pieces<T, PART, true><<<kSMs * 8, kBlock, 0, s>>>(g.n, g.m, g.rp, col, parent, pm,
+  k_hub_pieces<T, PART, true><<<num_sms() * 8, kBlock, 0, s>>>(g.n, g.m, g.rp, col, parent, pm,
                                                           hl, g.err);
   CCG_LAUNCH_CHECK();
   c.toc(s, "uf_hook_hubs", t2, 0);
@@ -1159,7 +1160,7 @@ void run_uf_tiled(const Csr &g, uint32_t *parent, const PartMap &pm, const UfTun
     int nch = 0;
     for (uint64_t a = 0; a < g.n; a += step, ++nch) {
       const uint64_t b = std::min<uint64_t>(g.n, a + step);
-      k_compress<<<grid_for(b - a, kBlock, kSMs * 32), kBlock, 0, s>>>(b, parent, a);
+      k_compress<<<grid_for(b - a, kBlock, num_sms() * 32), kBlock, 0, s>>>(b, parent, a);
       CCG_LAUNCH_CHECK();
       CCG_CUDA(cudaEventCreateWithFlags(&done[nch], cudaEventDisableTiming));
       CCG_CUDA(cudaEventRecord(done[nch], s));
@@ -1179,7 +1180,7 @@ void run_uf_tiled(const Csr &g, uint32_t *parent, const PartMap &pm, const UfTun
     cudaEventDestroy(copied);
     c.add(nch - 1, 0);
   } else {
-    k_compress<<<grid_for(g.n, kBlock, kSMs * 32), kBlock, 0, s>>>(g.n, parent);
+    k_compress<<<grid_for(g.n, kBlock, num_sms() * 32), kBlock, 0, s>>>(g.n, parent);
     CCG_LAUNCH_CHECK();
     c.toc(s, "uf_compress", t3, 3 * g.n * 4);
   }
@@ -1226,7 +1227,7 @@ void run_uf_afforest(const Csr &g, uint32_t *parent, const PartMap &pm, const Uf
   const T *col = static_cast<const T *>(g.col);
   const uint64_t si = (uint64_t)g.idb;
   const uint32_t hub_degree = tu.hub_degree;
-  const unsigned grid = grid_for(g.n, kBlock, kSMs * 32);
+  const unsigned grid = grid_for(g.n, kBlock, num_sms() * 32);
   uint64_t link_bytes = 0;
   if (link_tiles) {
     // link rounds as one tiled pass: the link-round entries of every row,
@@ -1246,7 +1247,7 @@ void run_uf_afforest(const Csr &g, uint32_t *parent, const PartMap &pm, const Uf
     CCG_LAUNCH_CHECK();
     c.toc(s, "uf_sample_link_tiled", t0, link_bytes);
     cudaEvent_t t1 = c.tic(s);
-    k_cut_union<<<kSMs * 16, kBlock, 0, s>>>(cut.as<uint2>(), cnt.as<unsigned long long>(),
+    k_cut_union<<<num_sms() * 16, kBlock, 0, s>>>(cut.as<uint2>(), cnt.as<unsigned long long>(),
                                              cut_cap, parent);
     CCG_LAUNCH_CHECK();
     c.toc(s, "uf_cut_union", t1, 0);
@@ -1265,7 +1266,7 @@ void run_uf_afforest(const Csr &g, uint32_t *parent, const PartMap &pm, const Uf
     }
     link_bytes = kAffRounds * round_bytes;
   }
-  k_compress<<<grid_for(g.n, kBlock, kSMs * 32), kBlock, 0, s>>>(g.n, parent);
+  k_compress<<<grid_for(g.n, kBlock, num_sms() * 32), kBlock, 0, s>>>(g.n, parent);
   CCG_LAUNCH_CHECK();
   // most frequent root of a sample = the giant component, if there is one;
   // with virtual ranks (up to 4096) one per rank, as each rank has its own
@@ -1306,12 +1307,12 @@ void run_uf_afforest(const Csr &g, uint32_t *parent, const PartMap &pm, const Uf
     c.recs.back().bytes = rest_bytes;
   }
   cudaEvent_t th = c.tic(s);
-  k_hub_pieces<T, PART, false><<<kSMs * 8, kBlock, 0, s>>>(g.n, g.m, g.rp, col, parent, pm, hl,
+  k_hub_pieces<T, PART, false><<<num_sms() * 8, kBlock, 0, s>>>(g.n, g.m, g.rp, col, parent, pm, hl,
                                                            g.err);
   CCG_LAUNCH_CHECK();
   c.toc(s, "uf_sample_hubs", th, 0);
   cudaEvent_t t2 = c.tic(s);
-  k_compress<<<grid_for(g.n, kBlock, kSMs * 32), kBlock, 0, s>>>(g.n, parent);
+  k_compress<<<grid_for(g.n, kBlock, num_sms() * 32), kBlock, 0, s>>>(g.n, parent);
   CCG_LAUNCH_CHECK();
   c.toc(s, "uf_compress", t2, 3 * g.n * 4);
   c.add((link_tiles ? 2 : 1 + kAffRounds) + 6, link_bytes + rest_bytes + 6 * g.n * 4);
@@ -1431,7 +1432,7 @@ HostShares host_shares(const uint64_t *rp, const void *col, int idb, uint64_t n,
 void widen_labels(const uint32_t *in, void *out, int out_bytes, uint64_t n, cudaStream_t s,
                   Counters &c) {
   if (n == 0) return;
-  unsigned grid = grid_for(n, kBlock, kSMs * 32);
+  unsigned grid = grid_for(n, kBlock, num_sms() * 32);
   if (out_bytes == 8)
     k_widen<uint64_t><<<grid, kBlock, 0, s>>>(in, static_cast<uint64_t *>(out), n);
   else
@@ -1442,7 +1443,7 @@ void widen_labels(const uint32_t *in, void *out, int out_bytes, uint64_t n, cuda
 
 void sanitize_ids(const Csr &g, uint32_t *col32, cudaStream_t s, Counters &c) {
   if (g.n == 0) return;
-  unsigned grid = grid_for(std::max(g.n, g.m / 4), kBlock, kSMs * 32);
+  unsigned grid = grid_for(std::max(g.n, g.m / 4), kBlock, num_sms() * 32);
   if (g.idb == 8)
     k_sanitize<uint64_t><<<grid, kBlock, 0, s>>>(g.n, g.m, g.rp,
                                                  static_cast<const uint64_t *>(g.col), col32, g.err);
@@ -1480,9 +1481,15 @@ void sanitize_ids(const Csr &g, uint32_t *col32, cudaStream_t s, Counters &c) {
 // every call; calls whose work overlaps on the GPU (different streams, or
 // different host threads) race on it and must be serialised by the caller.
 //
+// The call is synchronous: it waits on the caller's stream for the error word
+// before it returns.
+//
 // Set-up: the first call on a device looks up the device address of the
-// scratch array (cudaGetSymbolAddress) with that device current; make that
-// first call before any stream capture that should contain this solve.
+// scratch array (cudaGetSymbolAddress) with that device current, and it is
+// also the first launch of these kernels on that device, so CUDA's lazy
+// module loading may allocate and synchronise during it.  Make one warm-up
+// call per device before the point where allocation is forbidden, and before
+// any stream capture begins on that device.
 // ============================================================================
 #include <algorithm>
 #include <mutex>
@@ -1493,6 +1500,13 @@ constexpr uint32_t kNoAllocWords = 1u << 20;                  // 4 MiB
 constexpr uint32_t kNoAllocHeader = 64;                       // counter, error word, padding
 constexpr uint32_t kNoAllocHubCap = kNoAllocWords - kNoAllocHeader;
 constexpr uint32_t kNoAllocHubDegree = 32;
+// The entry guard admits a graph only if min(n, m_dir / (kNoAllocHubDegree + 1)
+// + 1) <= kNoAllocHubCap: a graph has at most m_dir / (degree + 1) rows above
+// the hub degree, so the hub list cannot overflow.  An overflow word
+// (kErrOverflow) would therefore mean a broken guard, reported as
+// CC_ERR_UNSUPPORTED, not as bad caller input.
+static_assert(kNoAllocHeader + kNoAllocHubCap <= kNoAllocWords, "hub list outside the scratch");
+static_assert(kNoAllocHeader >= 2, "the header holds the hub counter and the error word");
 
 static __device__ __align__(256) uint32_t g_noalloc_scratch[kNoAllocWords];
 
@@ -1535,12 +1549,12 @@ extern "C" int cc_gpu_run_noalloc(const uint64_t *row_ptr, const uint32_t *col, 
   uint32_t *hubs = scratch + kNoAllocHeader;
   if (cudaMemsetAsync(scratch, 0, 2 * sizeof(uint32_t), s) != cudaSuccess) return CC_ERR_CUDA;
   const PartMap pm(n, 1);
-  const unsigned grid = grid_for(n, kBlock, kSMs * 32);
+  const unsigned grid = grid_for(n, kBlock, num_sms() * 32);
   k_init<uint32_t, false><<<grid, kBlock, 0, s>>>(n, m_dir, row_ptr, col, labels_out, pm, err);
   k_hook<uint32_t, false, RowSink><<<grid, kBlock, 0, s>>>(
       n, m_dir, row_ptr, col, labels_out, pm, kNoAllocHubDegree,
       RowSink{hubs, kNoAllocHubCap, nhubs}, err);
-  k_hook_hubs<uint32_t, false><<<kSMs * 8, kBlock, 0, s>>>(n, row_ptr, col, labels_out, pm, hubs,
+  k_hook_hubs<uint32_t, false><<<num_sms() * 8, kBlock, 0, s>>>(n, row_ptr, col, labels_out, pm, hubs,
                                                            kNoAllocHubCap, nhubs, err);
   k_compress<<<grid, kBlock, 0, s>>>(n, labels_out);
   if (cudaGetLastError() != cudaSuccess) return CC_ERR_CUDA;
@@ -1548,5 +1562,6 @@ extern "C" int cc_gpu_run_noalloc(const uint64_t *row_ptr, const uint32_t *col, 
   if (cudaMemcpyAsync(&host_err, err, sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess)
     return CC_ERR_CUDA;
   if (cudaStreamSynchronize(s) != cudaSuccess) return CC_ERR_CUDA;
+  if (host_err == kErrOverflow) return CC_ERR_UNSUPPORTED;
   return host_err ? CC_ERR_INVALID : CC_OK;
 }

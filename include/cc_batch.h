@@ -56,6 +56,16 @@ void cc_batch_tuning_default(cc_batch_tuning *t);
 int cc_batch_run(cc_ctx *ctx, const cc_batch *b, const cc_batch_tuning *tuning,
                  uint32_t *labels_out, uint32_t labels_where);
 
+/* The plain path that the batched solve is measured against: one
+   cc_ctx_run(algo, one rank) per graph, looped in C++ on ctx's stream (each
+   solve ends with its stream synchronisation, as a caller solving the graphs
+   one by one would see).  Device arrays only; labels_out: total_n uint32 on
+   the device.  Before the loop one kernel writes per-graph row offsets that
+   start at 0 (held by ctx for the next call).  The per-graph loop of the
+   reference's drivers (app/exp_contraction.cpp:75-155) has this shape. */
+int cc_batch_run_plain(cc_ctx *ctx, const cc_batch *b, cc_algo algo, const cc_config *cfg,
+                       uint64_t seed, uint32_t *labels_out);
+
 /* Time candidate schedules on *b (device arrays) and write the fastest per
    size bucket to *out.  reps: timed repetitions per candidate. */
 int cc_batch_autotune(cc_ctx *ctx, const cc_batch *b, int reps, cc_batch_tuning *out);

@@ -44,6 +44,11 @@ int cc_gen_rhg(uint64_t n, double avg_deg, double gamma, uint64_t seed, uint32_t
                cc_host_graph *out);
 /* The disk radius R that cc_gen_rhg uses for (n, avg_deg, gamma). */
 double cc_gen_rhg_radius(uint64_t n, double avg_deg, double gamma);
+/* Test aid: the number of vertex pairs on which g (a cc_gen_rhg result for the
+   same arguments) disagrees with the model's edge test applied to every pair,
+   O(n^2); ~0 for bad arguments. */
+uint64_t cc_gen_rhg_verify(uint64_t n, double avg_deg, double gamma, uint64_t seed,
+                           const cc_host_graph *g);
 
 void cc_host_graph_free(cc_host_graph *g);
 

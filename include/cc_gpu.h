@@ -182,13 +182,18 @@ int cc_csr_validate(const cc_csr *g, int check_sym);
  * (and CC_EXP with one rank): labels_out[v] = minimum vertex id of v's
  * component.  All pointers are device pointers: row_ptr (n+1), col (m_dir
  * uint32 ids, symmetric CSR), labels_out (n uint32).  stream is a
- * cudaStream_t (NULL = default stream); the call returns when the solve is
- * done.  Scratch lives in a fixed 4 MiB device array that every GPU loading
- * the library keeps until exit; graphs with min(n, m_dir/33 + 1) > 1,048,512
- * are rejected with CC_ERR_UNSUPPORTED.  All calls share that array: calls
- * that overlap on the GPU race and must be serialised by the caller.  The
- * first call on a device looks up the array's device address; make it before
- * any stream capture that should contain this solve.
+ * cudaStream_t (NULL = default stream).  The call is synchronous: it waits on
+ * `stream` until the solve is done and returns its status (CC_ERR_INVALID for
+ * offsets that are not monotone or exceed m_dir, or an id >= n).  Scratch
+ * lives in a fixed 4 MiB device array that every GPU loading the library
+ * keeps until exit; graphs with min(n, m_dir/33 + 1) > 1,048,512 are rejected
+ * with CC_ERR_UNSUPPORTED before any launch.  All calls share that array:
+ * calls that overlap on the GPU race and must be serialised by the caller.
+ * The first call on a device looks up the array's device address and is the
+ * first launch of its kernels there, which CUDA's lazy module loading may
+ * turn into an allocation and a synchronisation: make one warm-up call per
+ * device before allocation becomes forbidden, and before any stream capture
+ * begins on that device.
  */
 int cc_gpu_run_noalloc(const uint64_t *row_ptr, const uint32_t *col, uint64_t n,
                        uint64_t m_dir, uint32_t *labels_out, void *stream);

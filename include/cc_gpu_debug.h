@@ -9,6 +9,7 @@
 #define CC_GPU_DEBUG_H_
 
 #include "cc_gpu.h"
+#include "cc_serve.h"
 
 #ifdef __cplusplus
 extern "C" {
@@ -39,6 +40,17 @@ int cc_debug_contract(const cc_csr *g, const uint32_t *cl, uint64_t ncl,
 int cc_debug_local_components(const cc_csr *g, uint32_t *labels_out);
 /* Stable radix sort of n device uint64 keys on bits [0, bits). */
 int cc_debug_radix_sort(uint64_t *keys, uint64_t n, int bits);
+/* Test hook: caps every iterative round loop of ctx's solves (decomposition,
+   label and shortcut propagation) at `cap` rounds (0 restores the default
+   n + 2), so that a test reaches CC_ERR_NO_CONVERGENCE without a faulty
+   kernel; the context stays usable. */
+int cc_debug_set_round_cap(cc_ctx *ctx, uint32_t cap);
+/* Test hook: the next request submitted to s fails on purpose at `where`
+   (1: staging, as if its device allocation failed - collect returns
+   CC_ERR_OOM; 2: its launch, as if a launch failed - collect returns
+   CC_ERR_CUDA; use a graph above the one-CTA size for 2, a failed one-CTA
+   launch fails every small request of that launch).  0 cancels. */
+int cc_serve_debug_fail_next(cc_server *s, int where);
 /* Shortcut propagation on a uint32 device graph from the given labels. */
 int cc_debug_shortcut(const cc_csr *g, uint32_t *labels_inout, uint32_t hitters,
                       uint32_t *rounds_out);

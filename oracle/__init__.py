@@ -43,25 +43,68 @@ _SYMS = {
     "or_labels": (C.c_int, [C.c_uint64, _U64P, _U64P, _U64P]),
     "or_shortcut": (C.c_int, [C.c_uint64, _U64P, _U64P, _U64P, C.c_uint64]),
 }
+
+
+class _HostGraphC(C.Structure):  # cc_host_graph of include/cc_gen.h
+    _fields_ = [("n", C.c_uint64), ("m_dir", C.c_uint64), ("row_ptr", C.c_void_p),
+                ("col", C.c_void_p), ("id_bytes", C.c_uint32), ("pad_", C.c_uint32)]
+
+
+_GEN_SYMS = {
+    "or_gen_gnm": (C.c_int, [C.c_uint64, C.c_uint64, C.c_uint64, C.c_uint32, C.POINTER(_HostGraphC)]),
+    "or_gen_grid": (C.c_int, [C.c_uint64, C.c_uint64, C.c_double, C.c_uint64, C.c_uint32,
+                              C.POINTER(_HostGraphC)]),
+    "or_gen_rhg": (C.c_int, [C.c_uint64, C.c_double, C.c_double, C.c_uint64, C.c_uint32,
+                             C.POINTER(_HostGraphC)]),
+    "or_graph_free": (None, [C.POINTER(_HostGraphC)]),
+}
 _lib = None
 
 
+GEN_SRC = HERE.parent / "components_gb300" / "csrc" / "gen.cpp"
+GEN_DEPS = [GEN_SRC, HERE.parent / "components_gb300" / "csrc" / "rhg.h",
+            HERE.parent / "include" / "cc_gen.h", HERE / "inputs.cpp"]
+
+
+def _run(cmd: list[str]) -> subprocess.CompletedProcess:
+    return subprocess.run(cmd, capture_output=True, text=True)
+
+
 def build(force: bool = False) -> Path:
-    """Compile cc_oracle.c with gcc (OpenMP when available)."""
+    """Compile cc_oracle.c with gcc and the input generators (the library's
+    generator source, hidden symbols, plus inputs.cpp) with g++, OpenMP when
+    available, into one libccoracle.so."""
     BUILD.mkdir(exist_ok=True)
     src = HERE / "cc_oracle.c"
-    if not force and LIB.exists() and LIB.stat().st_mtime >= src.stat().st_mtime:
+    deps = [src] + GEN_DEPS
+    if not force and LIB.exists() and all(LIB.stat().st_mtime >= d.stat().st_mtime for d in deps):
         return LIB
     cc = shutil.which("gcc") or "gcc"
-    base = [cc, "-O2", "-std=c11", "-fPIC", "-shared", "-ffp-contract=off"]
-    tmp = LIB.with_suffix(".so.tmp")
-    r = subprocess.run(base + ["-fopenmp", "-o", str(tmp), str(src), "-lm"], capture_output=True, text=True)
-    if r.returncode != 0:
-        r = subprocess.run(base + ["-o", str(tmp), str(src), "-lm"], capture_output=True, text=True)
-    if r.returncode != 0:
-        raise RuntimeError("oracle build failed:\n" + r.stderr)
-    tmp.replace(LIB)
-    return LIB
+    cxx = shutil.which("g++") or "g++"
+    err = ""
+    for omp in (["-fopenmp"], []):
+        objs = [BUILD / "cc_oracle.o", BUILD / "gen.o", BUILD / "inputs.o"]
+        steps = [
+            [cc, "-O2", "-std=c11", "-fPIC", "-ffp-contract=off", *omp, "-c", str(src), "-o", str(objs[0])],
+            [cxx, "-O3", "-std=c++17", "-fPIC", "-ffp-contract=off", "-fvisibility=hidden", *omp,
+             "-c", str(GEN_SRC), "-o", str(objs[1])],
+            [cxx, "-O2", "-std=c++17", "-fPIC", "-c", str(HERE / "inputs.cpp"), "-o", str(objs[2])],
+        ]
+        tmp = LIB.with_suffix(".so.tmp")
+        link = [cxx, "-shared", *omp, "-o", str(tmp)] + [str(o) for o in objs] + ["-lm"]
+        ok = True
+        for cmd in steps + [link]:
+            r = _run(cmd)
+            if r.returncode != 0:
+                err, ok = r.stderr, False
+                break
+        for o in objs:
+            if o.exists():
+                o.unlink()
+        if ok:
+            tmp.replace(LIB)
+            return LIB
+    raise RuntimeError("oracle build failed:\n" + err)
 
 
 def lib() -> C.CDLL:
@@ -70,11 +113,66 @@ def lib() -> C.CDLL:
         if not LIB.exists():
             build()
         _lib = C.CDLL(str(LIB))
-        for name, (res, args) in _SYMS.items():
+        for name, (res, args) in list(_SYMS.items()) + list(_GEN_SYMS.items()):
             fn = getattr(_lib, name)
             fn.restype = res
             fn.argtypes = args
     return _lib
+
+
+class HostCSR:
+    """A host CSR (numpy row_ptr uint64, col uint32 or uint64) that the
+    oracle's own input path built; numpy() and n / m / id_bytes match the
+    library's StaticGraph, so every function here takes either."""
+
+    def __init__(self, row_ptr: np.ndarray, col: np.ndarray):
+        self.row_ptr, self.col = row_ptr, col
+
+    @property
+    def n(self) -> int:
+        return int(self.row_ptr.shape[0]) - 1
+
+    @property
+    def m(self) -> int:
+        return int(self.col.shape[0])
+
+    @property
+    def id_bytes(self) -> int:
+        return int(self.col.itemsize)
+
+    def numpy(self):
+        return self.row_ptr, self.col.astype(np.uint64)
+
+
+def _take(fn, *args) -> HostCSR:
+    hg = _HostGraphC()
+    st = getattr(lib(), fn)(*args, C.byref(hg))
+    if st != 0:
+        raise RuntimeError(f"{fn}: status {st}")
+    try:
+        n, m = hg.n, hg.m_dir
+        rp = np.ctypeslib.as_array(C.cast(hg.row_ptr, C.POINTER(C.c_uint64)), shape=(n + 1,)).copy()
+        ct = C.c_uint32 if hg.id_bytes == 4 else C.c_uint64
+        col = (np.ctypeslib.as_array(C.cast(hg.col, C.POINTER(ct)), shape=(m,)).copy() if m
+               else np.zeros(0, np.uint32 if hg.id_bytes == 4 else np.uint64))
+    finally:
+        lib().or_graph_free(C.byref(hg))
+    return HostCSR(rp, col)
+
+
+def gen_rhg(n: int, avg_deg: float = 16.0, gamma: float = 2.6, seed: int = 1,
+            id_bytes: int = 4) -> HostCSR:
+    """The library's random hyperbolic graph, built on the host by the
+    oracle's copy of the generator (no GPU library loaded)."""
+    return _take("or_gen_rhg", n, avg_deg, gamma, seed, id_bytes)
+
+
+def gen_grid(X: int, Y: int, p: float = 0.5, seed: int = 1, id_bytes: int = 4) -> HostCSR:
+    return _take("or_gen_grid", X, Y, p, seed, id_bytes)
+
+
+def gen_gnm(n: int, m: int, seed: int = 1, id_bytes: int = 8) -> HostCSR:
+    return _take("or_gen_gnm", n, m, seed, id_bytes)
 
 
 def _u64(a) -> np.ndarray:

@@ -96,3 +96,21 @@ def test_batch_bad_local_id_is_reported(cuda):
     with pytest.raises(_lib.CCError) as ei:
         B.batch_run(bad.to_device("cuda:0"))
     assert ei.value.status == _lib.CC_ERR_INVALID
+
+
+def test_batch_4096_config_scale(cuda):
+    """The batched configuration itself: 4096 G(n, m) graphs, n log-uniform in
+    [2^8, 2^18], average degree uniform in [0.5, 8].  Batched labels equal the
+    plain path (one cc_ctx_run per graph, looped in C++) and the oracle."""
+    import torch
+    bt = B.gen_batch(4096, 8, 18, 0.5, 8.0, seed=1)
+    want = _want(bt)
+    D = bt.to_device("cuda:0")
+    ctx = cc.Context(0)
+    tune = B.autotune(D, ctx, reps=1)
+    got = B.batch_run(D, ctx, tune).cpu().numpy().view(np.uint32)
+    assert np.array_equal(got, want)
+    plain = torch.full((bt.total_n,), -1, dtype=torch.int32, device="cuda:0")
+    B.plain_run(D, ctx, plain, "exp", cc.Config(seed=1001))
+    assert np.array_equal(plain.cpu().numpy().view(np.uint32), want)
+    ctx.close()

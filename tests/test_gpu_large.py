@@ -1,5 +1,7 @@
-"""GPU parity at the full benchmark sizes: G(n=2^20, m=2^22) with 64-bit ids
-and the 8192 x 8192 bond-percolation grid (p = 0.5) with 32-bit ids.  The
+"""GPU parity at the full benchmark sizes: G(n=2^20, m=2^22) with 64-bit ids,
+the 8192 x 8192 bond-percolation grid (p = 0.5) with 32-bit ids and the
+random hyperbolic graph of 2^26 vertices (d = 16, gamma = 2.6, 32-bit ids,
+about 1.1e9 directed entries: the headline configuration).  The
 oracle's union-find still finishes in seconds at these sizes, so labels are
 compared entry for entry; size-independent checks (every label is a
 component minimum, labels constant along every edge) run beside it."""
@@ -68,3 +70,25 @@ def test_grid_exp_ldd_path(cuda, grid):
     got = _solve_dev(G, "exp", 64, cc.Config(seed=1002, sequential_limit=0))
     assert np.array_equal(got, want)
     _properties(G, got)
+
+
+@pytest.fixture(scope="module")
+def rhg26():
+    G = cc.gen_rhg(1 << 26, 16.0, 2.6, seed=1, id_bytes=4)
+    return G, oracle.uf_labels(G)
+
+
+def test_rhg_2_26_full_size(cuda, rhg26):
+    """Labels of the headline graph equal the union-find's for exp_contraction
+    with one rank and with 16 virtual ranks, and for all_reduce."""
+    import torch
+    G, want = rhg26
+    D = G.to_device("cuda:0")
+    lab = torch.empty(G.n, dtype=torch.int32, device="cuda:0")
+    for algo, P in (("exp", 1), ("exp", 16), ("allreduce", 1)):
+        lab.fill_(-1)
+        cc.SOLVERS[algo](cc.Config(seed=1001), 0, P).FindComponents(D.with_parts(P), lab)
+        got = lab.cpu().numpy().view(np.uint32).astype(np.uint64)
+        assert np.array_equal(got, want), (algo, P)
+    del D, lab
+    torch.cuda.empty_cache()

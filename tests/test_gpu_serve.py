@@ -111,3 +111,46 @@ def test_invalid_request_is_reported(cuda):
         assert ei.value.status == _lib.CC_ERR_INVALID
         lab, _ = srv.wait(tg, timeout_s=60)
         assert np.array_equal(lab, cc.find_components(good, "exp"))
+
+
+def test_thousand_requests_from_two_hundred_graphs(cuda):
+    """A serving stream at scale: 1,200 requests drawn from 240 distinct seeded
+    graphs (the three families, n log-uniform in [2^10, 2^18], degree uniform
+    in [1, 16]) arriving as a Poisson stream; every request's labels equal
+    the graph solved alone (the plain path, itself checked against the
+    oracle)."""
+    rng = np.random.default_rng(17)
+    pool = []
+    for i in range(240):
+        kind = i % 3
+        n = int(2 ** rng.uniform(10, 18))
+        d = float(rng.uniform(1, 16))
+        if kind == 0:
+            pool.append(cc.gen_gnm(n, max(1, int(n * d / 2)), seed=7000 + i, id_bytes=4))
+        elif kind == 1:
+            side = max(2, int(round(np.sqrt(n))))
+            pool.append(cc.gen_grid(side, side, 0.5, seed=7000 + i))
+        else:
+            pool.append(cc.gen_rhg(n, d, 2.6, seed=7000 + i))
+    alone = [cc.find_components(G, "exp") for G in pool]
+    for j in range(0, len(pool), 8):
+        assert np.array_equal(alone[j].astype(np.uint64), oracle.uf_labels(pool[j])), j
+    picks = rng.integers(0, len(pool), 1200)
+    gaps = rng.exponential(0.0002, len(picks))
+    with Server() as srv:
+        tickets = []
+
+        def producer():
+            for j, g in zip(picks, gaps):
+                tickets.append(srv.submit(pool[int(j)]))
+                time.sleep(float(g))
+
+        th = threading.Thread(target=producer)
+        th.start()
+        th.join()
+        for t, j in zip(tickets, picks):
+            lab, _ = srv.wait(t, timeout_s=300)
+            assert np.array_equal(lab, alone[int(j)]), int(j)
+        st = srv.stats()
+        assert st["completed"] == st["collected"] == len(picks)
+        assert st["batches"] < len(picks) and st["bytes_in_use"] == 0

@@ -71,10 +71,51 @@ def test_reference_arm_rank0_only():
     r1 = _bench({"RANK": "1", "WORLD_SIZE": "2", "LOCAL_RANK": "1"}, "--impl", "reference", "--gpus", "2")
     assert r1.returncode == 0 and r1.stdout.strip() == ""
     r0 = _bench({"RANK": "0", "WORLD_SIZE": "2", "LOCAL_RANK": "0"}, "--impl", "reference", "--gpus", "2",
-                "--grid", "256", "--steps", "1", "--warmup", "0")
+                "--workload", "grid", "--grid", "256", "--steps", "1", "--warmup", "0")
     assert r0.returncode == 0, r0.stderr[-2000:]
     lines = [ln for ln in r0.stdout.splitlines() if ln.startswith("{")]
     assert len(lines) == 1
     line = json.loads(lines[0])
     assert line["impl"] == "reference" and line["n_gpus"] == 2 and line["value"] > 0
     assert line["e2e"]["value"] == line["value"] and line["cpu_baseline"]["kind"] == "port"
+
+
+_NO_GPU_LIB = r"""
+import json, sys
+sys.path.insert(0, sys.argv[1])
+import bench
+args = bench.parse_args(["--impl", "reference", "--rhg-log2n", "12", "--steps", "1", "--warmup", "0"])
+line = bench.reference_arm(args, bench.Workload("rhg", args), 1)
+maps = open("/proc/self/maps").read()
+print(json.dumps({"line": line, "gpu_lib": "libccgpu" in maps, "gen_lib": "libccgen" in maps,
+                  "imported": any(m.startswith("components_gb300") for m in sys.modules)}))
+"""
+
+
+def test_reference_arm_loads_no_library_of_ours():
+    """The reference arm builds its graph through the oracle's own input path:
+    components_gb300 is never imported, and neither libccgpu.so nor
+    libccgen.so is mapped into the process."""
+    r = subprocess.run([sys.executable, "-c", _NO_GPU_LIB, str(ROOT)], cwd=ROOT,
+                       capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr[-2000:]
+    d = json.loads(r.stdout.strip().splitlines()[-1])
+    assert not d["gpu_lib"] and not d["gen_lib"] and not d["imported"]
+    assert d["line"]["impl"] == "reference" and d["line"]["value"] > 0
+
+
+def test_both_arms_build_the_same_graph_and_config():
+    """Workload.ours() (libccgen) and Workload.oracle() (the oracle's linked
+    copy of the generators) give the same CSR, so both arms print the same
+    config dict."""
+    import numpy as np
+    sys.path.insert(0, str(ROOT))
+    import bench
+    for wl_name, extra in (("rhg", ["--rhg-log2n", "13"]), ("grid", ["--grid", "96"])):
+        args = bench.parse_args(["--workload", wl_name, *extra])
+        wl = bench.Workload(wl_name, args)
+        a, b = wl.ours(), wl.oracle()
+        ra, ca = a.numpy()
+        rb, cb = b.numpy()
+        assert np.array_equal(ra, rb) and np.array_equal(ca, cb)
+        assert wl.config(a.n, a.m, 2) == wl.config(b.n, b.m, 2)
