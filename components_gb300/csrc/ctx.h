@@ -38,7 +38,7 @@ struct cc_ctx {
   cc_stats prof_total{};      // per-kernel sums over the solves since profiling was switched on
   uint64_t prof_solves = 0;
   ccg::BatchCache *batch = nullptr;  // last recorded batch solve (CUDA graph)
-  DevBuf plain_rp;  // per-graph offsets of cc_batch_run_plain (kept for the next call)
+  ccg::DevBuf plain_rp;  // per-graph offsets of cc_batch_run_plain (kept for the next call)
   // host threads and page-locked staging of the streamed input (made on first use)
   std::unique_ptr<ccg::HostStager> stager;
 };

@@ -175,6 +175,20 @@ def gen_gnm(n: int, m: int, seed: int = 1, id_bytes: int = 8) -> HostCSR:
     return _take("or_gen_gnm", n, m, seed, id_bytes)
 
 
+def induced_prefix(G, k: int) -> HostCSR:
+    """The subgraph induced by vertices [0, k) of G (rows 0 .. k-1, entries
+    below k kept): a bounded sample of a graph for timing the CPU baseline.
+    On an angularly ordered hyperbolic graph it is one contiguous sector."""
+    rp, col = G.numpy()
+    k = min(int(k), G.n)
+    head = col[: int(rp[k])]
+    keep = head < k
+    cm = np.concatenate([[0], np.cumsum(keep, dtype=np.uint64)]).astype(np.uint64)
+    new_rp = cm[rp[: k + 1].astype(np.int64)]
+    dt = np.uint32 if G.id_bytes == 4 else np.uint64
+    return HostCSR(new_rp.astype(np.uint64), head[keep].astype(dt))
+
+
 def _u64(a) -> np.ndarray:
     return np.ascontiguousarray(np.asarray(a), dtype=np.uint64)
 
