@@ -88,12 +88,25 @@ class Workload:
             self.flags = f"-gen grid_2d -n {side} -m {side} -p 0.5"
         self.args = args
 
-    def ours(self):
-        """The graph for the GPU arm (components_gb300 host generators)."""
+    def ours_host(self):
+        """The graph from the library's host generators (libccgen)."""
         import components_gb300 as cc
         if self.name == "rhg":
             return cc.gen_rhg(self.n, RHG_DEG, RHG_GAMMA, seed=INPUT_SEED, id_bytes=4)
         return cc.gen_grid(self.args.grid, self.args.grid, GRID_P, seed=INPUT_SEED, id_bytes=4)
+
+    def ours_device(self, device):
+        """The GPU arm's graph, built on the device by the library's device
+        generators (the host generators' graph bit for bit), and its host copy
+        (for the end-to-end steps and the checks)."""
+        import components_gb300 as cc
+        if self.name == "rhg":
+            D = cc.gen_rhg_device(self.n, RHG_DEG, RHG_GAMMA, seed=INPUT_SEED, id_bytes=4, device=device)
+        else:
+            D = cc.gen_grid_device(self.args.grid, self.args.grid, GRID_P, seed=INPUT_SEED, id_bytes=4,
+                                   device=device)
+        H = cc.StaticGraph(D.row_ptr.cpu().numpy().view(np.uint64), D.col.cpu().numpy().view(np.uint32))
+        return H, D
 
     def oracle(self):
         """The same graph through the oracle's own input path."""
@@ -288,13 +301,14 @@ def gpu_arm(args, wl: Workload, rank: int, world: int, local: int) -> dict | Non
     import torch
     import components_gb300 as cc
 
-    G = wl.ours()
+    t_gen = time.perf_counter()
+    G, D = wl.ours_device(f"cuda:{local}")
+    gen_s = time.perf_counter() - t_gen
     n, m = G.n, G.m
     conf = cc.Config(seed=ALGO_SEED, beta=BETA, sequential_limit=SEQ)
     ctx = cc.Context(local)
     ctx.set_tuning(hook_mode=args.hook_mode, tile_vertices=args.tile, tile_threads=args.tile_threads)
     stream = torch.cuda.ExternalStream(ctx.stream_handle)
-    D = G.to_device(f"cuda:{local}")
     lab = torch.empty(n, dtype=torch.int32, device=f"cuda:{local}")
     solver = cc.ExponentialContraction(conf, 0, 1, ctx)
 
@@ -411,6 +425,7 @@ def gpu_arm(args, wl: Workload, rank: int, world: int, local: int) -> dict | Non
         "kernel_share": share,
         "per_kernel": per_kernel,
         "solve_ms_mean": solve_ms_mean,
+        "generated_on_device_s": gen_s,
         "labels_match_oracle": checked,
         "clocks": clock,
         "cpu_baseline": cpu,

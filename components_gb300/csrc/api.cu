@@ -486,10 +486,13 @@ int ctx_run(cc_ctx *C, const cc_csr *g, cc_algo algo, const cc_config *cfg_in, u
           dc.few_hubs = hs.few_hubs;
           dc.valid = true;
         }
-        streamed = dc.tiles;
+        // the tiled pass, or sampled linking whose link rounds stay in
+        // their tiles: both run under the transfer
+        streamed = dc.tiles || dc.link_tiles;
+        hsrc.sampled = !dc.tiles;
       }
     }
-    if (streamed) {
+    if (streamed && !hsrc.sampled) {  // degree bytes: the tiled pass's offsets only
       if (!C->stager) C->stager.reset(new ccg::HostStager());
       hsrc.stager = C->stager.get();
     }

@@ -8,6 +8,7 @@
 
 #include "../../include/cc_gpu.h"
 #include "ctx.h"
+#include "rhg.h"
 
 namespace ccg {
 namespace {
@@ -80,6 +81,150 @@ __global__ void k_keys_to_csr(const uint64_t *__restrict__ keys, uint64_t nk, ui
   }
   const uint64_t mask = (1ull << b) - 1;
   for (uint64_t e = t; e < nk; e += stride) col[e] = (T)(keys[e] & mask);
+}
+
+// ---- random hyperbolic graph (rhg.h holds the model and the exact test) ----
+// Points are kept as structure-of-arrays in the vertex (angular) order.
+struct RhgPts {
+  double *a, *b, *s, *x, *y;
+  uint64_t *phi;
+  uint32_t *band;
+  __device__ __forceinline__ rhg::Point get(uint64_t v) const {
+    rhg::Point p;
+    p.a = a[v];
+    p.b = b[v];
+    p.s = s[v];
+    p.x = x[v];
+    p.y = y[v];
+    p.phi = phi[v];
+    p.band = (int)band[v];
+    return p;
+  }
+};
+// Per band: its vertices in increasing id (bl + band_start[b] ..), and its
+// 2^L[b] + 1 cell starts (absolute positions in bl) at cell_off[b].
+struct RhgBands {
+  const uint32_t *bl;
+  const uint64_t *band_start;  // nb + 1
+  const uint64_t *cell;        // all bands' cell starts
+  const uint64_t *cell_off;    // nb
+  const int *L;                // nb
+};
+
+__global__ void k_rhg_keys(rhg::Params P, uint64_t *__restrict__ keys) {
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < P.n;
+       i += (uint64_t)gridDim.x * blockDim.x)
+    keys[i] = rhg::angle_key(P, i);
+}
+
+// points in vertex order, and the band keys (band << 32) | v for grouping
+__global__ void k_rhg_points(rhg::Params P, const uint64_t *__restrict__ keys, RhgPts pt,
+                             uint64_t *__restrict__ bkeys) {
+  for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < P.n;
+       v += (uint64_t)gridDim.x * blockDim.x) {
+    const rhg::Point p = rhg::point(P, keys[v]);
+    pt.a[v] = p.a;
+    pt.b[v] = p.b;
+    pt.s[v] = p.s;
+    pt.x[v] = p.x;
+    pt.y[v] = p.y;
+    pt.phi[v] = p.phi;
+    pt.band[v] = (uint32_t)p.band;
+    bkeys[v] = ((uint64_t)p.band << 32) | v;
+  }
+}
+
+// band_start[b] = first sorted band key of band >= b, b in [0, nb]
+__global__ void k_rhg_band_starts(const uint64_t *__restrict__ bkeys, uint64_t n, int nb,
+                                  uint64_t *__restrict__ band_start, uint32_t *__restrict__ bl) {
+  const uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+  if (t <= (uint64_t)nb) {
+    uint64_t lo = 0, hi = n;
+    while (lo < hi) {
+      const uint64_t mid = (lo + hi) >> 1;
+      if ((bkeys[mid] >> 32) < t) lo = mid + 1;
+      else hi = mid;
+    }
+    band_start[t] = lo;
+  }
+  for (uint64_t i = t; i < n; i += (uint64_t)gridDim.x * blockDim.x) bl[i] = (uint32_t)bkeys[i];
+}
+
+// cell starts: entry j of band b = first vertex of the band whose cell is >= j
+__global__ void k_rhg_cells(RhgBands B, RhgPts pt, int nb, uint64_t total,
+                            uint64_t *__restrict__ cell) {
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < total;
+       i += (uint64_t)gridDim.x * blockDim.x) {
+    int b = 0;
+    while (b + 1 < nb && B.cell_off[b + 1] <= i) ++b;
+    const uint64_t j = i - B.cell_off[b];
+    const int L = B.L[b];
+    uint64_t lo = B.band_start[b], hi = B.band_start[b + 1];
+    while (lo < hi) {
+      const uint64_t mid = (lo + hi) >> 1;
+      if (rhg::cell_of(pt.phi[B.bl[mid]], L) < j) lo = mid + 1;
+      else hi = mid;
+    }
+    cell[i] = lo;
+  }
+}
+
+// Every neighbour of v (the candidate search of the host generator): with
+// out == nullptr count them into deg[v], else write (v << idbits) | w keys
+// from out[start].
+__global__ void k_rhg_neighbours(rhg::Params P, RhgPts pt, RhgBands B, uint32_t *__restrict__ deg,
+                                 const uint64_t *__restrict__ rp, uint64_t *__restrict__ out) {
+  for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < P.n;
+       v += (uint64_t)gridDim.x * blockDim.x) {
+    const rhg::Point pv = pt.get(v);
+    uint64_t cnt = 0, e = out ? rp[v] : 0;
+    for (int b = 0; b < P.nb; ++b) {
+      const uint64_t bs = B.band_start[b], be = B.band_start[b + 1];
+      if (bs == be) continue;
+      const int L = B.L[b];
+      uint64_t half = 0;
+      const bool win = L > 0 && rhg::window(P, pv, b, &half);
+      uint64_t r0a, r0b, r1a = 0, r1b = 0;  // one or two ranges of positions in bl
+      if (!win) {
+        r0a = bs;
+        r0b = be;
+      } else {
+        const uint64_t lo = pv.phi - half, hi = pv.phi + half;
+        const uint64_t *c = B.cell + B.cell_off[b];
+        const uint64_t c0 = rhg::cell_of(lo, L), c1 = rhg::cell_of(hi, L);
+        if (lo > pv.phi || hi < pv.phi) {  // the window crosses angle 0
+          r0a = c[c0];
+          r0b = be;
+          r1a = bs;
+          r1b = c[c1 + 1];
+        } else {
+          r0a = c[c0];
+          r0b = c[c1 + 1];
+        }
+      }
+      for (int part = 0; part < 2; ++part) {
+        const uint64_t ka = part ? r1a : r0a, kb = part ? r1b : r0b;
+        for (uint64_t k = ka; k < kb; ++k) {
+          const uint32_t w = B.bl[k];
+          if (w == v) continue;
+          const uint64_t pw_phi = pt.phi[w];
+          if (win && pw_phi - (pv.phi - half) > 2 * half) continue;
+          if (!rhg::adjacent(P, pv, pt.get(w))) continue;
+          if (out) out[e++] = (v << P.idbits) | w;
+          else ++cnt;
+        }
+      }
+    }
+    if (!out) deg[v] = (uint32_t)cnt;
+  }
+}
+
+template <class T>
+__global__ void k_keys_low(const uint64_t *__restrict__ keys, uint64_t nk, int b, T *__restrict__ col) {
+  const uint64_t mask = (1ull << b) - 1;
+  for (uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; e < nk;
+       e += (uint64_t)gridDim.x * blockDim.x)
+    col[e] = (T)(keys[e] & mask);
 }
 
 int bits_for_n(uint64_t x) {
@@ -171,6 +316,91 @@ int cc_gen_gnm_device(cc_ctx *ctx, uint64_t n, uint64_t m, uint64_t seed, uint32
     else
       ccg::k_keys_to_csr<uint32_t><<<grid, ccg::kBlock, 0, s>>>(uniq.as<uint64_t>(), u, n, b, row_ptr,
                                                                 static_cast<uint32_t *>(col));
+    CCG_LAUNCH_CHECK();
+    CCG_CUDA(cudaStreamSynchronize(s));
+  });
+}
+
+int cc_gen_rhg_device(cc_ctx *ctx, uint64_t n, double avg_deg, double gamma, uint64_t seed,
+                      uint32_t id_bytes, uint64_t *row_ptr, void *col, uint64_t cap,
+                      uint64_t *m_dir) {
+  return ccg::guard([&] {
+    if ((id_bytes != 4 && id_bytes != 8) || !row_ptr || !m_dir || (cap && !col))
+      throw Error(CC_ERR_INVALID, "bad hyperbolic generator arguments");
+    rhg::Params P;
+    const int st = rhg::make_params(n, avg_deg, gamma, seed, &P);
+    if (st != CC_OK) throw Error(st, "bad hyperbolic generator parameters");
+    cc_ctx *C = ctx ? ctx : ccg::default_context();
+    CCG_CUDA(cudaSetDevice(C->device));
+    cudaStream_t s = C->stream;
+    ccg::Counters c;
+    const unsigned grid = ccg::grid_for(n, ccg::kBlock, ccg::num_sms() * 16);
+    // points in angular order
+    DevBuf keys(8 * n, s, C->pool), tmp(8 * n, s, C->pool);
+    ccg::k_rhg_keys<<<grid, ccg::kBlock, 0, s>>>(P, keys.as<uint64_t>());
+    CCG_LAUNCH_CHECK();
+    const uint64_t *sk = ccg::radix_sort_u64(keys.as<uint64_t>(), tmp.as<uint64_t>(), n, 64, s, C->pool, c);
+    DevBuf pa(8 * n, s, C->pool), pb(8 * n, s, C->pool), ps(8 * n, s, C->pool), px(8 * n, s, C->pool),
+        py(8 * n, s, C->pool), pphi(8 * n, s, C->pool), pband(4 * n, s, C->pool), bkeys(8 * n, s, C->pool);
+    const ccg::RhgPts pt{pa.as<double>(), pb.as<double>(), ps.as<double>(), px.as<double>(),
+                         py.as<double>(), pphi.as<uint64_t>(), pband.as<uint32_t>()};
+    ccg::k_rhg_points<<<grid, ccg::kBlock, 0, s>>>(P, sk, pt, bkeys.as<uint64_t>());
+    CCG_LAUNCH_CHECK();
+    // vertices grouped by band, increasing id inside a band
+    uint64_t *bsort = (sk == keys.as<uint64_t>()) ? tmp.as<uint64_t>() : keys.as<uint64_t>();
+    int bbits = 32;
+    while ((1 << (bbits - 32)) <= P.nb) ++bbits;
+    const uint64_t *gk = ccg::radix_sort_u64(bkeys.as<uint64_t>(), bsort, n, bbits, s, C->pool, c);
+    DevBuf bl(4 * n, s, C->pool), bstart(8 * (P.nb + 1), s, C->pool);
+    ccg::k_rhg_band_starts<<<grid, ccg::kBlock, 0, s>>>(gk, n, P.nb, bstart.as<uint64_t>(),
+                                                        bl.as<uint32_t>());
+    CCG_LAUNCH_CHECK();
+    std::vector<uint64_t> hb(P.nb + 1);
+    CCG_CUDA(cudaMemcpyAsync(hb.data(), bstart.p, 8 * (P.nb + 1), cudaMemcpyDeviceToHost, s));
+    CCG_CUDA(cudaStreamSynchronize(s));
+    // angular cells per band
+    std::vector<int> hL(P.nb);
+    std::vector<uint64_t> hoff(P.nb);
+    uint64_t total = 0;
+    for (int b = 0; b < P.nb; ++b) {
+      hL[b] = rhg::cell_bits(hb[b + 1] - hb[b]);
+      hoff[b] = total;
+      total += (1ull << hL[b]) + 1;
+    }
+    DevBuf dL(4 * P.nb, s, C->pool), doff(8 * P.nb, s, C->pool), cells(8 * total, s, C->pool);
+    CCG_CUDA(cudaMemcpyAsync(dL.p, hL.data(), 4 * P.nb, cudaMemcpyHostToDevice, s));
+    CCG_CUDA(cudaMemcpyAsync(doff.p, hoff.data(), 8 * P.nb, cudaMemcpyHostToDevice, s));
+    const ccg::RhgBands B{bl.as<uint32_t>(), bstart.as<uint64_t>(), cells.as<uint64_t>(),
+                          doff.as<uint64_t>(), dL.as<int>()};
+    ccg::k_rhg_cells<<<ccg::grid_for(total, ccg::kBlock, ccg::num_sms() * 16), ccg::kBlock, 0, s>>>(
+        B, pt, P.nb, total, cells.as<uint64_t>());
+    CCG_LAUNCH_CHECK();
+    keys.release();
+    tmp.release();
+    bkeys.release();
+    // degrees, offsets, then every row's keys at its offsets
+    DevBuf deg(4 * n, s, C->pool);
+    ccg::k_rhg_neighbours<<<grid, ccg::kBlock, 0, s>>>(P, pt, B, deg.as<uint32_t>(), nullptr, nullptr);
+    CCG_LAUNCH_CHECK();
+    uint64_t m = 0;
+    ccg::offsets_from_counts(deg.as<uint32_t>(), n, 0, row_ptr, s, C->pool, c);
+    CCG_CUDA(cudaMemcpyAsync(&m, row_ptr + n, 8, cudaMemcpyDeviceToHost, s));
+    CCG_CUDA(cudaStreamSynchronize(s));
+    *m_dir = m;
+    if (m >= (1ull << 32)) throw Error(CC_ERR_UNSUPPORTED, "2^32 directed entries or more");
+    if (m > cap) throw Error(CC_ERR_INVALID, "col capacity below the generated entries");
+    if (m == 0) return;
+    DevBuf ek(8 * m, s, C->pool), et(8 * m, s, C->pool);
+    ccg::k_rhg_neighbours<<<grid, ccg::kBlock, 0, s>>>(P, pt, B, nullptr, row_ptr, ek.as<uint64_t>());
+    CCG_LAUNCH_CHECK();
+    // rows sorted: one sort of the (source, target) keys keeps every row in place
+    const uint64_t *sorted = ccg::radix_sort_u64(ek.as<uint64_t>(), et.as<uint64_t>(), m,
+                                                 2 * P.idbits, s, C->pool, c);
+    const unsigned egrid = ccg::grid_for(m, ccg::kBlock, ccg::num_sms() * 16);
+    if (id_bytes == 8)
+      ccg::k_keys_low<uint64_t><<<egrid, ccg::kBlock, 0, s>>>(sorted, m, P.idbits, static_cast<uint64_t *>(col));
+    else
+      ccg::k_keys_low<uint32_t><<<egrid, ccg::kBlock, 0, s>>>(sorted, m, P.idbits, static_cast<uint32_t *>(col));
     CCG_LAUNCH_CHECK();
     CCG_CUDA(cudaStreamSynchronize(s));
   });

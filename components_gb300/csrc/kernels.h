@@ -57,6 +57,7 @@ struct HostSource {
   void *labels_out = nullptr;  // host uint32 labels: each chunk is copied out on `copy`
                                // as soon as the final compression has finished it
   HostStager *stager = nullptr;  // when set: rows below 255 entries go as degree bytes
+  bool sampled = false;  // sampled linking (tiled link rounds) instead of the tiled pass
   mutable uint64_t h2d_bytes = 0;  // bytes the streamed pass copied to the device
 };
 void uf_components(const Csr &g, uint32_t *parent, const PartMap *pm,
@@ -95,6 +96,9 @@ void unique_sorted_keys(const uint64_t *sorted, uint64_t n, uint64_t *out, uint3
 // must stay below 2^32).
 void offsets_from_degrees(const uint8_t *deg, uint64_t count, uint64_t base, uint64_t *rp,
                           cudaStream_t s, cudaMemPool_t pool, Counters &c);
+// The same from uint32 counts (the sum of one call must stay below 2^32).
+void offsets_from_counts(const uint32_t *deg, uint64_t count, uint64_t base, uint64_t *rp,
+                         cudaStream_t s, cudaMemPool_t pool, Counters &c);
 uint64_t *radix_sort_u64(uint64_t *keys, uint64_t *tmp, uint64_t n, int bits,
                          cudaStream_t s, cudaMemPool_t pool, Counters &c);
 

@@ -40,11 +40,10 @@
 #endif
 
 #include <math.h>
-#if !defined(__CUDA_ARCH__)
+
 #include <cmath>
 #include <cstring>
 #include <vector>
-#endif
 
 #include "../../include/cc_gpu.h"
 
@@ -280,8 +279,7 @@ RHG_HD uint64_t cell_of(uint64_t phi, int L) { return L == 0 ? 0 : phi >> (64 - 
 
 }  // namespace rhg
 
-// ---- per-graph constants (host only) -------------------------------------------
-#if !defined(__CUDA_ARCH__)
+// ---- per-graph constants (host functions) --------------------------------------
 namespace rhg {
 
 // Expected average degree for radius R: (n - 1) * E[theta_max / pi], the
@@ -354,4 +352,3 @@ inline int make_params(uint64_t n, double avg_deg, double gamma, uint64_t seed, 
 }
 
 }  // namespace rhg
-#endif

@@ -546,6 +546,10 @@ struct GetDeg {
   const uint8_t *d;
   __device__ uint32_t operator()(uint64_t i) const { return d[i]; }
 };
+struct GetCount {
+  const uint32_t *d;
+  __device__ uint32_t operator()(uint64_t i) const { return d[i]; }
+};
 struct PutOffset {
   uint64_t *rp;
   uint64_t base;
@@ -588,6 +592,12 @@ void offsets_from_degrees(const uint8_t *deg, uint64_t count, uint64_t base, uin
                           cudaStream_t s, cudaMemPool_t pool, Counters &c) {
   if (count == 0) return;
   scan_generic(count, GetDeg{deg}, PutOffset{rp, base}, nullptr, s, pool, c);
+}
+
+void offsets_from_counts(const uint32_t *deg, uint64_t count, uint64_t base, uint64_t *rp,
+                         cudaStream_t s, cudaMemPool_t pool, Counters &c) {
+  if (count == 0) return;
+  scan_generic(count, GetCount{deg}, PutOffset{rp, base}, nullptr, s, pool, c);
 }
 
 uint64_t *radix_sort_u64(uint64_t *keys, uint64_t *tmp, uint64_t n, int bits, cudaStream_t s,

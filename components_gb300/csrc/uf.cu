@@ -1039,6 +1039,62 @@ TileShape tile_shape_uncached(uint64_t n, const UfTuning &tu) {
   return t;
 }
 
+// Final compression when the labels go to the caller's host uint32 array:
+// compress in chunks and copy each chunk out on the copy stream as soon as it
+// is final (a chunk's entries are written only by its own launch), so the
+// device-to-host copy overlaps the later chunks.  All launches are queued
+// first: a copy into pageable memory blocks the host.
+void compress_copy_out(uint64_t n, uint32_t *parent, const HostSource *hs, cudaStream_t s,
+                       Counters &c) {
+  constexpr int kOutChunks = 8;
+  const uint64_t step = ((n + kOutChunks - 1) / kOutChunks + 1023) / 1024 * 1024;
+  cudaEvent_t done[kOutChunks];
+  int nch = 0;
+  cudaEvent_t t3 = c.tic(s);
+  for (uint64_t a = 0; a < n; a += step, ++nch) {
+    const uint64_t b = std::min<uint64_t>(n, a + step);
+    k_compress<<<grid_for(b - a, kBlock, num_sms() * 32), kBlock, 0, s>>>(b, parent, a);
+    CCG_LAUNCH_CHECK();
+    CCG_CUDA(cudaEventCreateWithFlags(&done[nch], cudaEventDisableTiming));
+    CCG_CUDA(cudaEventRecord(done[nch], s));
+  }
+  c.toc(s, "uf_compress", t3, 3 * n * 4);
+  for (int k = 0; k < nch; ++k) {
+    const uint64_t a = (uint64_t)k * step, b = std::min<uint64_t>(n, a + step);
+    CCG_CUDA(cudaStreamWaitEvent(hs->copy, done[k], 0));
+    CCG_CUDA(cudaMemcpyAsync(static_cast<uint32_t *>(hs->labels_out) + a, parent + a, 4 * (b - a),
+                             cudaMemcpyDeviceToHost, hs->copy));
+    cudaEventDestroy(done[k]);
+  }
+  cudaEvent_t copied;  // the caller's stream ends after the last copy
+  CCG_CUDA(cudaEventCreateWithFlags(&copied, cudaEventDisableTiming));
+  CCG_CUDA(cudaEventRecord(copied, hs->copy));
+  CCG_CUDA(cudaStreamWaitEvent(s, copied, 0));
+  cudaEventDestroy(copied);
+  c.add(nch - 1, 0);
+}
+
+// Copy rows [v0, v1) of the caller's host CSR (their offsets v0 .. v1 and
+// their ids) into the device buffers of g on the copy stream, and make s wait
+// for them.
+template <class T>
+void copy_rows_in(const Csr &g, const HostSource *hs, uint64_t v0, uint64_t v1, cudaStream_t s) {
+  const uint64_t e0 = hs->rp[v0], e1 = hs->rp[v1];
+  if (e1 < e0 || e1 > g.m) throw Error(CC_ERR_INVALID, "CSR offsets are not monotone or exceed m_dir");
+  CCG_CUDA(cudaMemcpyAsync(const_cast<uint64_t *>(g.rp) + v0, hs->rp + v0, 8 * (v1 - v0 + 1),
+                           cudaMemcpyHostToDevice, hs->copy));
+  if (e1 > e0)
+    CCG_CUDA(cudaMemcpyAsync(const_cast<T *>(static_cast<const T *>(g.col)) + e0,
+                             static_cast<const T *>(hs->col) + e0, sizeof(T) * (e1 - e0),
+                             cudaMemcpyHostToDevice, hs->copy));
+  hs->h2d_bytes += 8 * (v1 - v0 + 1) + sizeof(T) * (e1 - e0);
+  cudaEvent_t ev;
+  CCG_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+  CCG_CUDA(cudaEventRecord(ev, hs->copy));
+  CCG_CUDA(cudaStreamWaitEvent(s, ev, 0));
+  cudaEventDestroy(ev);
+}
+
 template <class T, bool PART>
 void run_uf_tiled(const Csr &g, uint32_t *parent, const PartMap &pm, const UfTuning &tu,
                   cudaStream_t s, cudaMemPool_t pool, Counters &c, const HostSource *hs) {
@@ -1148,38 +1204,10 @@ void run_uf_tiled(const Csr &g, uint32_t *parent, const PartMap &pm, const UfTun
   c.toc(s, "uf_hook_hubs", t2, 0);
   // every vertex points at a tile-local root or at a final root: full
   // compression, writing only the entries that change
-  cudaEvent_t t3 = c.tic(s);
   if (hs && hs->labels_out) {
-    // host labels: compress in chunks and copy each chunk out on the copy
-    // stream as soon as it is final (a chunk's entries are written only by its
-    // own launch), so the device-to-host copy overlaps the later chunks.  All
-    // launches are queued first: a copy into pageable memory blocks the host.
-    constexpr int kOutChunks = 8;
-    const uint64_t step = ((g.n + kOutChunks - 1) / kOutChunks + 1023) / 1024 * 1024;
-    cudaEvent_t done[kOutChunks];
-    int nch = 0;
-    for (uint64_t a = 0; a < g.n; a += step, ++nch) {
-      const uint64_t b = std::min<uint64_t>(g.n, a + step);
-      k_compress<<<grid_for(b - a, kBlock, num_sms() * 32), kBlock, 0, s>>>(b, parent, a);
-      CCG_LAUNCH_CHECK();
-      CCG_CUDA(cudaEventCreateWithFlags(&done[nch], cudaEventDisableTiming));
-      CCG_CUDA(cudaEventRecord(done[nch], s));
-    }
-    c.toc(s, "uf_compress", t3, 3 * g.n * 4);
-    for (int k = 0; k < nch; ++k) {
-      const uint64_t a = (uint64_t)k * step, b = std::min<uint64_t>(g.n, a + step);
-      CCG_CUDA(cudaStreamWaitEvent(hs->copy, done[k], 0));
-      CCG_CUDA(cudaMemcpyAsync(static_cast<uint32_t *>(hs->labels_out) + a, parent + a,
-                               4 * (b - a), cudaMemcpyDeviceToHost, hs->copy));
-      cudaEventDestroy(done[k]);
-    }
-    cudaEvent_t copied;  // the caller's stream ends after the last copy
-    CCG_CUDA(cudaEventCreateWithFlags(&copied, cudaEventDisableTiming));
-    CCG_CUDA(cudaEventRecord(copied, hs->copy));
-    CCG_CUDA(cudaStreamWaitEvent(s, copied, 0));
-    cudaEventDestroy(copied);
-    c.add(nch - 1, 0);
+    compress_copy_out(g.n, parent, hs, s, c);
   } else {
+    cudaEvent_t t3 = c.tic(s);
     k_compress<<<grid_for(g.n, kBlock, num_sms() * 32), kBlock, 0, s>>>(g.n, parent);
     CCG_LAUNCH_CHECK();
     c.toc(s, "uf_compress", t3, 3 * g.n * 4);
@@ -1223,7 +1251,8 @@ Shares sample_shares(const Csr &g, const PartMap &pm, uint32_t tile, uint32_t hu
 
 template <class T, bool PART>
 void run_uf_afforest(const Csr &g, uint32_t *parent, const PartMap &pm, const UfTuning &tu,
-                     bool link_tiles, cudaStream_t s, cudaMemPool_t pool, Counters &c) {
+                     bool link_tiles, cudaStream_t s, cudaMemPool_t pool, Counters &c,
+                     const HostSource *hs = nullptr) {
   const T *col = static_cast<const T *>(g.col);
   const uint64_t si = (uint64_t)g.idb;
   const uint32_t hub_degree = tu.hub_degree;
@@ -1241,11 +1270,29 @@ void run_uf_afforest(const Csr &g, uint32_t *parent, const PartMap &pm, const Uf
     // offsets, the link-round ids, own parent
     link_bytes = 8 * (g.n + 1) + kAffRounds * g.n * si + 4 * g.n;
     cudaEvent_t t0 = c.tic(s);
-    k_tile3<T, PART, uint16_t, (int)kAffRounds><<<ts.grid, ts.threads, ts.smem, s>>>(
-        g.n, g.m, 0, g.n, g.rp, col, parent, pm, ts.tile, ts.stage, hub_degree, none,
-        cut.as<uint2>(), cut_cap, cnt.as<unsigned long long>(), g.err);
-    CCG_LAUNCH_CHECK();
-    c.toc(s, "uf_sample_link_tiled", t0, link_bytes);
+    if (!hs) {
+      k_tile3<T, PART, uint16_t, (int)kAffRounds><<<ts.grid, ts.threads, ts.smem, s>>>(
+          g.n, g.m, 0, g.n, g.rp, col, parent, pm, ts.tile, ts.stage, hub_degree, none,
+          cut.as<uint2>(), cut_cap, cnt.as<unsigned long long>(), g.err);
+      CCG_LAUNCH_CHECK();
+    } else {
+      // host input: tile-aligned chunks of rows cross the host link on the
+      // copy stream, and each chunk's tiles are linked as soon as it has
+      // landed, so the link pass runs under the transfer.  Link edges may
+      // lead to later tiles, so every cut edge waits for the cut union after
+      // the last chunk (a tile writes its vertices' parents when it ends).
+      const uint64_t chunk = (uint64_t)ts.grid * ts.tile;  // one full wave of CTAs
+      for (uint64_t v0 = 0; v0 < g.n; v0 += chunk) {
+        const uint64_t v1 = std::min<uint64_t>(g.n, v0 + chunk);
+        copy_rows_in<T>(g, hs, v0, v1, s);
+        const unsigned cgrid = (unsigned)std::min<uint64_t>((v1 - v0 + ts.tile - 1) / ts.tile, ts.grid);
+        k_tile3<T, PART, uint16_t, (int)kAffRounds><<<cgrid, ts.threads, ts.smem, s>>>(
+            g.n, g.m, v0, v1, g.rp, col, parent, pm, ts.tile, ts.stage, hub_degree, none,
+            cut.as<uint2>(), cut_cap, cnt.as<unsigned long long>(), g.err);
+        CCG_LAUNCH_CHECK();
+      }
+    }
+    c.toc(s, hs ? "uf_sample_link_streamed" : "uf_sample_link_tiled", t0, link_bytes);
     cudaEvent_t t1 = c.tic(s);
     k_cut_union<<<num_sms() * 16, kBlock, 0, s>>>(cut.as<uint2>(), cnt.as<unsigned long long>(),
                                              cut_cap, parent);
@@ -1311,10 +1358,14 @@ void run_uf_afforest(const Csr &g, uint32_t *parent, const PartMap &pm, const Uf
                                                            g.err);
   CCG_LAUNCH_CHECK();
   c.toc(s, "uf_sample_hubs", th, 0);
-  cudaEvent_t t2 = c.tic(s);
-  k_compress<<<grid_for(g.n, kBlock, num_sms() * 32), kBlock, 0, s>>>(g.n, parent);
-  CCG_LAUNCH_CHECK();
-  c.toc(s, "uf_compress", t2, 3 * g.n * 4);
+  if (hs && hs->labels_out) {
+    compress_copy_out(g.n, parent, hs, s, c);
+  } else {
+    cudaEvent_t t2 = c.tic(s);
+    k_compress<<<grid_for(g.n, kBlock, num_sms() * 32), kBlock, 0, s>>>(g.n, parent);
+    CCG_LAUNCH_CHECK();
+    c.toc(s, "uf_compress", t2, 3 * g.n * 4);
+  }
   c.add((link_tiles ? 2 : 1 + kAffRounds) + 6, link_bytes + rest_bytes + 6 * g.n * 4);
 }
 
@@ -1325,8 +1376,10 @@ constexpr uint64_t kL2Resident = 96ull << 20;
 template <class T, bool PART>
 void run_uf_mode(const Csr &g, uint32_t *parent, const PartMap &pm, const UfTuning &tu,
                  cudaStream_t s, cudaMemPool_t pool, Counters &c, const HostSource *hs) {
-  if (hs) {  // the caller decided on the host that the tiled pass fits this graph
-    run_uf_tiled<T, PART>(g, parent, pm, tu, s, pool, c, hs);
+  if (hs) {  // the caller decided on the host: the tiled pass, or sampled linking
+    // with tiled link rounds, both streamed under the host-to-device copy
+    if (hs->sampled) run_uf_afforest<T, PART>(g, parent, pm, tu, true, s, pool, c, hs);
+    else run_uf_tiled<T, PART>(g, parent, pm, tu, s, pool, c, hs);
     return;
   }
   int mode = tu.mode;

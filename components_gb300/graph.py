@@ -209,10 +209,19 @@ def gen_grid(X: int, Y: int, p: float = 0.5, seed: int = 1, id_bytes: int = 4,
 def _device_graph(fill, n: int, cap: int, id_bytes: int, device, num_parts: int) -> StaticGraph:
     import torch
     rp = torch.empty(n + 1, dtype=torch.int64, device=device)
-    col = torch.empty(max(cap, 1), dtype=torch.int32 if id_bytes == 4 else torch.int64, device=device)
+    dt = torch.int32 if id_bytes == 4 else torch.int64
+    col = torch.empty(max(cap, 1), dtype=dt, device=device)
     m = C.c_uint64()
     with torch.cuda.device(rp.device):
-        _lib.check(fill(rp.data_ptr(), col.data_ptr(), cap, C.byref(m)))
+        st = fill(rp.data_ptr(), col.data_ptr(), cap, C.byref(m))
+        if st == _lib.CC_ERR_INVALID and m.value > cap:  # an estimated capacity fell short
+            del col
+            cap = m.value
+            col = torch.empty(max(cap, 1), dtype=dt, device=device)
+            st = fill(rp.data_ptr(), col.data_ptr(), cap, C.byref(m))
+        _lib.check(st)
+    if m.value == cap:
+        return StaticGraph(rp, col[: max(cap, 0)], num_parts)
     return StaticGraph(rp, col[: m.value].clone(), num_parts)  # exact-size storage
 
 
@@ -229,6 +238,14 @@ def gen_gnm_device(n: int, m: int, seed: int = 1, id_bytes: int = 8, num_parts: 
     """gen_gnm built on the device (the same graph, torch CUDA tensors)."""
     return _device_graph(lambda rp, col, cap, mm: _lib.gpu().cc_gen_gnm_device(
         None, n, m, seed, id_bytes, rp, col, cap, mm), n, 2 * m, id_bytes, device, num_parts)
+
+
+def gen_rhg_device(n: int, avg_deg: float = 16.0, gamma: float = 2.6, seed: int = 1,
+                   id_bytes: int = 4, num_parts: int = 1, device="cuda") -> StaticGraph:
+    """gen_rhg built on the device (the same graph bit for bit, torch CUDA tensors)."""
+    cap = int(1.25 * n * avg_deg) + 4096
+    return _device_graph(lambda rp, col, cp, m: _lib.gpu().cc_gen_rhg_device(
+        None, n, avg_deg, gamma, seed, id_bytes, rp, col, cp, m), n, cap, id_bytes, device, num_parts)
 
 
 def gen_rhg(n: int, avg_deg: float = 16.0, gamma: float = 2.6, seed: int = 1, id_bytes: int = 4,

@@ -232,6 +232,16 @@ int cc_gen_grid_device(cc_ctx *ctx, uint64_t X, uint64_t Y, double p, uint64_t s
                        uint64_t *row_ptr, void *col, uint64_t cap, uint64_t *m_dir);
 int cc_gen_gnm_device(cc_ctx *ctx, uint64_t n, uint64_t m, uint64_t seed, uint32_t id_bytes,
                       uint64_t *row_ptr, void *col, uint64_t cap, uint64_t *m_dir);
+/* The random hyperbolic graph of cc_gen_rhg (cc_gen.h), built on the device:
+   the same CSR bit for bit (the model's per-point values and edge test are
+   evaluated with the same correctly rounded operations on host and device).
+   Stand-in for KaGen's rhg generator (lib/io/io_utils.h:72-73).  row_ptr:
+   n+1 device words; col: cap device ids; *m_dir receives the number of
+   directed entries (also when it exceeds cap, which gives CC_ERR_INVALID).
+   Needs about 60 bytes of device scratch per vertex plus 16 per entry. */
+int cc_gen_rhg_device(cc_ctx *ctx, uint64_t n, double avg_deg, double gamma, uint64_t seed,
+                      uint32_t id_bytes, uint64_t *row_ptr, void *col, uint64_t cap,
+                      uint64_t *m_dir);
 
 int cc_ctx_stats(cc_ctx *ctx, cc_stats *out);
 /* Device bytes the context holds in its arena (grows on demand, reused). */

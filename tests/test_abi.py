@@ -117,6 +117,11 @@ def test_size_limits_are_reported_before_any_device_call():
         _lib.CC_ERR_UNSUPPORTED
     assert lib.cc_gen_grid_device(None, 1 << 15, 1 << 15, 0.5, 1, 4, 0x1000, 0x2000, 1, C.byref(m)) == \
         _lib.CC_ERR_UNSUPPORTED
+    # bad model parameters are refused before any device call
+    assert lib.cc_gen_rhg_device(None, 1 << 32, 16.0, 2.6, 1, 4, 0x1000, 0x2000, 1, C.byref(m)) == \
+        _lib.CC_ERR_INVALID
+    assert lib.cc_gen_rhg_device(None, 1 << 10, 16.0, 1.9, 1, 4, 0x1000, 0x2000, 1, C.byref(m)) == \
+        _lib.CC_ERR_INVALID
 
 
 def test_host_validation():

@@ -209,3 +209,17 @@ def test_device_generators_equal_host_generators(cuda):
     G = cc.gen_grid_device(700, 500, 0.5, seed=6)
     lab = cc.find_components(G, "exp")
     assert np.array_equal(lab.cpu().numpy().view(np.uint32).astype(np.uint64), oracle.uf_labels(G))
+
+
+@pytest.mark.parametrize("n,d,gamma,seed,idb", [(1 << 12, 16.0, 2.6, 1, 4), (3000, 4.0, 2.2, 2, 8),
+                                               (1 << 16, 8.0, 3.0, 5, 4), (1 << 20, 16.0, 2.6, 1, 4),
+                                               (100, 32.0, 2.4, 9, 4)])
+def test_device_rhg_equals_host_rhg(cuda, n, d, gamma, seed, idb):
+    """cc_gen_rhg_device builds the host generator's hyperbolic graph bit for
+    bit: the model's values and edge test are correctly rounded operations on
+    both sides."""
+    H = cc.gen_rhg(n, d, gamma, seed=seed, id_bytes=idb)
+    D = cc.gen_rhg_device(n, d, gamma, seed=seed, id_bytes=idb)
+    rp, col = D.numpy()
+    assert np.array_equal(rp, np.asarray(H.row_ptr, np.uint64))
+    assert np.array_equal(col, np.asarray(H.col).astype(np.uint64))

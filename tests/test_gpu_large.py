@@ -78,6 +78,16 @@ def rhg26():
     return G, oracle.uf_labels(G)
 
 
+def test_rhg_2_26_device_generator(cuda, rhg26):
+    """The GPU arm of the benchmark builds the headline graph on the device;
+    it is the host generator's graph (the one the CPU arm solves) bit for bit."""
+    G, _ = rhg26
+    D = cc.gen_rhg_device(1 << 26, 16.0, 2.6, seed=1, id_bytes=4)
+    assert D.m == G.m
+    assert np.array_equal(D.row_ptr.cpu().numpy().view(np.uint64), np.asarray(G.row_ptr))
+    assert np.array_equal(D.col.cpu().numpy().view(np.uint32), np.asarray(G.col))
+
+
 def test_rhg_2_26_full_size(cuda, rhg26):
     """Labels of the headline graph equal the union-find's for exp_contraction
     with one rank and with 16 virtual ranks, and for all_reduce."""

@@ -105,16 +105,17 @@ def test_reference_arm_loads_no_library_of_ours():
 
 
 def test_both_arms_build_the_same_graph_and_config():
-    """Workload.ours() (libccgen) and Workload.oracle() (the oracle's linked
-    copy of the generators) give the same CSR, so both arms print the same
-    config dict."""
+    """Workload.ours_host() (libccgen) and Workload.oracle() (the oracle's
+    linked copy of the generators) give the same CSR, so both arms print the
+    same config dict (the GPU arm's device generators give that CSR too: a
+    GPU test checks them against the host generators)."""
     import numpy as np
     sys.path.insert(0, str(ROOT))
     import bench
     for wl_name, extra in (("rhg", ["--rhg-log2n", "13"]), ("grid", ["--grid", "96"])):
         args = bench.parse_args(["--workload", wl_name, *extra])
         wl = bench.Workload(wl_name, args)
-        a, b = wl.ours(), wl.oracle()
+        a, b = wl.ours_host(), wl.oracle()
         ra, ca = a.numpy()
         rb, cb = b.numpy()
         assert np.array_equal(ra, rb) and np.array_equal(ca, cb)
