@@ -492,7 +492,7 @@ int ctx_run(cc_ctx *C, const cc_csr *g, cc_algo algo, const cc_config *cfg_in, u
         hsrc.sampled = !dc.tiles;
       }
     }
-    if (streamed && !hsrc.sampled) {  // degree bytes: the tiled pass's offsets only
+    if (streamed) {  // host threads encode the offsets as degree bytes
       if (!C->stager) C->stager.reset(new ccg::HostStager());
       hsrc.stager = C->stager.get();
     }

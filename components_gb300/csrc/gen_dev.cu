@@ -150,22 +150,29 @@ __global__ void k_rhg_band_starts(const uint64_t *__restrict__ bkeys, uint64_t n
   for (uint64_t i = t; i < n; i += (uint64_t)gridDim.x * blockDim.x) bl[i] = (uint32_t)bkeys[i];
 }
 
-// cell starts: entry j of band b = first vertex of the band whose cell is >= j
-__global__ void k_rhg_cells(RhgBands B, RhgPts pt, int nb, uint64_t total,
-                            uint64_t *__restrict__ cell) {
-  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < total;
-       i += (uint64_t)gridDim.x * blockDim.x) {
-    int b = 0;
-    while (b + 1 < nb && B.cell_off[b + 1] <= i) ++b;
-    const uint64_t j = i - B.cell_off[b];
+// Cell starts: entry j of band b = the first position of the band whose cell
+// is >= j.  Inside a band the vertices are in increasing angle, so the cells
+// are non-decreasing along the band: position k writes the entries of the
+// cells from just after its predecessor's cell up to its own (and the last
+// position of a band those after its own).  gk: the sorted (band << 32) | v
+// keys; threads t < nb fill empty bands.
+__global__ void k_rhg_cells(RhgBands B, RhgPts pt, const uint64_t *__restrict__ gk, uint64_t n,
+                            int nb, uint64_t *__restrict__ cell) {
+  const uint64_t t0 = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+  if (t0 < (uint64_t)nb && B.band_start[t0] == B.band_start[t0 + 1]) {
+    const uint64_t cnt = (1ull << B.L[t0]) + 1;
+    for (uint64_t j = 0; j < cnt; ++j) cell[B.cell_off[t0] + j] = B.band_start[t0];
+  }
+  for (uint64_t k = t0; k < n; k += (uint64_t)gridDim.x * blockDim.x) {
+    const int b = (int)(gk[k] >> 32);
     const int L = B.L[b];
-    uint64_t lo = B.band_start[b], hi = B.band_start[b + 1];
-    while (lo < hi) {
-      const uint64_t mid = (lo + hi) >> 1;
-      if (rhg::cell_of(pt.phi[B.bl[mid]], L) < j) lo = mid + 1;
-      else hi = mid;
-    }
-    cell[i] = lo;
+    uint64_t *c = cell + B.cell_off[b];
+    const uint64_t ck = rhg::cell_of(pt.phi[(uint32_t)gk[k]], L);
+    const bool first = k == B.band_start[b], last = k + 1 == B.band_start[b + 1];
+    const uint64_t from = first ? 0 : rhg::cell_of(pt.phi[(uint32_t)gk[k - 1]], L) + 1;
+    for (uint64_t j = from; j <= ck; ++j) c[j] = k;
+    if (last)
+      for (uint64_t j = ck + 1; j <= (1ull << L); ++j) c[j] = k + 1;
   }
 }
 
@@ -372,8 +379,7 @@ int cc_gen_rhg_device(cc_ctx *ctx, uint64_t n, double avg_deg, double gamma, uin
     CCG_CUDA(cudaMemcpyAsync(doff.p, hoff.data(), 8 * P.nb, cudaMemcpyHostToDevice, s));
     const ccg::RhgBands B{bl.as<uint32_t>(), bstart.as<uint64_t>(), cells.as<uint64_t>(),
                           doff.as<uint64_t>(), dL.as<int>()};
-    ccg::k_rhg_cells<<<ccg::grid_for(total, ccg::kBlock, ccg::num_sms() * 16), ccg::kBlock, 0, s>>>(
-        B, pt, P.nb, total, cells.as<uint64_t>());
+    ccg::k_rhg_cells<<<grid, ccg::kBlock, 0, s>>>(B, pt, gk, n, P.nb, cells.as<uint64_t>());
     CCG_LAUNCH_CHECK();
     keys.release();
     tmp.release();

@@ -96,6 +96,12 @@ void unique_sorted_keys(const uint64_t *sorted, uint64_t n, uint64_t *out, uint3
 // must stay below 2^32).
 void offsets_from_degrees(const uint8_t *deg, uint64_t count, uint64_t base, uint64_t *rp,
                           cudaStream_t s, cudaMemPool_t pool, Counters &c);
+// The same with escapes: a degree byte of 255 stands for the exact degree of
+// that row, found in esc (nesc (row, degree) pairs sorted by row; rows are
+// absolute: first_row + i for entry i).
+void offsets_from_degrees_esc(const uint8_t *deg, uint64_t count, uint64_t first_row, uint64_t base,
+                              const uint2 *esc, uint32_t nesc, uint64_t *rp, cudaStream_t s,
+                              cudaMemPool_t pool, Counters &c);
 // The same from uint32 counts (the sum of one call must stay below 2^32).
 void offsets_from_counts(const uint32_t *deg, uint64_t count, uint64_t base, uint64_t *rp,
                          cudaStream_t s, cudaMemPool_t pool, Counters &c);

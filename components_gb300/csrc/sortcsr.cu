@@ -550,6 +550,26 @@ struct GetCount {
   const uint32_t *d;
   __device__ uint32_t operator()(uint64_t i) const { return d[i]; }
 };
+// Degree bytes with escapes: byte 255 stands for the exact degree held by the
+// (row, degree) pair of that row in esc (sorted by row).
+struct GetDegEsc {
+  const uint8_t *d;
+  const uint2 *esc;
+  uint32_t nesc;
+  uint32_t first_row;
+  __device__ uint32_t operator()(uint64_t i) const {
+    const uint32_t x = d[i];
+    if (x != 255) return x;
+    const uint32_t row = first_row + (uint32_t)i;
+    uint32_t lo = 0, hi = nesc;
+    while (lo < hi) {
+      const uint32_t mid = (lo + hi) >> 1;
+      if (esc[mid].x < row) lo = mid + 1;
+      else hi = mid;
+    }
+    return lo < nesc ? esc[lo].y : 0u;
+  }
+};
 struct PutOffset {
   uint64_t *rp;
   uint64_t base;
@@ -592,6 +612,14 @@ void offsets_from_degrees(const uint8_t *deg, uint64_t count, uint64_t base, uin
                           cudaStream_t s, cudaMemPool_t pool, Counters &c) {
   if (count == 0) return;
   scan_generic(count, GetDeg{deg}, PutOffset{rp, base}, nullptr, s, pool, c);
+}
+
+void offsets_from_degrees_esc(const uint8_t *deg, uint64_t count, uint64_t first_row, uint64_t base,
+                              const uint2 *esc, uint32_t nesc, uint64_t *rp, cudaStream_t s,
+                              cudaMemPool_t pool, Counters &c) {
+  if (count == 0) return;
+  scan_generic(count, GetDegEsc{deg, esc, nesc, (uint32_t)first_row}, PutOffset{rp, base}, nullptr, s,
+               pool, c);
 }
 
 void offsets_from_counts(const uint32_t *deg, uint64_t count, uint64_t base, uint64_t *rp,

@@ -1074,25 +1074,102 @@ void compress_copy_out(uint64_t n, uint32_t *parent, const HostSource *hs, cudaS
   c.add(nch - 1, 0);
 }
 
+// Staging of the row offsets of a streamed host CSR as degree bytes with
+// escapes: one byte per row, 255 for rows of 255 entries or more, whose exact
+// degrees follow as (row, degree) pairs.  Host side in page-locked memory
+// (encoded by the context's host threads while the copy engine moves the
+// previous chunk), device side in pool memory; each chunk's escapes take the
+// next slice of the escape area.
+struct DegreeStage {
+  uint8_t *hdeg = nullptr;
+  uint2 *hesc = nullptr;
+  DevBuf ddeg, desc;
+  uint64_t esc_used = 0, esc_cap = 0;
+  DegreeStage(const Csr &g, const HostSource *hs, cudaStream_t s, cudaMemPool_t pool) {
+    if (!hs->stager) return;
+    esc_cap = g.m / 255 + 2;
+    const uint64_t deg_bytes = (g.n + 15) / 16 * 16;
+    uint8_t *base = hs->stager->staging(deg_bytes + 8 * esc_cap);
+    if (!base) return;
+    hdeg = base;
+    hesc = reinterpret_cast<uint2 *>(base + deg_bytes);
+    ddeg.alloc(g.n, s, pool);
+    desc.alloc(8 * esc_cap, s, pool);
+  }
+  // Encode rows [v0, v1) (host threads); false when a degree does not fit 32
+  // bits (offsets not monotone: the kernels report them) - send offsets.
+  bool encode(const HostSource *hs, uint64_t v0, uint64_t v1, uint32_t *nesc) {
+    if (!hdeg) return false;
+    constexpr uint64_t kPart = 1 << 16;
+    const unsigned parts = (unsigned)((v1 - v0 + kPart - 1) / kPart);
+    std::vector<std::vector<uint2>> esc(parts);
+    std::atomic<int> bad{0};
+    hs->stager->pool.run(parts, [&](unsigned i) {
+      const uint64_t a = v0 + (uint64_t)i * kPart, b = std::min<uint64_t>(v1, a + kPart);
+      uint64_t prev = hs->rp[a];
+      for (uint64_t v = a; v < b; ++v) {
+        const uint64_t nx = hs->rp[v + 1], d = nx - prev;  // wraps to huge when not monotone
+        prev = nx;
+        if (d < 255) {
+          hdeg[v] = (uint8_t)d;
+        } else {
+          hdeg[v] = 255;
+          if (d >= (1ull << 32)) bad.store(1);
+          esc[i].push_back(make_uint2((uint32_t)v, (uint32_t)d));
+        }
+      }
+    });
+    if (bad.load()) return false;
+    uint64_t k = 0;
+    for (auto &e : esc) k += e.size();
+    if (esc_used + k > esc_cap) return false;
+    uint2 *dst = hesc + esc_used;
+    for (auto &e : esc)
+      for (const uint2 &x : e) *dst++ = x;
+    *nesc = (uint32_t)k;
+    return true;
+  }
+};
+
 // Copy rows [v0, v1) of the caller's host CSR (their offsets v0 .. v1 and
 // their ids) into the device buffers of g on the copy stream, and make s wait
-// for them.
+// for them.  With a degree stage, every chunk but the first sends its offsets
+// as degree bytes with escapes and the device rebuilds them (the first goes as
+// offsets, so that the copy engine starts at once).
 template <class T>
-void copy_rows_in(const Csr &g, const HostSource *hs, uint64_t v0, uint64_t v1, cudaStream_t s) {
+void copy_rows_in(const Csr &g, const HostSource *hs, uint64_t v0, uint64_t v1, cudaStream_t s,
+                  DegreeStage *ds = nullptr, cudaMemPool_t pool = nullptr, Counters *c = nullptr) {
   const uint64_t e0 = hs->rp[v0], e1 = hs->rp[v1];
   if (e1 < e0 || e1 > g.m) throw Error(CC_ERR_INVALID, "CSR offsets are not monotone or exceed m_dir");
-  CCG_CUDA(cudaMemcpyAsync(const_cast<uint64_t *>(g.rp) + v0, hs->rp + v0, 8 * (v1 - v0 + 1),
-                           cudaMemcpyHostToDevice, hs->copy));
+  uint32_t nesc = 0;
+  const uint64_t esc_at = ds ? ds->esc_used : 0;
+  const bool coded = ds && v0 > 0 && e1 - e0 < (1ull << 32) && ds->encode(hs, v0, v1, &nesc);
+  if (coded) {
+    CCG_CUDA(cudaMemcpyAsync(ds->ddeg.as<uint8_t>() + v0, ds->hdeg + v0, v1 - v0,
+                             cudaMemcpyHostToDevice, hs->copy));
+    if (nesc)
+      CCG_CUDA(cudaMemcpyAsync(ds->desc.as<uint2>() + esc_at, ds->hesc + esc_at, 8ull * nesc,
+                               cudaMemcpyHostToDevice, hs->copy));
+    ds->esc_used += nesc;
+    hs->h2d_bytes += (v1 - v0) + 8ull * nesc;
+  } else {
+    CCG_CUDA(cudaMemcpyAsync(const_cast<uint64_t *>(g.rp) + v0, hs->rp + v0, 8 * (v1 - v0 + 1),
+                             cudaMemcpyHostToDevice, hs->copy));
+    hs->h2d_bytes += 8 * (v1 - v0 + 1);
+  }
   if (e1 > e0)
     CCG_CUDA(cudaMemcpyAsync(const_cast<T *>(static_cast<const T *>(g.col)) + e0,
                              static_cast<const T *>(hs->col) + e0, sizeof(T) * (e1 - e0),
                              cudaMemcpyHostToDevice, hs->copy));
-  hs->h2d_bytes += 8 * (v1 - v0 + 1) + sizeof(T) * (e1 - e0);
+  hs->h2d_bytes += sizeof(T) * (e1 - e0);
   cudaEvent_t ev;
   CCG_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
   CCG_CUDA(cudaEventRecord(ev, hs->copy));
   CCG_CUDA(cudaStreamWaitEvent(s, ev, 0));
   cudaEventDestroy(ev);
+  if (coded)
+    offsets_from_degrees_esc(ds->ddeg.as<uint8_t>() + v0, v1 - v0, v0, e0, ds->desc.as<uint2>() + esc_at,
+                             nesc, const_cast<uint64_t *>(g.rp) + v0, s, pool, *c);
 }
 
 template <class T, bool PART>
@@ -1282,9 +1359,10 @@ void run_uf_afforest(const Csr &g, uint32_t *parent, const PartMap &pm, const Uf
       // lead to later tiles, so every cut edge waits for the cut union after
       // the last chunk (a tile writes its vertices' parents when it ends).
       const uint64_t chunk = (uint64_t)ts.grid * ts.tile;  // one full wave of CTAs
+      DegreeStage ds(g, hs, s, pool);
       for (uint64_t v0 = 0; v0 < g.n; v0 += chunk) {
         const uint64_t v1 = std::min<uint64_t>(g.n, v0 + chunk);
-        copy_rows_in<T>(g, hs, v0, v1, s);
+        copy_rows_in<T>(g, hs, v0, v1, s, &ds, pool, &c);
         const unsigned cgrid = (unsigned)std::min<uint64_t>((v1 - v0 + ts.tile - 1) / ts.tile, ts.grid);
         k_tile3<T, PART, uint16_t, (int)kAffRounds><<<cgrid, ts.threads, ts.smem, s>>>(
             g.n, g.m, v0, v1, g.rp, col, parent, pm, ts.tile, ts.stage, hub_degree, none,
