@@ -350,8 +350,11 @@ def gpu_arm(args, wl: Workload, rank: int, world: int, local: int) -> dict | Non
         solver.FindComponents(Hp, hlab)
     barrier()
     t0 = time.perf_counter()
+    step_s = []
     for _ in range(args.steps):
-        solver.FindComponents(Hp, hlab)
+        ts = time.perf_counter()
+        solver.FindComponents(Hp, hlab)  # returns once the labels are in hlab
+        step_s.append(time.perf_counter() - ts)
     barrier()
     e2e_s = (time.perf_counter() - t0) / args.steps
     e2e_st = solver.last_stats  # bytes the library moved over the host link in the last step
@@ -419,7 +422,9 @@ def gpu_arm(args, wl: Workload, rank: int, world: int, local: int) -> dict | Non
                 "h2d_note": "CSR copied from pinned host memory inside the timed call (row offsets of "
                             "rows under 255 entries may cross as one degree byte each when the "
                             "graph is streamed under the tiled pass)",
-                "ms_per_step": e2e_s * 1e3},
+                "ms_per_step": e2e_s * 1e3,
+                "ms_min_median_max": [min(step_s) * 1e3, statistics.median(step_s) * 1e3,
+                                      max(step_s) * 1e3]},
         "gpu_launches": launches,
         "roofline": roof,
         "kernel_share": share,
@@ -460,17 +465,20 @@ def workload_options(args, name):
     if name == "gnm":
         G = cc.gen_gnm(1 << 20, 1 << 22, seed=INPUT_SEED, id_bytes=8)
         desc = "G(n=2^20, m=2^22) uniform endpoints, u64 ids"
+        D = G.to_device("cuda:0")
     else:
-        G = cc.gen_rhg(1 << args.rhg_log2n, RHG_DEG, RHG_GAMMA, seed=INPUT_SEED, id_bytes=4)
+        D = cc.gen_rhg_device(1 << args.rhg_log2n, RHG_DEG, RHG_GAMMA, seed=INPUT_SEED, id_bytes=4)
+        G = cc.StaticGraph(D.row_ptr.cpu().numpy().view(np.uint64), D.col.cpu().numpy().view(np.uint32))
         desc = f"RHG n=2^{args.rhg_log2n}, d=16, gamma=2.6 (threshold model), u32 ids"
     gen_s = time.time() - t0
     want = oracle.uf_labels(G) if not args.no_check else None
-    D = G.to_device("cuda:0")
     dt = torch.int32 if G.id_bytes == 4 else torch.int64
     lab = torch.empty(G.n, dtype=dt, device="cuda:0")
     peak, _ = peaks()
-    for algo, P, seq in [("exp", 1, 1), ("exp", 16, 1), ("exp", 16, 0), ("allreduce", 1, 1),
-                         ("shortcuts", 1, 1), ("local", 1, 1)]:
+    lines = {"exp1": ("exp", 1, 1), "exp16": ("exp", 16, 1), "exp16seq0": ("exp", 16, 0),
+             "allreduce": ("allreduce", 1, 1), "shortcuts": ("shortcuts", 1, 1), "local": ("local", 1, 1)}
+    for key in args.options.split(","):
+        algo, P, seq = lines[key]
         ctx = cc.Context(0)
         solver = cc.SOLVERS[algo](cc.Config(seed=ALGO_SEED, sequential_limit=seq), 0, P, ctx)
         ms, kern, st = _timed_solves(solver, D, lab, args.steps, args.warmup, ctx)
@@ -666,6 +674,8 @@ def parse_args(argv=None):
                     help="hook schedule (cc_tuning.hook_mode: 0 auto, 1 global, 2 tiled, 3 sampled)")
     ap.add_argument("--tile", type=int, default=0, help="cc_tuning.tile_vertices (0 = default)")
     ap.add_argument("--tile-threads", type=int, default=0, help="cc_tuning.tile_threads")
+    ap.add_argument("--options", default="exp1,exp16,exp16seq0,allreduce,shortcuts,local",
+                    help="--workload gnm | rhg-options: the option lines to run, comma-separated")
     ap.add_argument("--batch-k", type=int, default=4096)
     ap.add_argument("--serve-requests", type=int, default=600)
     ap.add_argument("--serve-pool", type=int, default=24)
