@@ -48,6 +48,28 @@ void throw_on_error_word(int e) {
   if (e == kErrOverflow) throw Error(CC_ERR_INVALID, "CSR offsets disagree with m_dir");
   if (e) throw Error(CC_ERR_INVALID, "CSR check failed");
 }
+
+// Per-kernel CUDA-event times of c's records into st.kernels.
+void collect_kernel_stats(Counters &c, cc_stats &st) {
+  st.nkernels = 0;
+  for (auto &r : c.recs) {
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, r.a, r.b);
+    uint32_t k = 0;
+    for (; k < st.nkernels; ++k)
+      if (std::strncmp(st.kernels[k].name, r.name, sizeof(st.kernels[k].name)) == 0) break;
+    if (k == st.nkernels) {
+      if (st.nkernels >= CC_MAX_KSTATS) continue;
+      std::memset(&st.kernels[k], 0, sizeof(st.kernels[k]));
+      std::strncpy(st.kernels[k].name, r.name, sizeof(st.kernels[k].name) - 1);
+      st.nkernels++;
+    }
+    st.kernels[k].launches += 1;
+    st.kernels[k].ms += ms;
+    st.kernels[k].bytes += r.bytes;
+  }
+  c.clear_recs();
+}
 }  // namespace ccg
 
 namespace {
@@ -381,27 +403,6 @@ struct Solver {
   }
 };
 
-void collect_kernel_stats(Counters &c, cc_stats &st) {
-  st.nkernels = 0;
-  for (auto &r : c.recs) {
-    float ms = 0.f;
-    cudaEventElapsedTime(&ms, r.a, r.b);
-    uint32_t k = 0;
-    for (; k < st.nkernels; ++k)
-      if (std::strncmp(st.kernels[k].name, r.name, sizeof(st.kernels[k].name)) == 0) break;
-    if (k == st.nkernels) {
-      if (st.nkernels >= CC_MAX_KSTATS) continue;
-      std::memset(&st.kernels[k], 0, sizeof(st.kernels[k]));
-      std::strncpy(st.kernels[k].name, r.name, sizeof(st.kernels[k].name) - 1);
-      st.nkernels++;
-    }
-    st.kernels[k].launches += 1;
-    st.kernels[k].ms += ms;
-    st.kernels[k].bytes += r.bytes;
-  }
-  c.clear_recs();
-}
-
 // Adds one profiled solve to the context's running totals.
 void accumulate_profile(cc_ctx *C, const cc_stats &st) {
   cc_stats &t = C->prof_total;
@@ -572,7 +573,7 @@ int ctx_run(cc_ctx *C, const cc_csr *g, cc_algo algo, const cc_config *cfg_in, u
     st.bytes_algorithmic = c.bytes;
     st.kernel_launches = c.launches;
     st.num_components = ncomp;
-    collect_kernel_stats(c, st);
+    ccg::collect_kernel_stats(c, st);
     C->stats = st;
     if (C->prof) accumulate_profile(C, st);
   });

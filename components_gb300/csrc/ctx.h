@@ -50,6 +50,8 @@ std::string &last_error();
 
 // The calling thread's context on the current device (made on first use).
 cc_ctx *default_context();
+// Per-kernel CUDA-event times of c's records into st.kernels (st.nkernels reset).
+void collect_kernel_stats(Counters &c, cc_stats &st);
 
 template <class F>
 int guard(F &&f) {

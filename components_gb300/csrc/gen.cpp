@@ -220,12 +220,13 @@ void rhg_layout(const rhg::Params &P, RhgLayout &lay) {
 void rhg_neighbours(const rhg::Params &P, const RhgLayout &lay, uint64_t v,
                     std::vector<uint32_t> &out) {
   const rhg::Point &pv = lay.pt[v];
+  const double inv_s = pv.s > 0.0 ? 1.0 / pv.s : 0.0;
   for (int b = 0; b < P.nb; ++b) {
     const std::vector<uint32_t> &bp = lay.band[b];
     if (bp.empty()) continue;
     uint64_t half = 0;
     const int L = lay.L[b];
-    const bool win = L > 0 && rhg::window(P, pv, b, &half);
+    const bool win = L > 0 && rhg::window(P, pv, b, inv_s, &half);
     auto scan = [&](uint64_t k0, uint64_t k1) {
       for (uint64_t k = k0; k < k1; ++k) {
         const uint32_t w = bp[k];

@@ -5,6 +5,7 @@
 // the KaGen generators of the reference drivers (lib/io/io_utils.h:59-83).
 #include <algorithm>
 #include <cmath>
+#include <cstring>
 
 #include "../../include/cc_gpu.h"
 #include "ctx.h"
@@ -184,13 +185,14 @@ __global__ void k_rhg_neighbours(rhg::Params P, RhgPts pt, RhgBands B, uint32_t 
   for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < P.n;
        v += (uint64_t)gridDim.x * blockDim.x) {
     const rhg::Point pv = pt.get(v);
+    const double inv_s = pv.s > 0.0 ? 1.0 / pv.s : 0.0;
     uint64_t cnt = 0, e = out ? rp[v] : 0;
     for (int b = 0; b < P.nb; ++b) {
       const uint64_t bs = B.band_start[b], be = B.band_start[b + 1];
       if (bs == be) continue;
       const int L = B.L[b];
       uint64_t half = 0;
-      const bool win = L > 0 && rhg::window(P, pv, b, &half);
+      const bool win = L > 0 && rhg::window(P, pv, b, inv_s, &half);
       uint64_t r0a, r0b, r1a = 0, r1b = 0;  // one or two ranges of positions in bl
       if (!win) {
         r0a = bs;
@@ -340,9 +342,12 @@ int cc_gen_rhg_device(cc_ctx *ctx, uint64_t n, double avg_deg, double gamma, uin
     cc_ctx *C = ctx ? ctx : ccg::default_context();
     CCG_CUDA(cudaSetDevice(C->device));
     cudaStream_t s = C->stream;
-    ccg::Counters c;
+    ccg::Counters c;  // with the context's profiling on, every phase is timed (cc_ctx_stats)
+    c.prof = C->prof;
+    c.pool = &C->ev_pool;
     const unsigned grid = ccg::grid_for(n, ccg::kBlock, ccg::num_sms() * 16);
     // points in angular order
+    cudaEvent_t t0 = c.tic(s);
     DevBuf keys(8 * n, s, C->pool), tmp(8 * n, s, C->pool);
     ccg::k_rhg_keys<<<grid, ccg::kBlock, 0, s>>>(P, keys.as<uint64_t>());
     CCG_LAUNCH_CHECK();
@@ -351,8 +356,12 @@ int cc_gen_rhg_device(cc_ctx *ctx, uint64_t n, double avg_deg, double gamma, uin
         py(8 * n, s, C->pool), pphi(8 * n, s, C->pool), pband(4 * n, s, C->pool), bkeys(8 * n, s, C->pool);
     const ccg::RhgPts pt{pa.as<double>(), pb.as<double>(), ps.as<double>(), px.as<double>(),
                          py.as<double>(), pphi.as<uint64_t>(), pband.as<uint32_t>()};
+    c.toc(s, "gen_angle_sort", t0, 0);
+    t0 = c.tic(s);
     ccg::k_rhg_points<<<grid, ccg::kBlock, 0, s>>>(P, sk, pt, bkeys.as<uint64_t>());
     CCG_LAUNCH_CHECK();
+    c.toc(s, "gen_points", t0, 0);
+    t0 = c.tic(s);
     // vertices grouped by band, increasing id inside a band
     uint64_t *bsort = (sk == keys.as<uint64_t>()) ? tmp.as<uint64_t>() : keys.as<uint64_t>();
     int bbits = 32;
@@ -362,6 +371,7 @@ int cc_gen_rhg_device(cc_ctx *ctx, uint64_t n, double avg_deg, double gamma, uin
     ccg::k_rhg_band_starts<<<grid, ccg::kBlock, 0, s>>>(gk, n, P.nb, bstart.as<uint64_t>(),
                                                         bl.as<uint32_t>());
     CCG_LAUNCH_CHECK();
+    c.toc(s, "gen_bands", t0, 0);
     std::vector<uint64_t> hb(P.nb + 1);
     CCG_CUDA(cudaMemcpyAsync(hb.data(), bstart.p, 8 * (P.nb + 1), cudaMemcpyDeviceToHost, s));
     CCG_CUDA(cudaStreamSynchronize(s));
@@ -379,15 +389,19 @@ int cc_gen_rhg_device(cc_ctx *ctx, uint64_t n, double avg_deg, double gamma, uin
     CCG_CUDA(cudaMemcpyAsync(doff.p, hoff.data(), 8 * P.nb, cudaMemcpyHostToDevice, s));
     const ccg::RhgBands B{bl.as<uint32_t>(), bstart.as<uint64_t>(), cells.as<uint64_t>(),
                           doff.as<uint64_t>(), dL.as<int>()};
+    t0 = c.tic(s);
     ccg::k_rhg_cells<<<grid, ccg::kBlock, 0, s>>>(B, pt, gk, n, P.nb, cells.as<uint64_t>());
     CCG_LAUNCH_CHECK();
+    c.toc(s, "gen_cells", t0, 0);
     keys.release();
     tmp.release();
     bkeys.release();
     // degrees, offsets, then every row's keys at its offsets
     DevBuf deg(4 * n, s, C->pool);
+    t0 = c.tic(s);
     ccg::k_rhg_neighbours<<<grid, ccg::kBlock, 0, s>>>(P, pt, B, deg.as<uint32_t>(), nullptr, nullptr);
     CCG_LAUNCH_CHECK();
+    c.toc(s, "gen_count", t0, 0);
     uint64_t m = 0;
     ccg::offsets_from_counts(deg.as<uint32_t>(), n, 0, row_ptr, s, C->pool, c);
     CCG_CUDA(cudaMemcpyAsync(&m, row_ptr + n, 8, cudaMemcpyDeviceToHost, s));
@@ -397,11 +411,15 @@ int cc_gen_rhg_device(cc_ctx *ctx, uint64_t n, double avg_deg, double gamma, uin
     if (m > cap) throw Error(CC_ERR_INVALID, "col capacity below the generated entries");
     if (m == 0) return;
     DevBuf ek(8 * m, s, C->pool), et(8 * m, s, C->pool);
+    t0 = c.tic(s);
     ccg::k_rhg_neighbours<<<grid, ccg::kBlock, 0, s>>>(P, pt, B, nullptr, row_ptr, ek.as<uint64_t>());
     CCG_LAUNCH_CHECK();
+    c.toc(s, "gen_fill", t0, 0);
     // rows sorted: one sort of the (source, target) keys keeps every row in place
+    t0 = c.tic(s);
     const uint64_t *sorted = ccg::radix_sort_u64(ek.as<uint64_t>(), et.as<uint64_t>(), m,
                                                  2 * P.idbits, s, C->pool, c);
+    c.toc(s, "gen_row_sort", t0, 0);
     const unsigned egrid = ccg::grid_for(m, ccg::kBlock, ccg::num_sms() * 16);
     if (id_bytes == 8)
       ccg::k_keys_low<uint64_t><<<egrid, ccg::kBlock, 0, s>>>(sorted, m, P.idbits, static_cast<uint64_t *>(col));
@@ -409,6 +427,13 @@ int cc_gen_rhg_device(cc_ctx *ctx, uint64_t n, double avg_deg, double gamma, uin
       ccg::k_keys_low<uint32_t><<<egrid, ccg::kBlock, 0, s>>>(sorted, m, P.idbits, static_cast<uint32_t *>(col));
     CCG_LAUNCH_CHECK();
     CCG_CUDA(cudaStreamSynchronize(s));
+    if (c.prof) {
+      cc_stats st;
+      std::memset(&st, 0, sizeof(st));
+      ccg::collect_kernel_stats(c, st);
+      st.kernel_launches = c.launches;
+      C->stats = st;
+    }
   });
 }
 

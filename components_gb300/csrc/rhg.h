@@ -204,6 +204,7 @@ struct Params {
   double two_cosh_R;      // 2 cosh R
   double cosh_aR_m1;      // cosh(alpha R) - 1
   double band_a[kMaxBands], band_b[kMaxBands], band_s[kMaxBands];  // e^k, e^-k, sinh k
+  double band_inv4s[kMaxBands];  // 1 / (4 sinh k) (0 for k = 0), for the window bound only
 };
 
 struct Point {
@@ -251,20 +252,23 @@ RHG_HD bool adjacent(const Params &P, const Point &u, const Point &w) {
 // Half-width, in phase units, of the angular window of band `band` around u
 // that holds every neighbour of u in that band; returns false when the whole
 // band must be scanned.
-RHG_HD bool window(const Params &P, const Point &u, int band, uint64_t *half) {
+RHG_HD bool window(const Params &P, const Point &u, int band, double inv_su, uint64_t *half) {
   const double se = P.band_s[band];
   if (se <= 0.0 || u.s <= 0.0) return false;
-  // q = sin^2(theta_max / 2) at the band's inner radius
-  const double q = div(sub(P.two_cosh_R, add(mul(u.a, P.band_b[band]), mul(u.b, P.band_a[band]))),
-                       mul(4.0, mul(u.s, se)));
+  // q = sin^2(theta_max / 2) at the band's inner radius.  Only a bound: the
+  // numerator has no cancellation for bands above the first (|r - k| <= R - 1),
+  // so q is good to a few 1e-16; the angle is then taken in single precision
+  // (relative error below 1e-6, well inside the widening).
+  const double q = (P.two_cosh_R - (u.a * P.band_b[band] + u.b * P.band_a[band])) * inv_su *
+                   P.band_inv4s[band];
   if (q >= 0.49) return false;  // theta_max >= ~88 degrees: scan the band
-  const double qq = q > 0.0 ? q : 0.0;
+  const float qf = (float)(q > 0.0 ? q : 0.0) * 1.000001f;
 #ifdef __CUDA_ARCH__
-  const double th = 2.0 * asin(sqrt(qq));
+  const float th = 2.0f * asinf(sqrtf(qf));
 #else
-  const double th = 2.0 * __builtin_asin(__builtin_sqrt(qq));
+  const float th = 2.0f * __builtin_asinf(__builtin_sqrtf(qf));
 #endif
-  const double wide = th * (1.0 + 1e-5) + 1e-8;  // radians
+  const double wide = (double)th * (1.0 + 1e-5) + 1e-8;  // radians
   *half = (uint64_t)(wide * (18446744073709551616.0 / (2.0 * kPi)));
   return true;
 }
@@ -347,6 +351,7 @@ inline int make_params(uint64_t n, double avg_deg, double gamma, uint64_t seed, 
     P->band_a[k] = exp_det((double)k);
     P->band_b[k] = div(1.0, P->band_a[k]);
     P->band_s[k] = mul(sub(P->band_a[k], P->band_b[k]), 0.5);
+    P->band_inv4s[k] = P->band_s[k] > 0.0 ? 1.0 / (4.0 * P->band_s[k]) : 0.0;
   }
   return CC_OK;
 }

@@ -241,11 +241,13 @@ def gen_gnm_device(n: int, m: int, seed: int = 1, id_bytes: int = 8, num_parts: 
 
 
 def gen_rhg_device(n: int, avg_deg: float = 16.0, gamma: float = 2.6, seed: int = 1,
-                   id_bytes: int = 4, num_parts: int = 1, device="cuda") -> StaticGraph:
-    """gen_rhg built on the device (the same graph bit for bit, torch CUDA tensors)."""
+                   id_bytes: int = 4, num_parts: int = 1, device="cuda", context=None) -> StaticGraph:
+    """gen_rhg built on the device (the same graph bit for bit, torch CUDA
+    tensors).  With a profiling context its phases are timed (context.stats())."""
     cap = int(1.25 * n * avg_deg) + 4096
+    h = context.handle if context is not None else None
     return _device_graph(lambda rp, col, cp, m: _lib.gpu().cc_gen_rhg_device(
-        None, n, avg_deg, gamma, seed, id_bytes, rp, col, cp, m), n, cap, id_bytes, device, num_parts)
+        h, n, avg_deg, gamma, seed, id_bytes, rp, col, cp, m), n, cap, id_bytes, device, num_parts)
 
 
 def gen_rhg(n: int, avg_deg: float = 16.0, gamma: float = 2.6, seed: int = 1, id_bytes: int = 4,
