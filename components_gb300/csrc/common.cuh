@@ -243,82 +243,51 @@ __global__ void k_row_pieces(uint64_t n, const uint64_t *__restrict__ rp, uint64
   }
 }
 }  // namespace
-// ---- flattened row minimum of a warp -------------------------------------------
+// ---- row minimum with loads in flight ------------------------------------------
 // The sweeps (label and shortcut rounds, decomposition relaxation, local
-// contraction) take, for every row v, the minimum of a value gathered at each
-// neighbour.  A warp takes 32 consecutive rows at a time and walks their
-// concatenated entries as one stream (lane k reads entry k of the stream: its
-// col load is coalesced however skewed the degrees), kSteps loads of 32
-// entries in flight, then every gather of those steps.  Each step's lanes of
-// one row are contiguous, so a segmented suffix minimum leaves the row's part
-// on its first lane, and the row's own lane pulls it with one shuffle.  Rows
-// above row_limit entries count as empty here (the *_pieces kernels fold
-// them).  Returns, on lane r, the minimum over row v0 + r of gather(u) (init
-// when it has no counted entries).
-template <class V, int kSteps, class Gather>
-__device__ __forceinline__ V warp_rows_min(uint64_t v0, uint64_t n, const uint64_t *__restrict__ rp,
-                                           const uint32_t *__restrict__ col, uint64_t row_limit,
-                                           V init, Gather gather) {
-  const unsigned lane = threadIdx.x & 31;
-  const uint64_t v = v0 + lane;
-  uint64_t eb = 0;
-  uint32_t deg = 0;
-  if (v < n) {
-    eb = __ldg(rp + v);
-    const uint64_t ee = __ldg(rp + v + 1);
-    if (ee - eb <= row_limit) deg = (uint32_t)(ee - eb);
+// contraction) take, for a row's entries [b, e), the minimum of a value
+// gathered at each neighbour.  One thread walks its row four entries at a
+// time: the four id loads, then the four gathers, are independent, so each
+// thread keeps four dependent load chains in flight instead of one.  (A
+// flattened 32-rows-per-warp stream was measured slower on the hyperbolic
+// graph: its row search and segmented minimum cost about 20 shuffles per 32
+// entries and left the kernel bound on the load/store pipe, while a thread's
+// own row of about 16 ids sits in two sectors that L1 keeps.)
+template <class V, class Gather>
+__device__ __forceinline__ V row_min_ilp(const uint32_t *__restrict__ col, uint64_t b, uint64_t e,
+                                         V best, Gather gather) {
+  uint64_t j = b;
+  for (; j + 4 <= e; j += 4) {
+    const uint32_t u0 = __ldg(col + j), u1 = __ldg(col + j + 1), u2 = __ldg(col + j + 2),
+                   u3 = __ldg(col + j + 3);
+    const V x0 = gather(u0), x1 = gather(u1), x2 = gather(u2), x3 = gather(u3);
+    const V a = x0 < x1 ? x0 : x1, c = x2 < x3 ? x2 : x3, m = a < c ? a : c;
+    best = m < best ? m : best;
   }
-  uint32_t inc = deg;
-#pragma unroll
-  for (int o = 1; o < 32; o <<= 1) {
-    const uint32_t t = __shfl_up_sync(0xffffffffu, inc, o);
-    if ((int)lane >= o) inc += t;
+  for (; j < e; ++j) {
+    const V x = gather(__ldg(col + j));
+    best = x < best ? x : best;
   }
-  const uint32_t total = __shfl_sync(0xffffffffu, inc, 31);
-  const uint32_t off = inc - deg;
-  V acc = init;
-  for (uint32_t f0 = 0; f0 < total; f0 += 32 * kSteps) {
-    uint32_t us[kSteps];
-    int rs[kSteps];
-#pragma unroll
-    for (int q = 0; q < kSteps; ++q) {
-      const uint32_t f = f0 + 32 * q + lane;
-      int r = 0;
-#pragma unroll
-      for (int step = 16; step; step >>= 1) {
-        const uint32_t o = __shfl_sync(0xffffffffu, off, r + step);
-        if (o <= f) r += step;
-      }
-      const uint32_t ro = __shfl_sync(0xffffffffu, off, r);
-      const uint64_t ebr = ((uint64_t)__shfl_sync(0xffffffffu, (uint32_t)(eb >> 32), r) << 32) |
-                           __shfl_sync(0xffffffffu, (uint32_t)eb, r);
-      const bool in = f < total;
-      rs[q] = in ? r : 32 + q;  // past the stream: a row of its own
-      us[q] = in ? __ldg(col + ebr + (f - ro)) : 0u;
-    }
-    V xs[kSteps];
-#pragma unroll
-    for (int q = 0; q < kSteps; ++q) xs[q] = rs[q] < 32 ? gather(us[q]) : init;
-#pragma unroll
-    for (int q = 0; q < kSteps; ++q) {
-      const uint32_t base = f0 + 32 * q;
-      if (base >= total) break;  // warp-uniform
-      V x = xs[q];
-      const int r = rs[q];
-#pragma unroll
-      for (int o = 1; o < 32; o <<= 1) {
-        const V y = __shfl_down_sync(0xffffffffu, x, o);
-        const int ry = __shfl_down_sync(0xffffffffu, r, o);
-        if (lane + o < 32 && ry == r && y < x) x = y;
-      }
-      // row `lane` meets this step at stream position max(off, base)
-      const bool meets = deg > 0 && off < base + 32 && off + deg > base;
-      const uint32_t head = (off > base ? off : base) - base;
-      const V part = __shfl_sync(0xffffffffu, x, meets ? head : 0);
-      if (meets && part < acc) acc = part;
-    }
+  return best;
+}
+// The same over a warp's piece [b, e) of a long row, lane-strided; the
+// caller reduces over the warp.
+template <class V, class Gather>
+__device__ __forceinline__ V piece_min_ilp(const uint32_t *__restrict__ col, uint64_t b, uint64_t e,
+                                           unsigned lane, V best, Gather gather) {
+  uint64_t j = b + lane;
+  for (; j + 96 < e; j += 128) {
+    const uint32_t u0 = __ldg(col + j), u1 = __ldg(col + j + 32), u2 = __ldg(col + j + 64),
+                   u3 = __ldg(col + j + 96);
+    const V x0 = gather(u0), x1 = gather(u1), x2 = gather(u2), x3 = gather(u3);
+    const V a = x0 < x1 ? x0 : x1, c = x2 < x3 ? x2 : x3, m = a < c ? a : c;
+    best = m < best ? m : best;
   }
-  return acc;
+  for (; j < e; j += 32) {
+    const V x = gather(__ldg(col + j));
+    best = x < best ? x : best;
+  }
+  return best;
 }
 
 // Entries [b, e) of work item h.

@@ -177,54 +177,125 @@ __global__ void k_rhg_cells(RhgBands B, RhgPts pt, const uint64_t *__restrict__ 
   }
 }
 
-// Every neighbour of v (the candidate search of the host generator): with
-// out == nullptr count them into deg[v], else write (v << idbits) | w keys
-// from out[start].
+// Candidate positions of v in band b: one or two ranges [r[0], r[1]) and
+// [r[2], r[3]) of bl; *win/*half describe the angular window (no window: the
+// whole band).
+__device__ __forceinline__ void rhg_band_ranges(const rhg::Params &P, const rhg::Point &pv,
+                                                double inv_s, const RhgBands &B, int b,
+                                                uint64_t r[4], bool *win, uint64_t *half) {
+  const uint64_t bs = B.band_start[b], be = B.band_start[b + 1];
+  r[0] = r[1] = r[2] = r[3] = bs;
+  *win = false;
+  *half = 0;
+  if (bs == be) return;
+  const int L = B.L[b];
+  *win = L > 0 && rhg::window(P, pv, b, inv_s, half);
+  if (!*win) {
+    r[1] = be;
+    return;
+  }
+  const uint64_t lo = pv.phi - *half, hi = pv.phi + *half;
+  const uint64_t *c = B.cell + B.cell_off[b];
+  const uint64_t c0 = rhg::cell_of(lo, L), c1 = rhg::cell_of(hi, L);
+  if (lo > pv.phi || hi < pv.phi) {  // the window crosses angle 0
+    r[0] = c[c0];
+    r[1] = be;
+    r[2] = bs;
+    r[3] = c[c1 + 1];
+  } else {
+    r[0] = c[c0];
+    r[1] = c[c1 + 1];
+  }
+}
+
+// Candidate w of v: a neighbour?
+__device__ __forceinline__ bool rhg_is_neighbour(const rhg::Params &P, const rhg::Point &pv, uint64_t v,
+                                                 bool win, uint64_t half, const RhgPts &pt, uint32_t w) {
+  if (w == v) return false;
+  if (win && pt.phi[w] - (pv.phi - half) > 2 * half) return false;
+  return rhg::adjacent(P, pv, pt.get(w));
+}
+
+// A vertex near the centre of the disk has candidates in the millions (the
+// whole inner bands, wide windows in the outer ones); one thread would walk
+// them alone for seconds.  Vertices with more than kRhgHeavy candidates go to
+// a list and are searched by a whole block each (k_rhg_heavy).
+constexpr uint64_t kRhgHeavy = 4096;
+
+// Every neighbour of v (the candidate search of the host generator), one
+// thread per vertex: with out == nullptr count them into deg[v], else write
+// (v << idbits) | w keys from out[rp[v]].  Heavy vertices are skipped (the
+// counting pass lists them in heavy / nheavy).
 __global__ void k_rhg_neighbours(rhg::Params P, RhgPts pt, RhgBands B, uint32_t *__restrict__ deg,
-                                 const uint64_t *__restrict__ rp, uint64_t *__restrict__ out) {
+                                 const uint64_t *__restrict__ rp, uint64_t *__restrict__ out,
+                                 uint32_t *__restrict__ heavy, unsigned int *__restrict__ nheavy) {
   for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < P.n;
        v += (uint64_t)gridDim.x * blockDim.x) {
     const rhg::Point pv = pt.get(v);
     const double inv_s = pv.s > 0.0 ? 1.0 / pv.s : 0.0;
+    uint64_t est = 0;
+    for (int b = 0; b < P.nb && est <= kRhgHeavy; ++b) {
+      uint64_t r[4], half;
+      bool win;
+      rhg_band_ranges(P, pv, inv_s, B, b, r, &win, &half);
+      est += (r[1] - r[0]) + (r[3] - r[2]);
+    }
+    if (est > kRhgHeavy) {
+      if (!out) heavy[atomicAdd(nheavy, 1u)] = (uint32_t)v;
+      continue;
+    }
     uint64_t cnt = 0, e = out ? rp[v] : 0;
     for (int b = 0; b < P.nb; ++b) {
-      const uint64_t bs = B.band_start[b], be = B.band_start[b + 1];
-      if (bs == be) continue;
-      const int L = B.L[b];
-      uint64_t half = 0;
-      const bool win = L > 0 && rhg::window(P, pv, b, inv_s, &half);
-      uint64_t r0a, r0b, r1a = 0, r1b = 0;  // one or two ranges of positions in bl
-      if (!win) {
-        r0a = bs;
-        r0b = be;
-      } else {
-        const uint64_t lo = pv.phi - half, hi = pv.phi + half;
-        const uint64_t *c = B.cell + B.cell_off[b];
-        const uint64_t c0 = rhg::cell_of(lo, L), c1 = rhg::cell_of(hi, L);
-        if (lo > pv.phi || hi < pv.phi) {  // the window crosses angle 0
-          r0a = c[c0];
-          r0b = be;
-          r1a = bs;
-          r1b = c[c1 + 1];
-        } else {
-          r0a = c[c0];
-          r0b = c[c1 + 1];
-        }
-      }
-      for (int part = 0; part < 2; ++part) {
-        const uint64_t ka = part ? r1a : r0a, kb = part ? r1b : r0b;
-        for (uint64_t k = ka; k < kb; ++k) {
+      uint64_t r[4], half;
+      bool win;
+      rhg_band_ranges(P, pv, inv_s, B, b, r, &win, &half);
+      for (int part = 0; part < 2; ++part)
+        for (uint64_t k = r[2 * part]; k < r[2 * part + 1]; ++k) {
           const uint32_t w = B.bl[k];
-          if (w == v) continue;
-          const uint64_t pw_phi = pt.phi[w];
-          if (win && pw_phi - (pv.phi - half) > 2 * half) continue;
-          if (!rhg::adjacent(P, pv, pt.get(w))) continue;
+          if (!rhg_is_neighbour(P, pv, v, win, half, pt, w)) continue;
           if (out) out[e++] = (v << P.idbits) | w;
           else ++cnt;
         }
-      }
     }
     if (!out) deg[v] = (uint32_t)cnt;
+  }
+}
+
+// The heavy vertices, one block each: the block's threads stride over every
+// candidate range; counting adds up a block total, writing takes positions
+// from a shared counter (the row order does not matter: the keys are sorted
+// afterwards).
+__global__ void k_rhg_heavy(rhg::Params P, RhgPts pt, RhgBands B, const uint32_t *__restrict__ heavy,
+                            const unsigned int *__restrict__ nheavy, uint32_t *__restrict__ deg,
+                            const uint64_t *__restrict__ rp, uint64_t *__restrict__ out) {
+  __shared__ unsigned long long bcount;
+  const unsigned int nh = *nheavy;
+  for (unsigned int h = blockIdx.x; h < nh; h += gridDim.x) {
+    const uint64_t v = heavy[h];
+    const rhg::Point pv = pt.get(v);
+    const double inv_s = pv.s > 0.0 ? 1.0 / pv.s : 0.0;
+    if (threadIdx.x == 0) bcount = 0;
+    __syncthreads();
+    unsigned long long mine = 0;
+    for (int b = 0; b < P.nb; ++b) {
+      uint64_t r[4], half;
+      bool win;
+      rhg_band_ranges(P, pv, inv_s, B, b, r, &win, &half);
+      for (int part = 0; part < 2; ++part)
+        for (uint64_t k = r[2 * part] + threadIdx.x; k < r[2 * part + 1]; k += blockDim.x) {
+          const uint32_t w = B.bl[k];
+          if (!rhg_is_neighbour(P, pv, v, win, half, pt, w)) continue;
+          if (out) out[rp[v] + atomicAdd(&bcount, 1ull)] = (v << P.idbits) | w;
+          else ++mine;
+        }
+    }
+    if (!out) {
+      for (int o = 16; o; o >>= 1) mine += __shfl_xor_sync(0xffffffffu, mine, o);
+      if ((threadIdx.x & 31) == 0 && mine) atomicAdd(&bcount, mine);
+    }
+    __syncthreads();
+    if (!out && threadIdx.x == 0) deg[v] = (uint32_t)bcount;
+    __syncthreads();
   }
 }
 
@@ -397,9 +468,15 @@ int cc_gen_rhg_device(cc_ctx *ctx, uint64_t n, double avg_deg, double gamma, uin
     tmp.release();
     bkeys.release();
     // degrees, offsets, then every row's keys at its offsets
-    DevBuf deg(4 * n, s, C->pool);
+    DevBuf deg(4 * n, s, C->pool), heavy(4 * n, s, C->pool), nheavy(4, s, C->pool);
+    CCG_CUDA(cudaMemsetAsync(nheavy.p, 0, 4, s));
+    const unsigned hgrid = (unsigned)ccg::num_sms() * 4;
     t0 = c.tic(s);
-    ccg::k_rhg_neighbours<<<grid, ccg::kBlock, 0, s>>>(P, pt, B, deg.as<uint32_t>(), nullptr, nullptr);
+    ccg::k_rhg_neighbours<<<grid, ccg::kBlock, 0, s>>>(P, pt, B, deg.as<uint32_t>(), nullptr, nullptr,
+                                                       heavy.as<uint32_t>(), nheavy.as<unsigned int>());
+    CCG_LAUNCH_CHECK();
+    ccg::k_rhg_heavy<<<hgrid, ccg::kBlock, 0, s>>>(P, pt, B, heavy.as<uint32_t>(), nheavy.as<unsigned int>(),
+                                                  deg.as<uint32_t>(), nullptr, nullptr);
     CCG_LAUNCH_CHECK();
     c.toc(s, "gen_count", t0, 0);
     uint64_t m = 0;
@@ -412,7 +489,11 @@ int cc_gen_rhg_device(cc_ctx *ctx, uint64_t n, double avg_deg, double gamma, uin
     if (m == 0) return;
     DevBuf ek(8 * m, s, C->pool), et(8 * m, s, C->pool);
     t0 = c.tic(s);
-    ccg::k_rhg_neighbours<<<grid, ccg::kBlock, 0, s>>>(P, pt, B, nullptr, row_ptr, ek.as<uint64_t>());
+    ccg::k_rhg_neighbours<<<grid, ccg::kBlock, 0, s>>>(P, pt, B, nullptr, row_ptr, ek.as<uint64_t>(),
+                                                       nullptr, nullptr);
+    CCG_LAUNCH_CHECK();
+    ccg::k_rhg_heavy<<<hgrid, ccg::kBlock, 0, s>>>(P, pt, B, heavy.as<uint32_t>(), nheavy.as<unsigned int>(),
+                                                  nullptr, row_ptr, ek.as<uint64_t>());
     CCG_LAUNCH_CHECK();
     c.toc(s, "gen_fill", t0, 0);
     // rows sorted: one sort of the (source, target) keys keeps every row in place

@@ -99,23 +99,19 @@ constexpr uint64_t kRowLimit = 64;  // rows above this are relaxed a warp per pi
 // One Gauss-Seidel style sweep: key[v] <- min(key[v], min_w key[w] + 2^32).
 // Stale neighbour reads are upper bounds of the fixpoint, so in-place updates
 // converge to the same keys as the reference's sweeps.
-__global__ void __launch_bounds__(kBlock) k_ldd_round(uint64_t n, const uint64_t *__restrict__ rp,
-                                                     const uint32_t *__restrict__ col, uint64_t *key,
-                                                     int *flag) {
-  const unsigned lane = threadIdx.x & 31;
-  const uint64_t warp = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
-  const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+__global__ void k_ldd_round(uint64_t n, const uint64_t *__restrict__ rp,
+                            const uint32_t *__restrict__ col, uint64_t *key, int *flag) {
   int changed = 0;
-  for (uint64_t v0 = warp * 32; v0 < n; v0 += nwarps * 32) {
-    const uint64_t best = warp_rows_min<uint64_t, 4>(
-        v0, n, rp, col, kRowLimit, ~0ull, [&](uint32_t u) { return ld_cg(key + u) + kOne; });
-    const uint64_t v = v0 + lane;
-    if (v < n) {
-      const uint64_t k = ld_cg(key + v);
-      if (best < k) {
-        st_cg(key + v, best);
-        changed = 1;
-      }
+  for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < n;
+       v += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t b = __ldg(rp + v), e = __ldg(rp + v + 1);
+    if (e - b > kRowLimit) continue;
+    const uint64_t k = ld_cg(key + v);
+    const uint64_t best =
+        row_min_ilp<uint64_t>(col, b, e, k, [&](uint32_t u) { return ld_cg(key + u) + kOne; });
+    if (best < k) {
+      st_cg(key + v, best);
+      changed = 1;
     }
   }
   warp_flag(changed, flag);
@@ -133,11 +129,8 @@ __global__ void k_ldd_round_pieces(const uint64_t *__restrict__ rp, const uint32
     uint32_t v;
     uint64_t b, e;
     row_piece(rpc, rp, h, v, b, e);
-    uint64_t best = ~0ull;
-    for (uint64_t j = b + lane; j < e; j += 32) {
-      uint64_t kw = ld_cg(key + __ldg(col + j)) + kOne;
-      best = kw < best ? kw : best;
-    }
+    uint64_t best = piece_min_ilp<uint64_t>(col, b, e, lane, ~0ull,
+                                            [&](uint32_t u) { return ld_cg(key + u) + kOne; });
 #pragma unroll
     for (int o = 16; o; o >>= 1) {
       uint64_t y = __shfl_xor_sync(0xffffffffu, best, o);
@@ -194,21 +187,16 @@ __global__ void k_local_init(uint64_t n, const uint32_t *__restrict__ vid, uint6
 // Jacobi sweep: out[v] = min over N[v] (closed neighbourhood) of in[].  Rows
 // above kRowLimit entries only store in[v] here; k_min_sweep_pieces folds
 // their neighbours in afterwards, one warp per piece of the row.
-__global__ void __launch_bounds__(kBlock) k_min_sweep(uint64_t n, const uint64_t *__restrict__ rp,
-                                                     const uint32_t *__restrict__ col,
-                                                     const uint64_t *__restrict__ in,
-                                                     uint64_t *__restrict__ out) {
-  const unsigned lane = threadIdx.x & 31;
-  const uint64_t warp = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
-  const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
-  for (uint64_t v0 = warp * 32; v0 < n; v0 += nwarps * 32) {
-    const uint64_t m = warp_rows_min<uint64_t, 4>(v0, n, rp, col, kRowLimit, ~0ull,
-                                                  [&](uint32_t u) { return __ldg(in + u); });
-    const uint64_t v = v0 + lane;
-    if (v < n) {
-      const uint64_t own = in[v];
-      out[v] = m < own ? m : own;
-    }
+__global__ void k_min_sweep(uint64_t n, const uint64_t *__restrict__ rp,
+                            const uint32_t *__restrict__ col, const uint64_t *__restrict__ in,
+                            uint64_t *__restrict__ out) {
+  for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < n;
+       v += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t b = __ldg(rp + v), e = __ldg(rp + v + 1);
+    uint64_t best = in[v];
+    if (e - b <= kRowLimit)
+      best = row_min_ilp<uint64_t>(col, b, e, best, [&](uint32_t u) { return __ldg(in + u); });
+    out[v] = best;
   }
 }
 
@@ -222,11 +210,8 @@ __global__ void k_min_sweep_pieces(const uint64_t *__restrict__ rp, const uint32
     uint32_t v;
     uint64_t b, e;
     row_piece(rpc, rp, h, v, b, e);
-    uint64_t best = ~0ull;
-    for (uint64_t j = b + lane; j < e; j += 32) {
-      const uint64_t kw = __ldg(in + __ldg(col + j));
-      best = kw < best ? kw : best;
-    }
+    uint64_t best = piece_min_ilp<uint64_t>(col, b, e, lane, ~0ull,
+                                            [&](uint32_t u) { return __ldg(in + u); });
 #pragma unroll
     for (int o = 16; o; o >>= 1) {
       const uint64_t y = __shfl_xor_sync(0xffffffffu, best, o);

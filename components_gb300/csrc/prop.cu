@@ -11,23 +11,18 @@ constexpr uint64_t kRowLimit = 64;
 // lab[v] <- min(lab[v], min_u lab[u]) in place.  The reference updates local
 // vertices in place during a sweep (SetVertexPayload) and sees ghosts from
 // the last exchange; on one device every vertex is local.
-__global__ void __launch_bounds__(kBlock) k_labels_round(uint64_t n, const uint64_t *__restrict__ rp,
-                                                        const uint32_t *__restrict__ col,
-                                                        uint32_t *lab, int *flag) {
-  const unsigned lane = threadIdx.x & 31;
-  const uint64_t warp = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
-  const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+__global__ void k_labels_round(uint64_t n, const uint64_t *__restrict__ rp,
+                               const uint32_t *__restrict__ col, uint32_t *lab, int *flag) {
   int changed = 0;
-  for (uint64_t v0 = warp * 32; v0 < n; v0 += nwarps * 32) {
-    const uint32_t best = warp_rows_min<uint32_t, 4>(v0, n, rp, col, kRowLimit, kNone,
-                                                     [&](uint32_t u) { return ld_cg(lab + u); });
-    const uint64_t v = v0 + lane;
-    if (v < n) {
-      const uint32_t l = ld_cg(lab + v);
-      if (best < l) {
-        st_cg(lab + v, best);
-        changed = 1;
-      }
+  for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < n;
+       v += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t b = __ldg(rp + v), e = __ldg(rp + v + 1);
+    if (e - b > kRowLimit) continue;
+    const uint32_t l = ld_cg(lab + v);
+    const uint32_t best = row_min_ilp<uint32_t>(col, b, e, l, [&](uint32_t u) { return ld_cg(lab + u); });
+    if (best < l) {
+      st_cg(lab + v, best);
+      changed = 1;
     }
   }
   warp_flag(changed, flag);
@@ -46,11 +41,8 @@ __global__ void k_labels_round_pieces(const uint64_t *__restrict__ rp,
     uint32_t v;
     uint64_t b, e;
     row_piece(rpc, rp, h, v, b, e);
-    uint32_t best = kNone;
-    for (uint64_t j = b + lane; j < e; j += 32) {
-      uint32_t x = ld_cg(lab + __ldg(col + j));
-      best = x < best ? x : best;
-    }
+    uint32_t best =
+        piece_min_ilp<uint32_t>(col, b, e, lane, kNone, [&](uint32_t u) { return ld_cg(lab + u); });
     best = __reduce_min_sync(0xffffffffu, best);
     if (lane == 0 && best < ld_cg(lab + v)) {
       atomicMin(lab + v, best);
@@ -68,23 +60,18 @@ __global__ void k_labels_round_pieces(const uint64_t *__restrict__ rp,
 //                              answers are applied to every u with nf[u]
 //                              equal to the target
 //   CheckConvergence (:359-376): stop when nf == f everywhere.
-__global__ void __launch_bounds__(kBlock) k_sc_min(uint64_t n, const uint64_t *__restrict__ rp,
-                                                  const uint32_t *__restrict__ col,
-                                                  const uint32_t *__restrict__ f,
-                                                  uint32_t *__restrict__ nf, uint32_t *__restrict__ upd) {
-  const unsigned lane = threadIdx.x & 31;
-  const uint64_t warp = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
-  const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
-  for (uint64_t v0 = warp * 32; v0 < n; v0 += nwarps * 32) {
-    // rows above kRowLimit: k_sc_min_pieces folds their neighbours in
-    const uint32_t m = warp_rows_min<uint32_t, 4>(v0, n, rp, col, kRowLimit, kNone,
-                                                  [&](uint32_t u) { return __ldg(f + u); });
-    const uint64_t v = v0 + lane;
-    if (v < n) {
-      const uint32_t l = f[v], best = m < l ? m : l;
-      nf[v] = best;
-      if (best < l) atomicMin(upd + l, best);
-    }
+__global__ void k_sc_min(uint64_t n, const uint64_t *__restrict__ rp,
+                         const uint32_t *__restrict__ col, const uint32_t *__restrict__ f,
+                         uint32_t *__restrict__ nf, uint32_t *__restrict__ upd) {
+  for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < n;
+       v += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t b = __ldg(rp + v), e = __ldg(rp + v + 1);
+    const uint32_t l = f[v];
+    uint32_t best = l;
+    if (e - b <= kRowLimit)  // longer rows: k_sc_min_pieces folds their neighbours in
+      best = row_min_ilp<uint32_t>(col, b, e, l, [&](uint32_t u) { return __ldg(f + u); });
+    nf[v] = best;
+    if (best < l) atomicMin(upd + l, best);
   }
 }
 
@@ -103,11 +90,8 @@ __global__ void k_sc_min_pieces(const uint64_t *__restrict__ rp, const uint32_t 
     uint32_t v;
     uint64_t b, e;
     row_piece(rpc, rp, h, v, b, e);
-    uint32_t best = kNone;
-    for (uint64_t j = b + lane; j < e; j += 32) {
-      uint32_t x = __ldg(f + __ldg(col + j));
-      best = x < best ? x : best;
-    }
+    uint32_t best =
+        piece_min_ilp<uint32_t>(col, b, e, lane, kNone, [&](uint32_t u) { return __ldg(f + u); });
     best = __reduce_min_sync(0xffffffffu, best);
     if (lane == 0) {
       const uint32_t l = f[v];
