@@ -424,7 +424,8 @@ def gpu_arm(args, wl: Workload, rank: int, world: int, local: int) -> dict | Non
                             "graph is streamed under the tiled pass)",
                 "ms_per_step": e2e_s * 1e3,
                 "ms_min_median_max": [min(step_s) * 1e3, statistics.median(step_s) * 1e3,
-                                      max(step_s) * 1e3]},
+                                      max(step_s) * 1e3],
+                "ms_steps": [round(x * 1e3, 3) for x in step_s]},
         "gpu_launches": launches,
         "roofline": roof,
         "kernel_share": share,
