@@ -118,6 +118,10 @@ GPU_SYMBOLS = {
                                     C.c_uint64, C.POINTER(C.c_uint64)]),
     "cc_gen_rhg_device": (C.c_int, [_P, C.c_uint64, C.c_double, C.c_double, C.c_uint64, C.c_uint32,
                                     _P, _P, C.c_uint64, C.POINTER(C.c_uint64)]),
+    "cc_read_metis_device": (C.c_int, [_P, C.c_char_p, C.c_uint32, _P, _P, C.c_uint64,
+                                       C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]),
+    "cc_read_binary_edges_device": (C.c_int, [_P, C.c_char_p, C.c_uint32, _P, _P, C.c_uint64,
+                                              C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]),
     "cc_component_sizes": (C.c_int, [_P, _P, C.c_uint32, C.c_uint32, C.c_uint64, _P, C.c_uint64,
                                      C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]),
     "cc_ctx_arena_bytes": (_U64, [_P]),

@@ -19,7 +19,8 @@ PKG = Path(__file__).resolve().parent
 ROOT = PKG.parent
 CSRC = PKG / "csrc"
 BUILD = PKG / "_build"
-CUDA_SOURCES = ["uf.cu", "sortcsr.cu", "ldd.cu", "prop.cu", "api.cu", "batch.cu", "serve.cu", "gen_dev.cu"]
+CUDA_SOURCES = ["uf.cu", "sortcsr.cu", "ldd.cu", "prop.cu", "api.cu", "batch.cu", "serve.cu", "gen_dev.cu",
+                "load_dev.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

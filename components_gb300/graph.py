@@ -142,6 +142,34 @@ def read_binary_edges(path: str, id_bytes: int = 4, num_parts: int = 1) -> Stati
     return _read("cc_read_binary_edges", path, id_bytes, num_parts)
 
 
+def _read_device(fn: str, path: str, id_bytes: int, num_parts: int, device, context) -> StaticGraph:
+    import torch
+    f = getattr(_lib.gpu(), fn)
+    h = context.handle if context is not None else None
+    n, m = C.c_uint64(), C.c_uint64()
+    _lib.check(f(h, str(path).encode(), id_bytes, None, None, 0, C.byref(n), C.byref(m)))  # size query
+    rp = torch.empty(n.value + 1, dtype=torch.int64, device=device)
+    dt = torch.int32 if id_bytes == 4 else torch.int64
+    col = torch.empty(max(m.value, 1), dtype=dt, device=device)
+    with torch.cuda.device(rp.device):
+        _lib.check(f(h, str(path).encode(), id_bytes, rp.data_ptr(), col.data_ptr(), m.value,
+                     C.byref(n), C.byref(m)))
+    return StaticGraph(rp, col[: m.value].clone(), num_parts)
+
+
+def read_metis_device(path: str, id_bytes: int = 4, num_parts: int = 1, device="cuda",
+                      context=None) -> StaticGraph:
+    """read_metis parsed and built on the device (the same CSR, torch CUDA
+    tensors): the file's bytes cross the host link once."""
+    return _read_device("cc_read_metis_device", path, id_bytes, num_parts, device, context)
+
+
+def read_binary_edges_device(path: str, id_bytes: int = 4, num_parts: int = 1, device="cuda",
+                             context=None) -> StaticGraph:
+    """read_binary_edges built on the device (the same CSR, torch CUDA tensors)."""
+    return _read_device("cc_read_binary_edges_device", path, id_bytes, num_parts, device, context)
+
+
 def load_graph(conf, id_bytes: int = 4, num_parts: int = 1) -> StaticGraph:
     """The input of the reference drivers (IOUtility::LoadGraph,
     io_utils.h:33-56) from a parsed Config: `-input file|edgefile|binary -in

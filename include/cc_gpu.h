@@ -243,6 +243,26 @@ int cc_gen_rhg_device(cc_ctx *ctx, uint64_t n, double avg_deg, double gamma, uin
                       uint32_t id_bytes, uint64_t *row_ptr, void *col, uint64_t cap,
                       uint64_t *m_dir);
 
+/*
+ * The reference's input files read straight into a device CSR: METIS text
+ * (GraphIO::ReadMETISFile, lib/io/graph_io.h:281-382) and the sorted binary
+ * edge file (GraphIO::ReadSortedBinaryFile, graph_io.h:910-1175).  The file's
+ * bytes cross the host link once; tokens, keys, the sort and the rows are
+ * built on the device, and the result is the CSR of cc_read_metis /
+ * cc_read_binary_edges (cc_gen.h) bit for bit: symmetric, rows sorted,
+ * self-loops and repeated edges dropped.  Size query: with row_ptr NULL only
+ * the header is read and *n and *m_dir receive the vertex count and an upper
+ * bound of the directed entries (nothing runs on the device).  Otherwise
+ * row_ptr holds n+1 device words and col cap device ids; *m_dir receives the
+ * entries (CC_ERR_INVALID when they exceed cap, or for an id outside [1, n]
+ * or a malformed file).  METIS files below 4 GB.  ctx NULL: the default
+ * context (its page-locked staging holds the file).
+ */
+int cc_read_metis_device(cc_ctx *ctx, const char *path, uint32_t id_bytes, uint64_t *row_ptr,
+                         void *col, uint64_t cap, uint64_t *n, uint64_t *m_dir);
+int cc_read_binary_edges_device(cc_ctx *ctx, const char *path, uint32_t id_bytes, uint64_t *row_ptr,
+                                void *col, uint64_t cap, uint64_t *n, uint64_t *m_dir);
+
 int cc_ctx_stats(cc_ctx *ctx, cc_stats *out);
 /* Device bytes the context holds in its arena (grows on demand, reused). */
 uint64_t cc_ctx_arena_bytes(cc_ctx *ctx);

@@ -151,3 +151,28 @@ def test_cpp_load_graph(tmp_path):
     assert same(run("gen", "grid_2d", 30, 20, 0.5, 16.0, 2.2, 2), cc.gen_grid(30, 20, 0.5, seed=2))
     bad = subprocess.run([str(exe), "gen", "ba", "10", "10", "1", "1", "1", "1"], capture_output=True, text=True)
     assert bad.returncode == 1 and "not supported" in bad.stderr
+
+
+def test_device_loader_size_query(tmp_path):
+    """The device loaders' size query reads only the header on the host (no
+    device call): the vertex count and an upper bound of the entries; bad
+    files are refused there already."""
+    import ctypes as C
+    lib = _lib.gpu()
+    n, edges = 6, [(0, 1), (1, 2), (3, 4), (4, 5)]
+    pm = tmp_path / "g.graph"
+    write_metis(pm, n, edges)
+    pb = tmp_path / "g.bin"
+    pb.write_bytes(np.array([n, len(edges)], np.uint64).tobytes() + (np.array(edges, np.uint64) + 1).tobytes())
+    nn, mm = C.c_uint64(), C.c_uint64()
+    assert lib.cc_read_metis_device(None, str(pm).encode(), 4, None, None, 0, C.byref(nn), C.byref(mm)) == 0
+    assert nn.value == n and mm.value >= 2 * len(edges)
+    assert lib.cc_read_binary_edges_device(None, str(pb).encode(), 4, None, None, 0, C.byref(nn),
+                                           C.byref(mm)) == 0
+    assert nn.value == n and mm.value == 2 * len(edges)
+    (tmp_path / "nohdr.graph").write_text("% only a comment\n")
+    (tmp_path / "short.bin").write_bytes(np.array([3, 5], np.uint64).tobytes())
+    for fn, name in ((lib.cc_read_metis_device, "nohdr.graph"), (lib.cc_read_binary_edges_device, "short.bin"),
+                     (lib.cc_read_metis_device, "missing.graph")):
+        assert fn(None, str(tmp_path / name).encode(), 4, None, None, 0, C.byref(nn), C.byref(mm)) == \
+            _lib.CC_ERR_INVALID, name
