@@ -294,41 +294,74 @@ namespace rhg {
 // space does not, and underestimates the degree).
 inline double avg_degree(uint64_t n, double alpha, double R) {
   const int N = 1200;
-  std::vector<double> r(N), w(N), sh(N);
+  std::vector<double> r(N), w(N), sh(N), W(N + 1, 0.0);
   double wsum = 0.0;
   for (int i = 0; i < N; ++i) {
     r[i] = (i + 0.5) * R / N;
     w[i] = std::sinh(alpha * r[i]);
     wsum += w[i];
+    W[i + 1] = W[i] + w[i];
     sh[i] = std::sinh(r[i]);
   }
   const double coshR = std::cosh(R);
+  // theta is symmetric: the pairs j > i counted twice, the diagonal once; the
+  // pairs with r_i + r_j <= R (a prefix of j, r ascending) all have theta = pi
   double acc = 0.0;
   for (int i = 0; i < N; ++i) {
+    int jfull = (int)std::floor((R - r[i]) * N / R - 0.5);  // last j with r_j <= R - r_i
+    while (jfull + 1 < N && r[i] + r[jfull + 1] <= R) ++jfull;
+    while (jfull >= 0 && r[i] + r[jfull] > R) --jfull;
     double row = 0.0;
-    for (int j = 0; j < N; ++j) {
-      double th;
-      if (r[i] + r[j] <= R) {
-        th = kPi;
-      } else {
-        double q = (coshR - std::cosh(r[i] - r[j])) / (2.0 * sh[i] * sh[j]);
-        th = q >= 1.0 ? kPi : (q <= 0.0 ? 0.0 : 2.0 * std::asin(std::sqrt(q)));
-      }
+    const int j0 = i + 1;
+    if (jfull >= j0) row += kPi * (W[jfull + 1] - W[j0]);
+    for (int j = std::max(j0, jfull + 1); j < N; ++j) {
+      const double q = (coshR - std::cosh(r[i] - r[j])) / (2.0 * sh[i] * sh[j]);
+      const double th = q >= 1.0 ? kPi : (q <= 0.0 ? 0.0 : 2.0 * std::asin(std::sqrt(q)));
       row += w[j] * th;
     }
-    acc += w[i] * row;
+    double diag;
+    if (2.0 * r[i] <= R) {
+      diag = kPi;
+    } else {
+      const double q = (coshR - 1.0) / (2.0 * sh[i] * sh[i]);
+      diag = q >= 1.0 ? kPi : (q <= 0.0 ? 0.0 : 2.0 * std::asin(std::sqrt(q)));
+    }
+    acc += w[i] * (2.0 * row + w[i] * diag);
   }
   return (double)(n - 1) * acc / (wsum * wsum * kPi);
 }
 
-// Bisection on the average degree (decreasing in R), rounded to a multiple of
+// The radius for the target degree: a bracketed root of log avg_degree(R) -
+// log deg (decreasing in R) by the Illinois variant of regula falsi, a few
+// evaluations instead of forty bisection steps, then rounded to a multiple of
 // 2^-32 so that the last bits of the platform's sinh / asin cannot move it.
 inline double target_radius(uint64_t n, double alpha, double deg) {
+  // in log space the degree falls about linearly in R (as e^(-R/2)), which
+  // regula falsi solves in a few steps
+  auto f = [&](double R) { return std::log(avg_degree(n, alpha, R)) - std::log(deg); };
   double lo = 1e-3, hi = 2.0 * std::log((double)n) + 40.0;
-  for (int it = 0; it < 40; ++it) {
-    double mid = 0.5 * (lo + hi);
-    if (avg_degree(n, alpha, mid) > deg) lo = mid;
-    else hi = mid;
+  double flo = f(lo), fhi = f(hi);
+  if (!(flo > 0.0) || !(fhi < 0.0)) return std::ldexp(std::nearbyint(std::ldexp(0.5 * (lo + hi), 32)), -32);
+  int side = 0;
+  for (int it = 0; it < 200 && hi - lo > 1e-12 * hi; ++it) {
+    double mid = (lo * fhi - hi * flo) / (fhi - flo);
+    if (!(mid > lo && mid < hi)) mid = 0.5 * (lo + hi);
+    const double fm = f(mid);
+    if (fm == 0.0) {
+      lo = hi = mid;
+      break;
+    }
+    if (fm > 0.0) {
+      lo = mid;
+      flo = fm;
+      if (side == 1) fhi *= 0.5;
+      side = 1;
+    } else {
+      hi = mid;
+      fhi = fm;
+      if (side == -1) flo *= 0.5;
+      side = -1;
+    }
   }
   return std::ldexp(std::nearbyint(std::ldexp(0.5 * (lo + hi), 32)), -32);
 }
