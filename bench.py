@@ -611,13 +611,19 @@ def workload_serve(args):
         del D
     torch.cuda.empty_cache()
     gen_s = time.time() - t0
-    reqs = [pool[int(j)] for j in rng.integers(0, len(pool), args.serve_requests)]
+    picks = [int(j) for j in rng.integers(0, len(pool), args.serve_requests)]
+    reqs = [pool[j] for j in picks]
     edges = sum(G.m for G in reqs)
-    # plain path, closed loop: one request after the other
-    plain = []
+    # plain path, closed loop: one request after the other (one label array
+    # kept per pool graph; repeated solves of a graph must agree with it)
+    plain, plain_same = {}, True
     t0 = time.perf_counter()
-    for G in reqs:
-        plain.append(cc.find_components(G, "exp"))
+    for j, G in zip(picks, reqs):
+        lab = cc.find_components(G, "exp")
+        if j in plain:
+            plain_same &= bool(np.array_equal(lab, plain[j]))
+        else:
+            plain[j] = lab
     plain_s = time.perf_counter() - t0
     # served: capacity (closed loop), then an open-loop Poisson stream at 80 %
     with Server(budget_bytes=120 << 30) as srv:
@@ -628,7 +634,6 @@ def workload_serve(args):
         cap_s = time.perf_counter() - t0
         rate = 0.8 * len(reqs) / cap_s
         gaps = rng.exponential(1.0 / rate, len(reqs))
-        results = [None] * len(reqs)
         infos = [None] * len(reqs)
         tickets = [None] * len(reqs)
 
@@ -650,12 +655,13 @@ def workload_serve(args):
         th = threading.Thread(target=producer)
         th.start()
         th.join()
+        same = plain_same
         for i in range(len(reqs)):
-            results[i], infos[i] = srv.wait(tickets[i])
+            lab, infos[i] = srv.wait(tickets[i])
+            same &= bool(np.array_equal(lab, plain[picks[i]]))
         served_s = max(x["done_s"] for x in infos) - min(x["submit_s"] for x in infos)
         st = srv.stats()
     lat = np.array([(x["done_s"] - x["submit_s"]) * 1e3 for x in infos])
-    same = all(np.array_equal(a, b) for a, b in zip(results, plain))
     print(json.dumps({
         "workload": "serve", "requests": len(reqs), "pool_graphs": len(pool),
         "edges_total": edges, "metric": "p50/p99 latency (ms) and graphs/s",
