@@ -221,10 +221,12 @@ __global__ void __launch_bounds__(kBlock) k_emit(uint64_t n, const uint64_t *__r
     const uint64_t v = v0 + lane;
     uint64_t eb = 0;
     uint32_t deg = 0, cv = 0, lo = 0, hi = 0xffffffffu;  // lo, hi: v's rank when part
+    bool hub = false;
     if (v < n) {
       eb = __ldg(rp + v);
       const uint64_t ee = __ldg(rp + v + 1);
       if (ee - eb <= hub_limit) deg = (uint32_t)(ee - eb);
+      else hub = true;
       cv = cl[v];
       if (part) pm.bounds((uint32_t)v, lo, hi);
     }
@@ -236,9 +238,52 @@ __global__ void __launch_bounds__(kBlock) k_emit(uint64_t n, const uint64_t *__r
     }
     const uint32_t total = __shfl_sync(0xffffffffu, inc, 31);
     const uint32_t off = inc - deg;
+    constexpr int kSteps = (int)kEmitSteps;
+    // Virtual ranks, the 32 rows in one rank and none of them a hub row (the
+    // common case): the rows' entries are one contiguous range, and an entry
+    // is kept only if it leaves the rank, which needs no row.  Each step
+    // loads and tests 32 entries; only a step that keeps some (a few in a
+    // hundred on the hyperbolic graph) finds the rows of its entries.
+    const uint32_t lo0 = __shfl_sync(0xffffffffu, lo, 0), hi0 = __shfl_sync(0xffffffffu, hi, 0);
+    if (part && !__any_sync(0xffffffffu, hub || (v < n && (lo != lo0 || hi != hi0)))) {
+      const uint64_t base = ((uint64_t)__shfl_sync(0xffffffffu, (uint32_t)(eb >> 32), 0) << 32) |
+                            __shfl_sync(0xffffffffu, (uint32_t)eb, 0);
+      for (uint32_t f0 = 0; f0 < total; f0 += 32 * kSteps) {
+        uint32_t us[kSteps];
+#pragma unroll
+        for (int q = 0; q < kSteps; ++q) {
+          const uint32_t f = f0 + 32 * q + lane;
+          us[q] = f < total ? load_id(col, base + f) : lo0;  // past the range: inside the rank
+        }
+#pragma unroll
+        for (int q = 0; q < kSteps; ++q) {
+          if (f0 + 32 * q >= total) break;  // warp-uniform
+          const uint32_t u = us[q];
+          const bool out = u < lo0 || u >= hi0;
+          if (!__any_sync(0xffffffffu, out)) continue;
+          const uint32_t f = f0 + 32 * q + lane;
+          int r = 0;
+#pragma unroll
+          for (int step = 16; step; step >>= 1) {
+            const uint32_t o = __shfl_sync(0xffffffffu, off, r + step);
+            if (o <= f) r += step;
+          }
+          const uint32_t cvr = __shfl_sync(0xffffffffu, cv, r);
+          bool keep = false;
+          uint64_t key = 0;
+          if (out) {
+            const uint32_t cu = cl[u];
+            key = ((uint64_t)cvr << b) | cu;
+            keep = cu != cvr;
+          }
+          st.put(keep, key, lane);
+        }
+        if (st.fill >= st.trigger) st.flush(lane, keys, cnt);
+      }
+      continue;
+    }
     // four steps of 32 entries at a time: their loads are issued together
     // (one load in flight per warp left the pass latency-bound)
-    constexpr int kSteps = (int)kEmitSteps;
     for (uint32_t f0 = 0; f0 < total; f0 += 32 * kSteps) {
       uint32_t us[kSteps];
       int rs[kSteps];
