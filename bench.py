@@ -588,8 +588,8 @@ def workload_serve(args):
     n log-uniform in [2^10, 2^22], degree uniform in [1, 16]) through the
     continuous-batching server, against the plain path (one cc_gpu_run per
     request with host buffers) on the same requests.  The pool of distinct
-    graphs is built by the device generators (requests arrive as host CSRs,
-    so each is copied back once); the requests draw from it."""
+    graphs is built by the device generators and kept in page-locked host
+    memory (requests arrive as host CSRs); the requests draw from it."""
     import torch
     import components_gb300 as cc
     from components_gb300.serve import Server
@@ -607,7 +607,7 @@ def workload_serve(args):
             D = cc.gen_grid_device(side, side, 0.5, seed=1000 + i)
         else:
             D = cc.gen_rhg_device(n, d, 2.6, seed=1000 + i)
-        pool.append(_to_host(D))
+        pool.append(_to_host(D).pinned())  # page-locked: both paths copy at the link's rate
         del D
     torch.cuda.empty_cache()
     gen_s = time.time() - t0
