@@ -287,8 +287,12 @@ int shortcut_propagate(const Csr &g, uint32_t *lab, uint32_t hitters, int max_ro
     cudaEvent_t t0 = c.tic(s);
     k_sc_min<<<grid, kBlock, 0, s>>>(g.n, g.rp, col, f, nf, updb.as<uint32_t>());
     CCG_LAUNCH_CHECK();
+    c.toc(s, "sc_min", t0, 8 * (g.n + 1) + g.m * 4 + g.m * 4 + 2 * g.n * 4);
+    cudaEvent_t t0p = c.tic(s);
     k_sc_min_pieces<<<num_sms() * 8, kBlock, 0, s>>>(g.rp, col, rpc, f, nf, updb.as<uint32_t>());
     CCG_LAUNCH_CHECK();
+    c.toc(s, "sc_min_pieces", t0p, 0);
+    cudaEvent_t t0j = c.tic(s);
     if (hitters) {
       CCG_CUDA(cudaMemsetAsync(cnt.p, 0, 4 * g.n, s));
       k_sc_count<<<grid, kBlock, 0, s>>>(g.n, nf, cnt.as<uint32_t>());
@@ -302,7 +306,7 @@ int shortcut_propagate(const Csr &g, uint32_t *lab, uint32_t hitters, int max_ro
     k_sc_jump<<<grid, kBlock, 0, s>>>(g.n, f, nf, updb.as<uint32_t>(),
                                       hitters ? heavy.as<uint8_t>() : nullptr, dev_flag);
     CCG_LAUNCH_CHECK();
-    c.toc(s, "shortcut_round", t0, 8 * (g.n + 1) + g.m * 4 + g.m * 4 + 2 * g.n * 4 + 4 * g.n * 4 + 4 * g.n);
+    c.toc(s, "sc_jump", t0j, 4 * g.n * 4 + 4 * g.n);
     CCG_CUDA(cudaMemcpyAsync((void *)host_flag, dev_flag, sizeof(int), cudaMemcpyDeviceToHost, s));
     CCG_CUDA(cudaStreamSynchronize(s));
     ++rounds;
