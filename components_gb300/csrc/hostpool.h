@@ -110,9 +110,12 @@ struct HostStager {
     }
     return pinned;
   }
+  // Three quarters of the host cores: the calling thread waits on the device
+  // while the workers encode, and a fully subscribed host left a worker
+  // descheduled now and then (a solve then waited 30-50 ms for its chunk).
   static unsigned workers() {
     const unsigned hc = std::thread::hardware_concurrency();
-    return hc > 1 ? hc - 1 : 0;
+    return hc > 2 ? hc * 3 / 4 - 1 : 0;
   }
 };
 
