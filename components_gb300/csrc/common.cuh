@@ -247,8 +247,9 @@ __global__ void k_row_pieces(uint64_t n, const uint64_t *__restrict__ rp, uint64
 // The sweeps (label and shortcut rounds, decomposition relaxation, local
 // contraction) take, for a row's entries [b, e), the minimum of a value
 // gathered at each neighbour.  One thread walks its row four entries at a
-// time: the four id loads, then the four gathers, are independent, so each
-// thread keeps four dependent load chains in flight instead of one.  (A
+// time: one 16-byte load of four ids (from the row's first 16-byte boundary
+// on), then four independent gathers, so each thread keeps four dependent
+// load chains in flight instead of one.  (A
 // flattened 32-rows-per-warp stream was measured slower on the hyperbolic
 // graph: its row search and segmented minimum cost about 20 shuffles per 32
 // entries and left the kernel bound on the load/store pipe, while a thread's
@@ -257,10 +258,14 @@ template <class V, class Gather>
 __device__ __forceinline__ V row_min_ilp(const uint32_t *__restrict__ col, uint64_t b, uint64_t e,
                                          V best, Gather gather) {
   uint64_t j = b;
+  // ids one at a time up to a 16-byte boundary, then four per load
+  for (; j < e && (reinterpret_cast<uintptr_t>(col + j) & 15u); ++j) {
+    const V x = gather(__ldg(col + j));
+    best = x < best ? x : best;
+  }
   for (; j + 4 <= e; j += 4) {
-    const uint32_t u0 = __ldg(col + j), u1 = __ldg(col + j + 1), u2 = __ldg(col + j + 2),
-                   u3 = __ldg(col + j + 3);
-    const V x0 = gather(u0), x1 = gather(u1), x2 = gather(u2), x3 = gather(u3);
+    const uint4 u = __ldg(reinterpret_cast<const uint4 *>(col + j));
+    const V x0 = gather(u.x), x1 = gather(u.y), x2 = gather(u.z), x3 = gather(u.w);
     const V a = x0 < x1 ? x0 : x1, c = x2 < x3 ? x2 : x3, m = a < c ? a : c;
     best = m < best ? m : best;
   }
