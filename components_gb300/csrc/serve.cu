@@ -231,7 +231,6 @@ struct Server {
     CCG_CUDA(cudaMemsetAsync(r->lab.as<uint32_t>() + g.n, 0, 4, copy_stream));
     CCG_CUDA(cudaEventCreateWithFlags(&r->copied, cudaEventDisableTiming));
     CCG_CUDA(cudaEventRecord(r->copied, copy_stream));
-    if (!small(g)) r->tu = schedule(g);
   }
 
   // A request that could not be launched: done, reported as failed by collect.
@@ -524,6 +523,10 @@ int cc_serve_submit(cc_server *h, const cc_csr *g, uint64_t *ticket) {
   if (r->need > s.cfg.hbm_budget_bytes) return CC_ERR_BUSY;
   r->t_submit = now_s();
   r->inject = s.inject_next.exchange(0);
+  // the hook schedule of a large graph is host work on the request's own
+  // CSR: done here, on the client's thread, it stays off the worker that
+  // admits, stages and launches for every client
+  if (!s.small(*g)) r->tu = Server::schedule(*g);
   {
     std::lock_guard<std::mutex> lk(s.mu);
     r->id = s.next_id++;

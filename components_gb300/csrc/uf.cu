@@ -258,18 +258,22 @@ struct PieceSink {
 // passes.
 constexpr uint32_t kAffRounds = 2;
 
-// Entry of a row of d entries that link round r uses (r < min(d, kAffRounds)):
-// the row's first entries.  On sorted rows these are the smallest neighbour
-// ids, which on hyperbolic graphs are often hubs: the link rounds then already
-// join the giant component (entries spread through the row were measured to
-// leave it in pieces, and the remaining pass then does most of the work).
-__host__ __device__ __forceinline__ uint64_t link_pos(uint64_t d, uint32_t r) {
-  (void)d;
-  return r;
+// Entry of row v (d entries) that link round r uses (r < min(d, kAffRounds)):
+// even rows take their first entries, odd rows their last ones.  The last
+// entries of row 2k-1 and the first entries of row 2k lie on both sides of
+// the offset rp[2k], in the same sector, so a pair of rows costs one sector of
+// ids instead of one each: the link pass reads about half of the id array's
+// sectors.  (Every row's first entries were used before; on sorted rows of a
+// hyperbolic graph the first entries often lead to hubs, and a CPU simulation
+// of the 2^22 graph leaves 7.9 k vertices outside the giant component after
+// the alternating link rounds against 24.4 k with the first entries; entries
+// spread through each row had left the giant component in pieces.)
+__host__ __device__ __forceinline__ uint64_t link_pos(uint64_t v, uint64_t d, uint32_t r) {
+  return (v & 1) ? d - 1 - r : (uint64_t)r;
 }
-__host__ __device__ __forceinline__ bool is_link_pos(uint64_t d, uint64_t j) {
+__host__ __device__ __forceinline__ bool is_link_pos(uint64_t v, uint64_t d, uint64_t j) {
   for (uint32_t r = 0; r < kAffRounds && r < d; ++r)
-    if (link_pos(d, r) == j) return true;
+    if (link_pos(v, d, r) == j) return true;
   return false;
 }
 
@@ -281,7 +285,7 @@ __global__ void k_aff_link(uint64_t n, uint64_t m, const uint64_t *__restrict__ 
        v += (uint64_t)gridDim.x * blockDim.x) {
     Row row;
     if (!load_row(rp, v, m, err, row) || row.e - row.b <= r) continue;
-    const uint64_t u = (uint64_t)__ldg(col + row.b + link_pos(row.e - row.b, r));
+    const uint64_t u = (uint64_t)__ldg(col + row.b + link_pos(v, row.e - row.b, r));
     if (u >= n) {
       set_err(err, kErrBadId);
       continue;
@@ -387,7 +391,7 @@ __global__ void k_aff_rest(uint64_t n, uint64_t m, const uint64_t *__restrict__ 
     uint32_t lo = 0, hi = 0xffffffffu;  // v's rank
     if (PART) pm.bounds((uint32_t)v, lo, hi);
     for (uint64_t k = row.b; k < row.e; ++k) {
-      if (is_link_pos(row.e - row.b, k - row.b)) continue;  // linked already
+      if (is_link_pos(v, row.e - row.b, k - row.b)) continue;  // linked already
       uint64_t u = (uint64_t)__ldg(col + k);
       if (u >= n) {
         set_err(err, kErrBadId);
@@ -437,7 +441,7 @@ __global__ void k_hub_pieces(uint64_t n, uint64_t m, const uint64_t *__restrict_
       }
       if (LESS) {
         if (u < v && (uint32_t)u >= lo) uf_union(p, v, (uint32_t)u);
-      } else if (!is_link_pos(re - rb, k - rb)) {  // the link rounds took those
+      } else if (!is_link_pos(v, re - rb, k - rb)) {  // the link rounds took those
         if ((uint32_t)u >= lo && (uint32_t)u < hi) uf_union(p, v, (uint32_t)u);
       }
     }
@@ -661,7 +665,7 @@ __global__ void __launch_bounds__(1024, 2)
         for (uint32_t r = 0; r < R; ++r)
 #pragma unroll
           for (uint32_t j = 0; j < (uint32_t)LINK; ++j)
-            id[r][j] = j < deg[r] ? __ldg(col + rb[r] + link_pos(re[r] - rb[r], j)) : (T)0;
+            id[r][j] = j < deg[r] ? __ldg(col + rb[r] + link_pos(t0 + g0 + 32 * r + lane, re[r] - rb[r], j)) : (T)0;
 #pragma unroll
         for (uint32_t r = 0; r < R; ++r) {
           const uint32_t i = g0 + 32 * r + lane;
@@ -861,7 +865,7 @@ __global__ void k_cut_sample(uint64_t n, uint64_t m, const uint64_t *__restrict_
     if (e < b || e > m) continue;
     // the link-round entries of the row
     for (uint32_t r = 0; r < kAffRounds && r < e - b; ++r) {
-      const uint64_t u = (uint64_t)__ldg(col + b + link_pos(e - b, r));
+      const uint64_t u = (uint64_t)__ldg(col + b + link_pos(v, e - b, r));
       if (u >= n || u == v) continue;
       ++ltot;
       lcross += u / tile != v / tile;
@@ -1536,7 +1540,7 @@ HostShares host_shares(const uint64_t *rp, const void *col, int idb, uint64_t n,
     const uint64_t b = rp[v], e = rp[v + 1];
     if (e < b || e > m) continue;  // malformed rows are reported by the kernels
     for (uint32_t r = 0; r < kAffRounds && r < e - b; ++r) {
-      const uint64_t u = id(b + link_pos(e - b, r));
+      const uint64_t u = id(b + link_pos(v, e - b, r));
       if (u >= n || u == v) continue;
       ++ltot;
       lcross += u / tile != v / tile;
