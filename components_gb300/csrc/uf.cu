@@ -259,17 +259,18 @@ struct PieceSink {
 constexpr uint32_t kAffRounds = 2;
 
 // Entry of row v (d entries) that link round r uses (r < min(d, kAffRounds)):
-// even rows take their first entries, odd rows their last ones.  The last
-// entries of row 2k-1 and the first entries of row 2k lie on both sides of
-// the offset rp[2k], in the same sector, so a pair of rows costs one sector of
-// ids instead of one each: the link pass reads about half of the id array's
-// sectors.  (Every row's first entries were used before; on sorted rows of a
-// hyperbolic graph the first entries often lead to hubs, and a CPU simulation
-// of the 2^22 graph leaves 7.9 k vertices outside the giant component after
-// the alternating link rounds against 24.4 k with the first entries; entries
-// spread through each row had left the giant component in pieces.)
+// the row's first entries.  On sorted rows these are the smallest neighbour
+// ids, which on hyperbolic graphs are often hubs: the link rounds then already
+// join the giant component (entries spread through the row were measured to
+// leave it in pieces, and the remaining pass then does most of the work).
+// Alternating by row parity (odd rows their last entries, so that two rows
+// share the sector of ids they read) cut the pass's DRAM bytes by only 6 % and
+// made it 21 % slower: a larger neighbour cannot take the one-CAS hook and
+// goes through the union queue.
 __host__ __device__ __forceinline__ uint64_t link_pos(uint64_t v, uint64_t d, uint32_t r) {
-  return (v & 1) ? d - 1 - r : (uint64_t)r;
+  (void)v;
+  (void)d;
+  return r;
 }
 __host__ __device__ __forceinline__ bool is_link_pos(uint64_t v, uint64_t d, uint64_t j) {
   for (uint32_t r = 0; r < kAffRounds && r < d; ++r)
