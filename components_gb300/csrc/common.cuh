@@ -160,6 +160,18 @@ inline unsigned grid_for(uint64_t work, int block = kBlock, unsigned cap = num_s
   return (unsigned)g;
 }
 
+// One CTA per resident slot (the occupancy of `kernel` at `block` threads and
+// its static shared memory on every SM), at most one per `block` rows of
+// work: for kernels whose CTAs each walk one contiguous range of the rows.
+template <class K>
+inline unsigned resident_grid(K kernel, int block, uint64_t work) {
+  int per_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, block, 0) != cudaSuccess ||
+      per_sm <= 0)
+    per_sm = 1;
+  return grid_for(work, block, (unsigned)(per_sm * num_sms()));
+}
+
 // ---- device helpers --------------------------------------------------------
 
 // Loads that bypass L1 so that values written by other SMs during the same
@@ -209,6 +221,20 @@ __host__ __device__ __forceinline__ uint64_t mix64(uint64_t z) {
 }
 __host__ __device__ __forceinline__ uint64_t hash3(uint64_t seed, uint64_t a, uint64_t b) {
   return mix64(mix64(mix64(seed) ^ a) ^ (b * 0xd6e8feb86659fd93ull));
+}
+
+// a[l] = min(a[l], x) for the lanes with act set, called by all 32 lanes of
+// the warp: lanes with the same l are merged first (one atomic per distinct l),
+// and the atomic is skipped when a[l] already holds x or less.  Entries only
+// decrease while the kernel runs, so a stale read is never below the true
+// entry and a skip it allows is right; the read goes through L1 so that a
+// label shared by many rows is not one L2 line every warp reads.
+__device__ __forceinline__ void warp_min_to(uint32_t *a, bool act, uint32_t l, uint32_t x) {
+  const unsigned am = __ballot_sync(0xffffffffu, act);
+  if (!act) return;
+  const unsigned peers = __match_any_sync(am, l);
+  const uint32_t mn = __reduce_min_sync(peers, x);
+  if ((threadIdx.x & 31) == (unsigned)(__ffs(peers) - 1) && mn < a[l]) atomicMin(a + l, mn);
 }
 
 // Warp-aggregated "any lane set" flag: one atomicOr per warp.

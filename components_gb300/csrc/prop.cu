@@ -60,18 +60,37 @@ __global__ void k_labels_round_pieces(const uint64_t *__restrict__ rp,
 //                              answers are applied to every u with nf[u]
 //                              equal to the target
 //   CheckConvergence (:359-376): stop when nf == f everywhere.
+// The update to label l is the minimum over the rows labelled l.  From the
+// second round on most rows share a few labels (a hundred thousand rows per
+// label on a 2^20-vertex hyperbolic graph), so the updates go through
+// warp_min_to: one atomic per distinct label in a warp, none when the entry
+// already holds as little.
+// act (null: every row) marks the rows with a neighbour whose label changed
+// in the previous round.  A row without one keeps its label and sends no
+// update: its neighbours' minimum m is the previous round's, that round set
+// nf[v] <= m, and the jump only lowered it, so min(f[v], m) = f[v].
+__device__ __forceinline__ bool bit_of(const uint32_t *bits, uint64_t v) {
+  return (bits[v >> 5] >> (v & 31)) & 1u;
+}
 __global__ void k_sc_min(uint64_t n, const uint64_t *__restrict__ rp,
                          const uint32_t *__restrict__ col, const uint32_t *__restrict__ f,
-                         uint32_t *__restrict__ nf, uint32_t *__restrict__ upd) {
-  for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < n;
+                         uint32_t *__restrict__ nf, uint32_t *upd,
+                         const uint32_t *__restrict__ act) {
+  const uint64_t span = (n + 31) / 32 * 32;  // warp-uniform trip count
+  for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < span;
        v += (uint64_t)gridDim.x * blockDim.x) {
-    const uint64_t b = __ldg(rp + v), e = __ldg(rp + v + 1);
-    const uint32_t l = f[v];
-    uint32_t best = l;
-    if (e - b <= kRowLimit)  // longer rows: k_sc_min_pieces folds their neighbours in
-      best = row_min_ilp<uint32_t>(col, b, e, l, [&](uint32_t u) { return __ldg(f + u); });
-    nf[v] = best;
-    if (best < l) atomicMin(upd + l, best);
+    uint32_t l = 0, best = 0;
+    if (v < n) {
+      l = f[v];
+      best = l;
+      if (!act || bit_of(act, v)) {
+        const uint64_t b = __ldg(rp + v), e = __ldg(rp + v + 1);
+        if (e - b <= kRowLimit)  // longer rows: k_sc_min_pieces folds their neighbours in
+          best = row_min_ilp<uint32_t>(col, b, e, l, [&](uint32_t u) { return __ldg(f + u); });
+      }
+      nf[v] = best;
+    }
+    warp_min_to(upd, best < l, l, best);
   }
 }
 
@@ -81,7 +100,7 @@ __global__ void k_sc_min(uint64_t n, const uint64_t *__restrict__ rp,
 // pieces are the row's minimum, so nf and upd end as with one pass per row.
 __global__ void k_sc_min_pieces(const uint64_t *__restrict__ rp, const uint32_t *__restrict__ col,
                                 RowPieces rpc, const uint32_t *__restrict__ f, uint32_t *nf,
-                                uint32_t *upd) {
+                                uint32_t *upd, const uint32_t *__restrict__ act) {
   const unsigned lane = threadIdx.x & 31;
   const uint64_t warp = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
   const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
@@ -90,6 +109,7 @@ __global__ void k_sc_min_pieces(const uint64_t *__restrict__ rp, const uint32_t 
     uint32_t v;
     uint64_t b, e;
     row_piece(rpc, rp, h, v, b, e);
+    if (act && !bit_of(act, v)) continue;  // warp-uniform: one row per piece
     uint32_t best =
         piece_min_ilp<uint32_t>(col, b, e, lane, kNone, [&](uint32_t u) { return __ldg(f + u); });
     best = __reduce_min_sync(0xffffffffu, best);
@@ -97,7 +117,7 @@ __global__ void k_sc_min_pieces(const uint64_t *__restrict__ rp, const uint32_t 
       const uint32_t l = f[v];
       if (best < l) {
         atomicMin(nf + v, best);
-        atomicMin(upd + l, best);
+        if (best < upd[l]) atomicMin(upd + l, best);  // entries only decrease
       }
     }
   }
@@ -118,24 +138,80 @@ __global__ void k_sc_heavy(uint64_t n, const uint32_t *__restrict__ cnt, uint32_
     if (cnt[v] > thresh) heavy[v] = 1;
 }
 
+// The jump, the labels that changed (one bit per vertex in chg, whole words
+// written by a warp) and their number (one atomic per block into *nchanged).
 __global__ void k_sc_jump(uint64_t n, const uint32_t *__restrict__ f, uint32_t *__restrict__ nf,
                           const uint32_t *__restrict__ upd, const uint8_t *__restrict__ heavy,
-                          int *flag) {
-  int changed = 0;
-  for (uint64_t u = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; u < n;
+                          uint32_t *__restrict__ chg, unsigned int *nchanged) {
+  __shared__ unsigned int block_changed;
+  if (threadIdx.x == 0) block_changed = 0;
+  __syncthreads();
+  const uint64_t span = (n + 31) / 32 * 32;  // warp-uniform trip count, 32-aligned lanes
+  for (uint64_t u = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; u < span;
        u += (uint64_t)gridDim.x * blockDim.x) {
-    uint32_t t = nf[u];
-    uint32_t r = t;
-    if (!heavy || heavy[t]) {
-      uint32_t a = f[t];  // request l(l'(u)) answered by the owner of l'(u)
-      r = a < r ? a : r;
+    bool changed = false;
+    if (u < n) {
+      const uint32_t t = nf[u];
+      uint32_t r = t;
+      if (!heavy || heavy[t]) {
+        const uint32_t a = f[t];  // request l(l'(u)) answered by the owner of l'(u)
+        r = a < r ? a : r;
+      }
+      const uint32_t up = upd[t];  // update messages addressed to target t
+      r = up < r ? up : r;
+      nf[u] = r;
+      changed = r != f[u];
     }
-    uint32_t up = upd[t];  // update messages addressed to target t
-    r = up < r ? up : r;
-    nf[u] = r;
-    changed |= (r != f[u]);
+    const unsigned b = __ballot_sync(0xffffffffu, changed);
+    if ((threadIdx.x & 31) == 0) {
+      chg[u >> 5] = b;
+      if (b) atomicAdd(&block_changed, (unsigned)__popc(b));
+    }
   }
-  warp_flag(changed, flag);
+  __syncthreads();
+  if (threadIdx.x == 0 && block_changed) atomicAdd(nchanged, block_changed);
+}
+
+// act |= the neighbours of every vertex whose bit is set in chg.  A row's ids
+// are sorted, so runs of neighbours in one 32-vertex word are merged into
+// one atomic; rows above kRowLimit entries go to k_sc_push_pieces.
+__global__ void k_sc_push(uint64_t n, const uint64_t *__restrict__ rp,
+                          const uint32_t *__restrict__ col, const uint32_t *__restrict__ chg,
+                          uint32_t *act) {
+  for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < n;
+       v += (uint64_t)gridDim.x * blockDim.x) {
+    if (!bit_of(chg, v)) continue;
+    const uint64_t b = __ldg(rp + v), e = __ldg(rp + v + 1);
+    if (e - b > kRowLimit) continue;
+    uint32_t word = kNone, bits = 0;
+    for (uint64_t k = b; k < e; ++k) {
+      const uint32_t w = __ldg(col + k);
+      if ((w >> 5) != word) {
+        if (bits) atomicOr(act + word, bits);
+        word = w >> 5;
+        bits = 0;
+      }
+      bits |= 1u << (w & 31);
+    }
+    if (bits) atomicOr(act + word, bits);
+  }
+}
+__global__ void k_sc_push_pieces(const uint64_t *__restrict__ rp, const uint32_t *__restrict__ col,
+                                 RowPieces rpc, const uint32_t *__restrict__ chg, uint32_t *act) {
+  const unsigned lane = threadIdx.x & 31;
+  const uint64_t warp = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
+  const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+  const uint64_t ni = min((uint64_t)*rpc.count, rpc.cap);
+  for (uint64_t h = warp; h < ni; h += nwarps) {
+    uint32_t v;
+    uint64_t b, e;
+    row_piece(rpc, rp, h, v, b, e);
+    if (!bit_of(chg, v)) continue;
+    for (uint64_t k = b + lane; k < e; k += 32) {
+      const uint32_t w = __ldg(col + k);
+      atomicOr(act + (w >> 5), 1u << (w & 31));
+    }
+  }
 }
 
 // ---- composition / canonicalisation -----------------------------------------
@@ -266,7 +342,9 @@ int shortcut_propagate(const Csr &g, uint32_t *lab, uint32_t hitters, int max_ro
   if (g.n == 0) return 0;
   const uint32_t *col = static_cast<const uint32_t *>(g.col);
   unsigned grid = grid_for(g.n, kBlock, num_sms() * 32);
-  DevBuf nfb(4 * g.n, s, pool), updb(4 * g.n, s, pool);
+  const uint64_t words = (g.n + 31) / 32;
+  DevBuf nfb(4 * g.n, s, pool), updb(4 * g.n, s, pool), chgb(4 * words, s, pool),
+      actb(4 * words, s, pool);
   const uint64_t cap = row_pieces_cap(g.m, kRowLimit);
   DevBuf items(8 * cap, s, pool), npieces(4, s, pool);
   const RowPieces rpc{items.as<uint2>(), cap, npieces.as<unsigned int>()};
@@ -280,16 +358,32 @@ int shortcut_propagate(const Csr &g, uint32_t *lab, uint32_t hitters, int max_ro
   k_row_pieces<<<grid, kBlock, 0, s>>>(g.n, g.rp, kRowLimit, rpc);
   CCG_LAUNCH_CHECK();
   uint32_t *f = lab, *nf = nfb.as<uint32_t>();
+  const uint64_t min_bytes = 8 * (g.n + 1) + g.m * 4 + g.m * 4 + 2 * g.n * 4;
   int rounds = 0;
+  bool sparse = false;  // visit only the rows next to a label changed last round
   for (;;) {
     if (rounds >= max_rounds) return -1;
     CCG_CUDA(cudaMemsetAsync(updb.p, 0xff, 4 * g.n, s));
+    if (sparse) {
+      CCG_CUDA(cudaMemsetAsync(actb.p, 0, 4 * words, s));
+      cudaEvent_t tp = c.tic(s);
+      k_sc_push<<<grid, kBlock, 0, s>>>(g.n, g.rp, col, chgb.as<uint32_t>(), actb.as<uint32_t>());
+      CCG_LAUNCH_CHECK();
+      k_sc_push_pieces<<<num_sms() * 8, kBlock, 0, s>>>(g.rp, col, rpc, chgb.as<uint32_t>(),
+                                                        actb.as<uint32_t>());
+      CCG_LAUNCH_CHECK();
+      c.toc(s, "sc_push", tp, 0);
+    }
+    const uint32_t *act = sparse ? actb.as<uint32_t>() : nullptr;
     cudaEvent_t t0 = c.tic(s);
-    k_sc_min<<<grid, kBlock, 0, s>>>(g.n, g.rp, col, f, nf, updb.as<uint32_t>());
+    k_sc_min<<<grid, kBlock, 0, s>>>(g.n, g.rp, col, f, nf, updb.as<uint32_t>(), act);
     CCG_LAUNCH_CHECK();
-    c.toc(s, "sc_min", t0, 8 * (g.n + 1) + g.m * 4 + g.m * 4 + 2 * g.n * 4);
+    // algorithmic bytes of a round over every row (a round over the active
+    // rows only is not counted)
+    c.toc(s, "sc_min", t0, sparse ? 0 : min_bytes);
     cudaEvent_t t0p = c.tic(s);
-    k_sc_min_pieces<<<num_sms() * 8, kBlock, 0, s>>>(g.rp, col, rpc, f, nf, updb.as<uint32_t>());
+    k_sc_min_pieces<<<num_sms() * 8, kBlock, 0, s>>>(g.rp, col, rpc, f, nf, updb.as<uint32_t>(),
+                                                     act);
     CCG_LAUNCH_CHECK();
     c.toc(s, "sc_min_pieces", t0p, 0);
     cudaEvent_t t0j = c.tic(s);
@@ -304,7 +398,8 @@ int shortcut_propagate(const Csr &g, uint32_t *lab, uint32_t hitters, int max_ro
     }
     CCG_CUDA(cudaMemsetAsync(dev_flag, 0, sizeof(int), s));
     k_sc_jump<<<grid, kBlock, 0, s>>>(g.n, f, nf, updb.as<uint32_t>(),
-                                      hitters ? heavy.as<uint8_t>() : nullptr, dev_flag);
+                                      hitters ? heavy.as<uint8_t>() : nullptr, chgb.as<uint32_t>(),
+                                      reinterpret_cast<unsigned int *>(dev_flag));
     CCG_LAUNCH_CHECK();
     c.toc(s, "sc_jump", t0j, 4 * g.n * 4 + 4 * g.n);
     CCG_CUDA(cudaMemcpyAsync((void *)host_flag, dev_flag, sizeof(int), cudaMemcpyDeviceToHost, s));
@@ -312,11 +407,16 @@ int shortcut_propagate(const Csr &g, uint32_t *lab, uint32_t hitters, int max_ro
     ++rounds;
     // min sweep (offsets, ids, one label gather per edge, own r/w) + jump
     // (own label, two gathers, write)
-    c.add(3, 8 * (g.n + 1) + g.m * 4 + g.m * 4 + 2 * g.n * 4 + 4 * g.n * 4 + 4 * g.n);
+    c.add(3, min_bytes + 4 * g.n * 4 + 4 * g.n);
     uint32_t *t = f;
     f = nf;
     nf = t;
-    if (*host_flag == 0) break;
+    const uint32_t changed = static_cast<uint32_t>(*host_flag);  // labels lowered this round
+    if (changed == 0) break;
+    // when few labels changed, the next round pushes a mark to their
+    // neighbours and visits only those rows (the first rounds lower nearly
+    // every label and run over all rows)
+    sparse = 16ull * changed <= g.n;
   }
   if (f != lab) CCG_CUDA(cudaMemcpyAsync(lab, f, 4 * g.n, cudaMemcpyDeviceToDevice, s));
   return rounds;

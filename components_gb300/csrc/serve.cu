@@ -206,10 +206,12 @@ struct Server {
   // their tile).
   static UfTuning schedule(const cc_csr &g) {
     UfTuning tu;
-    // 2048 rows: the shares are compared with 50 %, 25 % and 10 %, and the
-    // sample is host work on the admission path (8192 rows took 0.25 ms)
+    // 512 rows: the shares are compared with 50 %, 25 % and 10 % (a 512-row
+    // sample of rows with a few entries each is within about 2 % of them), and
+    // the sample runs on the submitting thread over a CSR that is cold in the
+    // host caches: 2048 rows cost about 0.4 ms a request there
     const HostShares sh = host_shares(g.row_ptr, g.col, (int)g.id_bytes, g.n, g.m_dir,
-                                      tu.tile_vertices, tu.hub_degree, 2048);
+                                      tu.tile_vertices, tu.hub_degree, 512);
     const uint64_t ws = 8 * (g.n + 1) + g.m_dir * (uint64_t)g.id_bytes + 4 * g.n;
     if (g.n >= 4ull * tu.tile_vertices && sh.tiles) tu.mode = kUfTiled;
     else if (ws <= (96ull << 20) && sh.few_hubs) tu.mode = kUfGlobal;

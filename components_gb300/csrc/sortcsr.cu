@@ -100,96 +100,84 @@ __global__ void k_radix_scatter(const uint64_t *__restrict__ keys, uint64_t *__r
 
 // ---- contraction -----------------------------------------------------------
 
-// Keys a CTA has written already: an open-addressing set in shared memory.
+// Keys a CTA has written already: a direct-mapped set in shared memory.
 // Cut edges between two clusters repeat many times on graphs with large
 // components (every edge between two of them gives the same key), so dropping
-// repeats before they are written shrinks the sort that follows.  A key that
-// finds no free slot in a few probes is written anyway, so the set only ever
-// drops true repeats.  ~0 marks a free slot and is never a key (cluster ids
-// are below n < 2^32, so both halves cannot be all ones).
+// repeats before they are written shrinks the sort that follows.  A key
+// replaces whatever its slot held, so the set follows the CTA's current rows
+// (each CTA walks one contiguous range of rows, whose keys repeat within a few
+// hundred rows) instead of filling up with the first keys it saw.  A key is
+// dropped only when its slot already holds it, which means the CTA has
+// written it before; a key evicted and seen again is written twice and the
+// sort drops the repeat.  ~0 marks a free slot and is never a key (cluster
+// ids are below n < 2^32, so both halves cannot be all ones).
 constexpr uint32_t kEmitSet = 2048;  // slots (16 KB)
 __device__ __forceinline__ void emit_set_clear(unsigned long long *set) {
   for (uint32_t i = threadIdx.x; i < kEmitSet; i += blockDim.x) set[i] = ~0ull;
   __syncthreads();
 }
 __device__ __forceinline__ bool emit_set_seen(unsigned long long *set, uint64_t key) {
-  uint32_t h = (uint32_t)mix64(key) & (kEmitSet - 1);
-#pragma unroll 1
-  for (int probe = 0; probe < 8; ++probe) {
-    const unsigned long long cur = atomicCAS(set + h, ~0ull, (unsigned long long)key);
-    if (cur == ~0ull) return false;  // inserted: the first time this CTA sees the key
-    if (cur == key) return true;
-    h = (h + 1) & (kEmitSet - 1);
-  }
-  return false;
+  const uint32_t h = (uint32_t)mix64(key) & (kEmitSet - 1);
+  if (set[h] == key) return true;  // read first: a repeat costs no atomic
+  return atomicExch(set + h, (unsigned long long)key) == key;
 }
 
 // Kept keys of one warp, staged in the warp's own shared-memory buffer and
 // written out with one global reservation per full buffer (one atomic per
 // warp step on the single counter would serialise where keys are many).
-// Repeats are dropped through the CTA's set when a buffer is written out, not
-// in the edge loop.  A warp's first buffer is written out early, at
-// kEmitTrial keys: unless a quarter of them equal the key staged before them,
-// the warp never consults the set (its keys come from small clusters, and the
-// set's 64-bit compare-and-swaps would only cost time); a warp that stops
-// finding repeats in the set stops too.  Warps never wait for one another.
+// Repeats are dropped twice: lanes of one step holding the same key keep one
+// copy (neighbouring rows of a cluster give the same key), and a buffer's keys
+// pass through the CTA's set when it is written out.  Warps never wait for
+// one another.
+__device__ __forceinline__ uint64_t shfl_up64(uint64_t x) {
+  const uint32_t lo = __shfl_up_sync(0xffffffffu, (uint32_t)x, 1);
+  const uint32_t hi = __shfl_up_sync(0xffffffffu, (uint32_t)(x >> 32), 1);
+  return ((uint64_t)hi << 32) | lo;
+}
 constexpr uint32_t kWarpKeys = 256;
 constexpr unsigned kEmitCtasPerSM = 32;
-constexpr uint32_t kEmitTrial = 64;
 constexpr uint32_t kEmitSteps = 4;  // 32-entry steps of k_emit between flush checks
+constexpr uint32_t kOutList = 160;  // per warp: entries that leave their rank, resolved together
 struct WarpKeys {
   uint64_t *buf;
   unsigned long long *set;
-  uint32_t steady;           // flush threshold after the trial
-  uint32_t fill = 0;         // warp-uniform
-  uint32_t trigger = kEmitTrial;  // flush once fill reaches this
-  bool dedup = true;         // warp-uniform
+  uint32_t trigger;   // flush once fill reaches this
+  uint32_t fill = 0;  // warp-uniform
   __device__ __forceinline__ void flush(unsigned lane, uint64_t *__restrict__ keys,
                                         unsigned long long *__restrict__ cnt) {
     __syncwarp();
-    uint32_t out = fill;
-    if (dedup && trigger == kEmitTrial) {
-      // the trial: keys equal to the one staged just before them predict
-      // repeats in the set; without them the keys come from small clusters
-      // and the set would only cost time
-      uint32_t reps = 0;
-      for (uint32_t k0 = 0; k0 < fill; k0 += 32) {
-        const uint32_t k = k0 + lane;
-        reps += __popc(__ballot_sync(0xffffffffu, k < fill && k > 0 && buf[k] == buf[k - 1]));
+    // survivors are packed in place: chunk k0's writes land below k0 + 32, in
+    // entries every lane has read already
+    uint32_t out = 0;
+    for (uint32_t k0 = 0; k0 < fill; k0 += 32) {
+      const uint32_t k = k0 + lane;
+      uint64_t key = 0;
+      bool keep = false;
+      if (k < fill) {
+        key = buf[k];
+        keep = !emit_set_seen(set, key);
       }
-      if (4 * reps < fill) dedup = false;
+      const unsigned m = __ballot_sync(0xffffffffu, keep);
+      if (keep) buf[out + __popc(m & ((1u << lane) - 1u))] = key;
+      out += __popc(m);
     }
-    if (dedup) {
-      // survivors are packed in place: chunk k0's writes land below k0 + 32,
-      // in entries every lane has read already
-      out = 0;
-      for (uint32_t k0 = 0; k0 < fill; k0 += 32) {
-        const uint32_t k = k0 + lane;
-        uint64_t key = 0;
-        bool keep = false;
-        if (k < fill) {
-          key = buf[k];
-          keep = !emit_set_seen(set, key);
-        }
-        const unsigned m = __ballot_sync(0xffffffffu, keep);
-        if (keep) buf[out + __popc(m & ((1u << lane) - 1u))] = key;
-        out += __popc(m);
-      }
-      __syncwarp();
-      if (4 * out > 3 * fill) dedup = false;
-    }
+    __syncwarp();
     unsigned long long pos0 = 0;
     if (lane == 0 && out) pos0 = atomicAdd(cnt, (unsigned long long)out);
     pos0 = __shfl_sync(0xffffffffu, pos0, 0);
     for (uint32_t k = lane; k < out; k += 32) keys[pos0 + k] = buf[k];
     __syncwarp();
     fill = 0;
-    trigger = steady;
   }
-  // one step of the warp: lanes with keep set add their key (the caller
-  // flushes at trigger, which leaves room for the steps that come before the
-  // next check)
+  // one step of the warp, all 32 lanes: the lanes with keep set add their key,
+  // except a lane whose key the lane before it also holds (lanes hold
+  // consecutive entries, and neighbouring entries of a cluster's rows give
+  // the same key).  The caller flushes at trigger, which leaves room for the
+  // steps that come before the next check.
   __device__ __forceinline__ void put(bool keep, uint64_t key, unsigned lane) {
+    const uint64_t prev = shfl_up64(key);
+    const bool prev_keep = __shfl_up_sync(0xffffffffu, keep, 1);
+    keep = keep && !(lane > 0 && prev_keep && prev == key);
     const unsigned m = __ballot_sync(0xffffffffu, keep);
     if (keep) buf[fill + __popc(m & ((1u << lane) - 1u))] = key;
     fill += __popc(m);
@@ -202,32 +190,57 @@ struct WarpKeys {
 // and walks their edges as one flattened, coalesced stream (lane k reads
 // entry k of the rows' concatenated adjacency; its row is the last lane whose
 // degree prefix sum is <= k), so skewed degrees keep every lane busy.  Rows
-// longer than hub_limit are left to k_emit_hubs.
+// longer than hub_limit are listed as (row, piece) items for k_emit_hubs,
+// which runs next on the same stream.
 template <class T>
 __global__ void __launch_bounds__(kBlock) k_emit(uint64_t n, const uint64_t *__restrict__ rp,
                                                  const T *__restrict__ col,
                                                  const uint32_t *__restrict__ cl, PartMap pm,
                                                  bool part, int b, uint64_t hub_limit,
+                                                 uint2 *__restrict__ hub_items, uint64_t hub_cap,
+                                                 unsigned int *__restrict__ n_hub_items,
                                                  uint64_t *__restrict__ keys,
                                                  unsigned long long *__restrict__ cnt) {
   __shared__ uint64_t wbuf[kBlock / 32][kWarpKeys];
+  __shared__ uint64_t wout[kBlock / 32][kOutList];
   __shared__ unsigned long long set[kEmitSet];
   const unsigned lane = lane_id(), wid = threadIdx.x >> 5;
   emit_set_clear(set);
   WarpKeys st{wbuf[wid], set, kWarpKeys - 32 * kEmitSteps};
-  const uint64_t warp = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
-  const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
-  for (uint64_t v0 = warp * 32; v0 < n; v0 += nwarps * 32) {
+  uint64_t *olist = wout[wid];
+  // the CTA's rows: one contiguous range (a multiple of 32 rows), so that the
+  // keys its set holds are those of its current rows
+  const uint64_t per = ((n + gridDim.x - 1) / gridDim.x + 31) / 32 * 32;
+  const uint64_t r1 = min(n, (blockIdx.x + 1) * per);
+  // each group's row offsets are loaded while the group before it is walked
+  uint64_t next_b = 0, next_e = 0;
+  if (blockIdx.x * per + 32 * wid + lane < n) {
+    next_b = __ldg(rp + blockIdx.x * per + 32 * wid + lane);
+    next_e = __ldg(rp + blockIdx.x * per + 32 * wid + lane + 1);
+  }
+  for (uint64_t v0 = blockIdx.x * per + 32 * wid; v0 < r1; v0 += blockDim.x) {
     const uint64_t v = v0 + lane;
     uint64_t eb = 0;
-    uint32_t deg = 0, cv = 0, lo = 0, hi = 0xffffffffu;  // lo, hi: v's rank when part
+    uint32_t deg = 0, lo = 0, hi = 0xffffffffu;  // lo, hi: v's rank when part
     bool hub = false;
+    const uint64_t cur_b = next_b, cur_e = next_e;
+    if (v0 + blockDim.x < r1 && v + blockDim.x < n) {
+      next_b = __ldg(rp + v + blockDim.x);
+      next_e = __ldg(rp + v + blockDim.x + 1);
+    }
     if (v < n) {
-      eb = __ldg(rp + v);
-      const uint64_t ee = __ldg(rp + v + 1);
-      if (ee - eb <= hub_limit) deg = (uint32_t)(ee - eb);
-      else hub = true;
-      cv = cl[v];
+      eb = cur_b;
+      const uint64_t ee = cur_e;
+      if (ee - eb <= hub_limit) {
+        deg = (uint32_t)(ee - eb);
+      } else {
+        // a long row becomes ceil(d / kEmitPiece) warp-sized work items
+        hub = true;
+        const uint32_t np = (uint32_t)((ee - eb + kEmitPiece - 1) / kEmitPiece);
+        const unsigned int slot = atomicAdd(n_hub_items, np);
+        for (uint32_t q = 0; q < np && (uint64_t)slot + q < hub_cap; ++q)
+          hub_items[slot + q] = make_uint2((uint32_t)v, q);
+      }
       if (part) pm.bounds((uint32_t)v, lo, hi);
     }
     uint32_t inc = deg;
@@ -248,6 +261,35 @@ __global__ void __launch_bounds__(kBlock) k_emit(uint64_t n, const uint64_t *__r
     if (part && !__any_sync(0xffffffffu, hub || (v < n && (lo != lo0 || hi != hi0)))) {
       const uint64_t base = ((uint64_t)__shfl_sync(0xffffffffu, (uint32_t)(eb >> 32), 0) << 32) |
                             __shfl_sync(0xffffffffu, (uint32_t)eb, 0);
+      // entries that leave the rank are listed as (offset, id) and resolved
+      // together (row search, both clusters, key) once per group, so that the
+      // group waits for one round of gathers instead of one per step
+      uint32_t on = 0;  // warp-uniform
+      auto drain = [&]() {
+        __syncwarp();
+        for (uint32_t k0 = 0; k0 < on; k0 += 32) {
+          const bool have = k0 + lane < on;
+          const uint64_t e = have ? olist[k0 + lane] : 0ull;
+          const uint32_t ff = (uint32_t)(e >> 32), u = (uint32_t)e;
+          int r = 0;
+#pragma unroll
+          for (int step = 16; step; step >>= 1) {
+            const uint32_t o = __shfl_sync(0xffffffffu, off, r + step);
+            if (o <= ff) r += step;
+          }
+          bool keep = false;
+          uint64_t key = 0;
+          if (have) {
+            const uint32_t cvr = cl[v0 + r], cu = cl[u];
+            key = ((uint64_t)cvr << b) | cu;
+            keep = cu != cvr;
+          }
+          st.put(keep, key, lane);
+          if (st.fill >= st.trigger) st.flush(lane, keys, cnt);
+        }
+        __syncwarp();
+        on = 0;
+      };
       for (uint32_t f0 = 0; f0 < total; f0 += 32 * kSteps) {
         uint32_t us[kSteps];
 #pragma unroll
@@ -257,31 +299,18 @@ __global__ void __launch_bounds__(kBlock) k_emit(uint64_t n, const uint64_t *__r
         }
 #pragma unroll
         for (int q = 0; q < kSteps; ++q) {
-          if (f0 + 32 * q >= total) break;  // warp-uniform
           const uint32_t u = us[q];
-          const bool out = u < lo0 || u >= hi0;
-          if (!__any_sync(0xffffffffu, out)) continue;
-          const uint32_t f = f0 + 32 * q + lane;
-          int r = 0;
-#pragma unroll
-          for (int step = 16; step; step >>= 1) {
-            const uint32_t o = __shfl_sync(0xffffffffu, off, r + step);
-            if (o <= f) r += step;
-          }
-          const uint32_t cvr = __shfl_sync(0xffffffffu, cv, r);
-          bool keep = false;
-          uint64_t key = 0;
-          if (out) {
-            const uint32_t cu = cl[u];
-            key = ((uint64_t)cvr << b) | cu;
-            keep = cu != cvr;
-          }
-          st.put(keep, key, lane);
+          const bool out = u < lo0 || u >= hi0;  // false past the range
+          const unsigned om = __ballot_sync(0xffffffffu, out);
+          if (out) olist[on + __popc(om & ((1u << lane) - 1u))] = ((uint64_t)(f0 + 32 * q + lane) << 32) | u;
+          on += __popc(om);
         }
-        if (st.fill >= st.trigger) st.flush(lane, keys, cnt);
+        if (on > kOutList - 32 * kSteps) drain();  // room for the next batch
       }
+      if (on) drain();
       continue;
     }
+    const uint32_t cv = v < n ? cl[v] : 0u;
     // four steps of 32 entries at a time: their loads are issued together
     // (one load in flight per warp left the pass latency-bound)
     for (uint32_t f0 = 0; f0 < total; f0 += 32 * kSteps) {
@@ -325,6 +354,131 @@ __global__ void __launch_bounds__(kBlock) k_emit(uint64_t n, const uint64_t *__r
   if (st.fill) st.flush(lane, keys, cnt);
 }
 
+// ---- the emit without virtual ranks: one thread per row ----------------------
+// Every entry then gathers its neighbour's cluster, as a sweep does, and most
+// keys repeat (local contraction's first level on the 2^20-vertex hyperbolic
+// graph: 56 % of the entries cross two clusters, 84 k distinct keys).  One
+// thread walks its row with 16-byte id loads and the gathers of a load in
+// flight, drops an entry inside its own cluster or in the cluster of the entry
+// it kept before, and stages the rest in its warp's buffer (one shared atomic
+// per group of lanes that stage together).  After each group of 32 rows the
+// warp passes its new keys through the CTA's set and keeps the survivors; they
+// are written out with one global reservation once 128 have gathered.  Warps
+// never wait for one another (a block-wide step per round of rows would hold
+// every row for the longest one).  Rows above kEmitRowLimit entries become hub
+// pieces.  Each CTA walks one contiguous range of rows, so its set holds the
+// keys of its rows.
+constexpr uint64_t kEmitRowLimit = 64;
+constexpr uint32_t kRowWarpKeys = 384;  // per warp: < 128 survivors + a group's new keys
+constexpr uint32_t kRowFlushAt = 128;
+
+__device__ __forceinline__ void stage_key(uint64_t key, uint64_t *wbuf, unsigned int *wfill,
+                                          uint64_t *__restrict__ keys,
+                                          unsigned long long *__restrict__ cnt) {
+  const unsigned am = __activemask();  // the lanes staging a key now
+  const unsigned lane = threadIdx.x & 31;
+  const int leader = __ffs(am) - 1;
+  unsigned int base = 0;
+  if ((int)lane == leader) base = atomicAdd(wfill, (unsigned)__popc(am));
+  base = __shfl_sync(am, base, leader);
+  const unsigned int slot = base + __popc(am & ((1u << lane) - 1u));
+  if (slot < kRowWarpKeys) wbuf[slot] = key;
+  else keys[atomicAdd(cnt, 1ull)] = key;  // the buffer is full: straight out (repeats allowed)
+}
+
+template <class T>
+__global__ void __launch_bounds__(kBlock) k_emit_rows(uint64_t n, const uint64_t *__restrict__ rp,
+                                                      const T *__restrict__ col,
+                                                      const uint32_t *__restrict__ cl, int b,
+                                                      uint2 *__restrict__ hub_items, uint64_t hub_cap,
+                                                      unsigned int *__restrict__ n_hub_items,
+                                                      uint64_t *__restrict__ keys,
+                                                      unsigned long long *__restrict__ cnt) {
+  __shared__ uint64_t wbufs[kBlock / 32][kRowWarpKeys];
+  __shared__ unsigned int wfills[kBlock / 32];
+  __shared__ unsigned long long set[kEmitSet];
+  const unsigned lane = lane_id(), wid = threadIdx.x >> 5;
+  uint64_t *wbuf = wbufs[wid];
+  unsigned int *wfill = &wfills[wid];
+  if (lane == 0) *wfill = 0;
+  emit_set_clear(set);  // synchronises the block
+  const uint64_t per = ((n + gridDim.x - 1) / gridDim.x + 31) / 32 * 32;
+  const uint64_t r1 = min(n, (blockIdx.x + 1) * per);
+  uint32_t kept = 0;  // warp-uniform: survivors at wbuf[0, kept)
+  for (uint64_t v0 = blockIdx.x * per + 32 * wid; v0 < r1; v0 += blockDim.x) {  // warp-uniform
+    const uint64_t v = v0 + lane;
+    if (v < r1) {
+      const uint64_t rb = __ldg(rp + v), re = __ldg(rp + v + 1);
+      if (re - rb > kEmitRowLimit) {
+        const uint32_t np = (uint32_t)((re - rb + kEmitPiece - 1) / kEmitPiece);
+        const unsigned int slot = atomicAdd(n_hub_items, np);
+        for (uint32_t q = 0; q < np && (uint64_t)slot + q < hub_cap; ++q)
+          hub_items[slot + q] = make_uint2((uint32_t)v, q);
+      } else if (re > rb) {
+        const uint32_t cv = cl[v];
+        uint32_t last = cv;  // the cluster of the last key this row staged
+        auto take = [&](uint32_t cu) {
+          if (cu != last && cu != cv) {
+            last = cu;
+            stage_key(((uint64_t)cv << b) | cu, wbuf, wfill, keys, cnt);
+          }
+        };
+        constexpr uint64_t V = 16 / sizeof(T);
+        uint64_t j = rb;
+        for (; j < re && (reinterpret_cast<uintptr_t>(col + j) & 15u); ++j)
+          take(__ldg(cl + (uint32_t)__ldg(col + j)));
+        for (; j + V <= re; j += V) {
+          if constexpr (sizeof(T) == 4) {
+            const uint4 w = __ldg(reinterpret_cast<const uint4 *>(col + j));
+            const uint32_t c0 = __ldg(cl + w.x), c1 = __ldg(cl + w.y), c2 = __ldg(cl + w.z),
+                           c3 = __ldg(cl + w.w);
+            take(c0);
+            take(c1);
+            take(c2);
+            take(c3);
+          } else {
+            const ulonglong2 w = __ldg(reinterpret_cast<const ulonglong2 *>(col + j));
+            const uint32_t c0 = __ldg(cl + (uint32_t)w.x), c1 = __ldg(cl + (uint32_t)w.y);
+            take(c0);
+            take(c1);
+          }
+        }
+        for (; j < re; ++j) take(__ldg(cl + (uint32_t)__ldg(col + j)));
+      }
+    }
+    __syncwarp();
+    // the group's new keys [kept, fill) through the set; survivors packed in
+    // place after the earlier ones (chunk k0's writes land below k0 + 32, in
+    // entries every lane has read already)
+    const uint32_t fill = min(*wfill, kRowWarpKeys);
+    uint32_t out = kept;
+    for (uint32_t k0 = kept; k0 < fill; k0 += 32) {
+      const uint32_t k = k0 + lane;
+      uint64_t key = 0;
+      bool keep = false;
+      if (k < fill) {
+        key = wbuf[k];
+        keep = !emit_set_seen(set, key);
+      }
+      const unsigned m = __ballot_sync(0xffffffffu, keep);
+      if (keep) wbuf[out + __popc(m & ((1u << lane) - 1u))] = key;
+      out += __popc(m);
+    }
+    kept = out;
+    if (kept >= kRowFlushAt || v0 + blockDim.x >= r1) {  // warp-uniform
+      unsigned long long pos0 = 0;
+      if (lane == 0 && kept) pos0 = atomicAdd(cnt, (unsigned long long)kept);
+      pos0 = __shfl_sync(0xffffffffu, pos0, 0);
+      __syncwarp();
+      for (uint32_t k = lane; k < kept; k += 32) keys[pos0 + k] = wbuf[k];
+      kept = 0;
+    }
+    __syncwarp();
+    if (lane == 0) *wfill = kept;
+    __syncwarp();
+  }
+}
+
 // One warp per piece of a hub row (rows longer than the k_emit limit):
 // kEmitPiece edges each, so the longest row is spread over many warps.
 template <class T>
@@ -365,21 +519,6 @@ __global__ void __launch_bounds__(kBlock) k_emit_hubs(
     }
   }
   if (st.fill) st.flush(lane, keys, cnt);
-}
-
-// Rows longer than `limit` (hubs) are listed for the warp-per-row kernel.
-__global__ void k_list_hubs(uint64_t n, const uint64_t *__restrict__ rp, uint64_t limit,
-                            uint2 *__restrict__ items, uint64_t cap, unsigned int *__restrict__ nh) {
-  for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < n;
-       v += (uint64_t)gridDim.x * blockDim.x) {
-    const uint64_t d = rp[v + 1] - rp[v];
-    if (d <= limit) continue;
-    // a long row becomes ceil(d / kEmitPiece) warp-sized work items
-    const uint32_t np = (uint32_t)((d + kEmitPiece - 1) / kEmitPiece);
-    const unsigned int slot = atomicAdd(nh, np);
-    for (uint32_t q = 0; q < np && (uint64_t)slot + q < cap; ++q)
-      items[slot + q] = make_uint2((uint32_t)v, q);
-  }
 }
 
 struct GetUniq {
@@ -447,24 +586,31 @@ void emit_keys(const Csr &g, const uint32_t *cl, const PartMap &pm, bool part, i
                uint64_t *keys, unsigned long long *cnt, cudaStream_t s, cudaMemPool_t pool,
                Counters &c) {
   const T *col = static_cast<const T *>(g.col);
-  // k_emit streams rows up to hub_limit entries; longer rows go to the
-  // piece-per-warp kernel so that one hub does not hold one warp for long.
-  const uint64_t hub_limit = 1024;
+  // k_emit streams rows up to hub_limit entries (k_emit_rows: kEmitRowLimit);
+  // longer rows go to the piece-per-warp kernel so that one hub does not hold
+  // one warp for long.
+  const uint64_t hub_limit = part ? 1024 : kEmitRowLimit;
   const uint64_t cap = g.m / (hub_limit + 1) + g.m / kEmitPiece + 2;
   DevBuf hubs(8 * cap, s, pool), nh(4, s, pool);
   CCG_CUDA(cudaMemsetAsync(nh.p, 0, 4, s));
-  unsigned grid = grid_for(g.n, kBlock, num_sms() * 32);
   const unsigned egrid = grid_for(g.n, kBlock, num_sms() * kEmitCtasPerSM);
   cudaEvent_t t0 = c.tic(s);
-  k_list_hubs<<<grid, kBlock, 0, s>>>(g.n, g.rp, hub_limit, hubs.as<uint2>(), cap,
-                                      nh.as<unsigned int>());
-  CCG_LAUNCH_CHECK();
-  k_emit<T><<<egrid, kBlock, 0, s>>>(g.n, g.rp, col, cl, pm, part, b, hub_limit, keys, cnt);
+  if (part) {
+    k_emit<T><<<egrid, kBlock, 0, s>>>(g.n, g.rp, col, cl, pm, part, b, hub_limit,
+                                       hubs.as<uint2>(), cap, nh.as<unsigned int>(), keys, cnt);
+  } else {
+    k_emit_rows<T><<<resident_grid(k_emit_rows<T>, kBlock, g.n), kBlock, 0, s>>>(
+        g.n, g.rp, col, cl, b, hubs.as<uint2>(), cap, nh.as<unsigned int>(), keys, cnt);
+  }
   CCG_LAUNCH_CHECK();
   k_emit_hubs<T><<<num_sms() * kEmitCtasPerSM, kBlock, 0, s>>>(g.rp, col, cl, pm, part, b, hubs.as<uint2>(), cap,
                                              nh.as<unsigned int>(), keys, cnt);
   CCG_LAUNCH_CHECK();
-  c.toc(s, "contract_emit", t0, 8 * (g.n + 1) + g.m * ((uint64_t)g.idb + 4) + 4 * g.n);
+  // algorithmic bytes: offsets, ids and own clusters; a neighbour's cluster
+  // is gathered per entry without virtual ranks, and with them only for the
+  // entries that leave their rank (about one in a hundred, not counted)
+  c.toc(s, "contract_emit", t0,
+        8 * (g.n + 1) + g.m * ((uint64_t)g.idb + (part ? 0 : 4)) + 4 * g.n);
   // relabel + compact: offsets, neighbour id and its cluster per edge, own
   // cluster per vertex (the emitted keys are counted at the sort)
   c.add(3, 8 * (g.n + 1) + g.m * ((uint64_t)g.idb + 4) + 4 * g.n);

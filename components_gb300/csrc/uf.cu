@@ -258,26 +258,29 @@ struct PieceSink {
 // passes.
 constexpr uint32_t kAffRounds = 2;
 
-// Entry of row v (d entries) that link round r uses (r < min(d, kAffRounds)):
-// the row's first entries.  On sorted rows these are the smallest neighbour
-// ids, which on hyperbolic graphs are often hubs: the link rounds then already
-// join the giant component (entries spread through the row were measured to
-// leave it in pieces, and the remaining pass then does most of the work).
-// Alternating by row parity (odd rows their last entries, so that two rows
-// share the sector of ids they read) cut the pass's DRAM bytes by only 6 % and
-// made it 21 % slower: a larger neighbour cannot take the one-CAS hook and
-// goes through the union queue.
+// Entry of row v (d entries) that link round r uses (r < min(d, kAffRounds)).
+// One rank (ALT false): the row's first entries.  On sorted rows these are the
+// smallest neighbour ids, which on hyperbolic graphs are often hubs: the link
+// rounds then already join the giant component (entries spread through the
+// row were measured to leave it in pieces).  Alternating by row parity (odd
+// rows their last entries) made that pass 21 % slower: a larger neighbour
+// cannot take the one-CAS hook and goes through the union queue.
+// Virtual ranks (ALT true): even rows their first entries, odd rows their
+// last.  With ranks the link rounds skip the entries that leave the rank, and
+// with the first entries the tile-crossing link edges that remain pile onto
+// a few vertices per rank: their global unions took 1.0-1.25 ms on the
+// 2^26-vertex hyperbolic graph with 16 ranks, against 0.26 ms alternating.
+// Which entries the rounds take changes no component, only the work.
+template <bool ALT>
 __host__ __device__ __forceinline__ uint64_t link_pos(uint64_t v, uint64_t d, uint32_t r) {
-  (void)v;
-  (void)d;
-  return r;
+  return (ALT && (v & 1)) ? d - 1 - r : (uint64_t)r;
 }
+template <bool ALT>
 __host__ __device__ __forceinline__ bool is_link_pos(uint64_t v, uint64_t d, uint64_t j) {
   for (uint32_t r = 0; r < kAffRounds && r < d; ++r)
-    if (link_pos(v, d, r) == j) return true;
+    if (link_pos<ALT>(v, d, r) == j) return true;
   return false;
 }
-
 
 template <class T, bool PART>
 __global__ void k_aff_link(uint64_t n, uint64_t m, const uint64_t *__restrict__ rp,
@@ -286,7 +289,7 @@ __global__ void k_aff_link(uint64_t n, uint64_t m, const uint64_t *__restrict__ 
        v += (uint64_t)gridDim.x * blockDim.x) {
     Row row;
     if (!load_row(rp, v, m, err, row) || row.e - row.b <= r) continue;
-    const uint64_t u = (uint64_t)__ldg(col + row.b + link_pos(v, row.e - row.b, r));
+    const uint64_t u = (uint64_t)__ldg(col + row.b + link_pos<PART>(v, row.e - row.b, r));
     if (u >= n) {
       set_err(err, kErrBadId);
       continue;
@@ -392,7 +395,7 @@ __global__ void k_aff_rest(uint64_t n, uint64_t m, const uint64_t *__restrict__ 
     uint32_t lo = 0, hi = 0xffffffffu;  // v's rank
     if (PART) pm.bounds((uint32_t)v, lo, hi);
     for (uint64_t k = row.b; k < row.e; ++k) {
-      if (is_link_pos(v, row.e - row.b, k - row.b)) continue;  // linked already
+      if (is_link_pos<PART>(v, row.e - row.b, k - row.b)) continue;  // linked already
       uint64_t u = (uint64_t)__ldg(col + k);
       if (u >= n) {
         set_err(err, kErrBadId);
@@ -442,7 +445,7 @@ __global__ void k_hub_pieces(uint64_t n, uint64_t m, const uint64_t *__restrict_
       }
       if (LESS) {
         if (u < v && (uint32_t)u >= lo) uf_union(p, v, (uint32_t)u);
-      } else if (!is_link_pos(v, re - rb, k - rb)) {  // the link rounds took those
+      } else if (!is_link_pos<PART>(v, re - rb, k - rb)) {  // the link rounds took those
         if ((uint32_t)u >= lo && (uint32_t)u < hi) uf_union(p, v, (uint32_t)u);
       }
     }
@@ -666,7 +669,7 @@ __global__ void __launch_bounds__(1024, 2)
         for (uint32_t r = 0; r < R; ++r)
 #pragma unroll
           for (uint32_t j = 0; j < (uint32_t)LINK; ++j)
-            id[r][j] = j < deg[r] ? __ldg(col + rb[r] + link_pos(t0 + g0 + 32 * r + lane, re[r] - rb[r], j)) : (T)0;
+            id[r][j] = j < deg[r] ? __ldg(col + rb[r] + link_pos<PART>(t0 + g0 + 32 * r + lane, re[r] - rb[r], j)) : (T)0;
 #pragma unroll
         for (uint32_t r = 0; r < R; ++r) {
           const uint32_t i = g0 + 32 * r + lane;
@@ -866,7 +869,7 @@ __global__ void k_cut_sample(uint64_t n, uint64_t m, const uint64_t *__restrict_
     if (e < b || e > m) continue;
     // the link-round entries of the row
     for (uint32_t r = 0; r < kAffRounds && r < e - b; ++r) {
-      const uint64_t u = (uint64_t)__ldg(col + b + link_pos(v, e - b, r));
+      const uint64_t u = (uint64_t)__ldg(col + b + link_pos<PART>(v, e - b, r));
       if (u >= n || u == v) continue;
       ++ltot;
       lcross += u / tile != v / tile;
@@ -1541,7 +1544,7 @@ HostShares host_shares(const uint64_t *rp, const void *col, int idb, uint64_t n,
     const uint64_t b = rp[v], e = rp[v + 1];
     if (e < b || e > m) continue;  // malformed rows are reported by the kernels
     for (uint32_t r = 0; r < kAffRounds && r < e - b; ++r) {
-      const uint64_t u = id(b + link_pos(v, e - b, r));
+      const uint64_t u = id(b + link_pos<false>(v, e - b, r));  // one rank
       if (u >= n || u == v) continue;
       ++ltot;
       lcross += u / tile != v / tile;

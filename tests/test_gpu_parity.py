@@ -86,6 +86,28 @@ def test_exp_options_and_beta(cuda):
             assert np.array_equal(gpu_labels(G, "exp", P, "device", conf), want), (kw, P)
 
 
+def test_ids_at_every_16_byte_offset(cuda):
+    """Device ids that start 4, 8 or 12 bytes past a 16-byte boundary (a view
+    into a larger tensor): the kernels that read ids 16 bytes at a time start
+    at the first 16-byte boundary of the array.  Every start gives the
+    oracle's labels, with virtual ranks (exp) and without (local)."""
+    import torch
+    G = cc.gen_rhg(1 << 15, 12.0, 2.6, seed=4)
+    want = oracle.uf_labels(G)
+    D = G.to_device("cuda:0")
+    for shift in (0, 1, 2, 3):
+        buf = torch.zeros(D.col.numel() + 4, dtype=torch.int32, device="cuda:0")
+        col = buf[shift:shift + D.col.numel()]
+        col.copy_(D.col)
+        assert (col.data_ptr() % 16 == 0) == (shift == 0)
+        for algo, P in (("exp", 4), ("exp", 16), ("local", 1)):
+            lab = torch.full((G.n,), -1, dtype=torch.int32, device="cuda:0")
+            cc.SOLVERS[algo](cc.Config(seed=1001, sequential_limit=0), 0, P).FindComponents(
+                StaticGraph(D.row_ptr, col, P), lab)
+            got = lab.cpu().numpy().view(np.uint32).astype(np.uint64)
+            assert np.array_equal(got, want), (shift, algo, P)
+
+
 def test_schedule_independence(cuda):
     """Randomness changes the contraction schedule, never the partition."""
     G = cc.gen_gnm(50000, 60000, seed=21, id_bytes=4)
