@@ -477,7 +477,8 @@ def workload_options(args, name):
     lab = torch.empty(G.n, dtype=dt, device="cuda:0")
     peak, _ = peaks()
     lines = {"exp1": ("exp", 1, 1), "exp16": ("exp", 16, 1), "exp16seq0": ("exp", 16, 0),
-             "allreduce": ("allreduce", 1, 1), "shortcuts": ("shortcuts", 1, 1), "local": ("local", 1, 1)}
+             "allreduce": ("allreduce", 1, 1), "shortcuts": ("shortcuts", 1, 1), "local": ("local", 1, 1),
+             "labels": ("labels", 1, 1)}
     for key in args.options.split(","):
         algo, P, seq = lines[key]
         ctx = cc.Context(0)

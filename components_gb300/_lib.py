@@ -28,7 +28,7 @@ ALGOS = {"exp": CC_EXP, "local": CC_LOCAL, "shortcuts": CC_SHORTCUTS, "labels": 
          "allreduce": CC_ALLREDUCE}
 
 CC_MAX_LEVELS = 64
-CC_MAX_KSTATS = 16
+CC_MAX_KSTATS = 32
 CC_PROF_KERNELS, CC_PROF_COMPONENTS = 1, 2
 
 

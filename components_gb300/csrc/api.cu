@@ -248,12 +248,9 @@ struct Solver {
       return;
     }
     DevBuf cl(4 * G.n, s, pool);
-    {
-      DevBuf k0(8 * G.n, s, pool), k1(8 * G.n, s, pool);
-      ccg::local_sweeps(G, vid, seed, level, cl.as<uint32_t>(), k0.as<uint64_t>(),
-                        k1.as<uint64_t>(), s, pool, c);
-      note_level(level, G, 2);
-    }
+    ccg::local_sweeps(G, vid, seed, level, cl.as<uint32_t>(), s, pool, c);
+    if (G.err) check_err();  // the first sweep checked the caller's ids
+    note_level(level, G, 2);
     ccg::Contracted H;
     ccg::contract_graph(G, cl.as<uint32_t>(), G.n, vid, nullptr, H, s, pool, c, nullptr);
     DevBuf sub(4 * (H.n ? H.n : 1), s, pool);
@@ -282,15 +279,31 @@ struct Solver {
 
   // Caller graph as a trusted uint32 graph: checked, and 64-bit ids narrowed
   // into a copy (32-bit ids are used in place once the check has passed).
+  // Caller graph as a uint32 graph for the propagation kernels.  64-bit ids
+  // are checked and narrowed into a copy (h.err null: trusted).  32-bit ids
+  // are used in place: the row offsets are checked here, the ids by the
+  // first sweep that reads them (h.err stays set until then), which saves a
+  // pass over the ids.
   Csr as_u32(const Csr &g, DevBuf &col32) {
-    if (g.idb != 4) col32.alloc(4 * (g.m ? g.m : 1), s, pool);
-    ccg::sanitize_ids(g, g.idb != 4 ? col32.as<uint32_t>() : nullptr, s, c);
-    check_err();
     Csr h = g;
-    if (g.idb != 4) h.col = col32.p;
     h.idb = 4;
-    h.err = nullptr;
+    if (g.idb != 4 || !g.err) {
+      if (g.idb != 4) col32.alloc(4 * (g.m ? g.m : 1), s, pool);
+      ccg::sanitize_ids(g, g.idb != 4 ? col32.as<uint32_t>() : nullptr, s, c);
+      check_err();
+      if (g.idb != 4) h.col = col32.p;
+      h.err = nullptr;
+    } else {
+      ccg::check_offsets(g, s, c);
+      check_err();
+    }
     return h;
+  }
+  // Result of a round loop: a bad id found by its first round is reported
+  // like any other input error.
+  void rounds_ok(int r, const char *what) {
+    if (r == ccg::kRoundsBadInput) check_err();
+    if (r < 0) throw Error(CC_ERR_NO_CONVERGENCE, what);
   }
 
   void run(cc_algo algo, const Csr &g, uint32_t P, uint32_t *lab) {
@@ -381,7 +394,7 @@ struct Solver {
           ccg::iota_u32(lab, n, s, c);
           int r = ccg::shortcut_propagate(G, lab, cfg.number_of_hitters, round_cap(C, G.n), s, pool, c,
                                           C->h_flag, C->d_flag);
-          if (r < 0) throw Error(CC_ERR_NO_CONVERGENCE, "shortcut propagation did not converge");
+          rounds_ok(r, "shortcut propagation did not converge");
           note_level(0, G, r);
         }
         break;
@@ -393,7 +406,7 @@ struct Solver {
         uint64_t cap = C->round_cap ? std::min<uint64_t>(n + 2, C->round_cap) : n + 2;
         int r = ccg::labels_propagate(G, lab, (int)std::min<uint64_t>(cap, 0x7fffffff), s, pool, c,
                                       C->h_flag, C->d_flag);
-        if (r < 0) throw Error(CC_ERR_NO_CONVERGENCE, "label propagation did not converge");
+        rounds_ok(r, "label propagation did not converge");
         note_level(0, G, r);
         break;
       }
@@ -892,9 +905,7 @@ int cc_debug_local_sweeps(const cc_csr *g, const uint32_t *vid, uint64_t seed, u
     cc_ctx *C = default_ctx();
     cudaStream_t s = C->stream;
     Counters c;
-    DevBuf k0(8 * (G.n ? G.n : 1), s, C->pool), k1(8 * (G.n ? G.n : 1), s, C->pool);
-    ccg::local_sweeps(G, vid, seed, level, cluster_out, k0.as<uint64_t>(), k1.as<uint64_t>(), s,
-                      C->pool, c);
+    ccg::local_sweeps(G, vid, seed, level, cluster_out, s, C->pool, c);
     CCG_CUDA(cudaStreamSynchronize(s));
   });
 }

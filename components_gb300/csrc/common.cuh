@@ -160,18 +160,6 @@ inline unsigned grid_for(uint64_t work, int block = kBlock, unsigned cap = num_s
   return (unsigned)g;
 }
 
-// One CTA per resident slot (the occupancy of `kernel` at `block` threads and
-// its static shared memory on every SM), at most one per `block` rows of
-// work: for kernels whose CTAs each walk one contiguous range of the rows.
-template <class K>
-inline unsigned resident_grid(K kernel, int block, uint64_t work) {
-  int per_sm = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, block, 0) != cudaSuccess ||
-      per_sm <= 0)
-    per_sm = 1;
-  return grid_for(work, block, (unsigned)(per_sm * num_sms()));
-}
-
 // ---- device helpers --------------------------------------------------------
 
 // Loads that bypass L1 so that values written by other SMs during the same

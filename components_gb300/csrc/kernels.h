@@ -107,6 +107,10 @@ void offsets_from_counts(const uint32_t *deg, uint64_t count, uint64_t base, uin
                          cudaStream_t s, cudaMemPool_t pool, Counters &c);
 uint64_t *radix_sort_u64(uint64_t *keys, uint64_t *tmp, uint64_t n, int bits,
                          cudaStream_t s, cudaMemPool_t pool, Counters &c);
+// Stable ranks of n 8-bit digits: rank[i] = position of element i when the
+// digits are sorted stably (ties in index order), inv[rank[i]] = i.
+void stable_digit_ranks(const uint8_t *dig, uint64_t n, uint32_t *rank, uint32_t *inv,
+                        cudaStream_t s, cudaMemPool_t pool, Counters &c);
 
 // Result of contracting a graph along a vertex map.
 struct Contracted {
@@ -139,6 +143,8 @@ constexpr int kGeoMax = 4096;
 int geo_table_build(double beta, std::vector<uint64_t> &t);
 void geo_table_upload(double beta, uint64_t *d_table, int *len_out, cudaStream_t s);
 
+// Row offsets of a caller's graph checked (rp[v] <= rp[v+1] <= m) into g.err.
+void check_offsets(const Csr &g, cudaStream_t s, Counters &c);
 // Bounds checks of a caller CSR (ids < n, offsets monotone and <= m; failures
 // go to g.err) and, when col32 is given, a uint32 copy of its ids.  Used
 // before kernels that assume a trusted uint32 graph.
@@ -156,11 +162,14 @@ int ldd_decompose(const Csr &g, const uint32_t *vid, uint64_t seed, uint32_t lev
 // Local contraction sweeps (local_contraction.h:157-300): uniform deviates in
 // [0,99], then two Jacobi sweeps of the lexicographic minimum over N[v].
 void local_sweeps(const Csr &g, const uint32_t *vid, uint64_t seed, uint32_t level,
-                  uint32_t *cluster, uint64_t *k0, uint64_t *k1, cudaStream_t s,
-                  cudaMemPool_t pool, Counters &c);
+                  uint32_t *cluster, cudaStream_t s, cudaMemPool_t pool, Counters &c);
 
 // ---- propagation kernels (prop.cu) -----------------------------------------
 // Min-label propagation rounds (propagation.h:72-149) on lab (in place).
+// Round loops return the number of rounds, -1 when max_rounds ran out, and
+// kRoundsBadInput when g.err is set (the caller's ids not checked yet: the
+// first round checks them) and an id was out of range; *g.err holds the code.
+constexpr int kRoundsBadInput = -2;
 int labels_propagate(const Csr &g, uint32_t *lab, int max_rounds, cudaStream_t s,
                      cudaMemPool_t pool, Counters &c, volatile int *host_flag, int *dev_flag);
 // Shortcut propagation rounds (shortcut_propagation.h:124-376).

@@ -174,34 +174,59 @@ __global__ void k_low_word(uint64_t n, const uint64_t *__restrict__ key, uint32_
 }
 
 // ---- local contraction (local_contraction.h:157-300) -----------------------
+// The sweeps take the minimum of the key (d, i) (deviate, then index) over a
+// neighbourhood, and the cluster is the index of that minimum.  Only the
+// order of the keys matters, so the sweeps run on each key's rank in that
+// order, a 32-bit value (a 4-byte gather per entry instead of 8), and the
+// index is read back through the inverse map.  The ranks are the stable ranks
+// of the deviates (ties in index order).
 __global__ void k_local_init(uint64_t n, const uint32_t *__restrict__ vid, uint64_t seed,
-                             uint32_t level, uint64_t *__restrict__ k0) {
+                             uint32_t level, uint8_t *__restrict__ dig) {
   for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n;
        i += (uint64_t)gridDim.x * blockDim.x) {
     // uniform integer in [0, 99] (reference: uniform_int_distribution(0, 99))
-    uint32_t d = (uint32_t)(((hash3(seed, vid[i], level) >> 32) * 100ull) >> 32);
-    k0[i] = ((uint64_t)d << 32) | (uint32_t)i;
+    dig[i] = (uint8_t)(((hash3(seed, vid[i], level) >> 32) * 100ull) >> 32);
   }
+}
+__global__ void k_local_clusters(uint64_t n, const uint32_t *__restrict__ best,
+                                 const uint32_t *__restrict__ inv, uint32_t *__restrict__ cl) {
+  for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < n;
+       v += (uint64_t)gridDim.x * blockDim.x)
+    cl[v] = inv[best[v]];
 }
 
 // Jacobi sweep: out[v] = min over N[v] (closed neighbourhood) of in[].  Rows
 // above kRowLimit entries only store in[v] here; k_min_sweep_pieces folds
 // their neighbours in afterwards, one warp per piece of the row.
+// CHECK (the first sweep over a caller's ids that no pass has checked): an id
+// >= n is skipped and recorded in *err, which the host reads before any
+// kernel trusts the ids.
+template <bool CHECK>
 __global__ void k_min_sweep(uint64_t n, const uint64_t *__restrict__ rp,
-                            const uint32_t *__restrict__ col, const uint64_t *__restrict__ in,
-                            uint64_t *__restrict__ out) {
+                            const uint32_t *__restrict__ col, const uint32_t *__restrict__ in,
+                            uint32_t *__restrict__ out, int *err) {
   for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < n;
        v += (uint64_t)gridDim.x * blockDim.x) {
     const uint64_t b = __ldg(rp + v), e = __ldg(rp + v + 1);
-    uint64_t best = in[v];
+    uint32_t best = in[v];
+    bool bad = false;
     if (e - b <= kRowLimit)
-      best = row_min_ilp<uint64_t>(col, b, e, best, [&](uint32_t u) { return __ldg(in + u); });
+      best = row_min_ilp<uint32_t>(col, b, e, best, [&](uint32_t u) {
+        if (CHECK && u >= n) {
+          bad = true;
+          return kNone;
+        }
+        return __ldg(in + u);
+      });
+    if (CHECK && bad) set_err(err, kErrBadId);
     out[v] = best;
   }
 }
 
-__global__ void k_min_sweep_pieces(const uint64_t *__restrict__ rp, const uint32_t *__restrict__ col,
-                                   RowPieces rpc, const uint64_t *__restrict__ in, uint64_t *out) {
+template <bool CHECK>
+__global__ void k_min_sweep_pieces(uint64_t n, const uint64_t *__restrict__ rp,
+                                   const uint32_t *__restrict__ col, RowPieces rpc,
+                                   const uint32_t *__restrict__ in, uint32_t *out, int *err) {
   const unsigned lane = threadIdx.x & 31;
   const uint64_t warp = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
   const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
@@ -210,14 +235,17 @@ __global__ void k_min_sweep_pieces(const uint64_t *__restrict__ rp, const uint32
     uint32_t v;
     uint64_t b, e;
     row_piece(rpc, rp, h, v, b, e);
-    uint64_t best = piece_min_ilp<uint64_t>(col, b, e, lane, ~0ull,
-                                            [&](uint32_t u) { return __ldg(in + u); });
-#pragma unroll
-    for (int o = 16; o; o >>= 1) {
-      const uint64_t y = __shfl_xor_sync(0xffffffffu, best, o);
-      best = y < best ? y : best;
-    }
-    if (lane == 0) atomicMin(reinterpret_cast<unsigned long long *>(out + v), (unsigned long long)best);
+    bool bad = false;
+    uint32_t best = piece_min_ilp<uint32_t>(col, b, e, lane, kNone, [&](uint32_t u) {
+      if (CHECK && u >= n) {
+        bad = true;
+        return kNone;
+      }
+      return __ldg(in + u);
+    });
+    if (CHECK && bad) set_err(err, kErrBadId);
+    best = __reduce_min_sync(0xffffffffu, best);
+    if (lane == 0) atomicMin(out + v, best);
   }
 }
 
@@ -291,33 +319,46 @@ int ldd_decompose(const Csr &g, const uint32_t *vid, uint64_t seed, uint32_t lev
 }
 
 void local_sweeps(const Csr &g, const uint32_t *vid, uint64_t seed, uint32_t level,
-                  uint32_t *cluster, uint64_t *k0, uint64_t *k1, cudaStream_t s, cudaMemPool_t pool,
-                  Counters &c) {
+                  uint32_t *cluster, cudaStream_t s, cudaMemPool_t pool, Counters &c) {
   if (g.n == 0) return;
   const uint32_t *col = static_cast<const uint32_t *>(g.col);
   unsigned grid = grid_for(g.n, kBlock, num_sms() * 32);
   const uint64_t cap = row_pieces_cap(g.m, kRowLimit);
-  DevBuf items(8 * cap, s, pool), cnt(4, s, pool);
+  DevBuf items(8 * cap, s, pool), cnt(4, s, pool), rank(4 * g.n, s, pool), best(4 * g.n, s, pool),
+      inv(4 * g.n, s, pool), digits(g.n, s, pool);
   CCG_CUDA(cudaMemsetAsync(cnt.p, 0, 4, s));
   const RowPieces rpc{items.as<uint2>(), cap, cnt.as<unsigned int>()};
-  k_local_init<<<grid, kBlock, 0, s>>>(g.n, vid, seed, level, k0);
+  cudaEvent_t tr = c.tic(s);
+  uint8_t *dig = digits.as<uint8_t>();
+  k_local_init<<<grid, kBlock, 0, s>>>(g.n, vid, seed, level, dig);
   CCG_LAUNCH_CHECK();
+  stable_digit_ranks(dig, g.n, rank.as<uint32_t>(), inv.as<uint32_t>(), s, pool, c);
+  c.toc(s, "local_rank", tr, 4 * g.n + g.n + 2 * g.n + 8 * g.n);
+  c.add(1, 4 * g.n + g.n);
   cudaEvent_t t0 = c.tic(s);
   k_row_pieces<<<grid, kBlock, 0, s>>>(g.n, g.rp, kRowLimit, rpc);
   CCG_LAUNCH_CHECK();
   for (int r = 0; r < 2; ++r) {  // N(v), then N(N(v))
-    const uint64_t *in = r ? k1 : k0;
-    uint64_t *out = r ? k0 : k1;
-    k_min_sweep<<<grid, kBlock, 0, s>>>(g.n, g.rp, col, in, out);
-    CCG_LAUNCH_CHECK();
-    k_min_sweep_pieces<<<num_sms() * 8, kBlock, 0, s>>>(g.rp, col, rpc, in, out);
+    const uint32_t *in = r ? best.as<uint32_t>() : rank.as<uint32_t>();
+    uint32_t *out = r ? rank.as<uint32_t>() : best.as<uint32_t>();
+    if (r == 0 && g.err) {  // the caller's ids, not checked yet
+      k_min_sweep<true><<<grid, kBlock, 0, s>>>(g.n, g.rp, col, in, out, g.err);
+      CCG_LAUNCH_CHECK();
+      k_min_sweep_pieces<true><<<num_sms() * 8, kBlock, 0, s>>>(g.n, g.rp, col, rpc, in, out,
+                                                                g.err);
+    } else {
+      k_min_sweep<false><<<grid, kBlock, 0, s>>>(g.n, g.rp, col, in, out, nullptr);
+      CCG_LAUNCH_CHECK();
+      k_min_sweep_pieces<false><<<num_sms() * 8, kBlock, 0, s>>>(g.n, g.rp, col, rpc, in, out,
+                                                                 nullptr);
+    }
     CCG_LAUNCH_CHECK();
   }
-  const uint64_t sweep = 8 * (g.n + 1) + g.m * 4 + g.m * 8 + 2 * g.n * 8;
+  const uint64_t sweep = 8 * (g.n + 1) + g.m * 4 + g.m * 4 + 2 * g.n * 4;
   c.toc(s, "local_sweeps", t0, 2 * sweep);
-  k_low_word<<<grid, kBlock, 0, s>>>(g.n, k0, cluster);
+  k_local_clusters<<<grid, kBlock, 0, s>>>(g.n, rank.as<uint32_t>(), inv.as<uint32_t>(), cluster);
   CCG_LAUNCH_CHECK();
-  c.add(6, 12 * g.n + 2 * sweep + 12 * g.n);
+  c.add(6, 12 * g.n + 2 * sweep);
 }
 
 }  // namespace ccg

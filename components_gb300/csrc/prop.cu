@@ -11,45 +11,91 @@ constexpr uint64_t kRowLimit = 64;
 // lab[v] <- min(lab[v], min_u lab[u]) in place.  The reference updates local
 // vertices in place during a sweep (SetVertexPayload) and sees ghosts from
 // the last exchange; on one device every vertex is local.
+// A lowered label sets its vertex's bit in chg and is counted (one atomic per
+// block into *nchanged).  act (null: every row) marks the rows to visit: the
+// neighbours of the labels lowered in the round before.  A row left out then
+// already sits at or below every neighbour's label: a neighbour whose label
+// last changed in round k is in round k's changed set, so the row is visited
+// in round k + 1 after that change; when a round changes no label, every row
+// is at its neighbours' minimum, as after a round over every row.
+__device__ __forceinline__ bool bit_of(const uint32_t *bits, uint64_t v) {
+  return (bits[v >> 5] >> (v & 31)) & 1u;
+}
+// CHECK (the first round over a caller's ids that no pass has checked): an
+// id >= n is skipped and recorded in *err; the host reads *err after the round
+// and stops before any kernel trusts the ids.
+template <bool CHECK>
 __global__ void k_labels_round(uint64_t n, const uint64_t *__restrict__ rp,
-                               const uint32_t *__restrict__ col, uint32_t *lab, int *flag) {
-  int changed = 0;
-  for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < n;
+                               const uint32_t *__restrict__ col, uint32_t *lab,
+                               const uint32_t *__restrict__ act, uint32_t *__restrict__ chg,
+                               unsigned int *nchanged, int *err) {
+  __shared__ unsigned int block_changed;
+  if (threadIdx.x == 0) block_changed = 0;
+  __syncthreads();
+  const uint64_t span = (n + 31) / 32 * 32;  // warp-uniform trip count, 32-aligned lanes
+  for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < span;
        v += (uint64_t)gridDim.x * blockDim.x) {
-    const uint64_t b = __ldg(rp + v), e = __ldg(rp + v + 1);
-    if (e - b > kRowLimit) continue;
-    const uint32_t l = ld_cg(lab + v);
-    const uint32_t best = row_min_ilp<uint32_t>(col, b, e, l, [&](uint32_t u) { return ld_cg(lab + u); });
-    if (best < l) {
-      st_cg(lab + v, best);
-      changed = 1;
+    bool changed = false;
+    if (v < n && (!act || bit_of(act, v))) {
+      const uint64_t b = __ldg(rp + v), e = __ldg(rp + v + 1);
+      if (e - b <= kRowLimit) {
+        const uint32_t l = ld_cg(lab + v);
+        bool bad = false;
+        const uint32_t best = row_min_ilp<uint32_t>(col, b, e, l, [&](uint32_t u) {
+          if (CHECK && u >= n) {
+            bad = true;
+            return kNone;
+          }
+          return ld_cg(lab + u);
+        });
+        if (CHECK && bad) set_err(err, kErrBadId);
+        if (best < l) {
+          st_cg(lab + v, best);
+          changed = true;
+        }
+      }
+    }
+    const unsigned bm = __ballot_sync(0xffffffffu, changed);
+    if ((threadIdx.x & 31) == 0 && bm) {
+      chg[v >> 5] = bm;  // the warp's own word (chg is cleared before the round)
+      atomicAdd(&block_changed, (unsigned)__popc(bm));
     }
   }
-  warp_flag(changed, flag);
+  __syncthreads();
+  if (threadIdx.x == 0 && block_changed) atomicAdd(nchanged, block_changed);
 }
 
 // Rows above kRowLimit entries, one warp per piece of the row.
-__global__ void k_labels_round_pieces(const uint64_t *__restrict__ rp,
+template <bool CHECK>
+__global__ void k_labels_round_pieces(uint64_t n, const uint64_t *__restrict__ rp,
                                       const uint32_t *__restrict__ col, RowPieces rpc, uint32_t *lab,
-                                      int *flag) {
+                                      const uint32_t *__restrict__ act, uint32_t *chg,
+                                      unsigned int *nchanged, int *err) {
   const unsigned lane = threadIdx.x & 31;
   const uint64_t warp = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
   const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
   const uint64_t ni = min((uint64_t)*rpc.count, rpc.cap);
-  int changed = 0;
   for (uint64_t h = warp; h < ni; h += nwarps) {
     uint32_t v;
     uint64_t b, e;
     row_piece(rpc, rp, h, v, b, e);
-    uint32_t best =
-        piece_min_ilp<uint32_t>(col, b, e, lane, kNone, [&](uint32_t u) { return ld_cg(lab + u); });
+    if (act && !bit_of(act, v)) continue;  // warp-uniform: one row per piece
+    bool bad = false;
+    uint32_t best = piece_min_ilp<uint32_t>(col, b, e, lane, kNone, [&](uint32_t u) {
+      if (CHECK && u >= n) {
+        bad = true;
+        return kNone;
+      }
+      return ld_cg(lab + u);
+    });
+    if (CHECK && bad) set_err(err, kErrBadId);
     best = __reduce_min_sync(0xffffffffu, best);
     if (lane == 0 && best < ld_cg(lab + v)) {
       atomicMin(lab + v, best);
-      changed = 1;
+      atomicOr(chg + (v >> 5), 1u << (v & 31));
+      atomicAdd(nchanged, 1u);  // a row of several pieces may count more than once
     }
   }
-  warp_flag(changed, flag);
 }
 
 // ---- ShortcutPropagation (shortcut_propagation.h:124-376) ------------------
@@ -69,13 +115,12 @@ __global__ void k_labels_round_pieces(const uint64_t *__restrict__ rp,
 // in the previous round.  A row without one keeps its label and sends no
 // update: its neighbours' minimum m is the previous round's, that round set
 // nf[v] <= m, and the jump only lowered it, so min(f[v], m) = f[v].
-__device__ __forceinline__ bool bit_of(const uint32_t *bits, uint64_t v) {
-  return (bits[v >> 5] >> (v & 31)) & 1u;
-}
+// CHECK: as in k_labels_round.
+template <bool CHECK>
 __global__ void k_sc_min(uint64_t n, const uint64_t *__restrict__ rp,
                          const uint32_t *__restrict__ col, const uint32_t *__restrict__ f,
                          uint32_t *__restrict__ nf, uint32_t *upd,
-                         const uint32_t *__restrict__ act) {
+                         const uint32_t *__restrict__ act, int *err) {
   const uint64_t span = (n + 31) / 32 * 32;  // warp-uniform trip count
   for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < span;
        v += (uint64_t)gridDim.x * blockDim.x) {
@@ -85,8 +130,16 @@ __global__ void k_sc_min(uint64_t n, const uint64_t *__restrict__ rp,
       best = l;
       if (!act || bit_of(act, v)) {
         const uint64_t b = __ldg(rp + v), e = __ldg(rp + v + 1);
+        bool bad = false;
         if (e - b <= kRowLimit)  // longer rows: k_sc_min_pieces folds their neighbours in
-          best = row_min_ilp<uint32_t>(col, b, e, l, [&](uint32_t u) { return __ldg(f + u); });
+          best = row_min_ilp<uint32_t>(col, b, e, l, [&](uint32_t u) {
+            if (CHECK && u >= n) {
+              bad = true;
+              return kNone;
+            }
+            return __ldg(f + u);
+          });
+        if (CHECK && bad) set_err(err, kErrBadId);
       }
       nf[v] = best;
     }
@@ -98,9 +151,11 @@ __global__ void k_sc_min(uint64_t n, const uint64_t *__restrict__ rp,
 // minimum is folded into nf[v] (which k_sc_min set to f[v]) and, when it is
 // below v's label, into the update addressed to that label; the minima over
 // pieces are the row's minimum, so nf and upd end as with one pass per row.
-__global__ void k_sc_min_pieces(const uint64_t *__restrict__ rp, const uint32_t *__restrict__ col,
-                                RowPieces rpc, const uint32_t *__restrict__ f, uint32_t *nf,
-                                uint32_t *upd, const uint32_t *__restrict__ act) {
+template <bool CHECK>
+__global__ void k_sc_min_pieces(uint64_t n, const uint64_t *__restrict__ rp,
+                                const uint32_t *__restrict__ col, RowPieces rpc,
+                                const uint32_t *__restrict__ f, uint32_t *nf, uint32_t *upd,
+                                const uint32_t *__restrict__ act, int *err) {
   const unsigned lane = threadIdx.x & 31;
   const uint64_t warp = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
   const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
@@ -110,8 +165,15 @@ __global__ void k_sc_min_pieces(const uint64_t *__restrict__ rp, const uint32_t 
     uint64_t b, e;
     row_piece(rpc, rp, h, v, b, e);
     if (act && !bit_of(act, v)) continue;  // warp-uniform: one row per piece
-    uint32_t best =
-        piece_min_ilp<uint32_t>(col, b, e, lane, kNone, [&](uint32_t u) { return __ldg(f + u); });
+    bool bad = false;
+    uint32_t best = piece_min_ilp<uint32_t>(col, b, e, lane, kNone, [&](uint32_t u) {
+      if (CHECK && u >= n) {
+        bad = true;
+        return kNone;
+      }
+      return __ldg(f + u);
+    });
+    if (CHECK && bad) set_err(err, kErrBadId);
     best = __reduce_min_sync(0xffffffffu, best);
     if (lane == 0) {
       const uint32_t l = f[v];
@@ -174,8 +236,8 @@ __global__ void k_sc_jump(uint64_t n, const uint32_t *__restrict__ f, uint32_t *
 
 // act |= the neighbours of every vertex whose bit is set in chg.  A row's ids
 // are sorted, so runs of neighbours in one 32-vertex word are merged into
-// one atomic; rows above kRowLimit entries go to k_sc_push_pieces.
-__global__ void k_sc_push(uint64_t n, const uint64_t *__restrict__ rp,
+// one atomic; rows above kRowLimit entries go to k_mark_neighbours_pieces.
+__global__ void k_mark_neighbours(uint64_t n, const uint64_t *__restrict__ rp,
                           const uint32_t *__restrict__ col, const uint32_t *__restrict__ chg,
                           uint32_t *act) {
   for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < n;
@@ -196,8 +258,9 @@ __global__ void k_sc_push(uint64_t n, const uint64_t *__restrict__ rp,
     if (bits) atomicOr(act + word, bits);
   }
 }
-__global__ void k_sc_push_pieces(const uint64_t *__restrict__ rp, const uint32_t *__restrict__ col,
-                                 RowPieces rpc, const uint32_t *__restrict__ chg, uint32_t *act) {
+__global__ void k_mark_neighbours_pieces(const uint64_t *__restrict__ rp,
+                                         const uint32_t *__restrict__ col, RowPieces rpc,
+                                         const uint32_t *__restrict__ chg, uint32_t *act) {
   const unsigned lane = threadIdx.x & 31;
   const uint64_t warp = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
   const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
@@ -311,27 +374,64 @@ int labels_propagate(const Csr &g, uint32_t *lab, int max_rounds, cudaStream_t s
   const uint32_t *col = static_cast<const uint32_t *>(g.col);
   unsigned grid = grid_for(g.n, kBlock, num_sms() * 32);
   const uint64_t cap = row_pieces_cap(g.m, kRowLimit);
-  DevBuf items(8 * cap, s, pool), cnt(4, s, pool);
+  const uint64_t words = (g.n + 31) / 32;
+  DevBuf items(8 * cap, s, pool), cnt(4, s, pool), chga(4 * words, s, pool),
+      chgb(4 * words, s, pool), actb(4 * words, s, pool);
   CCG_CUDA(cudaMemsetAsync(cnt.p, 0, 4, s));
   const RowPieces rpc{items.as<uint2>(), cap, cnt.as<unsigned int>()};
   k_row_pieces<<<grid, kBlock, 0, s>>>(g.n, g.rp, kRowLimit, rpc);
   CCG_LAUNCH_CHECK();
+  uint32_t *chg = chga.as<uint32_t>(), *chg_prev = chgb.as<uint32_t>();
+  unsigned int *nchanged = reinterpret_cast<unsigned int *>(dev_flag);
   int rounds = 0;
+  bool sparse = false;  // visit only the neighbours of the labels lowered last round
   const uint64_t round_bytes = 8 * (g.n + 1) + g.m * 4 + g.m * 4 + 2 * g.n * 4;
   for (;;) {
     if (rounds >= max_rounds) return -1;
     CCG_CUDA(cudaMemsetAsync(dev_flag, 0, sizeof(int), s));
+    CCG_CUDA(cudaMemsetAsync(chg, 0, 4 * words, s));
+    if (sparse) {
+      CCG_CUDA(cudaMemsetAsync(actb.p, 0, 4 * words, s));
+      cudaEvent_t tp = c.tic(s);
+      k_mark_neighbours<<<grid, kBlock, 0, s>>>(g.n, g.rp, col, chg_prev, actb.as<uint32_t>());
+      CCG_LAUNCH_CHECK();
+      k_mark_neighbours_pieces<<<num_sms() * 8, kBlock, 0, s>>>(g.rp, col, rpc, chg_prev,
+                                                        actb.as<uint32_t>());
+      CCG_LAUNCH_CHECK();
+      c.toc(s, "labels_push", tp, 0);
+    }
+    const uint32_t *act = sparse ? actb.as<uint32_t>() : nullptr;
+    const bool check = g.err && rounds == 0;  // the caller's ids, not checked yet
     cudaEvent_t t0 = c.tic(s);
-    k_labels_round<<<grid, kBlock, 0, s>>>(g.n, g.rp, col, lab, dev_flag);
+    if (check) {
+      k_labels_round<true><<<grid, kBlock, 0, s>>>(g.n, g.rp, col, lab, act, chg, nchanged, g.err);
+      CCG_LAUNCH_CHECK();
+      k_labels_round_pieces<true><<<num_sms() * 8, kBlock, 0, s>>>(g.n, g.rp, col, rpc, lab, act,
+                                                                   chg, nchanged, g.err);
+    } else {
+      k_labels_round<false><<<grid, kBlock, 0, s>>>(g.n, g.rp, col, lab, act, chg, nchanged,
+                                                    nullptr);
+      CCG_LAUNCH_CHECK();
+      k_labels_round_pieces<false><<<num_sms() * 8, kBlock, 0, s>>>(g.n, g.rp, col, rpc, lab, act,
+                                                                    chg, nchanged, nullptr);
+    }
     CCG_LAUNCH_CHECK();
-    k_labels_round_pieces<<<num_sms() * 8, kBlock, 0, s>>>(g.rp, col, rpc, lab, dev_flag);
-    CCG_LAUNCH_CHECK();
-    c.toc(s, "labels_round", t0, round_bytes);
+    // algorithmic bytes of a round over every row (a round over the active
+    // rows only is not counted)
+    c.toc(s, "labels_round", t0, sparse ? 0 : round_bytes);
     CCG_CUDA(cudaMemcpyAsync((void *)host_flag, dev_flag, sizeof(int), cudaMemcpyDeviceToHost, s));
+    if (check)
+      CCG_CUDA(cudaMemcpyAsync((void *)(host_flag + 1), g.err, sizeof(int), cudaMemcpyDeviceToHost, s));
     CCG_CUDA(cudaStreamSynchronize(s));
+    if (check && host_flag[1] != 0) return kRoundsBadInput;
     ++rounds;
     c.add(2, round_bytes);
-    if (*host_flag == 0) break;
+    const uint32_t changed = static_cast<uint32_t>(*host_flag);
+    if (changed == 0) break;
+    sparse = 16ull * changed <= g.n;
+    uint32_t *t = chg;
+    chg = chg_prev;
+    chg_prev = t;
   }
   return rounds;
 }
@@ -367,23 +467,33 @@ int shortcut_propagate(const Csr &g, uint32_t *lab, uint32_t hitters, int max_ro
     if (sparse) {
       CCG_CUDA(cudaMemsetAsync(actb.p, 0, 4 * words, s));
       cudaEvent_t tp = c.tic(s);
-      k_sc_push<<<grid, kBlock, 0, s>>>(g.n, g.rp, col, chgb.as<uint32_t>(), actb.as<uint32_t>());
+      k_mark_neighbours<<<grid, kBlock, 0, s>>>(g.n, g.rp, col, chgb.as<uint32_t>(),
+                                                actb.as<uint32_t>());
       CCG_LAUNCH_CHECK();
-      k_sc_push_pieces<<<num_sms() * 8, kBlock, 0, s>>>(g.rp, col, rpc, chgb.as<uint32_t>(),
+      k_mark_neighbours_pieces<<<num_sms() * 8, kBlock, 0, s>>>(g.rp, col, rpc, chgb.as<uint32_t>(),
                                                         actb.as<uint32_t>());
       CCG_LAUNCH_CHECK();
       c.toc(s, "sc_push", tp, 0);
     }
     const uint32_t *act = sparse ? actb.as<uint32_t>() : nullptr;
+    const bool check = g.err && rounds == 0;  // the caller's ids, not checked yet
     cudaEvent_t t0 = c.tic(s);
-    k_sc_min<<<grid, kBlock, 0, s>>>(g.n, g.rp, col, f, nf, updb.as<uint32_t>(), act);
+    if (check)
+      k_sc_min<true><<<grid, kBlock, 0, s>>>(g.n, g.rp, col, f, nf, updb.as<uint32_t>(), act, g.err);
+    else
+      k_sc_min<false><<<grid, kBlock, 0, s>>>(g.n, g.rp, col, f, nf, updb.as<uint32_t>(), act,
+                                              nullptr);
     CCG_LAUNCH_CHECK();
     // algorithmic bytes of a round over every row (a round over the active
     // rows only is not counted)
     c.toc(s, "sc_min", t0, sparse ? 0 : min_bytes);
     cudaEvent_t t0p = c.tic(s);
-    k_sc_min_pieces<<<num_sms() * 8, kBlock, 0, s>>>(g.rp, col, rpc, f, nf, updb.as<uint32_t>(),
-                                                     act);
+    if (check)
+      k_sc_min_pieces<true><<<num_sms() * 8, kBlock, 0, s>>>(g.n, g.rp, col, rpc, f, nf,
+                                                             updb.as<uint32_t>(), act, g.err);
+    else
+      k_sc_min_pieces<false><<<num_sms() * 8, kBlock, 0, s>>>(g.n, g.rp, col, rpc, f, nf,
+                                                              updb.as<uint32_t>(), act, nullptr);
     CCG_LAUNCH_CHECK();
     c.toc(s, "sc_min_pieces", t0p, 0);
     cudaEvent_t t0j = c.tic(s);
@@ -403,7 +513,10 @@ int shortcut_propagate(const Csr &g, uint32_t *lab, uint32_t hitters, int max_ro
     CCG_LAUNCH_CHECK();
     c.toc(s, "sc_jump", t0j, 4 * g.n * 4 + 4 * g.n);
     CCG_CUDA(cudaMemcpyAsync((void *)host_flag, dev_flag, sizeof(int), cudaMemcpyDeviceToHost, s));
+    if (check)
+      CCG_CUDA(cudaMemcpyAsync((void *)(host_flag + 1), g.err, sizeof(int), cudaMemcpyDeviceToHost, s));
     CCG_CUDA(cudaStreamSynchronize(s));
+    if (check && host_flag[1] != 0) return kRoundsBadInput;
     ++rounds;
     // min sweep (offsets, ids, one label gather per edge, own r/w) + jump
     // (own label, two gathers, write)
@@ -425,19 +538,23 @@ int shortcut_propagate(const Csr &g, uint32_t *lab, uint32_t hitters, int max_ro
 void compose_labels(const uint32_t *cl, const uint32_t *newid, const uint32_t *next,
                     const uint32_t *rep, uint32_t *out, uint64_t n, cudaStream_t s, Counters &c) {
   if (n == 0) return;
+  cudaEvent_t t0 = c.tic(s);
   k_compose<<<grid_for(n, kBlock, num_sms() * 32), kBlock, 0, s>>>(n, cl, newid, next, rep, out);
   CCG_LAUNCH_CHECK();
+  c.toc(s, "compose", t0, 16 * n);
   c.add(1, 16 * n);
 }
 
 void canonicalize(uint32_t *lab, uint32_t *scratch, uint64_t n, cudaStream_t s, Counters &c) {
   if (n == 0) return;
+  cudaEvent_t t0 = c.tic(s);
   CCG_CUDA(cudaMemsetAsync(scratch, 0xff, 4 * n, s));
   unsigned grid = grid_for(n, kBlock, num_sms() * 32);
   k_canon_min<<<grid, kBlock, 0, s>>>(n, scratch, lab);
   CCG_LAUNCH_CHECK();
   k_canon_apply<<<grid, kBlock, 0, s>>>(n, lab, scratch);
   CCG_LAUNCH_CHECK();
+  c.toc(s, "canonicalize", t0, 4 * n * 4);
   c.add(2, 4 * n * 4);
 }
 

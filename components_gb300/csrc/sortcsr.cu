@@ -98,6 +98,78 @@ __global__ void k_radix_scatter(const uint64_t *__restrict__ keys, uint64_t *__r
   }
 }
 
+// Stable ranks of n 8-bit digits without moving anything: the same per-tile
+// histograms and in-warp ranks as one radix pass, but each element writes its
+// destination (rank[i], coalesced) and the inverse map (inv[pos] = i, runs of
+// one digit per tile) instead of scattering keys.
+__global__ void k_digit_hist(const uint8_t *__restrict__ dig, uint64_t n, uint32_t ntiles,
+                             uint32_t *__restrict__ counts) {
+  __shared__ uint32_t h[kSortWarps][kRadix];
+  for (int i = threadIdx.x; i < kSortWarps * kRadix; i += blockDim.x) (&h[0][0])[i] = 0;
+  __syncthreads();
+  const unsigned w = threadIdx.x >> 5, lane = lane_id();
+  const uint64_t base = (uint64_t)blockIdx.x * kSortTile + (uint64_t)w * 32 * kSortItems;
+#pragma unroll 4
+  for (int i = 0; i < kSortItems; ++i) {
+    const uint64_t idx = base + (uint64_t)i * 32 + lane;
+    if (idx < n) atomicAdd(&h[w][dig[idx]], 1u);
+  }
+  __syncthreads();
+  for (int d = threadIdx.x; d < kRadix; d += blockDim.x) {
+    uint32_t t = 0;
+#pragma unroll
+    for (int k = 0; k < kSortWarps; ++k) t += h[k][d];
+    counts[(uint64_t)d * ntiles + blockIdx.x] = t;
+  }
+}
+__global__ void k_digit_rank(const uint8_t *__restrict__ dig, uint64_t n, uint32_t ntiles,
+                             const uint32_t *__restrict__ offs, uint32_t *__restrict__ rank,
+                             uint32_t *__restrict__ inv) {
+  __shared__ uint32_t wc[kSortWarps][kRadix];
+  __shared__ uint32_t gbase[kRadix];
+  for (int i = threadIdx.x; i < kSortWarps * kRadix; i += blockDim.x) (&wc[0][0])[i] = 0;
+  for (int d = threadIdx.x; d < kRadix; d += blockDim.x)
+    gbase[d] = offs[(uint64_t)d * ntiles + blockIdx.x];
+  __syncthreads();
+  const unsigned w = threadIdx.x >> 5, lane = lane_id();
+  const unsigned lt = (1u << lane) - 1u;
+  const uint64_t base = (uint64_t)blockIdx.x * kSortTile + (uint64_t)w * 32 * kSortItems;
+  uint32_t dg[kSortItems], rk[kSortItems];
+#pragma unroll
+  for (int i = 0; i < kSortItems; ++i) {
+    const uint64_t idx = base + (uint64_t)i * 32 + lane;
+    const uint32_t d = idx < n ? (uint32_t)dig[idx] : 0xffffu;
+    const unsigned peers = __match_any_sync(0xffffffffu, d);
+    const uint32_t before = __popc(peers & lt);
+    const uint32_t basecnt = d < kRadix ? wc[w][d] : 0u;
+    __syncwarp();
+    if (d < kRadix && before == 0) wc[w][d] = basecnt + __popc(peers);
+    __syncwarp();
+    dg[i] = d;
+    rk[i] = basecnt + before;
+  }
+  __syncthreads();
+  for (int d = threadIdx.x; d < kRadix; d += blockDim.x) {
+    uint32_t run = 0;
+#pragma unroll
+    for (int q = 0; q < kSortWarps; ++q) {
+      const uint32_t t = wc[q][d];
+      wc[q][d] = run;
+      run += t;
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int i = 0; i < kSortItems; ++i) {
+    if (dg[i] < kRadix) {
+      const uint64_t idx = base + (uint64_t)i * 32 + lane;
+      const uint32_t pos = gbase[dg[i]] + wc[w][dg[i]] + rk[i];
+      rank[idx] = pos;
+      inv[pos] = (uint32_t)idx;
+    }
+  }
+}
+
 // ---- contraction -----------------------------------------------------------
 
 // Keys a CTA has written already: a direct-mapped set in shared memory.
@@ -302,7 +374,8 @@ __global__ void __launch_bounds__(kBlock) k_emit(uint64_t n, const uint64_t *__r
           const uint32_t u = us[q];
           const bool out = u < lo0 || u >= hi0;  // false past the range
           const unsigned om = __ballot_sync(0xffffffffu, out);
-          if (out) olist[on + __popc(om & ((1u << lane) - 1u))] = ((uint64_t)(f0 + 32 * q + lane) << 32) | u;
+          if (out)
+            olist[on + __popc(om & ((1u << lane) - 1u))] = ((uint64_t)(f0 + 32 * q + lane) << 32) | u;
           on += __popc(om);
         }
         if (on > kOutList - 32 * kSteps) drain();  // room for the next batch
@@ -352,131 +425,6 @@ __global__ void __launch_bounds__(kBlock) k_emit(uint64_t n, const uint64_t *__r
     }
   }
   if (st.fill) st.flush(lane, keys, cnt);
-}
-
-// ---- the emit without virtual ranks: one thread per row ----------------------
-// Every entry then gathers its neighbour's cluster, as a sweep does, and most
-// keys repeat (local contraction's first level on the 2^20-vertex hyperbolic
-// graph: 56 % of the entries cross two clusters, 84 k distinct keys).  One
-// thread walks its row with 16-byte id loads and the gathers of a load in
-// flight, drops an entry inside its own cluster or in the cluster of the entry
-// it kept before, and stages the rest in its warp's buffer (one shared atomic
-// per group of lanes that stage together).  After each group of 32 rows the
-// warp passes its new keys through the CTA's set and keeps the survivors; they
-// are written out with one global reservation once 128 have gathered.  Warps
-// never wait for one another (a block-wide step per round of rows would hold
-// every row for the longest one).  Rows above kEmitRowLimit entries become hub
-// pieces.  Each CTA walks one contiguous range of rows, so its set holds the
-// keys of its rows.
-constexpr uint64_t kEmitRowLimit = 64;
-constexpr uint32_t kRowWarpKeys = 384;  // per warp: < 128 survivors + a group's new keys
-constexpr uint32_t kRowFlushAt = 128;
-
-__device__ __forceinline__ void stage_key(uint64_t key, uint64_t *wbuf, unsigned int *wfill,
-                                          uint64_t *__restrict__ keys,
-                                          unsigned long long *__restrict__ cnt) {
-  const unsigned am = __activemask();  // the lanes staging a key now
-  const unsigned lane = threadIdx.x & 31;
-  const int leader = __ffs(am) - 1;
-  unsigned int base = 0;
-  if ((int)lane == leader) base = atomicAdd(wfill, (unsigned)__popc(am));
-  base = __shfl_sync(am, base, leader);
-  const unsigned int slot = base + __popc(am & ((1u << lane) - 1u));
-  if (slot < kRowWarpKeys) wbuf[slot] = key;
-  else keys[atomicAdd(cnt, 1ull)] = key;  // the buffer is full: straight out (repeats allowed)
-}
-
-template <class T>
-__global__ void __launch_bounds__(kBlock) k_emit_rows(uint64_t n, const uint64_t *__restrict__ rp,
-                                                      const T *__restrict__ col,
-                                                      const uint32_t *__restrict__ cl, int b,
-                                                      uint2 *__restrict__ hub_items, uint64_t hub_cap,
-                                                      unsigned int *__restrict__ n_hub_items,
-                                                      uint64_t *__restrict__ keys,
-                                                      unsigned long long *__restrict__ cnt) {
-  __shared__ uint64_t wbufs[kBlock / 32][kRowWarpKeys];
-  __shared__ unsigned int wfills[kBlock / 32];
-  __shared__ unsigned long long set[kEmitSet];
-  const unsigned lane = lane_id(), wid = threadIdx.x >> 5;
-  uint64_t *wbuf = wbufs[wid];
-  unsigned int *wfill = &wfills[wid];
-  if (lane == 0) *wfill = 0;
-  emit_set_clear(set);  // synchronises the block
-  const uint64_t per = ((n + gridDim.x - 1) / gridDim.x + 31) / 32 * 32;
-  const uint64_t r1 = min(n, (blockIdx.x + 1) * per);
-  uint32_t kept = 0;  // warp-uniform: survivors at wbuf[0, kept)
-  for (uint64_t v0 = blockIdx.x * per + 32 * wid; v0 < r1; v0 += blockDim.x) {  // warp-uniform
-    const uint64_t v = v0 + lane;
-    if (v < r1) {
-      const uint64_t rb = __ldg(rp + v), re = __ldg(rp + v + 1);
-      if (re - rb > kEmitRowLimit) {
-        const uint32_t np = (uint32_t)((re - rb + kEmitPiece - 1) / kEmitPiece);
-        const unsigned int slot = atomicAdd(n_hub_items, np);
-        for (uint32_t q = 0; q < np && (uint64_t)slot + q < hub_cap; ++q)
-          hub_items[slot + q] = make_uint2((uint32_t)v, q);
-      } else if (re > rb) {
-        const uint32_t cv = cl[v];
-        uint32_t last = cv;  // the cluster of the last key this row staged
-        auto take = [&](uint32_t cu) {
-          if (cu != last && cu != cv) {
-            last = cu;
-            stage_key(((uint64_t)cv << b) | cu, wbuf, wfill, keys, cnt);
-          }
-        };
-        constexpr uint64_t V = 16 / sizeof(T);
-        uint64_t j = rb;
-        for (; j < re && (reinterpret_cast<uintptr_t>(col + j) & 15u); ++j)
-          take(__ldg(cl + (uint32_t)__ldg(col + j)));
-        for (; j + V <= re; j += V) {
-          if constexpr (sizeof(T) == 4) {
-            const uint4 w = __ldg(reinterpret_cast<const uint4 *>(col + j));
-            const uint32_t c0 = __ldg(cl + w.x), c1 = __ldg(cl + w.y), c2 = __ldg(cl + w.z),
-                           c3 = __ldg(cl + w.w);
-            take(c0);
-            take(c1);
-            take(c2);
-            take(c3);
-          } else {
-            const ulonglong2 w = __ldg(reinterpret_cast<const ulonglong2 *>(col + j));
-            const uint32_t c0 = __ldg(cl + (uint32_t)w.x), c1 = __ldg(cl + (uint32_t)w.y);
-            take(c0);
-            take(c1);
-          }
-        }
-        for (; j < re; ++j) take(__ldg(cl + (uint32_t)__ldg(col + j)));
-      }
-    }
-    __syncwarp();
-    // the group's new keys [kept, fill) through the set; survivors packed in
-    // place after the earlier ones (chunk k0's writes land below k0 + 32, in
-    // entries every lane has read already)
-    const uint32_t fill = min(*wfill, kRowWarpKeys);
-    uint32_t out = kept;
-    for (uint32_t k0 = kept; k0 < fill; k0 += 32) {
-      const uint32_t k = k0 + lane;
-      uint64_t key = 0;
-      bool keep = false;
-      if (k < fill) {
-        key = wbuf[k];
-        keep = !emit_set_seen(set, key);
-      }
-      const unsigned m = __ballot_sync(0xffffffffu, keep);
-      if (keep) wbuf[out + __popc(m & ((1u << lane) - 1u))] = key;
-      out += __popc(m);
-    }
-    kept = out;
-    if (kept >= kRowFlushAt || v0 + blockDim.x >= r1) {  // warp-uniform
-      unsigned long long pos0 = 0;
-      if (lane == 0 && kept) pos0 = atomicAdd(cnt, (unsigned long long)kept);
-      pos0 = __shfl_sync(0xffffffffu, pos0, 0);
-      __syncwarp();
-      for (uint32_t k = lane; k < kept; k += 32) keys[pos0 + k] = wbuf[k];
-      kept = 0;
-    }
-    __syncwarp();
-    if (lane == 0) *wfill = kept;
-    __syncwarp();
-  }
 }
 
 // One warp per piece of a hub row (rows longer than the k_emit limit):
@@ -586,25 +534,23 @@ void emit_keys(const Csr &g, const uint32_t *cl, const PartMap &pm, bool part, i
                uint64_t *keys, unsigned long long *cnt, cudaStream_t s, cudaMemPool_t pool,
                Counters &c) {
   const T *col = static_cast<const T *>(g.col);
-  // k_emit streams rows up to hub_limit entries (k_emit_rows: kEmitRowLimit);
-  // longer rows go to the piece-per-warp kernel so that one hub does not hold
-  // one warp for long.
-  const uint64_t hub_limit = part ? 1024 : kEmitRowLimit;
+  // k_emit streams rows up to hub_limit entries; longer rows go to the
+  // piece-per-warp kernel so that one hub does not hold one warp for long.
+  // (One thread per row, with the repeats dropped in a warp buffer and the
+  // CTA's set, was measured slower without virtual ranks: 7.5 ms against
+  // 5.3 ms for local contraction's first level on the 2^26-vertex hyperbolic
+  // graph.)
+  const uint64_t hub_limit = 1024;
   const uint64_t cap = g.m / (hub_limit + 1) + g.m / kEmitPiece + 2;
   DevBuf hubs(8 * cap, s, pool), nh(4, s, pool);
   CCG_CUDA(cudaMemsetAsync(nh.p, 0, 4, s));
   const unsigned egrid = grid_for(g.n, kBlock, num_sms() * kEmitCtasPerSM);
   cudaEvent_t t0 = c.tic(s);
-  if (part) {
-    k_emit<T><<<egrid, kBlock, 0, s>>>(g.n, g.rp, col, cl, pm, part, b, hub_limit,
-                                       hubs.as<uint2>(), cap, nh.as<unsigned int>(), keys, cnt);
-  } else {
-    k_emit_rows<T><<<resident_grid(k_emit_rows<T>, kBlock, g.n), kBlock, 0, s>>>(
-        g.n, g.rp, col, cl, b, hubs.as<uint2>(), cap, nh.as<unsigned int>(), keys, cnt);
-  }
+  k_emit<T><<<egrid, kBlock, 0, s>>>(g.n, g.rp, col, cl, pm, part, b, hub_limit, hubs.as<uint2>(),
+                                     cap, nh.as<unsigned int>(), keys, cnt);
   CCG_LAUNCH_CHECK();
-  k_emit_hubs<T><<<num_sms() * kEmitCtasPerSM, kBlock, 0, s>>>(g.rp, col, cl, pm, part, b, hubs.as<uint2>(), cap,
-                                             nh.as<unsigned int>(), keys, cnt);
+  k_emit_hubs<T><<<num_sms() * kEmitCtasPerSM, kBlock, 0, s>>>(
+      g.rp, col, cl, pm, part, b, hubs.as<uint2>(), cap, nh.as<unsigned int>(), keys, cnt);
   CCG_LAUNCH_CHECK();
   // algorithmic bytes: offsets, ids and own clusters; a neighbour's cluster
   // is gathered per entry without virtual ranks, and with them only for the
@@ -703,6 +649,21 @@ void offsets_from_counts(const uint32_t *deg, uint64_t count, uint64_t base, uin
                          cudaStream_t s, cudaMemPool_t pool, Counters &c) {
   if (count == 0) return;
   scan_generic(count, GetCount{deg}, PutOffset{rp, base}, nullptr, s, pool, c);
+}
+
+void stable_digit_ranks(const uint8_t *dig, uint64_t n, uint32_t *rank, uint32_t *inv,
+                        cudaStream_t s, cudaMemPool_t pool, Counters &c) {
+  if (n == 0) return;
+  if (n >= (1ull << 32)) throw Error(CC_ERR_UNSUPPORTED, "digit ranks: more than 2^32 elements");
+  const uint32_t ntiles = (uint32_t)((n + kSortTile - 1) / kSortTile);
+  DevBuf counts(4ull * kRadix * ntiles, s, pool);
+  k_digit_hist<<<ntiles, kBlock, 0, s>>>(dig, n, ntiles, counts.as<uint32_t>());
+  CCG_LAUNCH_CHECK();
+  scan_generic((uint64_t)kRadix * ntiles, GetArr{counts.as<uint32_t>()},
+               PutArr{counts.as<uint32_t>()}, nullptr, s, pool, c);
+  k_digit_rank<<<ntiles, kBlock, 0, s>>>(dig, n, ntiles, counts.as<uint32_t>(), rank, inv);
+  CCG_LAUNCH_CHECK();
+  c.add(2, 2 * n + 8 * n);
 }
 
 uint64_t *radix_sort_u64(uint64_t *keys, uint64_t *tmp, uint64_t n, int bits, cudaStream_t s,

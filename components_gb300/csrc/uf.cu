@@ -1580,9 +1580,27 @@ void widen_labels(const uint32_t *in, void *out, int out_bytes, uint64_t n, cuda
   c.add(1, n * 4 + n * (uint64_t)out_bytes);
 }
 
+__global__ void k_check_offsets(uint64_t n, uint64_t m, const uint64_t *__restrict__ rp, int *err) {
+  for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < n;
+       v += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t b = __ldg(rp + v), e = __ldg(rp + v + 1);
+    if (e < b || e > m) set_err(err, kErrBadOffsets);
+  }
+}
+
+void check_offsets(const Csr &g, cudaStream_t s, Counters &c) {
+  if (g.n == 0) return;
+  cudaEvent_t t0 = c.tic(s);
+  k_check_offsets<<<grid_for(g.n, kBlock, num_sms() * 32), kBlock, 0, s>>>(g.n, g.m, g.rp, g.err);
+  CCG_LAUNCH_CHECK();
+  c.toc(s, "check_offsets", t0, 8 * (g.n + 1));
+  c.add(1, 8 * (g.n + 1));
+}
+
 void sanitize_ids(const Csr &g, uint32_t *col32, cudaStream_t s, Counters &c) {
   if (g.n == 0) return;
   unsigned grid = grid_for(std::max(g.n, g.m / 4), kBlock, num_sms() * 32);
+  cudaEvent_t t0 = c.tic(s);
   if (g.idb == 8)
     k_sanitize<uint64_t><<<grid, kBlock, 0, s>>>(g.n, g.m, g.rp,
                                                  static_cast<const uint64_t *>(g.col), col32, g.err);
@@ -1590,6 +1608,7 @@ void sanitize_ids(const Csr &g, uint32_t *col32, cudaStream_t s, Counters &c) {
     k_sanitize<uint32_t><<<grid, kBlock, 0, s>>>(g.n, g.m, g.rp,
                                                  static_cast<const uint32_t *>(g.col), col32, g.err);
   CCG_LAUNCH_CHECK();
+  c.toc(s, "check_ids", t0, 8 * (g.n + 1) + g.m * ((uint64_t)g.idb + (col32 ? 4 : 0)));
   c.add(1, 8 * (g.n + 1) + g.m * ((uint64_t)g.idb + (col32 ? 4 : 0)));
 }
 

@@ -112,7 +112,7 @@ typedef struct cc_config {
 } cc_config;
 
 #define CC_MAX_LEVELS 64
-#define CC_MAX_KSTATS 16
+#define CC_MAX_KSTATS 32
 
 /* Per-kernel timing (CUDA events on the context stream), filled when
    profiling is on (cc_ctx_set_profiling). */

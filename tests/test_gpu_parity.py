@@ -185,11 +185,34 @@ def test_id_check_at_every_offset_of_col(cuda, idb):
         for pos in (0, 1, 2, G.m // 2, G.m - 2, G.m - 1):
             old = int(col[pos].item())
             col[pos] = G.n + 7
-            lab = torch.full((G.n,), -1, dtype=dt, device="cuda:0")
-            with pytest.raises(_lib.CCError) as ei:
-                cc.SOLVERS["shortcuts"](cc.Config(seed=1001), 0, 1).FindComponents(D, lab)
-            assert ei.value.status == _lib.CC_ERR_INVALID, (shift, pos)
+            for algo in ("shortcuts", "labels", "local"):
+                lab = torch.full((G.n,), -1, dtype=dt, device="cuda:0")
+                with pytest.raises(_lib.CCError) as ei:
+                    cc.SOLVERS[algo](cc.Config(seed=1001), 0, 1).FindComponents(D, lab)
+                assert ei.value.status == _lib.CC_ERR_INVALID, (shift, pos, algo)
             col[pos] = old
+
+
+def test_id_check_in_long_rows(cuda):
+    """A bad id inside a row of more than 64 entries (walked in pieces by a
+    warp each) is reported by every propagation option; the same graph with
+    the id repaired gives the oracle's labels."""
+    import torch
+    rows = [list(range(1, 201))] + [[0] for _ in range(200)] + [[202], [201]]
+    G = csr_from_rows(rows)
+    want = oracle.uf_labels(G)
+    D = G.to_device("cuda:0")
+    for algo in ("shortcuts", "labels", "local"):
+        lab = torch.full((G.n,), -1, dtype=torch.int32, device="cuda:0")
+        cc.SOLVERS[algo](cc.Config(seed=1001), 0, 1).FindComponents(D, lab)
+        assert np.array_equal(lab.cpu().numpy().astype(np.uint64), want), algo
+    col = D.col.clone()
+    col[150] = G.n + 3  # inside row 0 (200 entries)
+    for algo in ("shortcuts", "labels", "local"):
+        lab = torch.full((G.n,), -1, dtype=torch.int32, device="cuda:0")
+        with pytest.raises(_lib.CCError) as ei:
+            cc.SOLVERS[algo](cc.Config(seed=1001), 0, 1).FindComponents(StaticGraph(D.row_ptr, col), lab)
+        assert ei.value.status == _lib.CC_ERR_INVALID, algo
 
 
 @pytest.mark.parametrize("idb", [4, 8])
