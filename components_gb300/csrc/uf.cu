@@ -22,6 +22,7 @@
 #include <map>
 #include <mutex>
 #include <tuple>
+#include <type_traits>
 
 #include "hostpool.h"
 #include "kernels.h"
@@ -465,9 +466,8 @@ __global__ void k_iota_parent(uint64_t n, uint32_t *p) {
 // its tile-local root, and only the edges that leave the tile go to a global
 // list.  This is the reference's partition-local pass with the CTA as the
 // rank (FindLocalComponents, exponential_contraction.h:391-411).
-// Shared-memory parent entries are 16 bits wide when the tile has at most
-// 65536 vertices (twice the tile for the same shared memory) and 32 bits
-// otherwise.
+// Shared-memory parent entries are 16 bits wide in the hook pass and 32 bits
+// in link mode (TileParent below).
 __device__ __forceinline__ uint32_t ts_cas(uint16_t *a, uint32_t c, uint32_t v) {
   return atomicCAS(reinterpret_cast<unsigned short *>(a), (unsigned short)c, (unsigned short)v);
 }
@@ -530,6 +530,15 @@ __device__ __forceinline__ uint64_t shfl64(uint64_t x, int src) {
 constexpr uint32_t kUnionQueue = 64;  // per warp: < 32 pending + up to 32 new
 constexpr uint32_t kTileMax = 65536;  // queue entries pack two 16-bit tile indices
 constexpr uint32_t kLinkGroups = 1;   // link mode: 32-row blocks per warp step (1 measured best of 1, 2, 4)
+// Parent entries of a tile in shared memory: 16 bits in the hook pass (twice
+// the vertices for the same shared memory: fewer tile-crossing edges on
+// grids), 32 bits in link mode with half the vertices.  Link mode hooks all
+// 32 rows of a warp at once, and a 16-bit CAS shares its 32-bit word with the
+// neighbouring row's entry: on the 2^26-vertex hyperbolic graph the link pass
+// took 1.10 ms on 16-bit entries (32768-vertex tiles) and 1.02 ms on 32-bit
+// entries (16384-vertex tiles), the 16-rank link pass 1.37 and 1.18 ms.
+template <int LINK>
+using TileParent = std::conditional_t<(LINK > 0), uint32_t, uint16_t>;
 
 template <class PT>
 size_t tile_smem_bytes(uint32_t tile, uint32_t threads, uint32_t stage) {
@@ -1017,23 +1026,25 @@ TileShape tile_shape(uint64_t n, const UfTuning &tu) {
 template <class T, bool PART, int LINK>
 TileShape tile_shape_uncached(uint64_t n, const UfTuning &tu) {
   TileShape t;
-  t.tile = tu.tile_vertices;
+  if (tu.tile_vertices < 32 || tu.tile_vertices > kTileMax)
+    throw Error(CC_ERR_INVALID, "tile_vertices must lie in [32, 65536]");
+  // link mode: 32-bit parents, half the vertices in the same shared memory
+  t.tile = LINK > 0 ? std::max<uint32_t>(32, tu.tile_vertices / 2) : tu.tile_vertices;
   t.threads = (int)tu.tile_threads;
-  if (t.tile < 32 || t.tile > kTileMax) throw Error(CC_ERR_INVALID, "tile_vertices must lie in [32, 65536]");
   if (t.threads < 32 || t.threads > 1024 || t.threads % 32)
     throw Error(CC_ERR_INVALID, "tile_threads must be a multiple of 32 up to 1024");
   int dev = 0, sm_smem = 0, blk_smem = 0;
   CCG_CUDA(cudaGetDevice(&dev));
   CCG_CUDA(cudaDeviceGetAttribute(&sm_smem, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev));
   CCG_CUDA(cudaDeviceGetAttribute(&blk_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
-  const size_t fixed = tile_smem_bytes<uint16_t>(t.tile, (uint32_t)t.threads, 0);
+  const size_t fixed = tile_smem_bytes<TileParent<LINK>>(t.tile, (uint32_t)t.threads, 0);
   const size_t reserve = 1024 + 64;  // per-CTA system reserve + static shared memory
   size_t room = (size_t)sm_smem / 2 > reserve + fixed ? (size_t)sm_smem / 2 - reserve - fixed : 0;
   if (room < 256 * 8) room = (size_t)blk_smem > 64 + fixed ? (size_t)blk_smem - 64 - fixed : 0;
   t.stage = (uint32_t)std::min<size_t>(room / 8, 8192);
   if (t.stage < 64) throw Error(CC_ERR_INVALID, "tile does not fit in shared memory");
-  t.smem = tile_smem_bytes<uint16_t>(t.tile, (uint32_t)t.threads, t.stage);
-  const void *fn = (const void *)k_tile3<T, PART, uint16_t, LINK>;
+  t.smem = tile_smem_bytes<TileParent<LINK>>(t.tile, (uint32_t)t.threads, t.stage);
+  const void *fn = (const void *)k_tile3<T, PART, TileParent<LINK>, LINK>;
   // the attribute only ever grows: launch shapes cached for other tiles keep working
   cudaFuncAttributes fa;
   CCG_CUDA(cudaFuncGetAttributes(&fa, fn));
@@ -1203,7 +1214,7 @@ void run_uf_tiled(const Csr &g, uint32_t *parent, const PartMap &pm, const UfTun
   const uint64_t tile_bytes = 8 * (g.n + 1) + g.m * si + 4 * g.n;
   cudaEvent_t t0 = c.tic(s);
   if (!hs) {
-    k_tile3<T, PART, uint16_t, 0><<<grid, threads, smem, s>>>(g.n, g.m, 0, g.n, g.rp, col, parent,
+    k_tile3<T, PART, TileParent<0>, 0><<<grid, threads, smem, s>>>(g.n, g.m, 0, g.n, g.rp, col, parent,
                                                            pm, tile, stage, tu.hub_degree, hl,
                                                            cut.as<uint2>(), cut_cap, ncut, g.err);
     CCG_LAUNCH_CHECK();
@@ -1265,7 +1276,7 @@ void run_uf_tiled(const Csr &g, uint32_t *parent, const PartMap &pm, const UfTun
       cudaEventDestroy(ev);
       if (coded) offsets_from_degrees(ddeg.as<uint8_t>() + v0, v1 - v0, e0, drp + v0, s, pool, c);
       const unsigned cgrid = (unsigned)std::min<uint64_t>((v1 - v0 + tile - 1) / tile, grid);
-      k_tile3<T, PART, uint16_t, 0><<<cgrid, threads, smem, s>>>(g.n, g.m, v0, v1, g.rp, col,
+      k_tile3<T, PART, TileParent<0>, 0><<<cgrid, threads, smem, s>>>(g.n, g.m, v0, v1, g.rp, col,
                                                               parent, pm, tile, stage,
                                                               tu.hub_degree, hl, cut.as<uint2>(),
                                                               cut_cap, ncut, g.err);
@@ -1356,7 +1367,7 @@ void run_uf_afforest(const Csr &g, uint32_t *parent, const PartMap &pm, const Uf
     link_bytes = 8 * (g.n + 1) + kAffRounds * g.n * si + 4 * g.n;
     cudaEvent_t t0 = c.tic(s);
     if (!hs) {
-      k_tile3<T, PART, uint16_t, (int)kAffRounds><<<ts.grid, ts.threads, ts.smem, s>>>(
+      k_tile3<T, PART, TileParent<(int)kAffRounds>, (int)kAffRounds><<<ts.grid, ts.threads, ts.smem, s>>>(
           g.n, g.m, 0, g.n, g.rp, col, parent, pm, ts.tile, ts.stage, hub_degree, none,
           cut.as<uint2>(), cut_cap, cnt.as<unsigned long long>(), g.err);
       CCG_LAUNCH_CHECK();
@@ -1372,7 +1383,7 @@ void run_uf_afforest(const Csr &g, uint32_t *parent, const PartMap &pm, const Uf
         const uint64_t v1 = std::min<uint64_t>(g.n, v0 + chunk);
         copy_rows_in<T>(g, hs, v0, v1, s, &ds, pool, &c);
         const unsigned cgrid = (unsigned)std::min<uint64_t>((v1 - v0 + ts.tile - 1) / ts.tile, ts.grid);
-        k_tile3<T, PART, uint16_t, (int)kAffRounds><<<cgrid, ts.threads, ts.smem, s>>>(
+        k_tile3<T, PART, TileParent<(int)kAffRounds>, (int)kAffRounds><<<cgrid, ts.threads, ts.smem, s>>>(
             g.n, g.m, v0, v1, g.rp, col, parent, pm, ts.tile, ts.stage, hub_degree, none,
             cut.as<uint2>(), cut_cap, cnt.as<unsigned long long>(), g.err);
         CCG_LAUNCH_CHECK();
