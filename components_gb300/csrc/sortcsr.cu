@@ -210,6 +210,7 @@ constexpr uint32_t kWarpKeys = 256;
 constexpr unsigned kEmitCtasPerSM = 32;
 constexpr uint32_t kEmitSteps = 4;  // 32-entry steps of k_emit between flush checks
 constexpr uint32_t kOutList = 160;  // per warp: entries that leave their rank, resolved together
+constexpr int kVecSteps = 4;        // 16-byte loads in flight per lane (virtual ranks, 32-bit ids)
 struct WarpKeys {
   uint64_t *buf;
   unsigned long long *set;
@@ -264,15 +265,16 @@ struct WarpKeys {
 // degree prefix sum is <= k), so skewed degrees keep every lane busy.  Rows
 // longer than hub_limit are listed as (row, piece) items for k_emit_hubs,
 // which runs next on the same stream.
-template <class T>
-__global__ void __launch_bounds__(kBlock) k_emit(uint64_t n, const uint64_t *__restrict__ rp,
+template <class T, bool VEC>
+__global__ void __launch_bounds__(kBlock, VEC ? 4 : 5) k_emit(uint64_t n, const uint64_t *__restrict__ rp,
                                                  const T *__restrict__ col,
                                                  const uint32_t *__restrict__ cl, PartMap pm,
                                                  bool part, int b, uint64_t hub_limit,
                                                  uint2 *__restrict__ hub_items, uint64_t hub_cap,
                                                  unsigned int *__restrict__ n_hub_items,
                                                  uint64_t *__restrict__ keys,
-                                                 unsigned long long *__restrict__ cnt) {
+                                                 unsigned long long *__restrict__ cnt,
+                                                 uint64_t m) {
   __shared__ uint64_t wbuf[kBlock / 32][kWarpKeys];
   __shared__ uint64_t wout[kBlock / 32][kOutList];
   __shared__ unsigned long long set[kEmitSet];
@@ -362,6 +364,57 @@ __global__ void __launch_bounds__(kBlock) k_emit(uint64_t n, const uint64_t *__r
         __syncwarp();
         on = 0;
       };
+      if constexpr (VEC && sizeof(T) == 4) {
+        {
+          // 16-byte loads: lane j of a step reads entries a0 + 4j .. a0 + 4j + 3
+          // (a0 = the group's first entry rounded down to a multiple of four),
+          // kVecSteps such loads per lane in flight together, which covers a
+          // typical 32-row group at once.  Entries outside the group are
+          // loaded and ignored; a vector that would reach past the id array is
+          // read entry by entry.
+          const uint64_t a0 = base & ~3ull;
+          const uint32_t head = (uint32_t)(base - a0);
+          const uint32_t nv = (head + total + 3) / 4;
+          for (uint32_t j0 = 0; j0 < nv; j0 += 32 * kVecSteps) {
+            uint4 w[kVecSteps];
+#pragma unroll
+            for (int q = 0; q < kVecSteps; ++q) {
+              const uint32_t j = j0 + 32 * q + lane;
+              const uint64_t e = a0 + 4ull * j;
+              w[q] = make_uint4(lo0, lo0, lo0, lo0);  // inside the rank: never kept
+              if (j < nv) {
+                if (e + 4 <= m) {
+                  w[q] = __ldg(reinterpret_cast<const uint4 *>(col + e));
+                } else {
+                  if (e < m) w[q].x = (uint32_t)col[e];
+                  if (e + 1 < m) w[q].y = (uint32_t)col[e + 1];
+                  if (e + 2 < m) w[q].z = (uint32_t)col[e + 2];
+                }
+              }
+            }
+#pragma unroll
+            for (int q = 0; q < kVecSteps; ++q) {
+              if (j0 + 32 * q >= nv) continue;  // warp-uniform
+              if (on > kOutList - 128) drain();  // room for this vector's entries
+              const uint32_t f4 = 4 * (j0 + 32 * q + lane);  // f of component 0, plus head
+              const uint32_t uu[4] = {w[q].x, w[q].y, w[q].z, w[q].w};
+#pragma unroll
+              for (int t = 0; t < 4; ++t) {
+                const uint32_t u = uu[t];
+                const bool in_group = f4 + t >= head && f4 + t - head < total;
+                const bool out = in_group && (u < lo0 || u >= hi0);
+                const unsigned om = __ballot_sync(0xffffffffu, out);
+                if (out)
+                  olist[on + __popc(om & ((1u << lane) - 1u))] =
+                      ((uint64_t)(f4 + t - head) << 32) | u;
+                on += __popc(om);
+              }
+            }
+          }
+          if (on) drain();
+          continue;
+        }
+      }
       for (uint32_t f0 = 0; f0 < total; f0 += 32 * kSteps) {
         uint32_t us[kSteps];
 #pragma unroll
@@ -452,18 +505,29 @@ __global__ void __launch_bounds__(kBlock) k_emit_hubs(
     const uint32_t cv = cl[v];
     uint32_t lo = 0, hi = 0xffffffffu;  // v's rank when part
     if (part) pm.bounds(v, lo, hi);
-    for (uint64_t e0 = eb; e0 < ee; e0 += 32) {
-      const uint64_t e = e0 + lane;
-      bool keep = false;
-      uint64_t key = 0;
-      if (e < ee) {
-        uint32_t u = load_id(col, e);
-        uint32_t cu = cl[u];
-        key = ((uint64_t)cv << b) | cu;
-        keep = cu != cv && (!part || u < lo || u >= hi);
+    // four steps of 32 entries at a time: their id loads are issued together,
+    // then the cluster gathers of the entries that can be kept (with virtual
+    // ranks only those that leave the rank: most entries of a hub row stay
+    // inside it)
+    constexpr int kSteps = (int)kEmitSteps;
+    for (uint64_t e0 = eb; e0 < ee; e0 += 32 * kSteps) {
+      uint32_t us[kSteps], cus[kSteps];
+#pragma unroll
+      for (int q = 0; q < kSteps; ++q) {
+        const uint64_t e = e0 + 32 * q + lane;
+        us[q] = e < ee ? load_id(col, e) : 0u;
       }
-      st.put(keep, key, lane);
-      if (st.fill >= st.trigger) st.flush(lane, keys, cnt);
+#pragma unroll
+      for (int q = 0; q < kSteps; ++q) {
+        const uint64_t e = e0 + 32 * q + lane;
+        const bool need = e < ee && (!part || us[q] < lo || us[q] >= hi);
+        cus[q] = need ? cl[us[q]] : cv;  // cv: not kept
+      }
+#pragma unroll
+      for (int q = 0; q < kSteps; ++q) {
+        st.put(cus[q] != cv, ((uint64_t)cv << b) | cus[q], lane);
+        if (st.fill >= st.trigger) st.flush(lane, keys, cnt);
+      }
     }
   }
   if (st.fill) st.flush(lane, keys, cnt);
@@ -546,8 +610,16 @@ void emit_keys(const Csr &g, const uint32_t *cl, const PartMap &pm, bool part, i
   CCG_CUDA(cudaMemsetAsync(nh.p, 0, 4, s));
   const unsigned egrid = grid_for(g.n, kBlock, num_sms() * kEmitCtasPerSM);
   cudaEvent_t t0 = c.tic(s);
-  k_emit<T><<<egrid, kBlock, 0, s>>>(g.n, g.rp, col, cl, pm, part, b, hub_limit, hubs.as<uint2>(),
-                                     cap, nh.as<unsigned int>(), keys, cnt);
+  // virtual ranks, 32-bit ids on a 16-byte aligned array: the rank-local
+  // groups stream their entries with 16-byte loads
+  if (part && sizeof(T) == 4 && (reinterpret_cast<uintptr_t>(col) & 15) == 0)
+    k_emit<T, true><<<egrid, kBlock, 0, s>>>(g.n, g.rp, col, cl, pm, part, b, hub_limit,
+                                             hubs.as<uint2>(), cap, nh.as<unsigned int>(), keys, cnt,
+                                             g.m);
+  else
+    k_emit<T, false><<<egrid, kBlock, 0, s>>>(g.n, g.rp, col, cl, pm, part, b, hub_limit,
+                                              hubs.as<uint2>(), cap, nh.as<unsigned int>(), keys,
+                                              cnt, g.m);
   CCG_LAUNCH_CHECK();
   k_emit_hubs<T><<<num_sms() * kEmitCtasPerSM, kBlock, 0, s>>>(
       g.rp, col, cl, pm, part, b, hubs.as<uint2>(), cap, nh.as<unsigned int>(), keys, cnt);
