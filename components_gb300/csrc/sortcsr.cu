@@ -365,73 +365,70 @@ __global__ void __launch_bounds__(kBlock, VEC ? 4 : 5) k_emit(uint64_t n, const 
         on = 0;
       };
       if constexpr (VEC && sizeof(T) == 4) {
-        {
-          // 16-byte loads: lane j of a step reads entries a0 + 4j .. a0 + 4j + 3
-          // (a0 = the group's first entry rounded down to a multiple of four),
-          // kVecSteps such loads per lane in flight together, which covers a
-          // typical 32-row group at once.  Entries outside the group are
-          // loaded and ignored; a vector that would reach past the id array is
-          // read entry by entry.
-          const uint64_t a0 = base & ~3ull;
-          const uint32_t head = (uint32_t)(base - a0);
-          const uint32_t nv = (head + total + 3) / 4;
-          for (uint32_t j0 = 0; j0 < nv; j0 += 32 * kVecSteps) {
-            uint4 w[kVecSteps];
+        // 16-byte loads: lane j of a step reads entries a0 + 4j .. a0 + 4j + 3
+        // (a0 = the group's first entry rounded down to a multiple of four),
+        // kVecSteps such loads per lane in flight together, which covers a
+        // typical 32-row group at once.  Entries outside the group are
+        // loaded and ignored; a vector that would reach past the id array is
+        // read entry by entry.
+        const uint64_t a0 = base & ~3ull;
+        const uint32_t head = (uint32_t)(base - a0);
+        const uint32_t nv = (head + total + 3) / 4;
+        for (uint32_t j0 = 0; j0 < nv; j0 += 32 * kVecSteps) {
+          uint4 w[kVecSteps];
 #pragma unroll
-            for (int q = 0; q < kVecSteps; ++q) {
-              const uint32_t j = j0 + 32 * q + lane;
-              const uint64_t e = a0 + 4ull * j;
-              w[q] = make_uint4(lo0, lo0, lo0, lo0);  // inside the rank: never kept
-              if (j < nv) {
-                if (e + 4 <= m) {
-                  w[q] = __ldg(reinterpret_cast<const uint4 *>(col + e));
-                } else {
-                  if (e < m) w[q].x = (uint32_t)col[e];
-                  if (e + 1 < m) w[q].y = (uint32_t)col[e + 1];
-                  if (e + 2 < m) w[q].z = (uint32_t)col[e + 2];
-                }
-              }
-            }
-#pragma unroll
-            for (int q = 0; q < kVecSteps; ++q) {
-              if (j0 + 32 * q >= nv) continue;  // warp-uniform
-              if (on > kOutList - 128) drain();  // room for this vector's entries
-              const uint32_t f4 = 4 * (j0 + 32 * q + lane);  // f of component 0, plus head
-              const uint32_t uu[4] = {w[q].x, w[q].y, w[q].z, w[q].w};
-#pragma unroll
-              for (int t = 0; t < 4; ++t) {
-                const uint32_t u = uu[t];
-                const bool in_group = f4 + t >= head && f4 + t - head < total;
-                const bool out = in_group && (u < lo0 || u >= hi0);
-                const unsigned om = __ballot_sync(0xffffffffu, out);
-                if (out)
-                  olist[on + __popc(om & ((1u << lane) - 1u))] =
-                      ((uint64_t)(f4 + t - head) << 32) | u;
-                on += __popc(om);
+          for (int q = 0; q < kVecSteps; ++q) {
+            const uint32_t j = j0 + 32 * q + lane;
+            const uint64_t e = a0 + 4ull * j;
+            w[q] = make_uint4(lo0, lo0, lo0, lo0);  // inside the rank: never kept
+            if (j < nv) {
+              if (e + 4 <= m) {
+                w[q] = __ldg(reinterpret_cast<const uint4 *>(col + e));
+              } else {
+                if (e < m) w[q].x = (uint32_t)col[e];
+                if (e + 1 < m) w[q].y = (uint32_t)col[e + 1];
+                if (e + 2 < m) w[q].z = (uint32_t)col[e + 2];
               }
             }
           }
-          if (on) drain();
-          continue;
-        }
-      }
-      for (uint32_t f0 = 0; f0 < total; f0 += 32 * kSteps) {
-        uint32_t us[kSteps];
 #pragma unroll
-        for (int q = 0; q < kSteps; ++q) {
-          const uint32_t f = f0 + 32 * q + lane;
-          us[q] = f < total ? load_id(col, base + f) : lo0;  // past the range: inside the rank
-        }
+          for (int q = 0; q < kVecSteps; ++q) {
+            if (j0 + 32 * q >= nv) continue;  // warp-uniform
+            if (on > kOutList - 128) drain();  // room for this vector's entries
+            const uint32_t f4 = 4 * (j0 + 32 * q + lane);  // f of component 0, plus head
+            const uint32_t uu[4] = {w[q].x, w[q].y, w[q].z, w[q].w};
 #pragma unroll
-        for (int q = 0; q < kSteps; ++q) {
-          const uint32_t u = us[q];
-          const bool out = u < lo0 || u >= hi0;  // false past the range
-          const unsigned om = __ballot_sync(0xffffffffu, out);
-          if (out)
-            olist[on + __popc(om & ((1u << lane) - 1u))] = ((uint64_t)(f0 + 32 * q + lane) << 32) | u;
-          on += __popc(om);
+            for (int t = 0; t < 4; ++t) {
+              const uint32_t u = uu[t];
+              const bool in_group = f4 + t >= head && f4 + t - head < total;
+              const bool out = in_group && (u < lo0 || u >= hi0);
+              const unsigned om = __ballot_sync(0xffffffffu, out);
+              if (out)
+                olist[on + __popc(om & ((1u << lane) - 1u))] =
+                    ((uint64_t)(f4 + t - head) << 32) | u;
+              on += __popc(om);
+            }
+          }
         }
-        if (on > kOutList - 32 * kSteps) drain();  // room for the next batch
+      } else {
+        for (uint32_t f0 = 0; f0 < total; f0 += 32 * kSteps) {
+          uint32_t us[kSteps];
+#pragma unroll
+          for (int q = 0; q < kSteps; ++q) {
+            const uint32_t f = f0 + 32 * q + lane;
+            us[q] = f < total ? load_id(col, base + f) : lo0;  // past the range: inside the rank
+          }
+#pragma unroll
+          for (int q = 0; q < kSteps; ++q) {
+            const uint32_t u = us[q];
+            const bool out = u < lo0 || u >= hi0;  // false past the range
+            const unsigned om = __ballot_sync(0xffffffffu, out);
+            if (out)
+              olist[on + __popc(om & ((1u << lane) - 1u))] = ((uint64_t)(f0 + 32 * q + lane) << 32) | u;
+            on += __popc(om);
+          }
+          if (on > kOutList - 32 * kSteps) drain();  // room for the next batch
+        }
       }
       if (on) drain();
       continue;
@@ -544,24 +541,34 @@ struct PutUniq {
     if (f) o[excl] = k[i];
   }
 };
-struct GetFlag {
-  const uint32_t *f;
-  __device__ uint32_t operator()(uint64_t i) const { return f[i] ? 1u : 0u; }
-};
-struct PutNewId {
-  uint32_t *o;  // may alias the flag array: each index is read then written once
-  __device__ void operator()(uint64_t i, uint32_t excl, uint32_t f) const {
-    o[i] = f ? excl : kNone;
+// New vertex ids of the component graph: the sources of the unique keys in
+// key order (the sorted keys of one source are adjacent), numbered by a scan
+// over the unique keys.  The first key of each source also gives that
+// vertex's row start and its original id.  Clusters with no key keep kNone
+// (set before the scan).
+struct GetSrcStart {
+  const uint64_t *uk;
+  const uint32_t *d_u;  // number of unique keys
+  int b;
+  __device__ uint32_t operator()(uint64_t i) const {
+    if (i >= *d_u) return 0u;
+    return (i == 0 || (uk[i] >> b) != (uk[i - 1] >> b)) ? 1u : 0u;
   }
 };
-
-__global__ void k_mark_src(const uint64_t *__restrict__ uk, const uint32_t *__restrict__ d_u,
-                           int b, uint32_t *__restrict__ flag) {
-  uint32_t u = *d_u;
-  for (uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; e < u;
-       e += (uint64_t)gridDim.x * blockDim.x)
-    flag[uk[e] >> b] = 1u;
-}
+struct PutSrcId {
+  const uint64_t *uk;
+  int b;
+  uint32_t *newid, *vid;
+  uint64_t *rp;
+  const uint32_t *vid_of_cluster;  // null: a cluster's id is its original id
+  __device__ void operator()(uint64_t i, uint32_t excl, uint32_t f) const {
+    if (!f) return;
+    const uint32_t c = (uint32_t)(uk[i] >> b);
+    newid[c] = excl;
+    vid[excl] = vid_of_cluster ? vid_of_cluster[c] : c;
+    rp[excl] = i;
+  }
+};
 
 __global__ void k_build_csr(const uint64_t *__restrict__ uk, const uint32_t *__restrict__ d_u,
                             int b, const uint32_t *__restrict__ newid, uint64_t *__restrict__ rp,
@@ -569,22 +576,9 @@ __global__ void k_build_csr(const uint64_t *__restrict__ uk, const uint32_t *__r
   uint32_t u = *d_u;
   const uint64_t mask = (b == 64) ? ~0ull : ((1ull << b) - 1);
   for (uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; e < u;
-       e += (uint64_t)gridDim.x * blockDim.x) {
-    uint64_t key = uk[e];
-    uint32_t s = (uint32_t)(key >> b);
-    if (e == 0 || (uint32_t)(uk[e - 1] >> b) != s) rp[newid[s]] = e;
-    col[e] = newid[(uint32_t)(key & mask)];
-  }
+       e += (uint64_t)gridDim.x * blockDim.x)
+    col[e] = newid[(uint32_t)(uk[e] & mask)];
   if (blockIdx.x == 0 && threadIdx.x == 0) rp[*d_nv] = u;
-}
-
-__global__ void k_vid(uint64_t ncl, const uint32_t *__restrict__ newid,
-                      const uint32_t *__restrict__ vid_of_cluster, uint32_t *__restrict__ vid) {
-  for (uint64_t c = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; c < ncl;
-       c += (uint64_t)gridDim.x * blockDim.x) {
-    uint32_t id = newid[c];
-    if (id != kNone) vid[id] = vid_of_cluster ? vid_of_cluster[c] : (uint32_t)c;
-  }
 }
 
 int bits_for(uint64_t x) {  // bits needed to hold values < x
@@ -803,34 +797,32 @@ void contract_graph(const Csr &g, const uint32_t *cl, uint64_t ncl,
   DevBuf d_u(4, s, pool), d_nv(4, s, pool);
   scan_generic(ne, GetUniq{sorted}, PutUniq{sorted, uk}, d_u.as<uint32_t>(), s, pool, c);
   c.add(0, 8 * ne + 8 * ne);  // dedup: read keys, write uniques (upper bound)
-  // source flags -> new ids (order preserving)
-  CCG_CUDA(cudaMemsetAsync(out.newid.p, 0, 4 * ncl, s));
-  k_mark_src<<<grid_for(ne, kBlock, num_sms() * 16), kBlock, 0, s>>>(uk, d_u.as<uint32_t>(), b,
-                                                               out.newid.as<uint32_t>());
-  CCG_LAUNCH_CHECK();
-  scan_generic(ncl, GetFlag{out.newid.as<uint32_t>()}, PutNewId{out.newid.as<uint32_t>()},
+  // new ids (order preserving), original ids and row starts from the unique
+  // keys alone: no pass over all ncl clusters but the kNone fill.  Every new
+  // vertex is the source of a unique key, so ne bounds their number.
+  CCG_CUDA(cudaMemsetAsync(out.newid.p, 0xff, 4 * ncl, s));
+  out.rp.alloc(8 * (ne + 1), s, pool);
+  out.vid.alloc(4 * ne, s, pool);
+  scan_generic(ne, GetSrcStart{uk, d_u.as<uint32_t>(), b},
+               PutSrcId{uk, b, out.newid.as<uint32_t>(), out.vid.as<uint32_t>(), out.rp.as<uint64_t>(),
+                        vid_of_cluster},
                d_nv.as<uint32_t>(), s, pool, c);
-  c.toc(s, "contract_dedup", td, 16 * ne + 8 * ncl);
+  c.toc(s, "contract_dedup", td, 16 * ne + 4 * ncl + 8 * ne);
   uint32_t uv[2];
   CCG_CUDA(cudaMemcpyAsync(&uv[0], d_u.p, 4, cudaMemcpyDeviceToHost, s));
   CCG_CUDA(cudaMemcpyAsync(&uv[1], d_nv.p, 4, cudaMemcpyDeviceToHost, s));
   CCG_CUDA(cudaStreamSynchronize(s));
   out.m = uv[0];
   out.n = uv[1];
-  out.rp.alloc(8 * (out.n + 1), s, pool);
   out.col.alloc(4 * out.m, s, pool);
-  out.vid.alloc(4 * (out.n ? out.n : 1), s, pool);
   cudaEvent_t tb = c.tic(s);
   k_build_csr<<<grid_for(out.m, kBlock, num_sms() * 16), kBlock, 0, s>>>(
       uk, d_u.as<uint32_t>(), b, out.newid.as<uint32_t>(), out.rp.as<uint64_t>(),
       out.col.as<uint32_t>(), d_nv.as<uint32_t>());
   CCG_LAUNCH_CHECK();
-  k_vid<<<grid_for(ncl, kBlock, num_sms() * 16), kBlock, 0, s>>>(ncl, out.newid.as<uint32_t>(),
-                                                           vid_of_cluster, out.vid.as<uint32_t>());
-  CCG_LAUNCH_CHECK();
-  // CSR rebuild: unique keys read, offsets + ids written, id map
-  c.toc(s, "contract_csr", tb, 8 * out.m + 8 * (out.n + 1) + 4 * out.m + 8 * ncl);
-  c.add(4, 8 * out.m + 8 * (out.n + 1) + 4 * out.m + 8 * ncl);
+  // CSR rebuild: unique keys read, ids written, one target id gathered each
+  c.toc(s, "contract_csr", tb, 8 * out.m + 4 * out.m + 4 * out.m);
+  c.add(2, 16 * out.m + 4 * ncl + 8 * ne);
 }
 
 }  // namespace ccg
