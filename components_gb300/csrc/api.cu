@@ -203,13 +203,16 @@ struct Solver {
   }
 
   // RunContractionLP / RunContractionBFS recursion (exponential_contraction.h:
-  // 364-389, 439-628): decompose, contract, recurse while m > limit.
-  void exp_levels(const Csr &G, const uint32_t *vid, uint32_t level, uint32_t *out) {
-    if (G.n == 0) return;
+  // 364-389, 439-628): decompose, contract, recurse while m > limit.  Returns
+  // true when no decomposition ran: out[i] is then vid of the smallest index
+  // of i's component (base_case), which is the component's smallest original
+  // id whenever vid increases with the index.
+  bool exp_levels(const Csr &G, const uint32_t *vid, uint32_t level, uint32_t *out) {
+    if (G.n == 0) return true;
     if (G.m <= limit || (int)level >= max_levels) {
       note_level(level, G, 0);
       base_case(G, vid, out);
-      return;
+      return true;
     }
     if (C->geo_beta != cfg.beta) {
       ccg::geo_table_upload(cfg.beta, C->d_geo, &C->geo_len, s);
@@ -235,6 +238,7 @@ struct Solver {
     exp_levels(G2, H.vid.as<uint32_t>(), level + 1, sub.as<uint32_t>());
     ccg::compose_labels(cl.as<uint32_t>(), H.newid.as<uint32_t>(), sub.as<uint32_t>(), vid, out,
                         G.n, s, c);
+    return false;
   }
 
   // LocalContraction::RunContraction recursion (local_contraction.h:157-300):
@@ -334,11 +338,17 @@ struct Solver {
           G.m = G0.m;
           G.rp = G0.rp.as<uint64_t>();
           G.col = G0.col.p;
-          exp_levels(G, G0.vid.as<uint32_t>(), 1, sub.as<uint32_t>());
+          const bool direct = exp_levels(G, G0.vid.as<uint32_t>(), 1, sub.as<uint32_t>());
           ccg::compose_labels(lab, G0.newid.as<uint32_t>(), sub.as<uint32_t>(), nullptr, lab, n,
                               s, c);
-          DevBuf scratch(4 * n, s, pool);
-          ccg::canonicalize(lab, scratch.as<uint32_t>(), n, s, c);
+          // Without a decomposition level the labels are canonical already:
+          // G0 numbers the local components in increasing order of their
+          // smallest ids (G0.vid increases), so the base case's smallest
+          // index per component is the component's smallest vertex id.
+          if (!direct) {
+            DevBuf scratch(4 * n, s, pool);
+            ccg::canonicalize(lab, scratch.as<uint32_t>(), n, s, c);
+          }
         }
         break;
       }
