@@ -25,33 +25,6 @@
 namespace ccg {
 namespace {
 
-// ---- shared-memory union-find -------------------------------------------------
-__device__ __forceinline__ uint32_t s_find(volatile uint32_t *p, uint32_t v) {
-  uint32_t cur = p[v];
-  if (cur == v) return v;
-  uint32_t prev = v, next;
-  while (cur > (next = p[cur])) {
-    p[prev] = next;
-    prev = cur;
-    cur = next;
-  }
-  return cur;
-}
-__device__ __forceinline__ void s_union(volatile uint32_t *p, uint32_t a, uint32_t b) {
-  uint32_t ra = s_find(p, a), rb = s_find(p, b);
-  while (ra != rb) {
-    if (ra < rb) {
-      uint32_t t = ra;
-      ra = rb;
-      rb = t;
-    }
-    uint32_t old = atomicCAS((uint32_t *)(p + ra), ra, rb);
-    if (old == ra) return;
-    ra = s_find(p, old);
-    rb = s_find(p, rb);
-  }
-}
-
 struct BatchArgs {
   const uint64_t *voff;
   const uint64_t *rp;
@@ -95,7 +68,7 @@ __global__ void k_batch_smem(BatchArgs a, const uint32_t *__restrict__ list, uin
             set_err(a.err, kErrBadId);
             continue;
           }
-          if (u < v) s_union(p, v, u);
+          if (u < v) smem_union<false>(p, v, u);
         }
       }
     } else {
@@ -113,7 +86,7 @@ __global__ void k_batch_smem(BatchArgs a, const uint32_t *__restrict__ list, uin
           set_err(a.err, kErrBadId);
           continue;
         }
-        if (u < lo) s_union(p, lo, u);
+        if (u < lo) smem_union<false>(p, lo, u);
       }
     }
     __syncthreads();

@@ -173,6 +173,58 @@ __device__ __forceinline__ void st_cg(uint64_t *p, uint64_t v) {
   __stcg(reinterpret_cast<unsigned long long *>(p), (unsigned long long)v);
 }
 
+// ---- union-find in shared memory ----------------------------------------------
+// Used by the tiled pass (uf.cu), the batched solve (batch.cu) and the server's
+// small graphs (serve.cu).  A non-root entry always points at a smaller index,
+// so the forest stays acyclic and each root is the smallest index of its tree;
+// a find points every entry it passes at its grandparent.  Entries are 16 or
+// 32 bits wide.
+__device__ __forceinline__ uint32_t smem_cas(uint16_t *a, uint32_t c, uint32_t v) {
+  return atomicCAS(reinterpret_cast<unsigned short *>(a), (unsigned short)c, (unsigned short)v);
+}
+__device__ __forceinline__ uint32_t smem_cas(uint32_t *a, uint32_t c, uint32_t v) {
+  return atomicCAS(reinterpret_cast<unsigned int *>(a), c, v);
+}
+template <class PT>
+__device__ __forceinline__ uint32_t smem_find(volatile PT *p, uint32_t v) {
+  uint32_t cur = p[v];
+  if (cur == v) return v;
+  uint32_t prev = v, next;
+  while (cur > (next = p[cur])) {
+    p[prev] = (PT)next;
+    prev = cur;
+    cur = next;
+  }
+  return cur;
+}
+// Union of a and b: the larger root is CAS'ed under the smaller one.  With
+// POINT_ENDS, both endpoints then point straight at the common root they saw
+// (an ancestor of both, never a root that could still be CAS'ed: an endpoint
+// other than that root has a parent already), so the next edges of a and b
+// start next to the root.
+template <bool POINT_ENDS, class PT>
+__device__ __forceinline__ void smem_union(volatile PT *p, uint32_t a, uint32_t b) {
+  uint32_t ra = smem_find(p, a), rb = smem_find(p, b);
+  while (ra != rb) {
+    if (ra < rb) {
+      const uint32_t t = ra;
+      ra = rb;
+      rb = t;
+    }
+    const uint32_t old = smem_cas(const_cast<PT *>(p + ra), ra, rb);
+    if (old == ra) {
+      ra = rb;
+      break;
+    }
+    ra = smem_find(p, old);
+    rb = smem_find(p, rb);
+  }
+  if (POINT_ENDS) {
+    if (a != ra) p[a] = (PT)ra;
+    if (b != ra) p[b] = (PT)ra;
+  }
+}
+
 template <class T>
 __device__ __forceinline__ uint32_t load_id(const T *col, uint64_t e) {
   return (uint32_t)__ldg(col + e);

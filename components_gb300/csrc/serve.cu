@@ -50,32 +50,6 @@ struct GraphDesc {
   uint32_t idb;
 };
 
-__device__ __forceinline__ uint32_t sv_find(volatile uint32_t *p, uint32_t v) {
-  uint32_t cur = p[v];
-  if (cur == v) return v;
-  uint32_t prev = v, next;
-  while (cur > (next = p[cur])) {
-    p[prev] = next;
-    prev = cur;
-    cur = next;
-  }
-  return cur;
-}
-__device__ __forceinline__ void sv_union(volatile uint32_t *p, uint32_t a, uint32_t b) {
-  uint32_t ra = sv_find(p, a), rb = sv_find(p, b);
-  while (ra != rb) {
-    if (ra < rb) {
-      uint32_t t = ra;
-      ra = rb;
-      rb = t;
-    }
-    uint32_t old = atomicCAS((uint32_t *)(p + ra), ra, rb);
-    if (old == ra) return;
-    ra = sv_find(p, old);
-    rb = sv_find(p, rb);
-  }
-}
-
 // One CTA per small graph of the batch; persistent CTAs pull descriptors.
 __global__ void k_serve_smem(const GraphDesc *__restrict__ descs, uint32_t count,
                              unsigned int *__restrict__ queue) {
@@ -105,7 +79,7 @@ __global__ void k_serve_smem(const GraphDesc *__restrict__ descs, uint32_t count
           set_err(err, kErrBadId);
           continue;
         }
-        if (u < v) sv_union(p, v, (uint32_t)u);
+        if (u < v) smem_union<false>(p, v, (uint32_t)u);
       }
     }
     __syncthreads();

@@ -468,49 +468,6 @@ __global__ void k_iota_parent(uint64_t n, uint32_t *p) {
 // rank (FindLocalComponents, exponential_contraction.h:391-411).
 // Shared-memory parent entries are 16 bits wide in the hook pass and 32 bits
 // in link mode (TileParent below).
-__device__ __forceinline__ uint32_t ts_cas(uint16_t *a, uint32_t c, uint32_t v) {
-  return atomicCAS(reinterpret_cast<unsigned short *>(a), (unsigned short)c, (unsigned short)v);
-}
-__device__ __forceinline__ uint32_t ts_cas(uint32_t *a, uint32_t c, uint32_t v) {
-  return atomicCAS(reinterpret_cast<unsigned int *>(a), c, v);
-}
-template <class PT>
-__device__ __forceinline__ uint32_t tw_find(volatile PT *p, uint32_t v) {
-  uint32_t cur = p[v];
-  if (cur == v) return v;
-  uint32_t prev = v, next;
-  while (cur > (next = p[cur])) {
-    p[prev] = (PT)next;
-    prev = cur;
-    cur = next;
-  }
-  return cur;
-}
-// Union of a and b; afterwards both endpoints point straight at the common
-// root they saw (an ancestor of both, never a root that could still be CAS'ed:
-// an endpoint different from that root has a parent already), so the next
-// edges of a and b start next to the root.
-template <class PT>
-__device__ __forceinline__ void tw_union(volatile PT *p, uint32_t a, uint32_t b) {
-  uint32_t ra = tw_find(p, a), rb = tw_find(p, b);
-  while (ra != rb) {
-    if (ra < rb) {
-      uint32_t t = ra;
-      ra = rb;
-      rb = t;
-    }
-    const uint32_t old = ts_cas(const_cast<PT *>(p + ra), ra, rb);
-    if (old == ra) {
-      ra = rb;
-      break;
-    }
-    ra = tw_find(p, old);
-    rb = tw_find(p, rb);
-  }
-  if (a != ra) p[a] = (PT)ra;
-  if (b != ra) p[b] = (PT)ra;
-}
-
 __device__ __forceinline__ uint64_t shfl64(uint64_t x, int src) {
   const uint32_t lo = __shfl_sync(0xffffffffu, (uint32_t)x, src);
   const uint32_t hi = __shfl_sync(0xffffffffu, (uint32_t)(x >> 32), src);
@@ -597,7 +554,7 @@ __global__ void __launch_bounds__(1024, 2)
             if (u >= tt && u - tt < len) {
               if (may_hook && !hooked && u < vv) {  // the hook needs a smaller parent
                 hooked = true;
-                uni = ts_cas(const_cast<PT *>(s + vi), vi, u - tt) != vi;
+                uni = smem_cas(const_cast<PT *>(s + vi), vi, u - tt) != vi;
               } else {
                 uni = true;
               }
@@ -611,7 +568,7 @@ __global__ void __launch_bounds__(1024, 2)
             emit = true;
           } else if (may_hook && !hooked) {
             hooked = true;
-            uni = ts_cas(const_cast<PT *>(s + vi), vi, u - tt) != vi;  // hooked, or queue
+            uni = smem_cas(const_cast<PT *>(s + vi), vi, u - tt) != vi;  // hooked, or queue
           } else {
             uni = true;
           }
@@ -623,7 +580,7 @@ __global__ void __launch_bounds__(1024, 2)
       if (qn >= 32) {  // a full union step: the newest 32 entries
         __syncwarp();
         const uint32_t w = q[qn - 32 + lane];
-        tw_union(s, w & 0xffffu, w >> 16);
+        smem_union<true>(s, w & 0xffffu, w >> 16);
         qn -= 32;
         __syncwarp();
       }
@@ -755,11 +712,11 @@ __global__ void __launch_bounds__(1024, 2)
     __syncwarp();
     if (lane < qn) {  // the queue's remainder
       const uint32_t w = q[lane];
-      tw_union(s, w & 0xffffu, w >> 16);
+      smem_union<true>(s, w & 0xffffu, w >> 16);
     }
     __syncthreads();
     // every vertex stores the global id of its tile-local root
-    for (uint32_t i = threadIdx.x; i < len; i += blockDim.x) p[t0 + i] = tt + tw_find(s, i);
+    for (uint32_t i = threadIdx.x; i < len; i += blockDim.x) p[t0 + i] = tt + smem_find(s, i);
     const unsigned int nc = min(ccount, stage_cap);
     if (LINK) {
       // Link rounds: many rows of a tile link to the same far vertex (a hub),
@@ -775,7 +732,7 @@ __global__ void __launch_bounds__(1024, 2)
       __syncthreads();
       for (uint32_t k = threadIdx.x; k < nc; k += blockDim.x) {
         uint2 c = cstage[k];
-        c.x = tt + tw_find(s, c.x);
+        c.x = tt + smem_find(s, c.x);
         const unsigned long long key = ((unsigned long long)c.x << 32) | c.y;
         uint32_t h = (uint32_t)(mix64(key) % slots);
         bool keep = true;
@@ -811,7 +768,7 @@ __global__ void __launch_bounds__(1024, 2)
       for (uint32_t k = threadIdx.x; k < nc; k += blockDim.x) {
         const uint2 c = cstage[k];
         const unsigned long long g = cbase + k;
-        if (g < cut_cap) cut[g] = make_uint2(tt + tw_find(s, c.x), c.y);
+        if (g < cut_cap) cut[g] = make_uint2(tt + smem_find(s, c.x), c.y);
         else set_err(err, kErrOverflow);
       }
     }
