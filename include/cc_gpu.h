@@ -293,8 +293,10 @@ typedef struct cc_tuning {
                               edges in hub rows, GLOBAL when the graph fits in
                               96 MB (L2-resident) with < 10 % hub edges, else
                               SAMPLED */
-  uint32_t tile_vertices;  /* vertices per CTA tile, 2 bytes of shared memory
-                              each (default 32768, 32 to 65536) */
+  uint32_t tile_vertices;  /* vertices per CTA tile of the TILED pass, 2 bytes
+                              of shared memory each (default 32768, 32 to
+                              65536); SAMPLED's tiled link rounds use half as
+                              many vertices, 4 bytes each */
   uint32_t tile_threads;   /* CTA size of the tiled pass (default 1024) */
   uint32_t hub_degree;     /* rows above are split into pieces of 2048 edges,
                               one warp per piece (default 32) */
