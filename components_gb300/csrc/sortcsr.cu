@@ -615,7 +615,12 @@ void emit_keys(const Csr &g, const uint32_t *cl, const PartMap &pm, bool part, i
                                               hubs.as<uint2>(), cap, nh.as<unsigned int>(), keys,
                                               cnt, g.m);
   CCG_LAUNCH_CHECK();
-  k_emit_hubs<T><<<num_sms() * kEmitCtasPerSM, kBlock, 0, s>>>(
+  // at most cap pieces, one warp each: a small graph gets a small grid (every
+  // CTA clears its 16 KB key set, which had cost 45 us per launch on the
+  // small level graphs of local contraction)
+  const unsigned hgrid = (unsigned)std::min<uint64_t>((uint64_t)num_sms() * kEmitCtasPerSM,
+                                                      (cap + kBlock / 32 - 1) / (kBlock / 32));
+  k_emit_hubs<T><<<hgrid, kBlock, 0, s>>>(
       g.rp, col, cl, pm, part, b, hubs.as<uint2>(), cap, nh.as<unsigned int>(), keys, cnt);
   CCG_LAUNCH_CHECK();
   // algorithmic bytes: offsets, ids and own clusters; a neighbour's cluster
