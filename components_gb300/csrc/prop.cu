@@ -5,7 +5,12 @@
 namespace ccg {
 namespace {
 
-constexpr uint64_t kRowLimit = 64;
+// Rows above a limit are relaxed a warp per piece of 2048 entries (the
+// *_pieces kernels); shorter rows a thread each.  On the 2^26-vertex
+// hyperbolic graph the best limit differs per option: label propagation
+// 25.7 / 19.2 / 18.1 ms and shortcuts 13.2 / 13.0 / 13.9 ms for limits of
+// 64 / 128 / 256 entries.
+constexpr uint64_t kLabelRowLimit = 256, kShortcutRowLimit = 128;
 
 // ---- Propagation (propagation.h:72-149) ------------------------------------
 // lab[v] <- min(lab[v], min_u lab[u]) in place.  The reference updates local
@@ -28,7 +33,7 @@ template <bool CHECK>
 __global__ void k_labels_round(uint64_t n, const uint64_t *__restrict__ rp,
                                const uint32_t *__restrict__ col, uint32_t *lab,
                                const uint32_t *__restrict__ act, uint32_t *__restrict__ chg,
-                               unsigned int *nchanged, int *err) {
+                               unsigned int *nchanged, int *err, uint64_t row_limit) {
   __shared__ unsigned int block_changed;
   if (threadIdx.x == 0) block_changed = 0;
   __syncthreads();
@@ -38,7 +43,7 @@ __global__ void k_labels_round(uint64_t n, const uint64_t *__restrict__ rp,
     bool changed = false;
     if (v < n && (!act || bit_of(act, v))) {
       const uint64_t b = __ldg(rp + v), e = __ldg(rp + v + 1);
-      if (e - b <= kRowLimit) {
+      if (e - b <= row_limit) {
         const uint32_t l = ld_cg(lab + v);
         bool bad = false;
         const uint32_t best = row_min_ilp<uint32_t>(col, b, e, l, [&](uint32_t u) {
@@ -65,7 +70,7 @@ __global__ void k_labels_round(uint64_t n, const uint64_t *__restrict__ rp,
   if (threadIdx.x == 0 && block_changed) atomicAdd(nchanged, block_changed);
 }
 
-// Rows above kRowLimit entries, one warp per piece of the row.
+// Rows above the row limit, one warp per piece of the row.
 template <bool CHECK>
 __global__ void k_labels_round_pieces(uint64_t n, const uint64_t *__restrict__ rp,
                                       const uint32_t *__restrict__ col, RowPieces rpc, uint32_t *lab,
@@ -120,7 +125,7 @@ template <bool CHECK>
 __global__ void k_sc_min(uint64_t n, const uint64_t *__restrict__ rp,
                          const uint32_t *__restrict__ col, const uint32_t *__restrict__ f,
                          uint32_t *__restrict__ nf, uint32_t *upd,
-                         const uint32_t *__restrict__ act, int *err) {
+                         const uint32_t *__restrict__ act, int *err, uint64_t row_limit) {
   const uint64_t span = (n + 31) / 32 * 32;  // warp-uniform trip count
   for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < span;
        v += (uint64_t)gridDim.x * blockDim.x) {
@@ -131,7 +136,7 @@ __global__ void k_sc_min(uint64_t n, const uint64_t *__restrict__ rp,
       if (!act || bit_of(act, v)) {
         const uint64_t b = __ldg(rp + v), e = __ldg(rp + v + 1);
         bool bad = false;
-        if (e - b <= kRowLimit)  // longer rows: k_sc_min_pieces folds their neighbours in
+        if (e - b <= row_limit)  // longer rows: k_sc_min_pieces folds their neighbours in
           best = row_min_ilp<uint32_t>(col, b, e, l, [&](uint32_t u) {
             if (CHECK && u >= n) {
               bad = true;
@@ -147,7 +152,7 @@ __global__ void k_sc_min(uint64_t n, const uint64_t *__restrict__ rp,
   }
 }
 
-// Rows above kRowLimit entries, one warp per piece of the row: each piece's
+// Rows above the row limit, one warp per piece of the row: each piece's
 // minimum is folded into nf[v] (which k_sc_min set to f[v]) and, when it is
 // below v's label, into the update addressed to that label; the minima over
 // pieces are the row's minimum, so nf and upd end as with one pass per row.
@@ -236,15 +241,15 @@ __global__ void k_sc_jump(uint64_t n, const uint32_t *__restrict__ f, uint32_t *
 
 // act |= the neighbours of every vertex whose bit is set in chg.  A row's ids
 // are sorted, so runs of neighbours in one 32-vertex word are merged into
-// one atomic; rows above kRowLimit entries go to k_mark_neighbours_pieces.
+// one atomic; rows above the row limit go to k_mark_neighbours_pieces.
 __global__ void k_mark_neighbours(uint64_t n, const uint64_t *__restrict__ rp,
                           const uint32_t *__restrict__ col, const uint32_t *__restrict__ chg,
-                          uint32_t *act) {
+                          uint32_t *act, uint64_t row_limit) {
   for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < n;
        v += (uint64_t)gridDim.x * blockDim.x) {
     if (!bit_of(chg, v)) continue;
     const uint64_t b = __ldg(rp + v), e = __ldg(rp + v + 1);
-    if (e - b > kRowLimit) continue;
+    if (e - b > row_limit) continue;
     uint32_t word = kNone, bits = 0;
     for (uint64_t k = b; k < e; ++k) {
       const uint32_t w = __ldg(col + k);
@@ -373,13 +378,13 @@ int labels_propagate(const Csr &g, uint32_t *lab, int max_rounds, cudaStream_t s
   if (g.n == 0) return 0;
   const uint32_t *col = static_cast<const uint32_t *>(g.col);
   unsigned grid = grid_for(g.n, kBlock, num_sms() * 32);
-  const uint64_t cap = row_pieces_cap(g.m, kRowLimit);
+  const uint64_t cap = row_pieces_cap(g.m, kLabelRowLimit);
   const uint64_t words = (g.n + 31) / 32;
   DevBuf items(8 * cap, s, pool), cnt(4, s, pool), chga(4 * words, s, pool),
       chgb(4 * words, s, pool), actb(4 * words, s, pool);
   CCG_CUDA(cudaMemsetAsync(cnt.p, 0, 4, s));
   const RowPieces rpc{items.as<uint2>(), cap, cnt.as<unsigned int>()};
-  k_row_pieces<<<grid, kBlock, 0, s>>>(g.n, g.rp, kRowLimit, rpc);
+  k_row_pieces<<<grid, kBlock, 0, s>>>(g.n, g.rp, kLabelRowLimit, rpc);
   CCG_LAUNCH_CHECK();
   uint32_t *chg = chga.as<uint32_t>(), *chg_prev = chgb.as<uint32_t>();
   unsigned int *nchanged = reinterpret_cast<unsigned int *>(dev_flag);
@@ -393,7 +398,8 @@ int labels_propagate(const Csr &g, uint32_t *lab, int max_rounds, cudaStream_t s
     if (sparse) {
       CCG_CUDA(cudaMemsetAsync(actb.p, 0, 4 * words, s));
       cudaEvent_t tp = c.tic(s);
-      k_mark_neighbours<<<grid, kBlock, 0, s>>>(g.n, g.rp, col, chg_prev, actb.as<uint32_t>());
+      k_mark_neighbours<<<grid, kBlock, 0, s>>>(g.n, g.rp, col, chg_prev, actb.as<uint32_t>(),
+                                                kLabelRowLimit);
       CCG_LAUNCH_CHECK();
       k_mark_neighbours_pieces<<<num_sms() * 8, kBlock, 0, s>>>(g.rp, col, rpc, chg_prev,
                                                         actb.as<uint32_t>());
@@ -404,13 +410,14 @@ int labels_propagate(const Csr &g, uint32_t *lab, int max_rounds, cudaStream_t s
     const bool check = g.err && rounds == 0;  // the caller's ids, not checked yet
     cudaEvent_t t0 = c.tic(s);
     if (check) {
-      k_labels_round<true><<<grid, kBlock, 0, s>>>(g.n, g.rp, col, lab, act, chg, nchanged, g.err);
+      k_labels_round<true><<<grid, kBlock, 0, s>>>(g.n, g.rp, col, lab, act, chg, nchanged, g.err,
+                                                    kLabelRowLimit);
       CCG_LAUNCH_CHECK();
       k_labels_round_pieces<true><<<num_sms() * 8, kBlock, 0, s>>>(g.n, g.rp, col, rpc, lab, act,
                                                                    chg, nchanged, g.err);
     } else {
       k_labels_round<false><<<grid, kBlock, 0, s>>>(g.n, g.rp, col, lab, act, chg, nchanged,
-                                                    nullptr);
+                                                    nullptr, kLabelRowLimit);
       CCG_LAUNCH_CHECK();
       k_labels_round_pieces<false><<<num_sms() * 8, kBlock, 0, s>>>(g.n, g.rp, col, rpc, lab, act,
                                                                     chg, nchanged, nullptr);
@@ -445,7 +452,7 @@ int shortcut_propagate(const Csr &g, uint32_t *lab, uint32_t hitters, int max_ro
   const uint64_t words = (g.n + 31) / 32;
   DevBuf nfb(4 * g.n, s, pool), updb(4 * g.n, s, pool), chgb(4 * words, s, pool),
       actb(4 * words, s, pool);
-  const uint64_t cap = row_pieces_cap(g.m, kRowLimit);
+  const uint64_t cap = row_pieces_cap(g.m, kShortcutRowLimit);
   DevBuf items(8 * cap, s, pool), npieces(4, s, pool);
   const RowPieces rpc{items.as<uint2>(), cap, npieces.as<unsigned int>()};
   DevBuf cnt, heavy;
@@ -455,7 +462,7 @@ int shortcut_propagate(const Csr &g, uint32_t *lab, uint32_t hitters, int max_ro
     CCG_CUDA(cudaMemsetAsync(heavy.p, 0, g.n, s));
   }
   CCG_CUDA(cudaMemsetAsync(npieces.p, 0, 4, s));
-  k_row_pieces<<<grid, kBlock, 0, s>>>(g.n, g.rp, kRowLimit, rpc);
+  k_row_pieces<<<grid, kBlock, 0, s>>>(g.n, g.rp, kShortcutRowLimit, rpc);
   CCG_LAUNCH_CHECK();
   uint32_t *f = lab, *nf = nfb.as<uint32_t>();
   const uint64_t min_bytes = 8 * (g.n + 1) + g.m * 4 + g.m * 4 + 2 * g.n * 4;
@@ -468,7 +475,7 @@ int shortcut_propagate(const Csr &g, uint32_t *lab, uint32_t hitters, int max_ro
       CCG_CUDA(cudaMemsetAsync(actb.p, 0, 4 * words, s));
       cudaEvent_t tp = c.tic(s);
       k_mark_neighbours<<<grid, kBlock, 0, s>>>(g.n, g.rp, col, chgb.as<uint32_t>(),
-                                                actb.as<uint32_t>());
+                                                actb.as<uint32_t>(), kShortcutRowLimit);
       CCG_LAUNCH_CHECK();
       k_mark_neighbours_pieces<<<num_sms() * 8, kBlock, 0, s>>>(g.rp, col, rpc, chgb.as<uint32_t>(),
                                                         actb.as<uint32_t>());
@@ -479,10 +486,11 @@ int shortcut_propagate(const Csr &g, uint32_t *lab, uint32_t hitters, int max_ro
     const bool check = g.err && rounds == 0;  // the caller's ids, not checked yet
     cudaEvent_t t0 = c.tic(s);
     if (check)
-      k_sc_min<true><<<grid, kBlock, 0, s>>>(g.n, g.rp, col, f, nf, updb.as<uint32_t>(), act, g.err);
+      k_sc_min<true><<<grid, kBlock, 0, s>>>(g.n, g.rp, col, f, nf, updb.as<uint32_t>(), act, g.err,
+                                             kShortcutRowLimit);
     else
       k_sc_min<false><<<grid, kBlock, 0, s>>>(g.n, g.rp, col, f, nf, updb.as<uint32_t>(), act,
-                                              nullptr);
+                                              nullptr, kShortcutRowLimit);
     CCG_LAUNCH_CHECK();
     // algorithmic bytes of a round over every row (a round over the active
     // rows only is not counted)
