@@ -598,7 +598,12 @@ void emit_keys(const Csr &g, const uint32_t *cl, const PartMap &pm, bool part, i
   // CTA's set, was measured slower without virtual ranks: 7.5 ms against
   // 5.3 ms for local contraction's first level on the 2^26-vertex hyperbolic
   // graph.)
-  const uint64_t hub_limit = 1024;
+  // With virtual ranks most row groups take the rank-local stream, which
+  // suits longer rows: the 16-rank emit on the 2^26-vertex hyperbolic graph
+  // took 2.14 / 1.91 / 1.80 / 1.85 / 2.04 ms with limits of 256 / 1024 / 4096
+  // / 16384 / 65536 entries; without ranks 1024 beats 4096 (5.22 against
+  // 5.44 ms over local contraction's levels).
+  const uint64_t hub_limit = part ? 4096 : 1024;
   const uint64_t cap = g.m / (hub_limit + 1) + g.m / kEmitPiece + 2;
   DevBuf hubs(8 * cap, s, pool), nh(4, s, pool);
   CCG_CUDA(cudaMemsetAsync(nh.p, 0, 4, s));
