@@ -486,6 +486,12 @@ __device__ __forceinline__ uint64_t shfl64(uint64_t x, int src) {
 // id of its tile-local root.
 constexpr uint32_t kUnionQueue = 64;  // per warp: < 32 pending + up to 32 new
 constexpr uint32_t kTileMax = 65536;  // queue entries pack two 16-bit tile indices
+// CTAs per SM of the cut union: the tiled pass's tile-crossing edges have
+// distinct endpoints and more threads in flight hide their latency (8192^2
+// grid: 0.270 / 0.246 / 0.224 ms at 16 / 32 / 64); the link rounds' crossing
+// edges pile onto a few hub roots, where more concurrent CASes fail and retry
+// (2^26 hyperbolic graph: 0.29 / 0.54 / 0.41 ms).
+constexpr unsigned kCutCtasTiled = 64, kCutCtasLink = 16;
 constexpr uint32_t kLinkGroups = 1;   // link mode: 32-row blocks per warp step (1 measured best of 1, 2, 4)
 // Parent entries of a tile in shared memory: 16 bits in the hook pass (twice
 // the vertices for the same shared memory: fewer tile-crossing edges on
@@ -1238,7 +1244,7 @@ void run_uf_tiled(const Csr &g, uint32_t *parent, const PartMap &pm, const UfTun
                                                               tu.hub_degree, hl, cut.as<uint2>(),
                                                               cut_cap, ncut, g.err);
       CCG_LAUNCH_CHECK();
-      k_cut_union<<<num_sms() * 16, kBlock, 0, s>>>(cut.as<uint2>(), ncut, cut_cap, parent, united);
+      k_cut_union<<<num_sms() * kCutCtasTiled, kBlock, 0, s>>>(cut.as<uint2>(), ncut, cut_cap, parent, united);
       CCG_LAUNCH_CHECK();
       CCG_CUDA(cudaMemcpyAsync(united, ncut, 8, cudaMemcpyDeviceToDevice, s));
     }
@@ -1246,7 +1252,7 @@ void run_uf_tiled(const Csr &g, uint32_t *parent, const PartMap &pm, const UfTun
   c.toc(s, hs ? "uf_tile_streamed" : "uf_tile", t0, tile_bytes);
   if (!hs) {
     cudaEvent_t t1 = c.tic(s);
-    k_cut_union<<<num_sms() * 16, kBlock, 0, s>>>(cut.as<uint2>(), ncut, cut_cap, parent);
+    k_cut_union<<<num_sms() * kCutCtasTiled, kBlock, 0, s>>>(cut.as<uint2>(), ncut, cut_cap, parent);
     CCG_LAUNCH_CHECK();
     c.toc(s, "uf_cut_union", t1, 0);
   }
@@ -1348,7 +1354,7 @@ void run_uf_afforest(const Csr &g, uint32_t *parent, const PartMap &pm, const Uf
     }
     c.toc(s, hs ? "uf_sample_link_streamed" : "uf_sample_link_tiled", t0, link_bytes);
     cudaEvent_t t1 = c.tic(s);
-    k_cut_union<<<num_sms() * 16, kBlock, 0, s>>>(cut.as<uint2>(), cnt.as<unsigned long long>(),
+    k_cut_union<<<num_sms() * kCutCtasLink, kBlock, 0, s>>>(cut.as<uint2>(), cnt.as<unsigned long long>(),
                                              cut_cap, parent);
     CCG_LAUNCH_CHECK();
     c.toc(s, "uf_cut_union", t1, 0);
