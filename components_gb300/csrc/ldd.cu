@@ -30,6 +30,11 @@
 #include "kernels.h"
 
 namespace ccg {
+// Sweeps bound to eight CTAs of 256 threads per SM (32 registers): the
+// id-checking first sweep had taken 38 registers, six CTAs per SM, and this
+// latency-bound gather runs faster with the two extra CTAs (local
+// contraction's sweeps on the 2^26 hyperbolic graph: 6.2 -> 5.9 ms).
+constexpr int kSweepCtasPerSM = 8;
 
 // exp(x) for x <= 0 from range reduction by ln 2 and a Taylor series, with a
 // fixed evaluation order (no library call, no contraction into FMA), so that
@@ -202,7 +207,7 @@ __global__ void k_local_clusters(uint64_t n, const uint32_t *__restrict__ best,
 // >= n is skipped and recorded in *err, which the host reads before any
 // kernel trusts the ids.
 template <bool CHECK>
-__global__ void k_min_sweep(uint64_t n, const uint64_t *__restrict__ rp,
+__global__ void __launch_bounds__(kBlock, kSweepCtasPerSM) k_min_sweep(uint64_t n, const uint64_t *__restrict__ rp,
                             const uint32_t *__restrict__ col, const uint32_t *__restrict__ in,
                             uint32_t *__restrict__ out, int *err) {
   for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < n;
