@@ -377,6 +377,16 @@ def gpu_arm(args, wl: Workload, rank: int, world: int, local: int) -> dict | Non
                 "frac": achieved / peak, "traffic": traffic,
                 "algorithmic_bytes_per_launch": per_launch_bytes, "ms_per_launch": per_launch_ms,
                 "peak_source": peak_src, "traffic_source": traffic_src}
+    # per-solve roofline (the survey's B_solve / t_solve): the library's sum of
+    # every launched kernel's algorithmic bytes over a solve, against the
+    # solve's CUDA-event time
+    solve_roof = None
+    if tot.get("solves") and tot.get("bytes_algorithmic") and tot.get("solve_ms"):
+        b_solve = tot["bytes_algorithmic"] / tot["solves"]
+        t_solve = tot["solve_ms"] / tot["solves"]
+        solve_roof = {"bytes_algorithmic_per_solve": b_solve, "ms_per_solve": t_solve,
+                      "achieved": b_solve / (t_solve * 1e-3) / 1e9, "peak": peak, "unit": "GB/s",
+                      "frac": b_solve / (t_solve * 1e-3) / 1e9 / peak}
     ksum = max(sum(x["ms"] for x in kstats.values()), 1e-12)
     share = {k: v["ms"] / ksum for k, v in kstats.items()}
     per_kernel = {k: {"launches_per_solve": v["launches"] / max(tot["solves"], 1),
@@ -428,6 +438,7 @@ def gpu_arm(args, wl: Workload, rank: int, world: int, local: int) -> dict | Non
                 "ms_steps": [round(x * 1e3, 3) for x in step_s]},
         "gpu_launches": launches,
         "roofline": roof,
+        "solve_roofline": solve_roof,
         "kernel_share": share,
         "per_kernel": per_kernel,
         "solve_ms_mean": solve_ms_mean,
