@@ -136,62 +136,152 @@ __device__ __forceinline__ void g_union(uint32_t *p, uint32_t a, uint32_t b) {
   }
 }
 
-// parent over the vertices of the large graphs, indexed by global vertex id
-// minus the first large vertex offset is not contiguous; it is indexed by
-// the global vertex id directly (the array spans total_n entries).
-__global__ void k_large_init(BatchArgs a, const Chunk *__restrict__ chunks, uint32_t nchunks,
+// Large graphs run sampled linking (Afforest: Sutton, Ben-Nun, Barak, IPDPS
+// 2018), as the single-graph solve does on graphs that do not suit the tiled
+// pass: every vertex links to its first two neighbours, the parents are
+// compressed, each graph's most frequent root in a sample of its vertices is
+// taken as its giant component, and only rows outside it process their
+// remaining entries (in both directions: an edge between a giant vertex and
+// another is processed from the other end).  Ids in the skipped entries are
+// never read.  The parent array is indexed by global vertex id (it spans
+// total_n entries; only the large graphs' entries are used).
+__global__ void k_large_iota(BatchArgs a, const Chunk *__restrict__ chunks, uint32_t nchunks,
                              uint32_t *__restrict__ par) {
   for (uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; t < (uint64_t)nchunks * kChunk;
        t += (uint64_t)gridDim.x * blockDim.x) {
-    Chunk c = chunks[t / kChunk];
-    uint64_t v0 = a.voff[c.graph];
-    uint32_t n = (uint32_t)(a.voff[c.graph + 1] - v0);
-    uint32_t v = c.first + (uint32_t)(t % kChunk);
+    const Chunk c = chunks[t / kChunk];
+    const uint64_t v0 = a.voff[c.graph];
+    const uint32_t n = (uint32_t)(a.voff[c.graph + 1] - v0);
+    const uint32_t v = c.first + (uint32_t)(t % kChunk);
     if (v >= n) continue;
-    uint32_t pv = (uint32_t)(v0 + v);
-    uint64_t b = a.rp[v0 + v], e = a.rp[v0 + v + 1];
-    if (e < b || e > a.total_m) {
-      set_err(a.err, kErrBadOffsets);
-    } else if (b < e) {
-      uint32_t u = __ldg(a.col + b);
-      if (u < v) pv = (uint32_t)(v0 + u);
-    }
-    par[v0 + v] = pv;
+    const uint64_t b = a.rp[v0 + v], e = a.rp[v0 + v + 1];
+    if (e < b || e > a.total_m) set_err(a.err, kErrBadOffsets);
+    par[v0 + v] = (uint32_t)(v0 + v);
   }
 }
 
-__global__ void k_large_hook(BatchArgs a, const Chunk *__restrict__ chunks, uint32_t nchunks,
-                             uint32_t *par, uint32_t hub_degree, uint32_t *__restrict__ hubs,
-                             uint64_t hub_cap, unsigned int *__restrict__ nh) {
+// Link round r: every vertex with more than r entries unites with its r-th
+// neighbour.
+__global__ void k_large_link(BatchArgs a, const Chunk *__restrict__ chunks, uint32_t nchunks,
+                             uint32_t *par, uint32_t r) {
   for (uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; t < (uint64_t)nchunks * kChunk;
        t += (uint64_t)gridDim.x * blockDim.x) {
-    Chunk c = chunks[t / kChunk];
-    uint64_t v0 = a.voff[c.graph];
-    uint32_t n = (uint32_t)(a.voff[c.graph + 1] - v0);
-    uint32_t v = c.first + (uint32_t)(t % kChunk);
+    const Chunk c = chunks[t / kChunk];
+    const uint64_t v0 = a.voff[c.graph];
+    const uint32_t n = (uint32_t)(a.voff[c.graph + 1] - v0);
+    const uint32_t v = c.first + (uint32_t)(t % kChunk);
     if (v >= n) continue;
-    uint64_t b = a.rp[v0 + v], e = a.rp[v0 + v + 1];
-    if (e < b || e > a.total_m) continue;  // reported by k_large_init
+    const uint64_t b = a.rp[v0 + v], e = a.rp[v0 + v + 1];
+    if (e < b || e > a.total_m || e - b <= r) continue;  // bad offsets: reported by k_large_iota
+    const uint32_t u = __ldg(a.col + b + r);
+    if (u >= n) {
+      set_err(a.err, kErrBadId);
+      continue;
+    }
+    g_union(par, (uint32_t)(v0 + v), (uint32_t)(v0 + u));
+  }
+}
+
+// Every large vertex points at its root (no union runs meanwhile).
+__global__ void k_large_compress(BatchArgs a, const Chunk *__restrict__ chunks, uint32_t nchunks,
+                                 uint32_t *par) {
+  for (uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; t < (uint64_t)nchunks * kChunk;
+       t += (uint64_t)gridDim.x * blockDim.x) {
+    const Chunk c = chunks[t / kChunk];
+    const uint64_t v0 = a.voff[c.graph];
+    const uint32_t n = (uint32_t)(a.voff[c.graph + 1] - v0);
+    const uint32_t v = c.first + (uint32_t)(t % kChunk);
+    if (v >= n) continue;
+    uint32_t r = (uint32_t)(v0 + v), nx;
+    while ((nx = par[r]) != r) r = nx;
+    if (par[v0 + v] != r) par[v0 + v] = r;
+  }
+}
+
+// Giant root of each large graph: the most frequent root among kModeSamples
+// hashed vertices of the graph (one CTA of kModeSamples threads per graph:
+// bitonic sort of the roots in shared memory, then the longest run).
+constexpr uint32_t kModeSamples = 256;
+__global__ void __launch_bounds__(kModeSamples) k_large_mode(BatchArgs a, const uint32_t *__restrict__ big,
+                                                             uint32_t nbig, const uint32_t *par,
+                                                             uint32_t *__restrict__ giant) {
+  __shared__ uint32_t sm[kModeSamples];
+  const uint32_t i = threadIdx.x;
+  for (uint32_t bi = blockIdx.x; bi < nbig; bi += gridDim.x) {
+    const uint32_t g = big[bi];
+    const uint64_t v0 = a.voff[g];
+    const uint64_t n = a.voff[g + 1] - v0;
+    uint32_t r = (uint32_t)(v0 + mix64(0x5eedull + (uint64_t)g * kModeSamples + i) % n), nx;
+    while ((nx = par[r]) != r) r = nx;
+    sm[i] = r;
+    __syncthreads();
+    for (uint32_t k = 2; k <= kModeSamples; k <<= 1) {
+      for (uint32_t j = k >> 1; j > 0; j >>= 1) {
+        const uint32_t ixj = i ^ j;
+        if (ixj > i) {
+          const uint32_t x = sm[i], y = sm[ixj];
+          if ((x > y) == ((i & k) == 0)) {
+            sm[i] = y;
+            sm[ixj] = x;
+          }
+        }
+        __syncthreads();
+      }
+    }
+    if (i == 0) {
+      uint32_t best = sm[0], best_len = 1, run = 1;
+      for (uint32_t k = 1; k < kModeSamples; ++k) {
+        run = sm[k] == sm[k - 1] ? run + 1 : 1;
+        if (run > best_len) {
+          best_len = run;
+          best = sm[k];
+        }
+      }
+      giant[g] = best;
+    }
+    __syncthreads();
+  }
+}
+
+// Rows outside their graph's giant root process their remaining entries (the
+// first two were linked); rows longer than hub_degree go to k_large_hubs.
+__global__ void k_large_rest(BatchArgs a, const Chunk *__restrict__ chunks, uint32_t nchunks,
+                             uint32_t *par, const uint32_t *__restrict__ giant, uint32_t hub_degree,
+                             uint32_t *__restrict__ hubs, uint64_t hub_cap,
+                             unsigned int *__restrict__ nh) {
+  for (uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; t < (uint64_t)nchunks * kChunk;
+       t += (uint64_t)gridDim.x * blockDim.x) {
+    const Chunk c = chunks[t / kChunk];
+    const uint64_t v0 = a.voff[c.graph];
+    const uint32_t n = (uint32_t)(a.voff[c.graph + 1] - v0);
+    const uint32_t v = c.first + (uint32_t)(t % kChunk);
+    if (v >= n) continue;
+    // compressed before this pass: a vertex that held the giant root then is
+    // in the giant component for good (a later walk may move it to an
+    // ancestor; such a row is then processed, which is only more work)
+    if (ld_cg(par + v0 + v) == giant[c.graph]) continue;
+    const uint64_t b = a.rp[v0 + v], e = a.rp[v0 + v + 1];
+    if (e < b || e > a.total_m || e - b <= 2) continue;
     if (e - b > hub_degree) {
-      uint32_t slot = atomicAdd(nh, 1u);
+      const uint32_t slot = atomicAdd(nh, 1u);
       if (slot < hub_cap) hubs[slot] = (uint32_t)(v0 + v);
       else set_err(a.err, kErrOverflow);
       continue;
     }
-    for (uint64_t k = b + 1; k < e; ++k) {
-      uint32_t u = __ldg(a.col + k);
+    for (uint64_t k = b + 2; k < e; ++k) {
+      const uint32_t u = __ldg(a.col + k);
       if (u >= n) {
         set_err(a.err, kErrBadId);
         continue;
       }
-      if (u < v) g_union(par, (uint32_t)(v0 + v), (uint32_t)(v0 + u));
+      g_union(par, (uint32_t)(v0 + v), (uint32_t)(v0 + u));
     }
-    if (b < e && __ldg(a.col + b) >= n) set_err(a.err, kErrBadId);
   }
 }
 
-// Hub rows: one warp per row.  The graph of a hub is found by binary search
-// over the vertex offsets of the large graphs.
+// Hub rows outside the giant component: one warp per row, every entry after
+// the two linked ones.  The graph of a hub is found by binary search over the
+// vertex offsets of the large graphs.
 __global__ void k_large_hubs(BatchArgs a, const uint32_t *__restrict__ big, uint32_t nbig,
                              uint32_t *par, const uint32_t *__restrict__ hubs, uint64_t hub_cap,
                              const unsigned int *__restrict__ nh) {
@@ -211,15 +301,14 @@ __global__ void k_large_hubs(BatchArgs a, const uint32_t *__restrict__ big, uint
     uint32_t gi = big[lo];
     uint64_t v0 = a.voff[gi];
     uint32_t n = (uint32_t)(a.voff[gi + 1] - v0);
-    uint32_t v = (uint32_t)(gv - v0);
     uint64_t b = a.rp[gv], e = a.rp[gv + 1];
-    for (uint64_t k = b + 1 + lane; k < e; k += 32) {
+    for (uint64_t k = b + 2 + lane; k < e; k += 32) {
       uint32_t u = __ldg(a.col + k);
       if (u >= n) {
         set_err(a.err, kErrBadId);
         continue;
       }
-      if (u < v) g_union(par, gv, (uint32_t)(v0 + u));
+      g_union(par, gv, (uint32_t)(v0 + u));
     }
   }
 }
@@ -269,7 +358,7 @@ BatchPlan plan_batch(const std::vector<uint64_t> &voff, const cc_batch_tuning &t
 }
 
 struct BatchDev {
-  DevBuf lists[CC_BATCH_BUCKETS], big, chunks, queues, par, hubs, nh;
+  DevBuf lists[CC_BATCH_BUCKETS], big, chunks, queues, par, hubs, nh, giant;
   uint64_t hub_cap = 0;
 };
 
@@ -290,6 +379,8 @@ void upload_plan(const BatchPlan &P, uint64_t total_n, uint64_t total_m, uint32_
                              cudaMemcpyHostToDevice, s));
   D.queues.alloc(4 * (CC_BATCH_BUCKETS + 1), s, pool);
   D.par.alloc(4 * (P.chunks.empty() ? 1 : total_n), s, pool);
+  // giant root per graph, indexed by graph id (the large graphs' ids ascend in P.big)
+  D.giant.alloc(4 * (P.big.empty() ? 1 : (uint64_t)P.big.back() + 1), s, pool);
   D.hub_cap = total_m / (hub_degree + 1) + 1;
   D.hubs.alloc(4 * D.hub_cap, s, pool);
   D.nh.alloc(4, s, pool);
@@ -330,18 +421,29 @@ void launch_batch(const BatchArgs &a, const BatchPlan &P, BatchDev &D, const cc_
     unsigned grid = grid_for((uint64_t)nch * kChunk, kBlock, num_sms() * 32);
     uint32_t *par = D.par.as<uint32_t>();
     const Chunk *ch = D.chunks.as<Chunk>();
-    k_large_init<<<grid, kBlock, 0, s>>>(a, ch, nch, par);
+    const uint32_t nbig = (uint32_t)P.big.size();
+    k_large_iota<<<grid, kBlock, 0, s>>>(a, ch, nch, par);
     CCG_LAUNCH_CHECK();
-    k_large_hook<<<grid, kBlock, 0, s>>>(a, ch, nch, par, t.hub_degree ? t.hub_degree : 32,
-                                         D.hubs.as<uint32_t>(), D.hub_cap, D.nh.as<unsigned int>());
+    for (uint32_t r = 0; r < 2; ++r) {
+      k_large_link<<<grid, kBlock, 0, s>>>(a, ch, nch, par, r);
+      CCG_LAUNCH_CHECK();
+    }
+    k_large_compress<<<grid, kBlock, 0, s>>>(a, ch, nch, par);
     CCG_LAUNCH_CHECK();
-    k_large_hubs<<<num_sms() * 8, kBlock, 0, s>>>(a, D.big.as<uint32_t>(), (uint32_t)P.big.size(), par,
+    k_large_mode<<<std::min<uint32_t>(nbig, (uint32_t)num_sms() * 8), kModeSamples, 0, s>>>(
+        a, D.big.as<uint32_t>(), nbig, par, D.giant.as<uint32_t>());
+    CCG_LAUNCH_CHECK();
+    k_large_rest<<<grid, kBlock, 0, s>>>(a, ch, nch, par, D.giant.as<uint32_t>(),
+                                         t.hub_degree ? t.hub_degree : 32, D.hubs.as<uint32_t>(),
+                                         D.hub_cap, D.nh.as<unsigned int>());
+    CCG_LAUNCH_CHECK();
+    k_large_hubs<<<num_sms() * 8, kBlock, 0, s>>>(a, D.big.as<uint32_t>(), nbig, par,
                                              D.hubs.as<uint32_t>(), D.hub_cap,
                                              D.nh.as<unsigned int>());
     CCG_LAUNCH_CHECK();
     k_large_finish<<<grid, kBlock, 0, s>>>(a, ch, nch, par);
     CCG_LAUNCH_CHECK();
-    c.add(4, 0);
+    c.add(8, 0);
   }
 }
 
