@@ -11,8 +11,9 @@
 //                 array in shared memory; threads stride over vertices
 //                 (vertex-parallel) or over edges with a binary search for the
 //                 source row (edge-parallel)
-//   large         the rest: grid-wide hook-and-compress on a global parent
-//                 array, hub rows one warp per row
+//   large         the rest: grid-wide sampled linking on a global parent
+//                 array (first two neighbours, a giant root per graph, then
+//                 only the rows outside it), hub rows one warp per row
 // The launches of one solve are recorded once into a CUDA graph and replayed
 // when the same batch and schedule come back.
 #include <algorithm>

@@ -11,7 +11,8 @@
  *
  * One solve runs a small fixed number of launches for all graphs: graphs up
  * to a tuned size are solved whole by one CTA each in shared memory; larger
- * graphs share a grid-wide hook-and-compress.  The schedule (CTA size,
+ * graphs share a grid-wide sampled linking (two neighbours per vertex, then
+ * only the rows outside each graph's largest component).  The schedule (CTA size,
  * shared-memory size bucket, vertex- or edge-parallel hooking) comes from a
  * cc_batch_tuning that cc_batch_autotune() measures per size bucket.
  */
@@ -42,7 +43,8 @@ typedef struct cc_batch_tuning {
                                              go to the grid-wide path */
   uint32_t threads[CC_BATCH_BUCKETS];     /* CTA size of bucket b */
   uint32_t edge_parallel[CC_BATCH_BUCKETS]; /* 1: threads stride over edges, 0: over vertices */
-  uint32_t hub_degree;                     /* grid-wide path: rows above go one warp per row */
+  uint32_t hub_degree;                     /* grid-wide path: rows above (outside the largest
+                                             component) go one warp per row */
   uint32_t use_graph;                      /* replay the launches as one CUDA graph */
 } cc_batch_tuning;
 
