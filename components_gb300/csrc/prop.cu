@@ -15,6 +15,12 @@ namespace {
 // hyperbolic graph the best limit differs per option: label propagation
 // 25.7 / 19.2 / 18.1 ms and shortcuts 13.2 / 13.0 / 13.9 ms for limits of
 // 64 / 128 / 256 entries.
+// A round visits only the rows next to the labels changed in the round before
+// once at most V / div labels changed: label propagation 16.9 / 16.3 ms with
+// div 16 / 2 (33.8 ms with div 1: every round through the neighbour marks)
+// and shortcuts 13.1 / 11.8 ms with div 16 / 8 (div 4 and 2 the same) on the
+// 2^26-vertex hyperbolic graph.
+constexpr uint64_t kLabelSparseDiv = 2, kShortcutSparseDiv = 8;
 constexpr uint64_t kLabelRowLimit = 256, kShortcutRowLimit = 128;
 
 // ---- Propagation (propagation.h:72-149) ------------------------------------
@@ -440,7 +446,7 @@ int labels_propagate(const Csr &g, uint32_t *lab, int max_rounds, cudaStream_t s
     c.add(2, round_bytes);
     const uint32_t changed = static_cast<uint32_t>(*host_flag);
     if (changed == 0) break;
-    sparse = 16ull * changed <= g.n;
+    sparse = kLabelSparseDiv * changed <= g.n;
     uint32_t *t = chg;
     chg = chg_prev;
     chg_prev = t;
@@ -542,7 +548,7 @@ int shortcut_propagate(const Csr &g, uint32_t *lab, uint32_t hitters, int max_ro
     // when few labels changed, the next round pushes a mark to their
     // neighbours and visits only those rows (the first rounds lower nearly
     // every label and run over all rows)
-    sparse = 16ull * changed <= g.n;
+    sparse = kShortcutSparseDiv * changed <= g.n;
   }
   if (f != lab) CCG_CUDA(cudaMemcpyAsync(lab, f, 4 * g.n, cudaMemcpyDeviceToDevice, s));
   return rounds;
