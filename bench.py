@@ -40,6 +40,7 @@ ranks time.
 from __future__ import annotations
 
 import argparse
+import gc
 import json
 import os
 import statistics
@@ -65,6 +66,22 @@ L2_BYTES = 129 * 1024 * 1024
 
 
 # ---- the two single-graph workloads -------------------------------------------
+class NoGC:
+    """Python's cyclic garbage collector paused over a timed region (after one
+    full collection), as timeit does: a full collection with torch loaded takes
+    about 25 ms, which would land in whichever timed step it fell into."""
+
+    def __enter__(self):
+        gc.collect()
+        self.was = gc.isenabled()
+        gc.disable()
+        return self
+
+    def __exit__(self, *a):
+        if self.was:
+            gc.enable()
+
+
 class Workload:
     """One graph family at one size: how each arm builds it and how the JSON
     line names it.  Both arms build the same graph bit for bit (the same
@@ -323,7 +340,7 @@ def gpu_arm(args, wl: Workload, rank: int, world: int, local: int) -> dict | Non
         solver.FindComponents(D, lab)
     ctx.set_profiling(True)
     barrier()
-    with ClockSampler(local) as clocks:
+    with ClockSampler(local) as clocks, NoGC():
         ev0 = torch.cuda.Event(enable_timing=True)
         ev1 = torch.cuda.Event(enable_timing=True)
         ev0.record(stream)
@@ -349,13 +366,14 @@ def gpu_arm(args, wl: Workload, rank: int, world: int, local: int) -> dict | Non
     for _ in range(max(1, args.warmup)):
         solver.FindComponents(Hp, hlab)
     barrier()
-    t0 = time.perf_counter()
-    step_s = []
-    for _ in range(args.steps):
-        ts = time.perf_counter()
-        solver.FindComponents(Hp, hlab)  # returns once the labels are in hlab
-        step_s.append(time.perf_counter() - ts)
-    barrier()
+    with NoGC():
+        t0 = time.perf_counter()
+        step_s = []
+        for _ in range(args.steps):
+            ts = time.perf_counter()
+            solver.FindComponents(Hp, hlab)  # returns once the labels are in hlab
+            step_s.append(time.perf_counter() - ts)
+        barrier()
     e2e_s = (time.perf_counter() - t0) / args.steps
     e2e_st = solver.last_stats  # bytes the library moved over the host link in the last step
     e2e_s = max_over_ranks(e2e_s, world, f"cuda:{local}")
@@ -540,11 +558,12 @@ def workload_batch(args):
     for _ in range(args.warmup):
         B.batch_run(D, ctx, tune, lab)
     torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        B.batch_run(D, ctx, tune, lab)
-    torch.cuda.synchronize()
-    batched_s = (time.perf_counter() - t0) / args.steps
+    with NoGC():
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            B.batch_run(D, ctx, tune, lab)
+        torch.cuda.synchronize()
+        batched_s = (time.perf_counter() - t0) / args.steps
     batched = lab.cpu().numpy().view(np.uint32).copy()
     # plain path, looped in C++: one cc_ctx_run per graph, inputs already on the device
     conf = cc.Config(seed=ALGO_SEED)
