@@ -114,3 +114,25 @@ def test_batch_4096_config_scale(cuda):
     B.plain_run(D, ctx, plain, "exp", cc.Config(seed=1001))
     assert np.array_equal(plain.cpu().numpy().view(np.uint32), want)
     ctx.close()
+
+
+def test_batch_large_graphs_sampled_linking(cuda):
+    """Graphs above the shared-memory sizes go through sampled linking with a
+    giant root per graph: a large graph whose hub row (more entries than the
+    hub threshold) lies outside its giant component, a large graph without a
+    giant component (average degree below one), and a large graph of
+    isolated vertices, between small graphs; labels equal the oracle's."""
+    n = 70000
+    path = [(v, v + 1) for v in range(0, 60000)]  # the giant component
+    star = [(60001, w) for w in range(60002, 60300)]  # a hub outside it
+    bridge = [(60400, 60401), (60401, 60402)]
+    hub_graph = cc.from_edges(n, path + star + bridge)
+    sparse = cc.gen_gnm(80000, 24000, seed=11)  # average degree 0.6
+    empty = cc.from_edges(52000, [])
+    small = [cc.gen_gnm(500, 900, seed=s) for s in range(3)]
+    bt = B.Batch.pack([small[0], hub_graph, small[1], sparse, empty, small[2]])
+    want = _want(bt)
+    t = B.default_tuning()
+    t.hub_degree = 32
+    got = B.batch_run(bt.to_device("cuda:0"), tuning=t).cpu().numpy().view(np.uint32)
+    assert np.array_equal(got, want)
