@@ -271,7 +271,11 @@ struct WarpKeys {
 // degree prefix sum is <= k), so skewed degrees keep every lane busy.  Rows
 // longer than hub_limit are listed as (row, piece) items for k_emit_hubs,
 // which runs next on the same stream.
-template <class T, bool VEC>
+// RANKS: the instance for virtual ranks (rank-local row groups, their list of
+// leaving entries); without ranks neither is compiled: local contraction's
+// emit 5.2 -> 5.0 ms on the 2^26 hyperbolic graph (the same at five and six
+// CTAs per SM).
+template <class T, bool VEC, bool RANKS>
 __global__ void __launch_bounds__(kBlock, VEC ? 4 : 5) k_emit(uint64_t n, const uint64_t *__restrict__ rp,
                                                  const T *__restrict__ col,
                                                  const uint32_t *__restrict__ cl, PartMap pm,
@@ -282,12 +286,12 @@ __global__ void __launch_bounds__(kBlock, VEC ? 4 : 5) k_emit(uint64_t n, const 
                                                  unsigned long long *__restrict__ cnt,
                                                  uint64_t m) {
   __shared__ uint64_t wbuf[kBlock / 32][kWarpKeys];
-  __shared__ uint64_t wout[kBlock / 32][kOutList];
+  __shared__ uint64_t wout[RANKS ? kBlock / 32 : 1][RANKS ? kOutList : 1];
   __shared__ unsigned long long set[kEmitSet];
   const unsigned lane = lane_id(), wid = threadIdx.x >> 5;
   emit_set_clear(set);
   WarpKeys st{wbuf[wid], set, kWarpKeys - 32 * kEmitSteps};
-  uint64_t *olist = wout[wid];
+  uint64_t *olist = wout[RANKS ? wid : 0];
   // the CTA's rows: one contiguous range (a multiple of 32 rows), so that the
   // keys its set holds are those of its current rows
   const uint64_t per = ((n + gridDim.x - 1) / gridDim.x + 31) / 32 * 32;
@@ -338,7 +342,7 @@ __global__ void __launch_bounds__(kBlock, VEC ? 4 : 5) k_emit(uint64_t n, const 
     // loads and tests 32 entries; only a step that keeps some (a few in a
     // hundred on the hyperbolic graph) finds the rows of its entries.
     const uint32_t lo0 = __shfl_sync(0xffffffffu, lo, 0), hi0 = __shfl_sync(0xffffffffu, hi, 0);
-    if (part && !__any_sync(0xffffffffu, hub || (v < n && (lo != lo0 || hi != hi0)))) {
+    if (RANKS && part && !__any_sync(0xffffffffu, hub || (v < n && (lo != lo0 || hi != hi0)))) {
       const uint64_t base = ((uint64_t)__shfl_sync(0xffffffffu, (uint32_t)(eb >> 32), 0) << 32) |
                             __shfl_sync(0xffffffffu, (uint32_t)eb, 0);
       // entries that leave the rank are listed as (offset, id) and resolved
@@ -618,13 +622,17 @@ void emit_keys(const Csr &g, const uint32_t *cl, const PartMap &pm, bool part, i
   // virtual ranks, 32-bit ids on a 16-byte aligned array: the rank-local
   // groups stream their entries with 16-byte loads
   if (part && sizeof(T) == 4 && (reinterpret_cast<uintptr_t>(col) & 15) == 0)
-    k_emit<T, true><<<egrid, kBlock, 0, s>>>(g.n, g.rp, col, cl, pm, part, b, hub_limit,
-                                             hubs.as<uint2>(), cap, nh.as<unsigned int>(), keys, cnt,
-                                             g.m);
+    k_emit<T, true, true><<<egrid, kBlock, 0, s>>>(g.n, g.rp, col, cl, pm, part, b, hub_limit,
+                                                   hubs.as<uint2>(), cap, nh.as<unsigned int>(), keys,
+                                                   cnt, g.m);
+  else if (part)
+    k_emit<T, false, true><<<egrid, kBlock, 0, s>>>(g.n, g.rp, col, cl, pm, part, b, hub_limit,
+                                                    hubs.as<uint2>(), cap, nh.as<unsigned int>(), keys,
+                                                    cnt, g.m);
   else
-    k_emit<T, false><<<egrid, kBlock, 0, s>>>(g.n, g.rp, col, cl, pm, part, b, hub_limit,
-                                              hubs.as<uint2>(), cap, nh.as<unsigned int>(), keys,
-                                              cnt, g.m);
+    k_emit<T, false, false><<<egrid, kBlock, 0, s>>>(g.n, g.rp, col, cl, pm, part, b, hub_limit,
+                                                     hubs.as<uint2>(), cap, nh.as<unsigned int>(),
+                                                     keys, cnt, g.m);
   CCG_LAUNCH_CHECK();
   // at most cap pieces, one warp each: a small graph gets a small grid (every
   // CTA clears its 16 KB key set, which had cost 45 us per launch on the
