@@ -363,7 +363,9 @@ def gpu_arm(args, wl: Workload, rank: int, world: int, local: int) -> dict | Non
     # ---- end to end through the C ABI with pinned host buffers ---------------
     Hp = G.pinned()
     hlab = torch.empty(n, dtype=torch.int32).pin_memory()
-    for _ in range(max(1, args.warmup)):
+    # untimed warm-up of the end-to-end path: at least five calls (the first
+    # timed steps after three had sometimes taken 1.5-2x a settled step)
+    for _ in range(max(5, args.warmup)):
         solver.FindComponents(Hp, hlab)
     barrier()
     with NoGC():
