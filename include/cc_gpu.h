@@ -184,7 +184,8 @@ int cc_csr_validate(const cc_csr *g, int check_sym);
  * uint32 ids, symmetric CSR), labels_out (n uint32).  stream is a
  * cudaStream_t (NULL = default stream).  The call is synchronous: it waits on
  * `stream` until the solve is done and returns its status (CC_ERR_INVALID for
- * offsets that are not monotone or exceed m_dir, or an id >= n).  Scratch
+ * offsets that are not monotone or exceed m_dir, or an id >= n), so it cannot
+ * be recorded into a CUDA graph by stream capture.  Scratch
  * lives in a fixed 4 MiB device array that every GPU loading the library
  * keeps until exit; graphs with min(n, m_dir/33 + 1) > 1,048,512 are rejected
  * with CC_ERR_UNSUPPORTED before any launch.  All calls share that array:
