@@ -130,6 +130,7 @@ GPU_SYMBOLS = {
     "cc_ctx_stream": (_P, [_P]),
     "cc_ctx_set_tuning": (C.c_int, [_P, C.POINTER(cc_tuning)]),
     "cc_ctx_get_tuning": (C.c_int, [_P, C.POINTER(cc_tuning)]),
+    "cc_ctx_set_host_reads": (C.c_int, [_P, C.c_int]),
     "cc_debug_geo_table": (C.c_int, [C.c_double, _P, C.c_int]),
     "cc_debug_hash3": (_U64, [_U64, _U64, _U64]),
     "cc_debug_ldd": (C.c_int, [C.POINTER(cc_csr), _P, _U64, _U32, C.c_double, C.c_int, _P, _P]),

@@ -452,6 +452,24 @@ void accumulate_profile(cc_ctx *C, const cc_stats &st) {
   C->prof_solves++;
 }
 
+// Device address of a page-locked host range [p, p + bytes) that kernels may
+// read: both ends registered with CUDA and mapped at the same address (unified
+// addressing), else false (pageable memory, or a range it cannot vouch for).
+bool mapped_range(const void *p, size_t bytes, const void **dev) {
+  if (!p || bytes == 0) return false;
+  const void *ends[2] = {p, static_cast<const char *>(p) + (bytes - 1)};
+  for (const void *q : ends) {
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, q) != cudaSuccess) {
+      cudaGetLastError();  // clear the sticky-free error of an unknown pointer
+      return false;
+    }
+    if (a.type != cudaMemoryTypeHost || a.devicePointer != q) return false;
+  }
+  *dev = p;
+  return true;
+}
+
 int ctx_run(cc_ctx *C, const cc_csr *g, cc_algo algo, const cc_config *cfg_in, uint64_t seed,
             void *labels_out, uint32_t labels_where) {
   return guard([&] {
@@ -516,11 +534,22 @@ int ctx_run(cc_ctx *C, const cc_csr *g, cc_algo algo, const cc_config *cfg_in, u
         hsrc.sampled = !dc.tiles;
       }
     }
-    if (streamed) {  // host threads encode the offsets as degree bytes
+    // Sampled linking reads each row's offsets and first entries, and whole
+    // rows only outside the giant component: from page-locked host buffers
+    // (mapped into the device's address space) the kernels read them in
+    // place, so most of the ids never cross the host link.
+    const void *rp_mapped = nullptr, *col_mapped = nullptr;
+    if (streamed && hsrc.sampled && C->in_place &&
+        mapped_range(g->row_ptr, 8 * (n + 1), &rp_mapped) && mapped_range(g->col, (size_t)idb * m, &col_mapped))
+      hsrc.in_place = true;
+    if (streamed && !hsrc.in_place) {  // host threads encode the offsets as degree bytes
       if (!C->stager) C->stager.reset(new ccg::HostStager());
       hsrc.stager = C->stager.get();
     }
-    if (g->where == CC_HOST) {
+    if (hsrc.in_place) {
+      G.rp = static_cast<const uint64_t *>(rp_mapped);
+      G.col = col_mapped;
+    } else if (g->where == CC_HOST) {
       rp_d.alloc(8 * (n + 1), s, C->pool);
       col_d.alloc((size_t)idb * (m ? m : 1), s, C->pool);
       if (streamed) {
@@ -802,6 +831,12 @@ int cc_ctx_set_tuning(cc_ctx *ctx, const cc_tuning *t) {
   if (t->tile_threads) u.tile_threads = t->tile_threads;
   if (t->hub_degree) u.hub_degree = t->hub_degree;
   ctx->uf = u;
+  return CC_OK;
+}
+
+int cc_ctx_set_host_reads(cc_ctx *ctx, int in_place) {
+  if (!ctx || (in_place != 0 && in_place != 1)) return CC_ERR_INVALID;
+  ctx->in_place = in_place == 1;
   return CC_OK;
 }
 

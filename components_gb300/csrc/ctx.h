@@ -32,6 +32,7 @@ struct cc_ctx {
   std::vector<cudaEvent_t> ev_pool;  // per-kernel profiling events, reused across solves
   ccg::UfTuning uf;  // hook-and-compress schedule (cc_ctx_set_tuning)
   uint32_t round_cap = 0;  // test hook: lower cap on the iterative rounds (0: n + 2)
+  bool in_place = true;    // sampled linking reads page-locked host input in place
   ccg::UfDecisionCache uf_cache;    // the last device graph's row-sample decisions
   ccg::UfDecisionCache host_cache;  // the last host graph's (streamed input)
   cc_stats stats{};

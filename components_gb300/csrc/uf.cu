@@ -1329,7 +1329,10 @@ void run_uf_afforest(const Csr &g, uint32_t *parent, const PartMap &pm, const Uf
     // offsets, the link-round ids, own parent
     link_bytes = 8 * (g.n + 1) + kAffRounds * g.n * si + 4 * g.n;
     cudaEvent_t t0 = c.tic(s);
-    if (!hs) {
+    if (!hs || hs->in_place) {
+      // host buffers read in place: the pass reads each row's offsets and link
+      // entries across the host link, the only ids most rows ever need (the
+      // remaining pass reads the rows outside the giant component)
       k_tile3<T, PART, TileParent<(int)kAffRounds>, (int)kAffRounds><<<ts.grid, ts.threads, ts.smem, s>>>(
           g.n, g.m, 0, g.n, g.rp, col, parent, pm, ts.tile, ts.stage, hub_degree, none,
           cut.as<uint2>(), cut_cap, cnt.as<unsigned long long>(), g.err);
@@ -1352,7 +1355,11 @@ void run_uf_afforest(const Csr &g, uint32_t *parent, const PartMap &pm, const Uf
         CCG_LAUNCH_CHECK();
       }
     }
-    c.toc(s, hs ? "uf_sample_link_streamed" : "uf_sample_link_tiled", t0, link_bytes);
+    c.toc(s, !hs ? "uf_sample_link_tiled" : hs->in_place ? "uf_sample_link_in_place" : "uf_sample_link_streamed",
+          t0, link_bytes);
+    // in place: the offsets and up to kAffRounds link entries a row (the link
+    // moves whole sectors around them)
+    if (hs && hs->in_place) hs->h2d_bytes = 8 * (g.n + 1) + std::min<uint64_t>(g.m, kAffRounds * g.n) * si;
     cudaEvent_t t1 = c.tic(s);
     k_cut_union<<<num_sms() * kCutCtasLink, kBlock, 0, s>>>(cut.as<uint2>(), cnt.as<unsigned long long>(),
                                              cut_cap, parent);

@@ -304,6 +304,21 @@ typedef struct cc_tuning {
 } cc_tuning;
 int cc_ctx_set_tuning(cc_ctx *ctx, const cc_tuning *t);
 int cc_ctx_get_tuning(cc_ctx *ctx, cc_tuning *t);
+/*
+ * HOST graphs solved by sampled linking (CC_EXP with one rank, CC_ALLREDUCE,
+ * when a sample of rows shows the link-round entries staying in their tiles):
+ * with in_place = 1 (the default) and row_ptr and col in page-locked memory
+ * (cudaHostAlloc / cudaHostRegister, mapped into the device's address space),
+ * the kernels read the offsets, each row's first entries and the rows outside
+ * the giant component straight from the caller's buffers, and nothing else of
+ * the ids crosses the host link; cc_stats.h2d_bytes then counts the offsets
+ * and the first two entries a row (at most m_dir) that the link pass reads
+ * (the link moves whole sectors around them).
+ * in_place = 0, or pageable buffers: the rows are copied to the device in
+ * chunks under the link pass.  Labels are the same either way.  (new, no
+ * counterpart in the reference: its input is in memory already)
+ */
+int cc_ctx_set_host_reads(cc_ctx *ctx, int in_place);
 
 #ifdef __cplusplus
 }

@@ -310,3 +310,37 @@ def test_streamed_host_input(cuda):
             got = lab.numpy().view(np.uint32 if idb == 4 else np.uint64).astype(np.uint64)
             assert np.array_equal(got, want), (idb, tile, "pinned")
             ctx.close()
+
+
+def test_sampled_host_input_read_in_place(cuda):
+    """Host graphs solved by sampled linking from page-locked buffers are read
+    in place (the offsets and each row's link entries counted as h2d bytes);
+    the same labels with in-place reads switched off (rows copied in chunks)
+    and from pageable buffers, for both id widths, with virtual ranks, and on a
+    sparse graph whose largest component holds 42 % of the vertices (most rows
+    read by the remaining pass)."""
+    import torch
+    graphs = [cc.gen_rhg(1 << 18, 16.0, 2.6, seed=4), cc.gen_rhg(1 << 18, 16.0, 2.6, seed=4, id_bytes=8),
+              cc.gen_rhg(1 << 18, 2.0, 2.2, seed=5)]
+    for G in graphs:
+        want = oracle.uf_labels(G)
+        n, idb = G.n, G.id_bytes
+        dt_t, dt_n = (torch.int32, np.uint32) if idb == 4 else (torch.int64, np.uint64)
+        ctx = cc.Context(0)
+        for algo, P in (("exp", 1), ("allreduce", 1), ("allreduce", 3)):
+            Pn = G.with_parts(P).pinned()
+            for in_place in (True, False):
+                ctx.set_host_reads(in_place)
+                lab = torch.full((n,), -1, dtype=dt_t).pin_memory()
+                solver = cc.SOLVERS[algo](cc.Config(seed=1001), 0, P, ctx)
+                solver.FindComponents(Pn, lab)
+                got = lab.numpy().view(dt_n).astype(np.uint64)
+                assert np.array_equal(got, want), (n, idb, algo, P, in_place)
+                h2d = solver.last_stats["h2d_bytes"]
+                if in_place:  # offsets and at most two link entries a row
+                    assert h2d == 8 * (n + 1) + min(G.m, 2 * n) * idb, (h2d, idb, algo, P)
+                else:  # every id copied
+                    assert h2d >= G.m * idb, (h2d, idb, algo, P)
+            ctx.set_host_reads(True)
+            assert np.array_equal(gpu_labels(G, algo, P, "host", ctx=ctx), want), (n, idb, algo, P, "pageable")
+        ctx.close()
