@@ -381,6 +381,12 @@ def gpu_arm(args, wl: Workload, rank: int, world: int, local: int) -> dict | Non
     e2e_s = max_over_ranks(e2e_s, world, f"cuda:{local}")
     e2e_value = whole_job_gedges(world, m, e2e_s * 1e3)
     got_host = hlab.numpy().view(np.uint32).copy()
+    # per-kernel CUDA-event times of one more (untimed) end-to-end call
+    ctx.set_profiling(True)
+    solver.FindComponents(Hp, hlab)
+    e2e_kernels = {k: round(v["ms"], 4) for k, v in solver.last_stats["kernels"].items()}
+    e2e_solve_ms = solver.last_stats["solve_ms"]
+    ctx.set_profiling(False)
     # the same call with the rows copied to the device in chunks instead of
     # read in place (what a caller with pageable buffers gets), for comparison
     ctx.set_host_reads(False)
@@ -477,6 +483,7 @@ def gpu_arm(args, wl: Workload, rank: int, world: int, local: int) -> dict | Non
                 "ms_min_median_max": [min(step_s) * 1e3, statistics.median(step_s) * 1e3,
                                       max(step_s) * 1e3],
                 "ms_steps": [round(x * 1e3, 3) for x in step_s],
+                "kernels_ms_one_call": e2e_kernels, "solve_ms_one_call": e2e_solve_ms,
                 "rows_copied": {"value": whole_job_gedges(world, m, copied_mean * 1e3), "unit": UNIT,
                                 "ms_per_step": copied_mean * 1e3,
                                 "ms_median": statistics.median(copied_s) * 1e3,

@@ -537,21 +537,25 @@ int ctx_run(cc_ctx *C, const cc_csr *g, cc_algo algo, const cc_config *cfg_in, u
     // Sampled linking reads each row's offsets and first entries, and whole
     // rows only outside the giant component: from page-locked host buffers
     // (mapped into the device's address space) the kernels read them in
-    // place, so most of the ids never cross the host link.
+    // place, so most of the ids never cross the host link.  (The tiled pass
+    // reads every id: its input is copied, which measured faster than the
+    // kernel's own reads across the link.)
     const void *rp_mapped = nullptr, *col_mapped = nullptr;
-    if (streamed && hsrc.sampled && C->in_place &&
-        mapped_range(g->row_ptr, 8 * (n + 1), &rp_mapped) && mapped_range(g->col, (size_t)idb * m, &col_mapped))
+    if (streamed && hsrc.sampled && C->host_reads > 0 &&
+        mapped_range(g->row_ptr, 8 * (n + 1), &rp_mapped) && mapped_range(g->col, (size_t)idb * m, &col_mapped)) {
       hsrc.in_place = true;
-    if (streamed && !hsrc.in_place) {  // host threads encode the offsets as degree bytes
+      hsrc.offsets_copied = C->host_reads == 2;
+    }
+    if (streamed && (!hsrc.in_place || hsrc.offsets_copied)) {  // host threads encode the offsets as degree bytes
       if (!C->stager) C->stager.reset(new ccg::HostStager());
       hsrc.stager = C->stager.get();
     }
-    if (hsrc.in_place) {
+    if (hsrc.in_place && !hsrc.offsets_copied) {
       G.rp = static_cast<const uint64_t *>(rp_mapped);
       G.col = col_mapped;
     } else if (g->where == CC_HOST) {
       rp_d.alloc(8 * (n + 1), s, C->pool);
-      col_d.alloc((size_t)idb * (m ? m : 1), s, C->pool);
+      if (!hsrc.in_place) col_d.alloc((size_t)idb * (m ? m : 1), s, C->pool);
       if (streamed) {
         // the copy stream may only write the buffers once they are allocated
         cudaEvent_t ev;
@@ -565,7 +569,7 @@ int ctx_run(cc_ctx *C, const cc_csr *g, cc_algo algo, const cc_config *cfg_in, u
       }
       st.h2d_bytes = n ? 8 * (n + 1) + (uint64_t)idb * m : 0;
       G.rp = rp_d.as<uint64_t>();
-      G.col = col_d.p;
+      G.col = hsrc.in_place ? col_mapped : col_d.p;
     } else {
       G.rp = g->row_ptr;
       G.col = g->col;
@@ -835,8 +839,8 @@ int cc_ctx_set_tuning(cc_ctx *ctx, const cc_tuning *t) {
 }
 
 int cc_ctx_set_host_reads(cc_ctx *ctx, int in_place) {
-  if (!ctx || (in_place != 0 && in_place != 1)) return CC_ERR_INVALID;
-  ctx->in_place = in_place == 1;
+  if (!ctx || in_place < 0 || in_place > 2) return CC_ERR_INVALID;
+  ctx->host_reads = in_place;
   return CC_OK;
 }
 

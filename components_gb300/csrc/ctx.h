@@ -32,7 +32,8 @@ struct cc_ctx {
   std::vector<cudaEvent_t> ev_pool;  // per-kernel profiling events, reused across solves
   ccg::UfTuning uf;  // hook-and-compress schedule (cc_ctx_set_tuning)
   uint32_t round_cap = 0;  // test hook: lower cap on the iterative rounds (0: n + 2)
-  bool in_place = true;    // sampled linking reads page-locked host input in place
+  int host_reads = 1;      // sampled linking of page-locked host input: 0 copy, 1 read in
+                           // place, 2 ids in place and offsets copied (cc_ctx_set_host_reads)
   ccg::UfDecisionCache uf_cache;    // the last device graph's row-sample decisions
   ccg::UfDecisionCache host_cache;  // the last host graph's (streamed input)
   cc_stats stats{};

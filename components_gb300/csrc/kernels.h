@@ -58,8 +58,9 @@ struct HostSource {
                                // as soon as the final compression has finished it
   HostStager *stager = nullptr;  // when set: rows below 255 entries go as degree bytes
   bool sampled = false;  // sampled linking (tiled link rounds) instead of the tiled pass
-  bool in_place = false;  // sampled: rp/col of the Csr are the device addresses of the
-                          // caller's page-locked buffers, read in place (nothing copied)
+  bool in_place = false;  // sampled: col of the Csr is the device address of the caller's
+                          // page-locked ids, read in place; rp too unless offsets_copied
+  bool offsets_copied = false;  // in place: the offsets cross in chunks (degree bytes)
   mutable uint64_t h2d_bytes = 0;  // bytes the streamed pass copied to the device
 };
 void uf_components(const Csr &g, uint32_t *parent, const PartMap *pm,

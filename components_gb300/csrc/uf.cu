@@ -1139,11 +1139,13 @@ void copy_rows_in(const Csr &g, const HostSource *hs, uint64_t v0, uint64_t v1, 
                              cudaMemcpyHostToDevice, hs->copy));
     hs->h2d_bytes += 8 * (v1 - v0 + 1);
   }
-  if (e1 > e0)
-    CCG_CUDA(cudaMemcpyAsync(const_cast<T *>(static_cast<const T *>(g.col)) + e0,
-                             static_cast<const T *>(hs->col) + e0, sizeof(T) * (e1 - e0),
-                             cudaMemcpyHostToDevice, hs->copy));
-  hs->h2d_bytes += sizeof(T) * (e1 - e0);
+  if (!hs->in_place) {  // in place: the kernels read the ids from the caller's buffer
+    if (e1 > e0)
+      CCG_CUDA(cudaMemcpyAsync(const_cast<T *>(static_cast<const T *>(g.col)) + e0,
+                               static_cast<const T *>(hs->col) + e0, sizeof(T) * (e1 - e0),
+                               cudaMemcpyHostToDevice, hs->copy));
+    hs->h2d_bytes += sizeof(T) * (e1 - e0);
+  }
   cudaEvent_t ev;
   CCG_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
   CCG_CUDA(cudaEventRecord(ev, hs->copy));
@@ -1329,7 +1331,7 @@ void run_uf_afforest(const Csr &g, uint32_t *parent, const PartMap &pm, const Uf
     // offsets, the link-round ids, own parent
     link_bytes = 8 * (g.n + 1) + kAffRounds * g.n * si + 4 * g.n;
     cudaEvent_t t0 = c.tic(s);
-    if (!hs || hs->in_place) {
+    if (!hs || (hs->in_place && !hs->offsets_copied)) {
       // host buffers read in place: the pass reads each row's offsets and link
       // entries across the host link, the only ids most rows ever need (the
       // remaining pass reads the rows outside the giant component)
@@ -1355,11 +1357,17 @@ void run_uf_afforest(const Csr &g, uint32_t *parent, const PartMap &pm, const Uf
         CCG_LAUNCH_CHECK();
       }
     }
-    c.toc(s, !hs ? "uf_sample_link_tiled" : hs->in_place ? "uf_sample_link_in_place" : "uf_sample_link_streamed",
+    c.toc(s,
+          !hs                   ? "uf_sample_link_tiled"
+          : !hs->in_place       ? "uf_sample_link_streamed"
+          : hs->offsets_copied  ? "uf_sample_link_ids_in_place"
+                                : "uf_sample_link_in_place",
           t0, link_bytes);
-    // in place: the offsets and up to kAffRounds link entries a row (the link
-    // moves whole sectors around them)
-    if (hs && hs->in_place) hs->h2d_bytes = 8 * (g.n + 1) + std::min<uint64_t>(g.m, kAffRounds * g.n) * si;
+    // in place: up to kAffRounds link entries a row, and the offsets unless
+    // they were copied (the link moves whole sectors around the entries)
+    if (hs && hs->in_place)
+      hs->h2d_bytes = (hs->offsets_copied ? hs->h2d_bytes : 8 * (g.n + 1)) +
+                      std::min<uint64_t>(g.m, kAffRounds * g.n) * si;
     cudaEvent_t t1 = c.tic(s);
     k_cut_union<<<num_sms() * kCutCtasLink, kBlock, 0, s>>>(cut.as<uint2>(), cnt.as<unsigned long long>(),
                                              cut_cap, parent);

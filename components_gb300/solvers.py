@@ -56,10 +56,11 @@ class Context:
         return {"hook_mode": t.hook_mode, "tile_vertices": t.tile_vertices,
                 "tile_threads": t.tile_threads, "hub_degree": t.hub_degree}
 
-    def set_host_reads(self, in_place: bool) -> None:
-        """Sampled linking of a host graph in page-locked memory: read it in
-        place (True, the default) or copy its rows in chunks (False)."""
-        _lib.check(_lib.gpu().cc_ctx_set_host_reads(self._h, 1 if in_place else 0))
+    def set_host_reads(self, mode: int) -> None:
+        """Sampled linking of a host graph in page-locked memory: 1 (True, the
+        default) reads it in place, 2 reads the ids in place and copies the
+        offsets in chunks, 0 (False) copies its rows in chunks."""
+        _lib.check(_lib.gpu().cc_ctx_set_host_reads(self._h, int(mode)))
 
     def set_profiling(self, on: bool, components: bool = False) -> None:
         """Per-kernel CUDA-event timing; with `components` also the component

@@ -314,6 +314,8 @@ int cc_ctx_get_tuning(cc_ctx *ctx, cc_tuning *t);
  * the ids crosses the host link; cc_stats.h2d_bytes then counts the offsets
  * and the first two entries a row (at most m_dir) that the link pass reads
  * (the link moves whole sectors around them).
+ * in_place = 2: the ids are read in place and the offsets copied in chunks
+ * (as one degree byte a row where they fit) under the link pass.
  * in_place = 0, or pageable buffers: the rows are copied to the device in
  * chunks under the link pass.  Labels are the same either way.  (new, no
  * counterpart in the reference: its input is in memory already)

@@ -292,7 +292,9 @@ def test_hook_modes_agree(cuda, mode):
 def test_streamed_host_input(cuda):
     """Host CSR copied in tile-aligned chunks under the tile pass (each chunk's
     cut edges united before the next chunk's tiles): same labels for pageable
-    and pinned buffers, both id widths, many chunks, with virtual ranks."""
+    and pinned buffers (with every setting of the in-place reads, which the
+    tiled pass does not take), both id widths, many chunks, with virtual
+    ranks."""
     import torch
     for idb in (4, 8):
         G = cc.gen_grid(1100, 900, 0.55, seed=12, id_bytes=idb)
@@ -305,20 +307,26 @@ def test_streamed_host_input(cuda):
                     assert np.array_equal(gpu_labels(G, algo, P, "host", ctx=ctx), want), (idb, tile, algo, P)
             Pn = G.pinned()
             dt = torch.int32 if idb == 4 else torch.int64
-            lab = torch.empty(G.n, dtype=dt).pin_memory()
-            cc.ExponentialContraction(cc.Config(seed=1001), 0, 1, ctx).FindComponents(Pn, lab)
-            got = lab.numpy().view(np.uint32 if idb == 4 else np.uint64).astype(np.uint64)
-            assert np.array_equal(got, want), (idb, tile, "pinned")
+            for mode in (1, 2, 0):  # read in place, ids in place, copied
+                ctx.set_host_reads(mode)
+                lab = torch.empty(G.n, dtype=dt).pin_memory()
+                solver = cc.ExponentialContraction(cc.Config(seed=1001), 0, 1, ctx)
+                solver.FindComponents(Pn, lab)
+                got = lab.numpy().view(np.uint32 if idb == 4 else np.uint64).astype(np.uint64)
+                assert np.array_equal(got, want), (idb, tile, "pinned", mode)
+                h2d = solver.last_stats["h2d_bytes"]  # the tiled pass copies in every mode
+                assert G.m * idb <= h2d <= 8 * (G.n + 1) + G.m * idb, (h2d, idb, tile, mode)
             ctx.close()
 
 
 def test_sampled_host_input_read_in_place(cuda):
     """Host graphs solved by sampled linking from page-locked buffers are read
     in place (the offsets and each row's link entries counted as h2d bytes);
-    the same labels with in-place reads switched off (rows copied in chunks)
-    and from pageable buffers, for both id widths, with virtual ranks, and on a
-    sparse graph whose largest component holds 42 % of the vertices (most rows
-    read by the remaining pass)."""
+    the same labels with only the ids read in place (offsets copied in chunks),
+    with in-place reads switched off (rows copied in chunks) and from pageable
+    buffers, in one chunk and in two, for both id widths, with virtual ranks,
+    and on a sparse graph whose largest component holds 42 % of the vertices
+    (most rows read by the remaining pass)."""
     import torch
     graphs = [cc.gen_rhg(1 << 18, 16.0, 2.6, seed=4), cc.gen_rhg(1 << 18, 16.0, 2.6, seed=4, id_bytes=8),
               cc.gen_rhg(1 << 18, 2.0, 2.2, seed=5)]
@@ -326,21 +334,26 @@ def test_sampled_host_input_read_in_place(cuda):
         want = oracle.uf_labels(G)
         n, idb = G.n, G.id_bytes
         dt_t, dt_n = (torch.int32, np.uint32) if idb == 4 else (torch.int64, np.uint64)
-        ctx = cc.Context(0)
-        for algo, P in (("exp", 1), ("allreduce", 1), ("allreduce", 3)):
-            Pn = G.with_parts(P).pinned()
-            for in_place in (True, False):
-                ctx.set_host_reads(in_place)
-                lab = torch.full((n,), -1, dtype=dt_t).pin_memory()
-                solver = cc.SOLVERS[algo](cc.Config(seed=1001), 0, P, ctx)
-                solver.FindComponents(Pn, lab)
-                got = lab.numpy().view(dt_n).astype(np.uint64)
-                assert np.array_equal(got, want), (n, idb, algo, P, in_place)
-                h2d = solver.last_stats["h2d_bytes"]
-                if in_place:  # offsets and at most two link entries a row
-                    assert h2d == 8 * (n + 1) + min(G.m, 2 * n) * idb, (h2d, idb, algo, P)
-                else:  # every id copied
-                    assert h2d >= G.m * idb, (h2d, idb, algo, P)
-            ctx.set_host_reads(True)
-            assert np.array_equal(gpu_labels(G, algo, P, "host", ctx=ctx), want), (n, idb, algo, P, "pageable")
-        ctx.close()
+        in_place = 8 * (n + 1) + min(G.m, 2 * n) * idb  # offsets, at most two link entries a row
+        for tile in (0, 1024):  # 1024: the rows cross in two chunks
+            ctx = cc.Context(0)
+            ctx.set_tuning(tile_vertices=tile)
+            for algo, P in (("exp", 1), ("allreduce", 1), ("allreduce", 3)):
+                Pn = G.with_parts(P).pinned()
+                for mode in (1, 2, 0):  # in place, ids in place, copied
+                    ctx.set_host_reads(mode)
+                    lab = torch.full((n,), -1, dtype=dt_t).pin_memory()
+                    solver = cc.SOLVERS[algo](cc.Config(seed=1001), 0, P, ctx)
+                    solver.FindComponents(Pn, lab)
+                    got = lab.numpy().view(dt_n).astype(np.uint64)
+                    assert np.array_equal(got, want), (n, idb, tile, algo, P, mode)
+                    h2d = solver.last_stats["h2d_bytes"]
+                    if mode == 1:
+                        assert h2d == in_place, (h2d, idb, tile, algo, P)
+                    elif mode == 2:  # later chunks' offsets as degree bytes
+                        assert h2d <= in_place and (tile == 0) == (h2d == in_place), (h2d, idb, tile, algo, P)
+                    else:  # every id copied
+                        assert h2d >= G.m * idb, (h2d, idb, tile, algo, P)
+                ctx.set_host_reads(1)
+                assert np.array_equal(gpu_labels(G, algo, P, "host", ctx=ctx), want), (n, idb, algo, P, "pageable")
+            ctx.close()
