@@ -452,10 +452,11 @@ void accumulate_profile(cc_ctx *C, const cc_stats &st) {
   C->prof_solves++;
 }
 
-// Device address of a page-locked host range [p, p + bytes) that kernels may
-// read: both ends registered with CUDA and mapped at the same address (unified
-// addressing), else false (pageable memory, or a range it cannot vouch for).
-bool mapped_range(const void *p, size_t bytes, const void **dev) {
+// Device address of a page-locked host range [p, p + bytes) that kernels on
+// `device` may read: both ends registered with CUDA against that device and
+// mapped at the same address (unified addressing), else false (pageable
+// memory, memory of another device's context, or a range it cannot vouch for).
+bool mapped_range(const void *p, size_t bytes, int device, const void **dev) {
   if (!p || bytes == 0) return false;
   const void *ends[2] = {p, static_cast<const char *>(p) + (bytes - 1)};
   for (const void *q : ends) {
@@ -464,7 +465,7 @@ bool mapped_range(const void *p, size_t bytes, const void **dev) {
       cudaGetLastError();  // clear the sticky-free error of an unknown pointer
       return false;
     }
-    if (a.type != cudaMemoryTypeHost || a.devicePointer != q) return false;
+    if (a.type != cudaMemoryTypeHost || a.devicePointer != q || a.device != device) return false;
   }
   *dev = p;
   return true;
@@ -542,7 +543,8 @@ int ctx_run(cc_ctx *C, const cc_csr *g, cc_algo algo, const cc_config *cfg_in, u
     // kernel's own reads across the link.)
     const void *rp_mapped = nullptr, *col_mapped = nullptr;
     if (streamed && hsrc.sampled && C->host_reads > 0 &&
-        mapped_range(g->row_ptr, 8 * (n + 1), &rp_mapped) && mapped_range(g->col, (size_t)idb * m, &col_mapped)) {
+        mapped_range(g->row_ptr, 8 * (n + 1), C->device, &rp_mapped) &&
+        mapped_range(g->col, (size_t)idb * m, C->device, &col_mapped)) {
       hsrc.in_place = true;
       hsrc.offsets_copied = C->host_reads == 2;
     }

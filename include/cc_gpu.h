@@ -308,7 +308,8 @@ int cc_ctx_get_tuning(cc_ctx *ctx, cc_tuning *t);
  * HOST graphs solved by sampled linking (CC_EXP with one rank, CC_ALLREDUCE,
  * when a sample of rows shows the link-round entries staying in their tiles):
  * with in_place = 1 (the default) and row_ptr and col in page-locked memory
- * (cudaHostAlloc / cudaHostRegister, mapped into the device's address space),
+ * (cudaHostAlloc / cudaHostRegister with the context's device current, mapped
+ * into the device's address space),
  * the kernels read the offsets, each row's first entries and the rows outside
  * the giant component straight from the caller's buffers, and nothing else of
  * the ids crosses the host link; cc_stats.h2d_bytes then counts the offsets
