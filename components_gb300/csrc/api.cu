@@ -462,7 +462,7 @@ bool mapped_range(const void *p, size_t bytes, int device, const void **dev) {
   for (const void *q : ends) {
     cudaPointerAttributes a;
     if (cudaPointerGetAttributes(&a, q) != cudaSuccess) {
-      cudaGetLastError();  // clear the sticky-free error of an unknown pointer
+      cudaGetLastError();  // an unknown pointer leaves a (non-sticky) error: clear it
       return false;
     }
     if (a.type != cudaMemoryTypeHost || a.devicePointer != q || a.device != device) return false;

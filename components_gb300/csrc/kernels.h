@@ -48,7 +48,8 @@ struct UfTuning {
 };
 // Host source of a caller graph whose device buffers are still empty: the
 // tiled pass copies tile-aligned chunks on `copy` and overlaps them with the
-// tile kernel (rp/col of the Csr are the destination device buffers).
+// tile kernel (rp/col of the Csr are the destination device buffers); read in
+// place, rp/col of the Csr are the device addresses of the caller's buffers.
 struct HostStager;
 struct HostSource {
   const uint64_t *rp;
@@ -61,7 +62,7 @@ struct HostSource {
   bool in_place = false;  // sampled: col of the Csr is the device address of the caller's
                           // page-locked ids, read in place; rp too unless offsets_copied
   bool offsets_copied = false;  // in place: the offsets cross in chunks (degree bytes)
-  mutable uint64_t h2d_bytes = 0;  // bytes the streamed pass copied to the device
+  mutable uint64_t h2d_bytes = 0;  // bytes the pass copied to the device or read in place
 };
 void uf_components(const Csr &g, uint32_t *parent, const PartMap *pm,
                    const UfTuning &tu, cudaStream_t s, cudaMemPool_t pool,
