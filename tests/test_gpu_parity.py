@@ -357,3 +357,34 @@ def test_sampled_host_input_read_in_place(cuda):
                 ctx.set_host_reads(1)
                 assert np.array_equal(gpu_labels(G, algo, P, "host", ctx=ctx), want), (n, idb, algo, P, "pageable")
             ctx.close()
+
+
+def test_registered_host_input_read_in_place(cuda):
+    """Existing host arrays registered with cudaHostRegister (what a caller
+    does to its graph buffers once) are read in place like page-locked
+    allocations; after unregistering, the same call copies them."""
+    import torch
+    cudart = torch.cuda.cudart()
+    G = cc.gen_rhg(1 << 18, 16.0, 2.6, seed=7)
+    want = oracle.uf_labels(G)
+    rp = np.ascontiguousarray(G.row_ptr, dtype=np.uint64)
+    col = np.ascontiguousarray(G.col, dtype=np.uint32)
+    n = G.n
+    for a in (rp, col):
+        assert int(cudart.cudaHostRegister(a.ctypes.data, a.nbytes, 0)) == 0
+    try:
+        H = cc.StaticGraph(rp, col)
+        ctx = cc.Context(0)
+        lab = np.full(n, 0xFFFFFFFF, np.uint32)
+        solver = cc.ExponentialContraction(cc.Config(seed=1001), 0, 1, ctx)
+        solver.FindComponents(H, lab)
+        assert np.array_equal(lab.astype(np.uint64), want)
+        assert solver.last_stats["h2d_bytes"] == 8 * (n + 1) + min(G.m, 2 * n) * 4
+    finally:
+        for a in (rp, col):
+            cudart.cudaHostUnregister(a.ctypes.data)
+    lab = np.full(n, 0xFFFFFFFF, np.uint32)
+    solver.FindComponents(H, lab)
+    assert np.array_equal(lab.astype(np.uint64), want)
+    assert solver.last_stats["h2d_bytes"] >= G.m * 4
+    ctx.close()
